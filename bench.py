@@ -1,0 +1,503 @@
+#!/usr/bin/env python
+"""Benchmark of the SEM operator-apply / PCG hot path on one GB300.
+
+Headline (`value`): GDOF/s of the FP64 Helmholtz operator with direct-stiffness
+summation and Dirichlet mask, mask(QQ'(nu lapl u + lambda B u)), on the
+256x256-element, N=8 deformed mesh (4,198,401 unique DOF), inputs resident in
+HBM, L2 flushed between steps.  `e2e` is the same metric through the public
+API with the input copied from pinned host memory and the result copied back
+every step.  Extra keys: PCG solves/s (FP64 vs mixed precision), the order
+sweep N=4/8/12/16, roofline, CPU baseline.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs independent replicas (the path does not shard), one per GPU,
+launched by torch.distributed.run; `value` sums all ranks' DOF over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "spectralelements.jl_gb300"))
+
+METRIC = "GDOF/s lapl+QQᵀ; PCG solves/s mixed vs FP64 plain at 1e-8 rel resid, 1 GB300"
+UNIT = "GDOF/s"
+N_ORDER, E_X, E_Y, AMP, NU, LAM = 8, 256, 256, 0.05, 1e-2, 1.0
+BYTES_PER_LOCAL = 48  # u, G11, G12, G22, B read + result written (FP64)
+WORKLOAD = ("hlmz+QQ'+mask apply mask(QQ'(nu lapl(u) + lambda B u)), 256x256 elements, N=8 "
+            "(9x9 GLL), nu=1e-2, lambda=1, sinusoidal deformation amp 0.05, Dirichlet on all sides")
+
+
+def sin_deform(amp):
+    import numpy as np
+
+    def deform(x, y):
+        r = 0.5 * (x + 1.0)
+        s = 0.5 * (y + 1.0)
+        b = amp * np.sin(np.pi * r) * np.sin(np.pi * s)
+        return r + b, s + b
+    return deform
+
+
+def unique_dof(n, Ex, Ey):
+    return (Ex * (n - 1) + 1) * (Ey * (n - 1) + 1)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """dram bytes per launch recorded from an ncu capture in profiles/<name>."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid = uuid
+        self.samples = []
+        self.proc = None
+        self.marks = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.uuid, f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        threading.Thread(target=self._read, daemon=True).start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append((time.time(), parts))
+
+    def mark(self, tag):
+        self.marks.append((tag, time.time()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        inside = [p for t, p in self.samples if t0 - 0.25 <= t <= t1 + 0.25]
+        use = inside if inside else [p for _, p in self.samples]
+        if not use:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(p[0]) for p in use if num(p[0]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for p in use:
+            for name, v in zip(names, p[3:7]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": num(use[0][1]),
+                "reasons": sorted(reasons), "samples": len(use),
+                "window": "timed region" if inside else "whole run (timed region shorter than the 200 ms sampling period)"}
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import semgb300 as S
+
+    torch.cuda.set_device(local_rank)
+    S.load()
+    lib = S.load()
+    dev = torch.device("cuda", local_rank)
+    uuid = str(torch.cuda.get_device_properties(dev).uuid)
+    sampler = ClockSampler(uuid if uuid.startswith("GPU-") else "GPU-" + uuid)
+    sampler.start()
+
+    msh = S.Mesh(N_ORDER + 1, N_ORDER + 1, E_X, E_Y, (False, False), sin_deform(AMP), bc="DDDD")
+    nx, ny = msh.shape
+    L = nx * ny
+    G = unique_dof(N_ORDER + 1, E_X, E_Y)
+    rng = np.random.default_rng(3)
+    u_h = rng.uniform(-1.0, 1.0, (nx, ny))
+    u = S.as_local(u_h)
+    out = msh.empty()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flags = S.SEM_GS | S.SEM_MASK
+
+    def apply():
+        S._lib.check(lib.sem_hlmz(msh.handle, None, NU, LAM, u.data_ptr(), out.data_ptr(), flags, sp))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        apply()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    lib.sem_timing_read(None, None)
+    lib.sem_timing_enable(1)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t0 = time.time()
+    for i in range(args.steps):
+        flush.fill_(float(i))  # L2 flush (512 MiB write), outside the timed events
+        ev[i][0].record(stream)
+        apply()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    t1 = time.time()
+    lib.sem_timing_enable(0)
+    import ctypes
+    kms, kn = ctypes.c_double(), ctypes.c_int()
+    lib.sem_timing_read(ctypes.byref(kms), ctypes.byref(kn))
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * G / (ms * 1e-3) / 1e9
+    kernel_ms = kms.value / max(1, kn.value)
+    clocks = sampler.summary(t0, t1)
+
+    # ---- e2e through the public API: pinned host input -> device -> host
+    x_pin = torch.from_numpy(np.asfortranarray(u_h)).pin_memory()
+    x_pin = x_pin if x_pin.stride() == (1, nx) else x_pin.t().contiguous().t().pin_memory()
+    y_pin = torch.empty_strided((nx, ny), (1, nx), dtype=torch.float64, pin_memory=True)
+    x_dev = msh.empty()
+    op = S.HelmholtzOp(msh, NU, LAM)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        x_dev.copy_(x_pin, non_blocking=True)
+        y = op(x_dev)
+        y_pin.copy_(y, non_blocking=True)
+        b.record(stream)
+        b.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append(a.elapsed_time(b))
+    e2e_step = sum(e2e_ms) / len(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_step], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e = {"value": world * G / (e2e_step * 1e-3) / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L, "ms_per_step": e2e_step,
+           "api": "semgb300.HelmholtzOp (sem_hlmz through ctypes), pinned host buffers"}
+    # parity of this very output against the F64 arithmetic
+    y_dev = op(u)
+    msh.set_precision(S.SEM_F64)
+    y64 = op(u)
+    t64 = time_apply(lambda: op(u), stream, 5)
+    msh.set_precision(S.SEM_F64_DF)
+    rel = (torch.linalg.norm(y_dev - y64) / torch.linalg.norm(y64)).item()
+
+    peak, peak_kind = load_peaks()
+    bytes_launch = BYTES_PER_LOCAL * L
+    achieved = bytes_launch / (kernel_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": profiled_traffic("k_apply_hlmz_df_256x256_n8.md"),
+                "kernel": "k_apply<PDF,9,8,3> (fused element operator, double-float)",
+                "kernel_ms": kernel_ms, "kernel_launches_timed": kn.value,
+                "algorithmic_bytes_per_launch": bytes_launch,
+                "flops_per_launch": (8 * 9 ** 3 + 7 * 9 ** 2) * E_X * E_Y,
+                "note": "FP64 runs at 1/64 of FP32 on GB300; the kernel computes in double-float on the FP32 pipe"}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded U(-1,1) field (seed 3) on the seeded deformed mesh",
+        "config": {"workload": WORKLOAD, "elements": [E_X, E_Y], "order": N_ORDER,
+                   "unique_dof": G, "local_dof": L,
+                   "arith": "double-float (FP32 pairs) with FP64 storage; rel-L2 vs native FP64 "
+                            f"{rel:.2e}",
+                   "l2": "flushed between timed steps (512 MiB write outside the events)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": roofline, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clocks,
+        "f64_native_apply": {"ms": t64, "GDOF/s": G / (t64 * 1e-3) / 1e9},
+    }
+    if not args.no_extras:
+        result["pcg"] = bench_pcg(S, msh, stream)
+        result["sweep"] = bench_sweep(S, stream)
+    sampler.stop()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline()
+    return result
+
+
+def time_apply(fn, stream, reps):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def fourier_forcing(msh_x, msh_y, seed, nmodes=16):
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    f = torch.zeros_like(msh_x)
+    for _ in range(nmodes):
+        kx, ky = rng.integers(1, 9, size=2)
+        c = rng.standard_normal() / (kx ** 2 + ky ** 2)
+        f += c * torch.sin(float(kx) * np.pi * msh_x) * torch.sin(float(ky) * np.pi * msh_y)
+    return f
+
+
+def bench_pcg(S, msh, stream):
+    """Jacobi PCG to 1e-8 relative residual: FP64 (double-float operator) vs
+    mixed precision (FP32 inner CG to 1e-4, <= 6 FP64 defect-correction sweeps)."""
+    import numpy as np
+    import torch
+    out = {}
+    # cfg2: Helmholtz 256x256, N=8, 16 Fourier modes (seed 2)
+    f = fourier_forcing(msh.x, msh.y, 2)
+    M = S.generateMask("DDDD", msh)
+    b = S.gatherScatter(S.mask(S.mass(f, msh), M), msh)
+    tol = 1e-8 * b.abs().max().item()
+    op = S.HelmholtzOp(msh, NU, LAM)
+    jac = S.Jacobi(op)
+    res = {}
+    for name, prec in (("fp64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED)):
+        info = {}
+        S.pcg(b, op, opM=jac, mult=msh.mult, tol=tol, precision=prec, info=info)  # warm
+        torch.cuda.synchronize()
+        t = time.time()
+        x = S.pcg(b, op, opM=jac, mult=msh.mult, tol=tol, precision=prec, info=info)
+        torch.cuda.synchronize()
+        dt = time.time() - t
+        res[name] = (x, dt, dict(info))
+    x64, dt64, i64 = res["fp64"]
+    xm, dtm, im = res["mixed"]
+    out["cfg2_helmholtz_256x256_n8"] = {
+        "tol_rel": 1e-8, "fp64": {"solves_per_s": 1 / dt64, "iters": i64["iters"],
+                                   "res_inf": i64["res_inf"], "res0_inf": i64["res0_inf"]},
+        "mixed": {"solves_per_s": 1 / dtm, "inner_iters": im["iters"], "outer": im["outer"],
+                  "res_inf": im["res_inf"],
+                  "rel_l2_vs_fp64": (torch.linalg.norm(xm - x64) / torch.linalg.norm(x64)).item()},
+        "mixed_over_fp64": dt64 / dtm}
+    # cfg1 / cfg3: Poisson 8x8, N=8, amp 0.1, exact solution sin(pi x) sin(pi y), 1e-10
+    m1 = S.Mesh(9, 9, 8, 8, (False, False), sin_deform(0.1), bc="DDDD")
+    ut = torch.sin(np.pi * m1.x) * torch.sin(np.pi * m1.y)
+    f1 = 2 * np.pi ** 2 * ut
+    M1 = S.generateMask("DDDD", m1)
+    b1 = S.gatherScatter(S.mask(S.mass(f1, m1), M1), m1)
+    op1 = S.HelmholtzOp(m1, 1.0, 0.0)
+    jac1 = S.Jacobi(op1)
+    r = {}
+    for name, prec, tolr in (("cfg1_fp64", S.SEM_F64_DF, 1e-10), ("cfg3_mixed", S.SEM_MIXED, 1e-10),
+                             ("cfg3_mixed_1e-8", S.SEM_MIXED, 1e-8), ("cfg1_fp64_1e-8", S.SEM_F64_DF, 1e-8)):
+        tol1 = tolr * b1.abs().max().item()
+        info = {}
+        S.pcg(b1, op1, opM=jac1, mult=m1.mult, tol=tol1, precision=prec, info=info)
+        torch.cuda.synchronize()
+        reps = 20
+        t = time.time()
+        for _ in range(reps):
+            x = S.pcg(b1, op1, opM=jac1, mult=m1.mult, tol=tol1, precision=prec, info=info)
+        torch.cuda.synchronize()
+        dt = (time.time() - t) / reps
+        r[name] = {"solves_per_s": 1 / dt, "iters": info["iters"], "outer": info["outer"],
+                   "res_inf": info["res_inf"], "tol_rel": tolr,
+                   "err_vs_exact_inf": (x - ut).abs().max().item()}
+    out["cfg1_cfg3_poisson_8x8_n8"] = r
+    return out
+
+
+def bench_sweep(S, stream):
+    """Apply GDOF/s across orders at ~4M unique DOF (double-float, L2-resident
+    inputs larger than L2)."""
+    import numpy as np
+    import torch
+    res = {}
+    for N, E in ((4, 500), (8, 256), (12, 167), (16, 125)):
+        m = S.Mesh(N + 1, N + 1, E, E, (False, False), sin_deform(AMP), bc="DDDD")
+        u = S.as_local(torch.rand(m.shape, dtype=torch.float64, device="cuda") * 2 - 1)
+        op = S.HelmholtzOp(m, NU, LAM)
+        ms = time_apply(lambda: op(u), stream, 10)
+        G = unique_dof(N + 1, E, E)
+        L = (N + 1) ** 2 * E * E
+        res[f"N{N}_E{E}"] = {"GDOF/s": G / (ms * 1e-3) / 1e9, "ms": ms,
+                             "GB/s_alg": BYTES_PER_LOCAL * L / (ms * 1e-3) / 1e9}
+        del m
+    return res
+
+
+# ---------------------------------------------------------------------------
+def reference_apply_timer(threads_note=True):
+    """The reference's CPU path, restated in NumPy (reference-faithful: dense
+    QQtx/QQty as the reference's Mesh stores them, BLAS gemms in ABu)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import sem_oracle as O
+    mo = O.Mesh(N_ORDER + 1, N_ORDER + 1, E_X, E_Y, (False, False), O.sin_deform(AMP), dense_qq=True)
+    M = O.generateMask(["D"] * 4, mo)
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-1.0, 1.0, mo.shape)
+
+    def step():
+        return O.mask(O.gatherScatter(O.hlmz(u, NU, LAM, mo), mo), M)
+    return step, mo
+
+
+def cpu_baseline():
+    """Bounded CPU sample on the host cores: the reference-faithful NumPy
+    restatement (kind 'port'), plus the optimised C/OpenMP oracle."""
+    import numpy as np
+    step, mo = reference_apply_timer()
+    step()
+    times = []
+    t_end = time.time() + 12.0
+    while time.time() < t_end or len(times) < 2:
+        t = time.time()
+        step()
+        times.append(time.time() - t)
+        if len(times) >= 10:
+            break
+    G = unique_dof(N_ORDER + 1, E_X, E_Y)
+    val = G / statistics.median(times) / 1e9
+    out = {"value": val, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+           "sample": f"{len(times)} applies of the full 256x256 N=8 workload, reference-faithful "
+                     "NumPy restatement (dense QQtx/QQty gemms as src/mesh.jl:44-45 stores them, "
+                     "BLAS threads = all host cores); median",
+           "ms_per_apply": 1e3 * statistics.median(times)}
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import sem_oracle_c as C
+        g = C.grid(N_ORDER + 1, E_X, E_Y, (False, False), "DDDD")
+        rng = np.random.default_rng(3)
+        u = rng.uniform(-1.0, 1.0, mo.shape)
+        C.apply(g, mo.Dr, mo.Ds, mo.G11, mo.G12, mo.G22, mo.B, u, nu=NU, k=LAM)
+        ts = []
+        for _ in range(5):
+            t = time.time()
+            C.apply(g, mo.Dr, mo.Ds, mo.G11, mo.G12, mo.G22, mo.B, u, nu=NU, k=LAM)
+            ts.append(time.time() - t)
+        out["optimised_c_openmp"] = {"value": G / statistics.median(ts) / 1e9, "unit": UNIT,
+                                     "threads": C.threads(), "ms_per_apply": 1e3 * statistics.median(ts)}
+    except Exception as e:  # the C oracle is optional for the baseline line
+        out["optimised_c_openmp"] = {"error": str(e)}
+    return out
+
+
+def run_reference(args):
+    step, _ = reference_apply_timer()
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t = time.time()
+        step()
+        times.append(time.time() - t)
+    ms = 1e3 * sum(times) / len(times)
+    G = unique_dof(N_ORDER + 1, E_X, E_Y)
+    val = G / (ms * 1e-3) / 1e9
+    cores = os.cpu_count()
+    return {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic: seeded U(-1,1) field (seed 3) on the seeded deformed mesh",
+            "config": {"workload": WORKLOAD, "elements": [E_X, E_Y], "order": N_ORDER,
+                       "unique_dof": G, "parallelism": "host cores (BLAS threads)"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} applies of the full workload, "
+                                       "reference-faithful NumPy restatement (Julia is not "
+                                       "available to run the reference itself)"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extras", action="store_true", help="skip the PCG and order-sweep extras")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        if args.steps > 20:
+            args.steps = 10
+        if args.warmup > 3:
+            args.warmup = 3
+        print(json.dumps(run_reference(args)))
+        return 0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    res = run_ours(args, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(res))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,197 @@
+/*
+ * sem_b200.h — C ABI of libsem_b200.so, the GB300 (sm_103a) implementation
+ * of the spectral-element operator-apply and solve hot path of
+ * SpectralElements.jl (ABu, lapl, mass, hlmz, gatherScatter, mask, pcg).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (enum sem_status).  On failure
+ *    sem_last_error() returns a message for the calling host thread.
+ *  - Fields ("local" vectors) are DEVICE pointers to column-major
+ *    (nr*Ex) x (ns*Ey) arrays of double: element (ex,ey) occupies rows
+ *    ex*nr .. ex*nr+nr-1 and columns ey*ns .. ey*ns+ns-1 (0-based), the
+ *    layout of the reference (src/semmesh.jl:19, src/ndgrid.jl:8-13).
+ *  - Small operator matrices (derivative / interpolation matrices, at most
+ *    32x32) are HOST pointers to column-major arrays.
+ *  - Calls are asynchronous on the given stream (a cudaStream_t, NULL = the
+ *    legacy default stream) except sem_mesh_create / sem_mesh_destroy and
+ *    the solvers, which synchronise the stream to return their result.
+ *  - The library never frees caller memory.  A mesh handle is not safe for
+ *    concurrent use from several host threads or streams at once.
+ *  - No entry point falls back to the CPU: without a usable CUDA device every
+ *    compute call returns SEM_ERR_CUDA.
+ */
+#ifndef SEM_B200_H
+#define SEM_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEM_ABI_VERSION 1
+
+typedef struct sem_mesh sem_mesh_t;
+typedef void* sem_stream_t; /* cudaStream_t */
+
+enum sem_status {
+  SEM_OK = 0,
+  SEM_ERR_BAD_ARG = 1,       /* invalid sizes, NULL pointers, aliasing   */
+  SEM_ERR_NOT_CONVERGED = 2, /* pcg reached maxiter (x is still returned) */
+  SEM_ERR_NAN = 3,           /* a NaN/Inf appeared in a solver residual   */
+  SEM_ERR_TIMEOUT = 4,       /* a bounded device wait ran out             */
+  SEM_ERR_CUDA = 5,          /* a CUDA runtime call failed                */
+  SEM_ERR_UNSUPPORTED = 6,   /* a valid request this build cannot serve   */
+  SEM_ERR_NO_MEMORY = 7      /* device allocation failed                  */
+};
+
+/* operator flags: the fused operators compose mask(QQ'(op(u))) on request */
+#define SEM_GS 1u   /* apply direct-stiffness summation QQ' (gatherScatter) */
+#define SEM_MASK 2u /* apply the handle's Dirichlet mask R'R afterwards     */
+
+/* arithmetic of the fused operators and of the solver */
+enum sem_precision {
+  SEM_F64 = 0,    /* native FP64 arithmetic                                  */
+  SEM_F64_DF = 1, /* FP64 in/out, double-float (FP32 pair) arithmetic, ~47 bit */
+  SEM_F32 = 2,    /* FP32 geometry copy and FP32 arithmetic (solver inner loop) */
+  SEM_MIXED = 3   /* solver only: FP32 inner CG inside FP64 defect correction */
+};
+
+/* geometry fields that sem_mesh_field can export */
+enum sem_field {
+  SEM_FIELD_X = 0, SEM_FIELD_Y = 1, SEM_FIELD_JAC = 2, SEM_FIELD_JACI = 3,
+  SEM_FIELD_RX = 4, SEM_FIELD_RY = 5, SEM_FIELD_SX = 6, SEM_FIELD_SY = 7,
+  SEM_FIELD_B = 8, SEM_FIELD_BI = 9, SEM_FIELD_G11 = 10, SEM_FIELD_G12 = 11,
+  SEM_FIELD_G22 = 12, SEM_FIELD_MULT = 13, SEM_FIELD_MASK = 14
+};
+
+typedef struct {
+  int nr, ns, Ex, Ey;         /* GLL points per direction, elements        */
+  int periodic_x, periodic_y; /* Mesh(...,ifperiodic) (src/mesh.jl:66-68)   */
+  const double* Dr;           /* host nr x nr derivative matrix            */
+  const double* Ds;           /* host ns x ns                              */
+  const double* wr;           /* host GLL weights (nr)                     */
+  const double* ws;           /* host GLL weights (ns)                     */
+  const double* x;            /* host deformed grid, local layout          */
+  const double* y;
+  /* optional host geometry: all four or none.  When given they are uploaded
+   * verbatim (the Julia Mesh already holds them); otherwise the Jacobian,
+   * B and G11/G12/G22 are computed on the device from x, y (src/jac.jl:24-40,
+   * src/mesh.jl:111-123). */
+  const double* G11;
+  const double* G12;
+  const double* G22;
+  const double* B;
+  const char* bc; /* 4 chars 'D'/'N' for xmin,xmax,ymin,ymax, or NULL = no mask */
+} sem_mesh_desc;
+
+/* ---- handle lifecycle: replaces the device-side image of Mesh (src/mesh.jl:25-133) */
+int sem_mesh_create(const sem_mesh_desc* desc, sem_mesh_t** out);
+int sem_mesh_destroy(sem_mesh_t* mesh);
+/* generateMask(bc,msh) (src/mesh.jl:149-175): set the handle's Dirichlet mask */
+int sem_mesh_set_bc(sem_mesh_t* mesh, const char* bc);
+/* select the arithmetic of the fused FP64 operators (SEM_F64 or SEM_F64_DF) */
+int sem_mesh_set_precision(sem_mesh_t* mesh, int precision);
+/* copy one geometry field (enum sem_field) into a caller device buffer */
+int sem_mesh_field(sem_mesh_t* mesh, int which, double* out, sem_stream_t stream);
+/* sizes: local rows (nr*Ex), local columns (ns*Ey) */
+int sem_mesh_dims(const sem_mesh_t* mesh, int64_t* nx, int64_t* ny);
+
+const char* sem_last_error(void);
+int sem_abi_version(void);
+
+/* ---- ABu(As,Br,u) (src/ABu.jl:9-37): v = (As (x) Br) u.
+ * As (ma x na) and Br (mb x nb) are host matrices, NULL = identity ([]).
+ * u is m x n, v is (m*mb/nb) x (n*ma/na); block sizes at most 32. */
+int sem_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
+            const double* u, int m, int n, double* v, sem_stream_t stream);
+
+/* ---- local operators on the handle's geometry; flags compose QQ' and mask.
+ * lapl(u,msh) (src/lapl.jl:26-36) */
+int sem_lapl(sem_mesh_t* mesh, const double* u, double* out, unsigned flags,
+             sem_stream_t stream);
+/* lapl(u,nu,msh) = nu .* lapl(u,msh) (src/lapl.jl:38-45); nu a device field */
+int sem_lapl_nu(sem_mesh_t* mesh, const double* nu, const double* u, double* out,
+                unsigned flags, sem_stream_t stream);
+/* hlmz(u,nu,k,msh) = nu .* lapl(u) + k .* mass(u) (src/hlmz.jl:12-19);
+ * nu_field (device) overrides the scalar nu when not NULL */
+int sem_hlmz(sem_mesh_t* mesh, const double* nu_field, double nu, double k,
+             const double* u, double* out, unsigned flags, sem_stream_t stream);
+/* variable-coefficient operator D'(nu G)D u + k B u with nu (device field)
+ * folded into G11/G12/G22 at every node, as examples/semPS.jl:163-165 and
+ * examples/p2d_explicit.jl:105-107 build G from visc */
+int sem_varcoef(sem_mesh_t* mesh, const double* nu_field, double k, const double* u,
+                double* out, unsigned flags, sem_stream_t stream);
+/* mass(u,msh) = B .* u (src/mass.jl:12-22) */
+int sem_mass(sem_mesh_t* mesh, const double* u, double* out, unsigned flags,
+             sem_stream_t stream);
+/* gatherScatter(u,msh) = QQ' u (src/gatherScatter.jl:8-21) */
+int sem_gather_scatter(sem_mesh_t* mesh, const double* u, double* out,
+                       sem_stream_t stream);
+/* mask(u,M) = M .* u (src/mask.jl:10-18); M a device array or NULL (copy) */
+int sem_mask(const double* M, const double* u, double* out, int64_t len,
+             sem_stream_t stream);
+/* mask with the handle's generateMask(bc,msh) pattern, no mask array read */
+int sem_mask_bc(sem_mesh_t* mesh, const double* u, double* out, sem_stream_t stream);
+
+/* functional lapl(u,M,[],[],QQtx,QQty,Dr,Ds,G11,G12,G22,mult) (src/lapl.jl:54-68):
+ * geometry per call (device G11/G12/G22), host Dr/Ds; QQ' and mask from flags,
+ * the mask from bc (NULL = no mask). */
+int sem_lapl_geom(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y,
+                  const char* bc, const double* Dr, const double* Ds,
+                  const double* G11, const double* G12, const double* G22,
+                  const double* u, double* out, unsigned flags, int precision,
+                  sem_stream_t stream);
+
+/* ---- solver: pcg(b,opA;opM,mult,ifv,tol,maxiter) (src/pcg.jl:16-60) with
+ * opA = mask(QQ'(hlmz(.,nu,k))) (src/diffusion.jl:36-45) */
+enum sem_precond { SEM_PRECOND_NONE = 0, SEM_PRECOND_JACOBI = 1 };
+
+typedef struct {
+  double nu;             /* scalar viscosity (ignored when nu_field set)    */
+  const double* nu_field;/* device nu folded into G (variable coefficient)   */
+  double k;              /* mass coefficient (bdfB[1] / lambda)             */
+  int precond;           /* enum sem_precond                                 */
+  int precision;         /* SEM_F64, SEM_F64_DF or SEM_MIXED                 */
+  double tol;            /* absolute Inf-norm tolerance on the residual      */
+  int maxiter;           /* <= 0: length(b), as the reference               */
+  double inner_tol;      /* SEM_MIXED: relative inner tolerance (1e-4)      */
+  int max_outer;         /* SEM_MIXED: defect-correction sweeps (6)          */
+  int check_every;       /* iterations between convergence reads (0 = auto) */
+  int mult_ones;         /* 1: unweighted dots, pcg's default mult=ones(size(b)) */
+} sem_pcg_opts;
+
+typedef struct {
+  int iters;        /* CG iterations (inner iterations summed for MIXED) */
+  int outer;        /* defect-correction sweeps (MIXED), else 0          */
+  double res_inf;   /* final Inf-norm of the residual                    */
+  double res0_inf;  /* Inf-norm of b                                     */
+  int converged;
+} sem_solve_info;
+
+int sem_pcg(sem_mesh_t* mesh, const sem_pcg_opts* opts, const double* b, double* x,
+            sem_solve_info* info, sem_stream_t stream);
+
+/* Jacobi diagonal of mask(QQ'(hlmz)) with masked entries set to 1 (new: the
+ * reference has no Jacobi preconditioner; derived from src/lapl.jl:70-81) */
+int sem_jacobi_diag(sem_mesh_t* mesh, const double* nu_field, double nu, double k,
+                    double* diag, sem_stream_t stream);
+
+/* ---- adjoint: per-local-copy derivative of lam' A(nu) u with respect to a
+ * G-folded nodal nu, g = -(G11 lr ur + G12 (lr us + ls ur) + G22 ls us); the
+ * pullback of resi(u,a) = rhs(a) - lhs(a)(u) at lam (src/adjoint.jl:13-16). */
+int sem_adjoint_grad(sem_mesh_t* mesh, const double* lam, const double* u,
+                     double* grad, unsigned flags, sem_stream_t stream);
+
+/* ---- instrumentation (no counterpart in the reference, which only prints
+ * @time): CUDA-event timing of every launch of the fused element-operator
+ * kernel while enabled; read returns the summed kernel time and the number of
+ * launches since the last read (and resets them). */
+int sem_timing_enable(int on);
+int sem_timing_read(double* total_ms, int* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEM_B200_H */

@@ -1,0 +1,349 @@
+// C ABI entry points: errors, mesh handles, operators.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "sem_internal.cuh"
+
+namespace sem {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  const int st = (e == cudaErrorMemoryAllocation) ? SEM_ERR_NO_MEMORY : SEM_ERR_CUDA;
+  return set_error(st, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+static int check_device(const sem_mesh* m) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  if (dev != m->device)
+    return set_error(SEM_ERR_BAD_ARG, "mesh handle lives on device %d but device %d is current",
+                     m->device, dev);
+  return SEM_OK;
+}
+
+static unsigned bc_bits(const char* bc) {
+  unsigned b = 0;
+  if (bc[0] == 'D') b |= M_DXMIN;
+  if (bc[1] == 'D') b |= M_DXMAX;
+  if (bc[2] == 'D') b |= M_DYMIN;
+  if (bc[3] == 'D') b |= M_DYMAX;
+  return b;
+}
+
+static int valid_bc(const char* bc) {
+  for (int i = 0; i < 4; ++i)
+    if (bc[i] != 'D' && bc[i] != 'N') return 0;
+  return 1;
+}
+
+static unsigned op_mode(const sem_mesh* m, unsigned flags) {
+  unsigned mode = m->g.topo;
+  if (flags & SEM_GS) mode |= M_GS;
+  if ((flags & SEM_MASK) && m->has_bc) mode |= M_MASK;
+  return mode;
+}
+
+}  // namespace sem
+
+using namespace sem;
+
+extern "C" {
+
+const char* sem_last_error(void) { return g_err; }
+
+int sem_abi_version(void) { return SEM_ABI_VERSION; }
+
+int sem_mesh_create(const sem_mesh_desc* d, sem_mesh_t** out) {
+  if (!d || !out) return set_error(SEM_ERR_BAD_ARG, "NULL descriptor or output");
+  *out = nullptr;
+  if (d->nr < 2 || d->ns < 2 || d->Ex < 1 || d->Ey < 1)
+    return set_error(SEM_ERR_BAD_ARG, "bad mesh sizes nr=%d ns=%d Ex=%d Ey=%d", d->nr, d->ns,
+                     d->Ex, d->Ey);
+  if (d->nr != d->ns)
+    return set_error(SEM_ERR_UNSUPPORTED, "nr != ns is not served (nr=%d ns=%d)", d->nr, d->ns);
+  if (d->nr > kMaxN)
+    return set_error(SEM_ERR_UNSUPPORTED, "at most %d GLL points per direction", kMaxN);
+  if (!d->Dr || !d->Ds || !d->wr || !d->ws || !d->x || !d->y)
+    return set_error(SEM_ERR_BAD_ARG, "Dr, Ds, wr, ws, x and y are required");
+  const int ng = (d->G11 != nullptr) + (d->G12 != nullptr) + (d->G22 != nullptr) + (d->B != nullptr);
+  if (ng != 0 && ng != 4) return set_error(SEM_ERR_BAD_ARG, "give all of G11, G12, G22, B or none");
+  if (d->bc && !valid_bc(d->bc)) return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
+  int dev = 0;
+  SEM_CUDA(cudaGetDevice(&dev));
+
+  const int n = d->nr;
+  OperatorSet* ops = nullptr;
+  SEM_CHECK(make_operator_set(d->Dr, d->Ds, n, &ops));
+
+  sem_mesh* m = (sem_mesh*)std::calloc(1, sizeof(sem_mesh));
+  m->device = dev;
+  m->g.n = n;
+  m->g.Ex = d->Ex;
+  m->g.Ey = d->Ey;
+  m->g.NX = (int64_t)n * d->Ex;
+  m->g.NY = (int64_t)n * d->Ey;
+  m->g.topo = (d->periodic_x ? M_PERX : 0u) | (d->periodic_y ? M_PERY : 0u);
+  m->has_bc = d->bc != nullptr;
+  if (d->bc) m->g.topo |= bc_bits(d->bc);
+  m->precision = SEM_F64_DF;
+  m->ops = ops;
+  m->Dr_h = (double*)std::malloc(sizeof(double) * n * n);
+  m->Ds_h = (double*)std::malloc(sizeof(double) * n * n);
+  m->wr_h = (double*)std::malloc(sizeof(double) * n);
+  m->ws_h = (double*)std::malloc(sizeof(double) * n);
+  std::memcpy(m->Dr_h, d->Dr, sizeof(double) * n * n);
+  std::memcpy(m->Ds_h, d->Ds, sizeof(double) * n * n);
+  std::memcpy(m->wr_h, d->wr, sizeof(double) * n);
+  std::memcpy(m->ws_h, d->ws, sizeof(double) * n);
+
+  const long long L = m->g.NX * m->g.NY;
+  const size_t bytes = sizeof(double) * (size_t)L;
+  double* blk = nullptr;
+  cudaError_t e = cudaMalloc(&blk, 6 * bytes);
+  if (e != cudaSuccess) {
+    sem_mesh_destroy(m);
+    return cuda_error(e, "cudaMalloc(mesh geometry)");
+  }
+  m->x = blk;
+  m->y = blk + L;
+  m->B = blk + 2 * L;
+  m->G11 = blk + 3 * L;
+  m->G12 = blk + 4 * L;
+  m->G22 = blk + 5 * L;
+  int st = SEM_OK;
+  if ((e = cudaMemcpy(m->x, d->x, bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(m->y, d->y, bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
+    st = cuda_error(e, "cudaMemcpy(grid)");
+  } else if (ng == 4) {
+    if ((e = cudaMemcpy(m->B, d->B, bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->G11, d->G11, bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->G12, d->G12, bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->G22, d->G22, bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+      st = cuda_error(e, "cudaMemcpy(geometry)");
+  } else {
+    st = build_geometry(m, d->x, d->y, 0);
+    if (st == SEM_OK && (e = cudaStreamSynchronize(0)) != cudaSuccess)
+      st = cuda_error(e, "geometry kernel");
+  }
+  if (st != SEM_OK) {
+    sem_mesh_destroy(m);
+    return st;
+  }
+  *out = m;
+  return SEM_OK;
+}
+
+int sem_mesh_destroy(sem_mesh_t* m) {
+  if (!m) return SEM_OK;
+  if (m->x) cudaFree(m->x);
+  if (m->G11_f) cudaFree(m->G11_f);
+  if (m->ws) cudaFree(m->ws);
+  if (m->ops) free_operator_set(m->ops);
+  std::free(m->Dr_h);
+  std::free(m->Ds_h);
+  std::free(m->wr_h);
+  std::free(m->ws_h);
+  std::free(m);
+  return SEM_OK;
+}
+
+int sem_mesh_set_bc(sem_mesh_t* m, const char* bc) {
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  m->g.topo &= ~(M_DXMIN | M_DXMAX | M_DYMIN | M_DYMAX);
+  if (!bc) {
+    m->has_bc = false;
+    return SEM_OK;
+  }
+  if (!valid_bc(bc)) return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
+  m->g.topo |= bc_bits(bc);
+  m->has_bc = true;
+  return SEM_OK;
+}
+
+int sem_mesh_set_precision(sem_mesh_t* m, int precision) {
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  if (precision != SEM_F64 && precision != SEM_F64_DF)
+    return set_error(SEM_ERR_BAD_ARG, "fused FP64 operators take SEM_F64 or SEM_F64_DF");
+  m->precision = precision;
+  return SEM_OK;
+}
+
+int sem_mesh_field(sem_mesh_t* m, int which, double* out, sem_stream_t stream) {
+  if (!m || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  SEM_CHECK(check_device(m));
+  return export_field(m, which, out, (cudaStream_t)stream);
+}
+
+int sem_mesh_dims(const sem_mesh_t* m, int64_t* nx, int64_t* ny) {
+  if (!m || !nx || !ny) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  *nx = m->g.NX;
+  *ny = m->g.NY;
+  return SEM_OK;
+}
+
+int sem_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
+            const double* u, int m, int n, double* v, sem_stream_t stream) {
+  if (!u || !v) return set_error(SEM_ERR_BAD_ARG, "NULL field");
+  if (m < 0 || n < 0) return set_error(SEM_ERR_BAD_ARG, "negative size");
+  if (u == v) return set_error(SEM_ERR_BAD_ARG, "ABu output must not alias its input");
+  if (Br) {
+    if (mb < 1 || nb < 1 || mb > kMaxBlock || nb > kMaxBlock)
+      return set_error(SEM_ERR_UNSUPPORTED, "Br must be at most %dx%d (got %dx%d)", kMaxBlock, kMaxBlock, mb, nb);
+    if (((long long)m * n) % nb != 0)
+      return set_error(SEM_ERR_BAD_ARG, "length(u) = %lld is not a multiple of size(Br,2) = %d", (long long)m * n, nb);
+    if (((long long)m * mb) % nb != 0)
+      return set_error(SEM_ERR_BAD_ARG, "m*mb/nb is not an integer");
+  }
+  if (As) {
+    if (ma < 1 || na < 1 || ma > kMaxBlock || na > kMaxBlock)
+      return set_error(SEM_ERR_UNSUPPORTED, "As must be at most %dx%d (got %dx%d)", kMaxBlock, kMaxBlock, ma, na);
+    if (n % na != 0) return set_error(SEM_ERR_BAD_ARG, "size(u,2) = %d is not a multiple of size(As,2) = %d", n, na);
+  }
+  if (As && Br && m % nb != 0)
+    return set_error(SEM_ERR_BAD_ARG, "with both factors size(u,1) must be a multiple of size(Br,2)");
+  return launch_abu(As, ma, na, Br, mb, nb, u, m, n, v, (cudaStream_t)stream);
+}
+
+static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, const double* nu,
+                 double nu_s, double k, sem_stream_t stream) {
+  if (!m || !u || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (u == out || (nu && nu == out))
+    return set_error(SEM_ERR_BAD_ARG, "output must not alias an input of a fused operator");
+  SEM_CHECK(check_device(m));
+  ApplyCall c;
+  c.u = u;
+  c.out = out;
+  c.G11 = m->G11;
+  c.G12 = m->G12;
+  c.G22 = m->G22;
+  c.B = m->B;
+  c.nu = nu;
+  c.nu_s = nu_s;
+  c.k_s = k;
+  c.mode = mode | (nu ? M_NU : 0u);
+  c.precision = m->precision;
+  c.skip = nullptr;
+  return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
+}
+
+int sem_lapl(sem_mesh_t* m, const double* u, double* out, unsigned flags, sem_stream_t stream) {
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  return fused(m, u, out, op_mode(m, flags) | M_STIFF, nullptr, 1.0, 0.0, stream);
+}
+
+int sem_lapl_nu(sem_mesh_t* m, const double* nu, const double* u, double* out, unsigned flags,
+                sem_stream_t stream) {
+  if (!m || !nu) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  return fused(m, u, out, op_mode(m, flags) | M_STIFF, nu, 1.0, 0.0, stream);
+}
+
+int sem_hlmz(sem_mesh_t* m, const double* nu_field, double nu, double k, const double* u,
+             double* out, unsigned flags, sem_stream_t stream) {
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  return fused(m, u, out, op_mode(m, flags) | M_STIFF | M_MASS, nu_field, nu, k, stream);
+}
+
+int sem_varcoef(sem_mesh_t* m, const double* nu_field, double k, const double* u, double* out,
+                unsigned flags, sem_stream_t stream) {
+  if (!m || !nu_field) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  unsigned mode = op_mode(m, flags) | M_STIFF | M_NUG | (k != 0.0 ? M_MASS : 0u);
+  // fused() adds M_NU for a non-NULL nu; the G-folded form replaces it
+  if (!u || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (u == out || nu_field == out)
+    return set_error(SEM_ERR_BAD_ARG, "output must not alias an input of a fused operator");
+  SEM_CHECK(check_device(m));
+  ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
+  c.u = u;
+  c.out = out;
+  c.G11 = m->G11;
+  c.G12 = m->G12;
+  c.G22 = m->G22;
+  c.B = m->B;
+  c.nu = nu_field;
+  c.nu_s = 1.0;
+  c.k_s = k;
+  c.mode = mode;
+  c.precision = m->precision;
+  return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
+}
+
+int sem_mass(sem_mesh_t* m, const double* u, double* out, unsigned flags, sem_stream_t stream) {
+  if (!m || !u || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  SEM_CHECK(check_device(m));
+  if (!(flags & (SEM_GS | SEM_MASK))) return launch_mass(m->g, m->B, u, out, (cudaStream_t)stream);
+  return fused(m, u, out, op_mode(m, flags) | M_MASS, nullptr, 1.0, 1.0, stream);
+}
+
+int sem_gather_scatter(sem_mesh_t* m, const double* u, double* out, sem_stream_t stream) {
+  if (!m || !u || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (u == out) return set_error(SEM_ERR_BAD_ARG, "gatherScatter output must not alias its input");
+  SEM_CHECK(check_device(m));
+  return launch_gather_scatter(m->g, u, out, m->g.topo, (cudaStream_t)stream);
+}
+
+int sem_mask(const double* M, const double* u, double* out, int64_t len, sem_stream_t stream) {
+  if (len < 0) return set_error(SEM_ERR_BAD_ARG, "negative length");
+  if (len > 0 && (!u || !out)) return set_error(SEM_ERR_BAD_ARG, "NULL field");
+  return launch_mask_array(M, u, out, len, (cudaStream_t)stream);
+}
+
+int sem_mask_bc(sem_mesh_t* m, const double* u, double* out, sem_stream_t stream) {
+  if (!m || !u || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  SEM_CHECK(check_device(m));
+  if (!m->has_bc) return set_error(SEM_ERR_BAD_ARG, "the mesh handle has no bc (sem_mesh_set_bc)");
+  return launch_mask_bc(m->g, u, out, m->g.topo, (cudaStream_t)stream);
+}
+
+int sem_lapl_geom(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y, const char* bc,
+                  const double* Dr, const double* Ds, const double* G11, const double* G12,
+                  const double* G22, const double* u, double* out, unsigned flags,
+                  int precision, sem_stream_t stream) {
+  if (nr < 2 || ns < 2 || Ex < 1 || Ey < 1) return set_error(SEM_ERR_BAD_ARG, "bad sizes");
+  if (nr != ns) return set_error(SEM_ERR_UNSUPPORTED, "nr != ns is not served");
+  if (!Dr || !Ds || !G11 || !G12 || !G22 || !u || !out)
+    return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (u == out) return set_error(SEM_ERR_BAD_ARG, "output must not alias an input");
+  if (bc && !valid_bc(bc)) return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
+  if (precision != SEM_F64 && precision != SEM_F64_DF)
+    return set_error(SEM_ERR_BAD_ARG, "precision must be SEM_F64 or SEM_F64_DF");
+  OperatorSet* ops = nullptr;
+  SEM_CHECK(make_operator_set(Dr, Ds, nr, &ops));
+  Grid g;
+  g.n = nr;
+  g.Ex = Ex;
+  g.Ey = Ey;
+  g.NX = (int64_t)nr * Ex;
+  g.NY = (int64_t)nr * Ey;
+  g.topo = (periodic_x ? M_PERX : 0u) | (periodic_y ? M_PERY : 0u) | (bc ? bc_bits(bc) : 0u);
+  unsigned mode = g.topo | M_STIFF;
+  if (flags & SEM_GS) mode |= M_GS;
+  if ((flags & SEM_MASK) && bc) mode |= M_MASK;
+  ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
+  c.u = u;
+  c.out = out;
+  c.G11 = G11;
+  c.G12 = G12;
+  c.G22 = G22;
+  c.nu_s = 1.0;
+  c.mode = mode;
+  c.precision = precision;
+  const int st = launch_apply(g, ops, c, (cudaStream_t)stream);
+  free_operator_set(ops);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,340 @@
+// Fused element operator kernel: mask(QQ'(nu .* D'GD u + k B u)) on the
+// reference's column-major local layout.
+//
+// Work decomposition.  One CTA owns a tile of TX x TY elements and N threads
+// per element.  A thread alternately owns one local row i (x-direction line
+// inside its element) and one local column j; the lines are exchanged through
+// shared memory.  The 1D operators are applied in even-odd form (GLL
+// derivative matrices are centro-antisymmetric), which cuts the multiply-adds
+// of an N-point line from N^2 to about N^2/2; the coefficients live in the
+// kernel parameter block (constant bank), so every multiply-add takes its
+// coefficient as a constant operand and no shared-memory read is spent on it.
+//
+//   A  row i   : load u(i,:) (coalesced across the tile), us = Ds u(i,:)
+//   B  column j: ur = Dr u(:,j)
+//   C  row i   : wr = G11 ur + G12 us, ws = G12 ur + G22 us, os = Ds' ws
+//   D  column j: or = Dr' wr(:,j)
+//   E  row i   : res = nu (or + os) + k B u, then QQ' inside the tile
+//                (x pairs, then y pairs) and the mask; points whose copies
+//                live in another tile are written unsummed and finished by
+//                k_dss_fixup.
+//
+// Reference: laplace (src/lapl.jl:70-81), hlmz (src/hlmz.jl:12-19),
+// gatherScatter (src/gatherScatter.jl:8-16 with src/semq.jl:6-25),
+// mask (src/mask.jl:10-18).
+#pragma once
+
+#include "sem_arith.cuh"
+
+namespace sem {
+
+template <class P, int N>
+struct ApplyArgs {
+  typedef typename P::io io;
+  typedef typename P::v v;
+  const io* u;
+  io* out;
+  const io* G11;
+  const io* G12;
+  const io* G22;
+  const io* B;
+  const io* nu;
+  v nu_s;
+  v k_s;
+  int Ex, Ey;
+  long long NX;
+  unsigned mode;
+  const int* skip;
+  EOCoef<N, v> Dr, Drt, Ds, Dst;
+};
+
+template <int N>
+struct TileShape {
+  static constexpr int TX = 8;
+  static constexpr int TY = N <= 4 ? 8 : (N <= 8 ? 4 : (N <= 12 ? 3 : 2));
+  static constexpr int SP = N | 1;  // odd line stride: conflict-free 8-byte accesses
+  static constexpr int ES = N * SP;
+  static constexpr int THREADS = TX * TY * N;
+};
+
+// y = D x for a centro-antisymmetric D given in even-odd form
+template <class P, int N>
+__device__ __forceinline__ void eo_apply(const EOCoef<N, typename P::v>& D,
+                                         const typename P::v (&x)[N], typename P::v (&y)[N]) {
+  typedef typename P::v V;
+  constexpr int M = N / 2;
+  V e[M], o[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    e[k] = P::add(x[k], x[N - 1 - k]);
+    o[k] = P::sub(x[k], x[N - 1 - k]);
+  }
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    V s = P::mul(D.A[i][0], o[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) s = P::fma(D.A[i][k], o[k], s);
+    V t = P::mul(D.Cc[i][0], e[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) t = P::fma(D.Cc[i][k], e[k], t);
+    if (N & 1) t = P::fma(D.cm[i], x[M], t);
+    y[i] = P::add(s, t);
+    y[N - 1 - i] = P::sub(s, t);
+  }
+  if (N & 1) {
+    V s = P::mul(D.mr[0], o[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) s = P::fma(D.mr[k], o[k], s);
+    y[M] = P::fin(s);
+  }
+}
+
+__host__ __device__ inline bool xcross_row(int ex, int i, int n, int Ex, int TX, bool perx) {
+  const int exl = ex % TX;
+  if (i == 0 && exl == 0 && (ex > 0 || perx)) return true;
+  if (i == n - 1 && (exl == TX - 1 || ex == Ex - 1) && (ex < Ex - 1 || perx)) return true;
+  return false;
+}
+
+template <class P, int N, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY* N)
+    k_apply(const __grid_constant__ ApplyArgs<P, N> a) {
+  typedef typename P::v V;
+  typedef typename P::io IO;
+  constexpr int SP = N | 1;
+  constexpr int ES = N * SP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* S1 = reinterpret_cast<V*>(smem_raw);
+  V* S2 = S1 + TX * TY * ES;
+
+  if (a.skip && *a.skip) return;
+  const int t = threadIdx.x;
+  const int elem = t / N;
+  const int lane = t - elem * N;
+  const int exl = elem % TX;
+  const int eyl = elem / TX;
+  const int ex = blockIdx.x * TX + exl;
+  const int ey = blockIdx.y * TY + eyl;
+  const bool valid = ex < a.Ex && ey < a.Ey;
+  const long long NX = a.NX;
+  const long long base = (long long)ex * N + lane + (long long)ey * N * NX;
+  const unsigned mode = a.mode;
+  const bool stiff = (mode & M_STIFF) != 0;
+  V* s1 = S1 + elem * ES;
+  V* s2 = S2 + elem * ES;
+
+  // ---- A: row `lane` of u; y-direction derivative
+  V u[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
+
+  V res[N];
+  if (stiff) {
+    V us[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) s1[j * SP + lane] = u[j];
+    eo_apply<P, N>(a.Ds, u, us);
+    __syncthreads();
+    // ---- B: column `lane`; x-direction derivative
+    {
+      V col[N], ur[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) col[i] = s1[lane * SP + i];
+      eo_apply<P, N>(a.Dr, col, ur);
+#pragma unroll
+      for (int i = 0; i < N; ++i) s2[lane * SP + i] = ur[i];
+    }
+    __syncthreads();
+    // ---- C: row `lane`; metric terms, transposed y-derivative
+    V os[N];
+    {
+      V ws[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const long long gi = base + (long long)j * NX;
+        V g11 = valid ? P::ld(a.G11 + gi) : P::zero();
+        V g12 = valid ? P::ld(a.G12 + gi) : P::zero();
+        V g22 = valid ? P::ld(a.G22 + gi) : P::zero();
+        V ur = s2[j * SP + lane];
+        V wr = P::fin(P::fma(g11, ur, P::mul(g12, us[j])));
+        ws[j] = P::fin(P::fma(g12, ur, P::mul(g22, us[j])));
+        if (mode & M_NUG) {
+          V nu = valid ? P::ld(a.nu + gi) : P::zero();
+          wr = P::fin(P::mul(nu, wr));
+          ws[j] = P::fin(P::mul(nu, ws[j]));
+        }
+        s1[j * SP + lane] = wr;
+      }
+      eo_apply<P, N>(a.Dst, ws, os);
+    }
+    __syncthreads();
+    // ---- D: column `lane`; transposed x-derivative
+    {
+      V col[N], o[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) col[i] = s1[lane * SP + i];
+      eo_apply<P, N>(a.Drt, col, o);
+#pragma unroll
+      for (int i = 0; i < N; ++i) s2[lane * SP + i] = o[i];
+    }
+    __syncthreads();
+    // ---- E: assemble
+#pragma unroll
+    for (int j = 0; j < N; ++j) res[j] = P::add(s2[j * SP + lane], os[j]);
+    if (mode & M_NU) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        V nu = valid ? P::ld(a.nu + base + (long long)j * NX) : P::zero();
+        res[j] = P::fin(P::mul(nu, res[j]));
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < N; ++j) res[j] = P::fin(P::mul(a.nu_s, res[j]));
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) res[j] = P::zero();
+  }
+  if (mode & M_MASS) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      V b = valid ? P::ld(a.B + base + (long long)j * NX) : P::zero();
+      V kb = P::fin(P::mul(a.k_s, b));
+      res[j] = P::fin(P::fma(kb, u[j], res[j]));
+    }
+  }
+
+  const bool gs = (mode & M_GS) != 0;
+  const bool perx = (mode & M_PERX) != 0;
+  const bool pery = (mode & M_PERY) != 0;
+  if (gs) {
+    // x pairs inside the tile: row n-1 of element exl with row 0 of exl+1
+    if (!stiff) __syncthreads();
+#pragma unroll
+    for (int j = 0; j < N; ++j) s1[j * SP + lane] = res[j];
+    __syncthreads();
+    if (lane == N - 1 && exl + 1 < TX && ex + 1 < a.Ex) {
+      const V* nb = S1 + (elem + 1) * ES;
+#pragma unroll
+      for (int j = 0; j < N; ++j) res[j] = P::add(res[j], nb[j * SP]);
+    }
+    if (lane == 0 && exl > 0) {
+      const V* nb = S1 + (elem - 1) * ES;
+#pragma unroll
+      for (int j = 0; j < N; ++j) res[j] = P::add(nb[j * SP + N - 1], res[j]);
+    }
+    // y pairs inside the tile: column n-1 of element eyl with column 0 of eyl+1
+    s2[lane] = res[0];
+    s2[(N - 1) * SP + lane] = res[N - 1];
+    __syncthreads();
+    if (eyl + 1 < TY && ey + 1 < a.Ey) res[N - 1] = P::add(res[N - 1], S2[(elem + TX) * ES + lane]);
+    if (eyl > 0) res[0] = P::add(S2[(elem - TX) * ES + (N - 1) * SP + lane], res[0]);
+  }
+  if (!valid) return;
+
+  const bool xc = gs && xcross_row(ex, lane, N, a.Ex, TX, perx);
+  const long long row = (long long)ex * N + lane;
+  const long long NY = (long long)a.Ey * N;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    bool raw = xc;
+    if (gs) {
+      if (j == 0 && eyl == 0 && (ey > 0 || pery)) raw = true;
+      if (j == N - 1 && (eyl == TY - 1 || ey == a.Ey - 1) && (ey < a.Ey - 1 || pery)) raw = true;
+    }
+    IO val = P::st(res[j]);
+    if (!raw && (mode & M_MASK)) {
+      const long long col = (long long)ey * N + j;
+      if (!mask_keep(row, col, NX, NY, mode)) val = val * (IO)0;
+    }
+    a.out[base + (long long)j * NX] = val;
+  }
+}
+
+// Finishes QQ' (and the mask) at the points whose copies sit in different
+// tiles: x interfaces every TX elements (+ the periodic wrap), y interfaces
+// every TY elements (+ wrap), and the corners where both meet.
+struct FixArgs {
+  int n, Ex, Ey, TX, TY;
+  long long NX, NY;
+  unsigned mode;
+  long long nxi, nyi;  // number of cross-tile interfaces in x and y
+  const int* skip;
+};
+
+__host__ __device__ inline long long fix_iface(long long q, int T, bool per) {
+  return per ? q * T : (q + 1) * T;  // interface index a: between elements a-1 and a
+}
+
+template <class IO>
+__global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
+  if (f.skip && *f.skip) return;
+  const bool perx = (f.mode & M_PERX) != 0;
+  const bool pery = (f.mode & M_PERY) != 0;
+  const bool msk = (f.mode & M_MASK) != 0;
+  const long long nX = f.nxi * f.NY;
+  const long long nY = f.nyi * f.NX;
+  const long long nC = f.nxi * f.nyi;
+  const long long total = nX + nY + nC;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    if (idx < nX) {
+      const long long q = idx / f.NY;
+      const long long c = idx - q * f.NY;
+      const long long ey = c / f.n;
+      const int j = (int)(c - ey * f.n);
+      if (xcross_row((int)ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner
+      const long long a = fix_iface(q, f.TX, perx);
+      const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
+      const long long rr = a * f.n;
+      const IO s = out[rl + c * f.NX] + out[rr + c * f.NX];
+      IO sl = s, sr = s;
+      if (msk) {
+        if (!mask_keep(rl, c, f.NX, f.NY, f.mode)) sl = s * (IO)0;
+        if (!mask_keep(rr, c, f.NX, f.NY, f.mode)) sr = s * (IO)0;
+      }
+      out[rl + c * f.NX] = sl;
+      out[rr + c * f.NX] = sr;
+    } else if (idx < nX + nY) {
+      const long long id2 = idx - nX;
+      const long long q = id2 / f.NX;
+      const long long r = id2 - q * f.NX;
+      const long long ex = r / f.n;
+      const int i = (int)(r - ex * f.n);
+      if (xcross_row((int)ex, i, f.n, f.Ex, f.TX, perx)) continue;  // corner
+      const long long b = fix_iface(q, f.TY, pery);
+      const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
+      const long long cr = b * f.n;
+      const IO s = out[r + cl * f.NX] + out[r + cr * f.NX];
+      IO sl = s, sr = s;
+      if (msk) {
+        if (!mask_keep(r, cl, f.NX, f.NY, f.mode)) sl = s * (IO)0;
+        if (!mask_keep(r, cr, f.NX, f.NY, f.mode)) sr = s * (IO)0;
+      }
+      out[r + cl * f.NX] = sl;
+      out[r + cr * f.NX] = sr;
+    } else {
+      const long long id3 = idx - nX - nY;
+      const long long q = id3 / f.nyi;
+      const long long p = id3 - q * f.nyi;
+      const long long a = fix_iface(q, f.TX, perx);
+      const long long b = fix_iface(p, f.TY, pery);
+      const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
+      const long long rr = a * f.n;
+      const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
+      const long long cr = b * f.n;
+      const IO s = (out[rl + cl * f.NX] + out[rr + cl * f.NX]) +
+                   (out[rl + cr * f.NX] + out[rr + cr * f.NX]);
+      const long long rs[2] = {rl, rr};
+      const long long cs[2] = {cl, cr};
+      for (int u = 0; u < 2; ++u)
+        for (int v = 0; v < 2; ++v) {
+          IO val = s;
+          if (msk && !mask_keep(rs[u], cs[v], f.NX, f.NY, f.mode)) val = s * (IO)0;
+          out[rs[u] + cs[v] * f.NX] = val;
+        }
+    }
+  }
+}
+
+}  // namespace sem

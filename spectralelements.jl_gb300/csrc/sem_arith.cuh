@@ -1,0 +1,140 @@
+// Arithmetic policies of the fused operator kernels.
+//
+//  PF64 : FP64 storage, native FP64 arithmetic.
+//  PF32 : FP32 storage and arithmetic (inner solve of the mixed-precision CG).
+//  PDF  : FP64 storage, double-float arithmetic on the FP32 pipe.  GB300 runs
+//         FP64 at about 1/64 of its FP32 rate, so a value is carried as an
+//         unevaluated sum h + l of two floats (about 47 significant bits after
+//         the input split below) and every product / sum is made error-free
+//         with the TwoProd (fma) and TwoSum transformations of Dekker and
+//         Knuth.  Accumulators stay unnormalised inside a dot product and are
+//         renormalised once (fin).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sem_internal.cuh"
+
+namespace sem {
+
+// ---------------------------------------------------------------------------
+// error-free transformations (contraction-proof intrinsics)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return {s, e};
+}
+
+__device__ __forceinline__ df df_norm(df a) { return fast_two_sum(a.h, a.l); }
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.h, b.h);
+  float e = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+  return fast_two_sum(s.h, e);
+}
+
+__device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
+
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+
+// unnormalised product (h = rounded product of the high parts)
+__device__ __forceinline__ df df_mul_u(df a, df b) {
+  float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return {p, e};
+}
+
+// unnormalised c + a*b: the high parts are summed with TwoSum, all error terms
+// are collected in l
+__device__ __forceinline__ df df_fma_u(df a, df b, df c) {
+  float p = __fmul_rn(a.h, b.h);
+  float pe = __fmaf_rn(a.h, b.h, -p);
+  pe = __fmaf_rn(a.h, b.l, pe);
+  pe = __fmaf_rn(a.l, b.h, pe);
+  df s = two_sum(p, c.h);
+  return {s.h, __fadd_rn(s.l, __fadd_rn(pe, c.l))};
+}
+
+// double -> (h, l): h keeps the leading 24 significand bits (truncated), l the
+// next 23, both extracted with integer operations so the FP64 pipe stays idle.
+// Exponents outside [2^-103, 2^127) take the conversion instructions instead.
+__device__ __forceinline__ df d2df(double x) {
+  const unsigned lo = (unsigned)__double2loint(x);
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned ed = (hi >> 20) & 0x7ffu;
+  if (ed - 920u < 231u) {
+    const unsigned hb = (__funnelshift_l(lo, hi, 3) + 0x40000000u) | (hi & 0x80000000u);
+    const unsigned pb = (hb & 0xff800000u) - 0x0B800000u;
+    const unsigned fb = pb | ((lo >> 6) & 0x007fffffu);
+    return {__uint_as_float(hb), __fsub_rn(__uint_as_float(fb), __uint_as_float(pb))};
+  }
+  const float h = __double2float_rz(x);
+  const float l = __double2float_rn(x - (double)h);
+  return {h, l};
+}
+
+__device__ __forceinline__ double df2d(df a) { return (double)a.h + (double)a.l; }
+
+// ---------------------------------------------------------------------------
+// policies
+// ---------------------------------------------------------------------------
+struct PF64 {
+  typedef double io;
+  typedef double v;
+  static constexpr int kPrecision = SEM_F64;
+  static __device__ __forceinline__ v ld(const io* p) { return __ldg(p); }
+  static __device__ __forceinline__ io st(v a) { return a; }
+  static __device__ __forceinline__ v zero() { return 0.0; }
+  static __device__ __forceinline__ v add(v a, v b) { return a + b; }
+  static __device__ __forceinline__ v sub(v a, v b) { return a - b; }
+  static __device__ __forceinline__ v mul(v a, v b) { return a * b; }
+  static __device__ __forceinline__ v fma(v a, v b, v c) { return __fma_rn(a, b, c); }
+  static __device__ __forceinline__ v fin(v a) { return a; }
+  static __host__ v from_double(double d) { return d; }
+};
+
+struct PF32 {
+  typedef float io;
+  typedef float v;
+  static constexpr int kPrecision = SEM_F32;
+  static __device__ __forceinline__ v ld(const io* p) { return __ldg(p); }
+  static __device__ __forceinline__ io st(v a) { return a; }
+  static __device__ __forceinline__ v zero() { return 0.0f; }
+  static __device__ __forceinline__ v add(v a, v b) { return a + b; }
+  static __device__ __forceinline__ v sub(v a, v b) { return a - b; }
+  static __device__ __forceinline__ v mul(v a, v b) { return a * b; }
+  static __device__ __forceinline__ v fma(v a, v b, v c) { return __fmaf_rn(a, b, c); }
+  static __device__ __forceinline__ v fin(v a) { return a; }
+  static __host__ v from_double(double d) { return (float)d; }
+};
+
+struct PDF {
+  typedef double io;
+  typedef df v;
+  static constexpr int kPrecision = SEM_F64_DF;
+  static __device__ __forceinline__ v ld(const io* p) { return d2df(__ldg(p)); }
+  static __device__ __forceinline__ io st(v a) { return df2d(a); }
+  static __device__ __forceinline__ v zero() { return {0.0f, 0.0f}; }
+  static __device__ __forceinline__ v add(v a, v b) { return df_add(a, b); }
+  static __device__ __forceinline__ v sub(v a, v b) { return df_sub(a, b); }
+  static __device__ __forceinline__ v mul(v a, v b) { return df_mul_u(a, b); }
+  static __device__ __forceinline__ v fma(v a, v b, v c) { return df_fma_u(a, b, c); }
+  static __device__ __forceinline__ v fin(v a) { return df_norm(a); }
+  static __host__ v from_double(double d) {
+    float h = (float)d;
+    float l = (float)(d - (double)h);
+    return {h, l};
+  }
+};
+
+}  // namespace sem

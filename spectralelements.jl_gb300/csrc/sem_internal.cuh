@@ -1,0 +1,182 @@
+// Internal declarations shared by the translation units of libsem_b200.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/sem_b200.h"
+
+namespace sem {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+int set_error(int status, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+#define SEM_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_error(e_, #call); \
+  } while (0)
+
+#define SEM_CHECK(status_expr)          \
+  do {                                  \
+    int s_ = (status_expr);             \
+    if (s_ != SEM_OK) return s_;        \
+  } while (0)
+
+constexpr int kMaxN = 17;       // GLL points per direction served by the fused kernels
+constexpr int kMaxBlock = 32;   // block size limit of the generic ABu kernel
+
+// ---------------------------------------------------------------------------
+// structured mesh description used by the kernels
+// ---------------------------------------------------------------------------
+// mode bits of the fused operators
+enum : unsigned {
+  M_MASS = 1u << 0,    // add k * B .* u
+  M_NU = 1u << 1,      // multiply the stiffness part by a nu field
+  M_GS = 1u << 2,      // direct-stiffness summation QQ'
+  M_MASK = 1u << 3,    // Dirichlet mask
+  M_PERX = 1u << 4,    // periodic in x
+  M_PERY = 1u << 5,    // periodic in y
+  M_DXMIN = 1u << 6,   // Dirichlet at xmin (only meaningful without M_PERX)
+  M_DXMAX = 1u << 7,
+  M_DYMIN = 1u << 8,
+  M_DYMAX = 1u << 9,
+  M_STIFF = 1u << 10,  // include the stiffness (lapl) part
+  M_NUG = 1u << 11,    // variable coefficient folded into G: D'(nu G)D
+  M_MULT1 = 1u << 12,  // solver dots without the SEM multiplicity weights
+};
+
+struct Grid {
+  int n;        // GLL points per direction (nr == ns)
+  int Ex, Ey;
+  int64_t NX, NY;  // local rows n*Ex, local columns n*Ey
+  unsigned topo;   // M_PERX | M_PERY | M_D* bits
+};
+
+// mask value of local point (r, c) under the topology bits
+__host__ __device__ inline bool mask_keep(int64_t r, int64_t c, int64_t NX, int64_t NY,
+                                          unsigned topo) {
+  if (!(topo & M_PERX)) {
+    if ((topo & M_DXMIN) && r == 0) return false;
+    if ((topo & M_DXMAX) && r == NX - 1) return false;
+  }
+  if (!(topo & M_PERY)) {
+    if ((topo & M_DYMIN) && c == 0) return false;
+    if ((topo & M_DYMAX) && c == NY - 1) return false;
+  }
+  return true;
+}
+
+// number of local copies of the global node behind local row r (1 or 2)
+__host__ __device__ inline int copies_1d(int64_t r, int n, int E, bool per) {
+  int64_t e = r / n;
+  int i = (int)(r - e * n);
+  int c = 1;
+  if (i == 0 && (e > 0 || per)) c = 2;
+  if (i == n - 1 && (e < E - 1 || per)) c = 2;
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// even-odd (centro-antisymmetric) 1D operator coefficients
+// ---------------------------------------------------------------------------
+// y = D x with D[n-1-i][n-1-k] = -D[i][k]:  e_k = x_k + x_{n-1-k},
+// o_k = x_k - x_{n-1-k} (k < m = n/2);  S_i = sum_k A[i][k] o_k,
+// T_i = sum_k C[i][k] e_k (+ cm[i] x_m for odd n);  y_i = S_i + T_i,
+// y_{n-1-i} = S_i - T_i;  odd n: y_m = sum_k mr[k] o_k.
+template <int N, class C>
+struct EOCoef {
+  static constexpr int M = N / 2;
+  C A[M][M];
+  C Cc[M][M];
+  C cm[M];
+  C mr[M];
+};
+
+template <int N, class C>
+struct DenseCoef {
+  C D[N][N];  // D[i][k]
+};
+
+// double-float value: h + l with |l| <= ulp(h)/2
+struct df {
+  float h, l;
+};
+
+// host helpers building coefficient sets from a column-major double matrix
+bool is_centro_antisymmetric(const double* D, int n, double rel_tol);
+void eo_from_dense(const double* D, int n, bool transpose, double* A, double* C, double* cm,
+                   double* mr);
+
+// ---------------------------------------------------------------------------
+// the mesh handle
+// ---------------------------------------------------------------------------
+struct OperatorSet;  // cached kernel coefficient blocks (sem_apply.cu)
+
+}  // namespace sem
+
+struct sem_mesh {
+  int device;
+  sem::Grid g;
+  bool has_bc;
+  int precision;           // SEM_F64 or SEM_F64_DF for the fused operators
+  double* Dr_h;            // host copies (n*n, column-major)
+  double* Ds_h;
+  double* wr_h;
+  double* ws_h;
+  // device geometry, local layout, double
+  double *x, *y, *B, *G11, *G12, *G22;
+  // FP32 copies for the mixed-precision inner solve (lazily created)
+  float *B_f, *G11_f, *G12_f, *G22_f;
+  sem::OperatorSet* ops;   // coefficient blocks for the kernels
+  // solver workspace (lazily created)
+  void* ws;
+  size_t ws_bytes;
+};
+
+namespace sem {
+
+// geometry (sem_geom.cu)
+int build_geometry(sem_mesh* m, const double* x_h, const double* y_h, cudaStream_t s);
+int export_field(const sem_mesh* m, int which, double* out, cudaStream_t s);
+int ensure_f32_geometry(sem_mesh* m, cudaStream_t s);
+
+// operator coefficients (sem_apply.cu)
+int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** out);
+void free_operator_set(OperatorSet* o);
+
+struct ApplyCall {
+  const void* u;
+  void* out;
+  const void* G11;
+  const void* G12;
+  const void* G22;
+  const void* B;
+  const void* nu;
+  double nu_s;
+  double k_s;
+  unsigned mode;   // M_* bits (topology bits included)
+  int precision;   // SEM_F64, SEM_F64_DF, SEM_F32
+  const int* skip; // device flag: when non-zero the launch does nothing (solver loops)
+};
+
+int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
+int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned mode, int precision,
+                     const int* skip, cudaStream_t s);
+
+// elementwise / structured kernels (sem_vec.cu)
+int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode, cudaStream_t s);
+int launch_mask_bc(const Grid& g, const double* u, double* out, unsigned topo, cudaStream_t s);
+int launch_mask_array(const double* M, const double* u, double* out, int64_t len, cudaStream_t s);
+int launch_mass(const Grid& g, const double* B, const double* u, double* out, cudaStream_t s);
+int launch_mult(const Grid& g, double* out, cudaStream_t s);
+int launch_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
+               const double* u, int m, int n, double* v, cudaStream_t s);
+
+unsigned topo_bits(const Grid& g);
+}  // namespace sem

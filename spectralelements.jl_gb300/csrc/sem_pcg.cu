@@ -1,0 +1,614 @@
+// Preconditioned CG (src/pcg.jl:16-60) on the device, the Jacobi diagonal and
+// the adjoint gradient kernel.
+//
+// One CG iteration is a fixed sequence of launches that all read a device
+// "done" flag first, so the host can enqueue many iterations ahead and only
+// read the flag back every `check_every` iterations; the iteration count and
+// the returned x are exactly those of the sequential loop.
+//
+//   pdir   : h = dinv .* r, p = h + beta p                      (r, dinv, p -> p)
+//   apply  : Ap = mask(QQ'(hlmz(p)))                            (fused kernel + fixup)
+//   dot    : partial sums of p .* Ap .* mult
+//   alpha  : alpha = t / pAp, k += 1                            (one block)
+//   update : x += alpha p, r -= alpha Ap, partial t' = r.h.mult, max|r|
+//   beta   : beta = t'/t, done = !(max|r| > tol) || k == maxiter
+//
+// Reductions are two-stage with a fixed grid, so results are deterministic.
+// mult = 1/(copies) is computed from the local index (1, 1/2 or 1/4).
+// Mixed precision (SEM_MIXED): FP64 defect correction x += A32^{-1} r with
+// r = b - A x recomputed in FP64 after every inner FP32 CG solve.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "sem_internal.cuh"
+
+namespace sem {
+
+namespace {
+
+constexpr int kRB = 304;  // reduction grid (fixed: deterministic sums)
+constexpr int kRT = 256;
+
+struct Scalars {
+  double t, t_prev, pAp, alpha, beta, rmax, tol;
+  int k, maxiter, done, converged, nan;
+};
+
+__device__ __forceinline__ double mult_at(long long idx, const Grid& g) {
+  if (g.topo & M_MULT1) return 1.0;
+  const long long c = idx / g.NX;
+  const long long r = idx - c * g.NX;
+  const int cc = copies_1d(r, g.n, g.Ex, (g.topo & M_PERX) != 0) *
+                 copies_1d(c, g.n, g.Ey, (g.topo & M_PERY) != 0);
+  return cc == 1 ? 1.0 : (cc == 2 ? 0.5 : 0.25);
+}
+
+__device__ __forceinline__ double nanmax(double a, double b) {
+  return (b > a || b != b) ? b : a;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce(double (&v)[NV], const bool (&is_max)[NV],
+                                             double* out) {
+  __shared__ double sh[NV][kRT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    double x = v[q];
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = is_max[q] ? nanmax(x, y) : x + y;
+    }
+    if (lane == 0) sh[q][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double x = sh[q][0];
+      for (int i = 1; i < kRT / 32; ++i) x = is_max[q] ? nanmax(x, sh[q][i]) : x + sh[q][i];
+      out[blockIdx.x * NV + q] = x;
+    }
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ void final_reduce(const double* part, int nparts,
+                                             const bool (&is_max)[NV], double (&res)[NV]) {
+  // single block, fixed order
+  double v[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = is_max[q] ? 0.0 : 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = is_max[q] ? nanmax(v[q], part[i * NV + q]) : v[q] + part[i * NV + q];
+  __shared__ double sh[NV][kRT];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) sh[q][threadIdx.x] = v[q];
+  __syncthreads();
+  for (int s = kRT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+        sh[q][threadIdx.x] = is_max[q] ? nanmax(sh[q][threadIdx.x], sh[q][threadIdx.x + s])
+                                       : sh[q][threadIdx.x] + sh[q][threadIdx.x + s];
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) res[q] = sh[q][0];
+}
+
+// x = 0, r = b (converted), p = 0; partials of t = r.h.mult and max|r|
+template <class T, class TB>
+__global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
+                       T* __restrict__ p, const T* __restrict__ dinv, double* part, Grid g) {
+  const long long L = g.NX * g.NY;
+  double t = 0.0, rm = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x) {
+    const T ri = (T)b[i];
+    x[i] = (T)0;
+    p[i] = (T)0;
+    r[i] = ri;
+    const T h = dinv ? ri * dinv[i] : ri;
+    t += (double)ri * (double)h * mult_at(i, g);
+    rm = nanmax(rm, fabs((double)ri));
+  }
+  double v[2] = {t, rm};
+  const bool mx[2] = {false, true};
+  block_reduce<2>(v, mx, part);
+}
+
+__global__ void k_scal_init(const double* part, int np, Scalars* sc, double tol, int maxiter) {
+  double res[2];
+  const bool mx[2] = {false, true};
+  final_reduce<2>(part, np, mx, res);
+  if (threadIdx.x == 0) {
+    sc->t = res[0];
+    sc->t_prev = 1.0;
+    sc->beta = 0.0;
+    sc->alpha = 0.0;
+    sc->rmax = res[1];
+    sc->tol = tol;
+    sc->k = 0;
+    sc->maxiter = maxiter;
+    sc->nan = res[1] != res[1];
+    sc->converged = !(res[1] > tol) && !sc->nan;
+    sc->done = !(res[1] > tol) || maxiter == 0;
+  }
+}
+
+template <class T>
+__global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ p,
+                       const Scalars* sc, long long L) {
+  if (sc->done) return;
+  const T beta = (T)sc->beta;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x) {
+    const T h = dinv ? r[i] * dinv[i] : r[i];
+    p[i] = h + beta * p[i];
+  }
+}
+
+template <class T>
+__global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, double* part,
+                          const Scalars* sc, Grid g) {
+  if (sc->done) return;
+  const long long L = g.NX * g.NY;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x)
+    s += (double)p[i] * (double)Ap[i] * mult_at(i, g);
+  double v[1] = {s};
+  const bool mx[1] = {false};
+  block_reduce<1>(v, mx, part);
+}
+
+__global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
+  if (sc->done) return;
+  double res[1];
+  const bool mx[1] = {false};
+  final_reduce<1>(part, np, mx, res);
+  if (threadIdx.x == 0) {
+    sc->pAp = res[0];
+    sc->alpha = sc->t / res[0];
+    sc->k += 1;
+  }
+}
+
+template <class T>
+__global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                         const T* __restrict__ Ap, const T* __restrict__ dinv, double* part,
+                         const Scalars* sc, Grid g) {
+  if (sc->done) return;
+  const long long L = g.NX * g.NY;
+  const T alpha = (T)sc->alpha;
+  double t = 0.0, rm = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x) {
+    x[i] = x[i] + alpha * p[i];
+    const T ri = r[i] - alpha * Ap[i];
+    r[i] = ri;
+    const T h = dinv ? ri * dinv[i] : ri;
+    t += (double)ri * (double)h * mult_at(i, g);
+    rm = nanmax(rm, fabs((double)ri));
+  }
+  double v[2] = {t, rm};
+  const bool mx[2] = {false, true};
+  block_reduce<2>(v, mx, part);
+}
+
+__global__ void k_scal_beta(const double* part, int np, Scalars* sc) {
+  if (sc->done) return;
+  double res[2];
+  const bool mx[2] = {false, true};
+  final_reduce<2>(part, np, mx, res);
+  if (threadIdx.x == 0) {
+    sc->t_prev = sc->t;
+    sc->t = res[0];
+    sc->beta = res[0] / sc->t_prev;
+    sc->rmax = res[1];
+    const bool nan = (res[1] != res[1]) || (sc->alpha != sc->alpha);
+    sc->nan = nan;
+    sc->converged = !(res[1] > sc->tol) && !nan;
+    sc->done = !(res[1] > sc->tol) || sc->k >= sc->maxiter || nan;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi diagonal (local part): nu*(sum_k Dr[k,i]^2 G11(k,j) + sum_l Ds[l,j]^2
+// G22(i,l) + 2 Dr[i,i] Ds[j,j] G12(i,j)) + k B(i,j), with nu pointwise folded
+// into G when a field is given
+// ---------------------------------------------------------------------------
+struct DiagArgs {
+  double Dr[kMaxN * kMaxN];
+  double Ds[kMaxN * kMaxN];
+  double nu, k;
+};
+
+__global__ void k_diag_local(const __grid_constant__ DiagArgs a, const double* __restrict__ G11,
+                             const double* __restrict__ G12, const double* __restrict__ G22,
+                             const double* __restrict__ B, const double* __restrict__ nuf,
+                             double* __restrict__ d, Grid g) {
+  const long long L = g.NX * g.NY;
+  const int n = g.n;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < L;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    const long long ex = r / n, ey = c / n;
+    const int i = (int)(r - ex * n), j = (int)(c - ey * n);
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const long long pr = ex * n + k + c * g.NX;
+      const long long ps = r + (ey * n + k) * g.NX;
+      const double dr = a.Dr[k + i * n], ds = a.Ds[k + j * n];
+      const double wr = nuf ? nuf[pr] : 1.0, ws = nuf ? nuf[ps] : 1.0;
+      s += dr * dr * G11[pr] * wr + ds * ds * G22[ps] * ws;
+    }
+    const double w0 = nuf ? nuf[idx] : 1.0;
+    s += 2.0 * a.Dr[i + i * n] * a.Ds[j + j * n] * G12[idx] * w0;
+    d[idx] = a.nu * s + a.k * B[idx];
+  }
+}
+
+// dinv = keep ? 1/d : 1 (masked entries of the diagonal are set to 1)
+template <class T>
+__global__ void k_diag_inv(const double* __restrict__ d, T* __restrict__ dinv, Grid g,
+                           unsigned topo, int has_mask) {
+  const long long L = g.NX * g.NY;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < L;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    const bool keep = !has_mask || mask_keep(r, c, g.NX, g.NY, topo);
+    dinv[idx] = keep ? (T)(1.0 / d[idx]) : (T)1;
+  }
+}
+
+__global__ void k_diag_mask(double* __restrict__ d, Grid g, unsigned topo) {
+  const long long L = g.NX * g.NY;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < L;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    if (!mask_keep(r, c, g.NX, g.NY, topo)) d[idx] = 1.0;
+  }
+}
+
+// r = b - Ax, max|r| partials (outer FP64 residual of the mixed solver)
+__global__ void k_residual(const double* __restrict__ b, const double* __restrict__ Ax,
+                           double* __restrict__ r, double* part, long long L) {
+  double rm = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = b[i] - Ax[i];
+    r[i] = v;
+    rm = nanmax(rm, fabs(v));
+  }
+  double v[1] = {rm};
+  const bool mx[1] = {true};
+  block_reduce<1>(v, mx, part);
+}
+
+__global__ void k_scal_max(const double* part, int np, double* out) {
+  double res[1];
+  const bool mx[1] = {true};
+  final_reduce<1>(part, np, mx, res);
+  if (threadIdx.x == 0) *out = res[0];
+}
+
+__global__ void k_axpy_f2d(double* __restrict__ x, const float* __restrict__ d, long long L) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] += (double)d[i];
+}
+
+__global__ void k_zero(double* __restrict__ x, long long L) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint gradient: g = -(G11 lr ur + G12 (lr us + ls ur) + G22 ls us)
+// ---------------------------------------------------------------------------
+__global__ void k_adjoint_grad(const __grid_constant__ DiagArgs a, const double* __restrict__ lam,
+                               const double* __restrict__ u, const double* __restrict__ G11,
+                               const double* __restrict__ G12, const double* __restrict__ G22,
+                               double* __restrict__ grad, Grid g) {
+  const long long L = g.NX * g.NY;
+  const int n = g.n;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < L;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    const long long ex = r / n, ey = c / n;
+    const int i = (int)(r - ex * n), j = (int)(c - ey * n);
+    double lr = 0, ls = 0, ur = 0, us = 0;
+    for (int k = 0; k < n; ++k) {
+      const long long pr = ex * n + k + c * g.NX;
+      const long long ps = r + (ey * n + k) * g.NX;
+      const double dr = a.Dr[i + k * n], ds = a.Ds[j + k * n];
+      lr = fma(dr, lam[pr], lr);
+      ur = fma(dr, u[pr], ur);
+      ls = fma(ds, lam[ps], ls);
+      us = fma(ds, u[ps], us);
+    }
+    grad[idx] = -(G11[idx] * lr * ur + G12[idx] * (lr * us + ls * ur) + G22[idx] * ls * us);
+  }
+}
+
+unsigned nblocks(long long L) {
+  long long b = (L + kRT - 1) / kRT;
+  if (b > kRB) b = kRB;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+// workspace layout (bytes, 256-aligned pieces)
+struct WS {
+  double *r, *p, *Ap, *dinv, *d, *x64tmp;  // FP64 vectors
+  float *r32, *p32, *Ap32, *x32, *dinv32;   // FP32 vectors (mixed)
+  double* part;
+  Scalars* sc;
+  double* dmax;
+  Scalars* sc_h;  // pinned host mirror
+};
+
+int get_ws(sem_mesh* m, bool mixed, WS& w) {
+  const long long L = m->g.NX * m->g.NY;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t v64 = al(sizeof(double) * L), v32 = al(sizeof(float) * L);
+  const size_t need = 6 * v64 + 5 * v32 + al(sizeof(double) * kRB * 4) + al(sizeof(Scalars)) + al(sizeof(double));
+  if (m->ws_bytes < need) {
+    if (m->ws) cudaFree(m->ws);
+    m->ws = nullptr;
+    m->ws_bytes = 0;
+    SEM_CUDA(cudaMalloc(&m->ws, need));
+    m->ws_bytes = need;
+  }
+  (void)mixed;
+  char* p = static_cast<char*>(m->ws);
+  w.r = (double*)p; p += v64;
+  w.p = (double*)p; p += v64;
+  w.Ap = (double*)p; p += v64;
+  w.dinv = (double*)p; p += v64;
+  w.d = (double*)p; p += v64;
+  w.x64tmp = (double*)p; p += v64;
+  w.r32 = (float*)p; p += v32;
+  w.p32 = (float*)p; p += v32;
+  w.Ap32 = (float*)p; p += v32;
+  w.x32 = (float*)p; p += v32;
+  w.dinv32 = (float*)p; p += v32;
+  w.part = (double*)p; p += al(sizeof(double) * kRB * 4);
+  w.sc = (Scalars*)p; p += al(sizeof(Scalars));
+  w.dmax = (double*)p;
+  static thread_local Scalars* host = nullptr;
+  if (!host) SEM_CUDA(cudaMallocHost(&host, sizeof(Scalars) + sizeof(double)));
+  w.sc_h = host;
+  return SEM_OK;
+}
+
+int diag_build(sem_mesh* m, const double* nu_field, double nu, double k, double* d, double* tmp,
+               cudaStream_t s) {
+  DiagArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const int n = m->g.n;
+  std::memcpy(a.Dr, m->Dr_h, sizeof(double) * n * n);
+  std::memcpy(a.Ds, m->Ds_h, sizeof(double) * n * n);
+  a.nu = nu_field ? 1.0 : nu;
+  a.k = k;
+  const long long L = m->g.NX * m->g.NY;
+  k_diag_local<<<nblocks(L) * 4, kRT, 0, s>>>(a, m->G11, m->G12, m->G22, m->B, nu_field, tmp, m->g);
+  SEM_CUDA(cudaGetLastError());
+  SEM_CHECK(launch_gather_scatter(m->g, tmp, d, m->g.topo, s));
+  return SEM_OK;
+}
+
+// run CG iterations until done; T = double (F64/DF operator) or float (F32)
+template <class T>
+int run_cg(sem_mesh* m, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, const T* dinv,
+           int op_precision, const double* nu_field, double nu, double k, int check_every,
+           Scalars* out, cudaStream_t s) {
+  const long long L = m->g.NX * m->g.NY;
+  ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
+  c.u = p;
+  c.out = Ap;
+  if (op_precision == SEM_F32) {
+    c.G11 = m->G11_f;
+    c.G12 = m->G12_f;
+    c.G22 = m->G22_f;
+    c.B = m->B_f;
+  } else {
+    c.G11 = m->G11;
+    c.G12 = m->G12;
+    c.G22 = m->G22;
+    c.B = m->B;
+  }
+  c.nu = nullptr;
+  c.nu_s = nu_field ? 1.0 : nu;
+  c.k_s = k;
+  c.mode = m->g.topo | M_STIFF | M_MASS | M_GS | (m->has_bc ? M_MASK : 0u);
+  if (nu_field) {
+    if (op_precision == SEM_F32)
+      return set_error(SEM_ERR_UNSUPPORTED, "a nu field is not served by the FP32 inner solve");
+    c.nu = nu_field;
+    c.mode |= M_NUG;
+  }
+  if (k == 0.0) c.mode &= ~M_MASS;
+  c.precision = op_precision;
+  c.skip = &w.sc->done;
+  const unsigned nb = nblocks(L);
+  for (;;) {
+    for (int it = 0; it < check_every; ++it) {
+      k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
+      SEM_CHECK(launch_apply(m->g, m->ops, c, s));
+      k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
+      k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+      k_update<T><<<nb, kRT, 0, s>>>(x, r, p, Ap, dinv, w.part, w.sc, gv);
+      k_scal_beta<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+    }
+    SEM_CUDA(cudaGetLastError());
+    SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    SEM_CUDA(cudaStreamSynchronize(s));
+    if (w.sc_h->done) break;
+  }
+  *out = *w.sc_h;
+  return SEM_OK;
+}
+
+}  // namespace
+
+}  // namespace sem
+
+using namespace sem;
+
+extern "C" {
+
+int sem_jacobi_diag(sem_mesh_t* m, const double* nu_field, double nu, double k, double* diag,
+                    sem_stream_t stream) {
+  if (!m || !diag) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  WS w;
+  SEM_CHECK(get_ws(m, false, w));
+  SEM_CHECK(diag_build(m, nu_field, nu, k, diag, w.d, s));
+  if (m->has_bc) {
+    k_diag_mask<<<nblocks(m->g.NX * m->g.NY) * 4, kRT, 0, s>>>(diag, m->g, m->g.topo);
+    SEM_CUDA(cudaGetLastError());
+  }
+  return SEM_OK;
+}
+
+int sem_adjoint_grad(sem_mesh_t* m, const double* lam, const double* u, double* grad,
+                     unsigned flags, sem_stream_t stream) {
+  if (!m || !lam || !u || !grad) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (grad == lam || grad == u) return set_error(SEM_ERR_BAD_ARG, "grad must not alias an input");
+  cudaStream_t s = (cudaStream_t)stream;
+  DiagArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const int n = m->g.n;
+  std::memcpy(a.Dr, m->Dr_h, sizeof(double) * n * n);
+  std::memcpy(a.Ds, m->Ds_h, sizeof(double) * n * n);
+  const long long L = m->g.NX * m->g.NY;
+  double* dst = grad;
+  WS w;
+  if (flags & SEM_GS) {
+    SEM_CHECK(get_ws(m, false, w));
+    dst = w.d;
+  }
+  k_adjoint_grad<<<nblocks(L) * 4, kRT, 0, s>>>(a, lam, u, m->G11, m->G12, m->G22, dst, m->g);
+  SEM_CUDA(cudaGetLastError());
+  if (flags & SEM_GS) SEM_CHECK(launch_gather_scatter(m->g, dst, grad, m->g.topo, s));
+  return SEM_OK;
+}
+
+int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
+            sem_solve_info* info, sem_stream_t stream) {
+  if (!m || !o || !b || !x) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (b == x) return set_error(SEM_ERR_BAD_ARG, "x must not alias b");
+  if (o->precond != SEM_PRECOND_NONE && o->precond != SEM_PRECOND_JACOBI)
+    return set_error(SEM_ERR_BAD_ARG, "unknown preconditioner %d", o->precond);
+  const int prec = o->precision;
+  if (prec != SEM_F64 && prec != SEM_F64_DF && prec != SEM_MIXED)
+    return set_error(SEM_ERR_BAD_ARG, "precision must be SEM_F64, SEM_F64_DF or SEM_MIXED");
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long L = m->g.NX * m->g.NY;
+  const int maxiter = o->maxiter > 0 ? o->maxiter : (int)(L > 2147483647LL ? 2147483647LL : L);
+  int check_every = o->check_every > 0 ? o->check_every : (L < 200000 ? 64 : 16);
+  WS w;
+  SEM_CHECK(get_ws(m, prec == SEM_MIXED, w));
+  const unsigned nb = nblocks(L);
+  const bool jac = o->precond == SEM_PRECOND_JACOBI;
+  Grid gv = m->g;
+  if (o->mult_ones) gv.topo |= M_MULT1;
+  if (jac) {
+    SEM_CHECK(diag_build(m, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
+    k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, m->g, m->g.topo, m->has_bc ? 1 : 0);
+    if (prec == SEM_MIXED)
+      k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, m->g, m->g.topo, m->has_bc ? 1 : 0);
+    SEM_CUDA(cudaGetLastError());
+  }
+  Scalars res;
+  std::memset(&res, 0, sizeof(res));
+  int outer = 0;
+  double res0 = 0.0;
+  if (prec != SEM_MIXED) {
+    k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
+    k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
+    SEM_CUDA(cudaGetLastError());
+    SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    SEM_CUDA(cudaStreamSynchronize(s));
+    res0 = w.sc_h->rmax;
+    res = *w.sc_h;
+    if (!w.sc_h->done)
+      SEM_CHECK(run_cg<double>(m, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
+                               o->nu, o->k, check_every, &res, s));
+  } else {
+    if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED does not take a nu field");
+    SEM_CHECK(ensure_f32_geometry(m, s));
+    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 6;
+    // x = 0, r = b
+    k_zero<<<nb, kRT, 0, s>>>(x, L);
+    k_residual<<<nb, kRT, 0, s>>>(b, x, w.r, w.part, L);  // r = b - 0
+    k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
+    SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SEM_CUDA(cudaStreamSynchronize(s));
+    double rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
+    res0 = rmax;
+    int total_it = 0;
+    ApplyCall c;
+    std::memset(&c, 0, sizeof(c));
+    c.u = x;
+    c.out = w.Ap;
+    c.G11 = m->G11;
+    c.G12 = m->G12;
+    c.G22 = m->G22;
+    c.B = m->B;
+    c.nu_s = o->nu;
+    c.k_s = o->k;
+    c.mode = m->g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (m->has_bc ? M_MASK : 0u);
+    c.precision = m->precision;
+    bool nan = rmax != rmax;
+    while (!(rmax <= o->tol) && !nan && outer < max_outer) {
+      ++outer;
+      // inner FP32 CG on A d = r to inner_tol * |r|_inf
+      k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, w.p32, jac ? w.dinv32 : nullptr, w.part, gv);
+      k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
+      SEM_CUDA(cudaGetLastError());
+      Scalars ir;
+      SEM_CHECK(run_cg<float>(m, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
+                              nullptr, o->nu, o->k, check_every, &ir, s));
+      total_it += ir.k;
+      k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
+      SEM_CHECK(launch_apply(m->g, m->ops, c, s));
+      k_residual<<<nb, kRT, 0, s>>>(b, w.Ap, w.r, w.part, L);
+      k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
+      SEM_CUDA(cudaGetLastError());
+      SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
+      SEM_CUDA(cudaStreamSynchronize(s));
+      rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
+      nan = rmax != rmax;
+    }
+    res.k = total_it;
+    res.rmax = rmax;
+    res.nan = nan;
+    res.converged = rmax <= o->tol;
+  }
+  if (info) {
+    info->iters = res.k;
+    info->outer = outer;
+    info->res_inf = res.rmax;
+    info->res0_inf = res0;
+    info->converged = res.converged;
+  }
+  if (res.nan) return set_error(SEM_ERR_NAN, "NaN/Inf in the residual after %d iterations", res.k);
+  if (!res.converged)
+    return set_error(SEM_ERR_NOT_CONVERGED, "warning: res: %.17g after %d iterations", res.rmax, res.k);
+  return SEM_OK;
+}
+
+}  // extern "C"

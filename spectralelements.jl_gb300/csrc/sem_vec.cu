@@ -1,0 +1,264 @@
+// Structured, memory-bound kernels: standalone QQ', masks, mass, mult and the
+// generic tensor-product apply ABu.
+#include <cstring>
+
+#include "sem_internal.cuh"
+
+namespace sem {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(long long n, int threads = kThreads, long long cap = 152LL * 32) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (unsigned)b;
+}
+
+// partner of local row r under direct-stiffness summation, or -1
+__device__ __forceinline__ long long partner(long long r, int n, int E, long long NX, bool per) {
+  const long long e = r / n;
+  const int i = (int)(r - e * n);
+  if (i == 0) {
+    if (e > 0) return r - 1;
+    if (per) return NX - 1;
+  }
+  if (i == n - 1) {
+    if (e < E - 1) return r + 1;
+    if (per) return 0;
+  }
+  return -1;
+}
+
+// QQ' u: x sums in increasing row order, then y sums in increasing column
+// order, so every copy of a global node receives bit-identical values
+// (src/gatherScatter.jl:8-16 applies QQtx then QQty).
+__global__ void k_gather_scatter(const double* __restrict__ u, double* __restrict__ out, Grid g,
+                                 unsigned mode) {
+  const long long total = g.NX * g.NY;
+  const bool perx = (mode & M_PERX) != 0, pery = (mode & M_PERY) != 0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    const long long pr = partner(r, g.n, g.Ex, g.NX, perx);
+    const long long pc = partner(c, g.n, g.Ey, g.NY, pery);
+    const long long r0 = (pr >= 0 && pr < r) ? pr : r;
+    const long long r1 = (pr >= 0 && pr < r) ? r : pr;
+    auto xsum = [&](long long cc) {
+      double s = u[r0 + cc * g.NX];
+      if (r1 >= 0) s += u[r1 + cc * g.NX];
+      return s;
+    };
+    double v;
+    if (pc < 0) {
+      v = xsum(c);
+    } else {
+      const long long c0 = pc < c ? pc : c, c1 = pc < c ? c : pc;
+      v = xsum(c0) + xsum(c1);
+    }
+    if ((mode & M_MASK) && !mask_keep(r, c, g.NX, g.NY, mode)) v = v * 0.0;
+    out[idx] = v;
+  }
+}
+
+__global__ void k_mask_bc(const double* __restrict__ u, double* __restrict__ out, Grid g,
+                          unsigned topo) {
+  const long long total = g.NX * g.NY;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    const double v = u[idx];
+    out[idx] = mask_keep(r, c, g.NX, g.NY, topo) ? v : v * 0.0;
+  }
+}
+
+__global__ void k_mask_array(const double* __restrict__ M, const double* __restrict__ u,
+                             double* __restrict__ out, long long len) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = M ? M[i] * u[i] : u[i];
+}
+
+__global__ void k_mass(const double* __restrict__ B, const double* __restrict__ u,
+                       double* __restrict__ out, long long len) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = B[i] * u[i];
+}
+
+// mult = 1 ./ QQ'(ones) (src/mesh.jl:94-96): 1 / (copies_x * copies_y)
+__global__ void k_mult(double* __restrict__ out, Grid g) {
+  const long long total = g.NX * g.NY;
+  const bool perx = (g.topo & M_PERX) != 0, pery = (g.topo & M_PERY) != 0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / g.NX;
+    const long long r = idx - c * g.NX;
+    const double cx = copies_1d(r, g.n, g.Ex, perx);
+    const double cy = copies_1d(c, g.n, g.Ey, pery);
+    out[idx] = 1.0 / (cx * cy);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ABu (src/ABu.jl:9-37)
+// ---------------------------------------------------------------------------
+struct Mat32 {
+  double a[kMaxBlock * kMaxBlock];  // row-major a[p*cols + k]
+  int rows, cols;
+};
+
+// Br side: Br applied to consecutive chunks of nb entries of the column-major
+// flattening of u (reshape(u, nb, :)), output reshaped back
+__global__ void k_abu_br(const __grid_constant__ Mat32 Br, const double* __restrict__ u,
+                         double* __restrict__ v, long long nchunks) {
+  const int mb = Br.rows, nb = Br.cols;
+  const long long total = nchunks * mb;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long ch = idx / mb;
+    const int p = (int)(idx - ch * mb);
+    const double* src = u + ch * nb;
+    double s = 0.0;
+    for (int k = 0; k < nb; ++k) s = fma(Br.a[p * nb + k], src[k], s);
+    v[idx] = s;
+  }
+}
+
+// As side: out[:, b*ma + q] = sum_l As[q,l] u[:, b*na + l]
+__global__ void k_abu_as(const __grid_constant__ Mat32 As, const double* __restrict__ u,
+                         double* __restrict__ v, long long m, long long nblk) {
+  const int ma = As.rows, na = As.cols;
+  const long long total = m * nblk * ma;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long col = idx / m;
+    const long long r = idx - col * m;
+    const long long b = col / ma;
+    const int q = (int)(col - b * ma);
+    const double* src = u + r + b * na * m;
+    double s = 0.0;
+    for (int l = 0; l < na; ++l) s = fma(As.a[q * na + l], src[(long long)l * m], s);
+    v[idx] = s;
+  }
+}
+
+// both sides, one output block (mb x ma) per block of u (nb x na), staged in
+// shared memory: out_blk = Br * u_blk * As'
+__global__ void k_abu_both(const __grid_constant__ Mat32 As, const __grid_constant__ Mat32 Br,
+                           const double* __restrict__ u, double* __restrict__ v, long long m,
+                           long long nbx, long long nby) {
+  extern __shared__ double sh[];
+  const int ma = As.rows, na = As.cols, mb = Br.rows, nb = Br.cols;
+  double* ub = sh;            // nb x na
+  double* tb = sh + nb * na;  // mb x na
+  const long long mo = m / nb * mb;
+  for (long long blk = blockIdx.x; blk < nbx * nby; blk += gridDim.x) {
+    const long long by = blk / nbx, bx = blk - by * nbx;
+    for (int t = threadIdx.x; t < nb * na; t += blockDim.x) {
+      const int k = t % nb, l = t / nb;
+      ub[t] = u[bx * nb + k + (by * na + l) * m];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < mb * na; t += blockDim.x) {
+      const int p = t % mb, l = t / mb;
+      double s = 0.0;
+      for (int k = 0; k < nb; ++k) s = fma(Br.a[p * nb + k], ub[k + l * nb], s);
+      tb[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < mb * ma; t += blockDim.x) {
+      const int p = t % mb, q = t / mb;
+      double s = 0.0;
+      for (int l = 0; l < na; ++l) s = fma(As.a[q * na + l], tb[p + l * mb], s);
+      v[bx * mb + p + (by * ma + q) * mo] = s;
+    }
+    __syncthreads();
+  }
+}
+
+void load_mat(Mat32& M, const double* colmajor, int rows, int cols) {
+  std::memset(&M, 0, sizeof(M));
+  M.rows = rows;
+  M.cols = cols;
+  for (int p = 0; p < rows; ++p)
+    for (int k = 0; k < cols; ++k) M.a[p * cols + k] = colmajor[p + (long long)k * rows];
+}
+
+}  // namespace
+
+unsigned topo_bits(const Grid& g) { return g.topo; }
+
+int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode,
+                          cudaStream_t s) {
+  k_gather_scatter<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(u, out, g, mode);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int launch_mask_bc(const Grid& g, const double* u, double* out, unsigned topo, cudaStream_t s) {
+  k_mask_bc<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(u, out, g, topo);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int launch_mask_array(const double* M, const double* u, double* out, int64_t len,
+                      cudaStream_t s) {
+  if (len == 0) return SEM_OK;
+  k_mask_array<<<grid_for(len), kThreads, 0, s>>>(M, u, out, len);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int launch_mass(const Grid& g, const double* B, const double* u, double* out, cudaStream_t s) {
+  const long long len = g.NX * g.NY;
+  k_mass<<<grid_for(len), kThreads, 0, s>>>(B, u, out, len);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int launch_mult(const Grid& g, double* out, cudaStream_t s) {
+  k_mult<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(out, g);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int launch_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
+               const double* u, int m, int n, double* v, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return SEM_OK;
+  if (As == nullptr && Br == nullptr) {
+    SEM_CUDA(cudaMemcpyAsync(v, u, sizeof(double) * (size_t)m * n, cudaMemcpyDeviceToDevice, s));
+    return SEM_OK;
+  }
+  if (Br != nullptr && As == nullptr) {
+    Mat32 B;
+    load_mat(B, Br, mb, nb);
+    const long long nchunks = (long long)m * n / nb;
+    k_abu_br<<<grid_for(nchunks * mb), kThreads, 0, s>>>(B, u, v, nchunks);
+    SEM_CUDA(cudaGetLastError());
+    return SEM_OK;
+  }
+  if (As != nullptr && Br == nullptr) {
+    Mat32 A;
+    load_mat(A, As, ma, na);
+    const long long nblk = n / na;
+    k_abu_as<<<grid_for((long long)m * nblk * ma), kThreads, 0, s>>>(A, u, v, m, nblk);
+    SEM_CUDA(cudaGetLastError());
+    return SEM_OK;
+  }
+  Mat32 A, B;
+  load_mat(A, As, ma, na);
+  load_mat(B, Br, mb, nb);
+  const long long nbx = m / nb, nby = n / na;
+  const size_t smem = sizeof(double) * (size_t)(nb * na + mb * na);
+  unsigned blocks = grid_for(nbx * nby, 1, 152LL * 16);
+  k_abu_both<<<blocks, 128, smem, s>>>(A, B, u, v, m, nbx, nby);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+}  // namespace sem

@@ -1,0 +1,195 @@
+#
+# SEMB200.jl — Julia binding of libsem_b200.so: new methods of SpectralElements.jl's
+# operator/solve functions for CuArray fields, calling the C ABI of
+# include/sem_b200.h through ccall.  Host Arrays keep using the package's own
+# CPU methods; CuArrays never take a CPU or CUDA.jl-broadcast path.
+#
+# Usage (after `using SpectralElements, CUDA`):
+#   include("SEMB200.jl"); using .SEMB200
+#   u  = CuArray(msh.x)                  # any local field of the mesh
+#   Au = lapl(u, msh)                    # -> sem_lapl
+#   op = SEMB200.HelmholtzOp(msh, ν, k, ['D','D','D','D'])
+#   x  = pcg(b, op; opM=SEMB200.Jacobi(op), mult=msh.mult, tol=1e-8)
+#
+module SEMB200
+
+using CUDA
+import SpectralElements: ABu, lapl, mass, hlmz, gatherScatter, mask, pcg, pcg!, Mesh
+
+const libsem = get(ENV, "SEM_B200_LIB", joinpath(@__DIR__, "..", "lib", "libsem_b200.so"))
+
+const SEM_OK = Cint(0)
+const SEM_ERR_NOT_CONVERGED = Cint(2)
+const SEM_GS = Cuint(1)
+const SEM_MASK = Cuint(2)
+const SEM_F64 = Cint(0)
+const SEM_F64_DF = Cint(1)
+const SEM_MIXED = Cint(3)
+
+struct MeshDesc
+    nr::Cint; ns::Cint; Ex::Cint; Ey::Cint
+    periodic_x::Cint; periodic_y::Cint
+    Dr::Ptr{Cdouble}; Ds::Ptr{Cdouble}; wr::Ptr{Cdouble}; ws::Ptr{Cdouble}
+    x::Ptr{Cdouble}; y::Ptr{Cdouble}
+    G11::Ptr{Cdouble}; G12::Ptr{Cdouble}; G22::Ptr{Cdouble}; B::Ptr{Cdouble}
+    bc::Ptr{UInt8}
+end
+
+struct PcgOpts
+    nu::Cdouble; nu_field::CuPtr{Cdouble}; k::Cdouble
+    precond::Cint; precision::Cint; tol::Cdouble; maxiter::Cint
+    inner_tol::Cdouble; max_outer::Cint; check_every::Cint; mult_ones::Cint
+end
+
+mutable struct SolveInfo
+    iters::Cint; outer::Cint; res_inf::Cdouble; res0_inf::Cdouble; converged::Cint
+end
+SolveInfo() = SolveInfo(0, 0, 0.0, 0.0, 0)
+
+lasterr() = unsafe_string(ccall((:sem_last_error, libsem), Cstring, ()))
+check(st) = st == SEM_OK || error("libsem_b200 status $st: $(lasterr())")
+stream() = CUDA.stream().handle
+
+# Mesh -> device handle cache: the Julia Mesh is immutable, so the handle is
+# built once from its host arrays (geometry uploaded verbatim).
+const HANDLES = IdDict{Any,Ptr{Cvoid}}()
+
+function handle(msh::Mesh)
+    get!(HANDLES, msh) do
+        d = Ref(MeshDesc(msh.nr, msh.ns, msh.Ex, msh.Ey, msh.ifperiodic[1], msh.ifperiodic[2],
+                         pointer(msh.Dr), pointer(msh.Ds), pointer(msh.wr), pointer(msh.ws),
+                         pointer(msh.x), pointer(msh.y), pointer(msh.G11), pointer(msh.G12),
+                         pointer(msh.G22), pointer(msh.B), Ptr{UInt8}(C_NULL)))
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        GC.@preserve msh check(ccall((:sem_mesh_create, libsem), Cint,
+                                     (Ref{MeshDesc}, Ref{Ptr{Cvoid}}), d, h))
+        finalizer(m -> ccall((:sem_mesh_destroy, libsem), Cint, (Ptr{Cvoid},), h[]), msh)
+        h[]
+    end
+end
+
+set_bc!(msh::Mesh, bc::Vector{Char}) =
+    check(ccall((:sem_mesh_set_bc, libsem), Cint, (Ptr{Cvoid}, Cstring), handle(msh), String(bc)))
+
+# ---- ABu(As,Br,u) (src/ABu.jl:9-37); [] = identity
+function ABu(As::AbstractArray, Br::AbstractArray, u::CuArray{Float64,2})
+    m, n = size(u)
+    A = length(As) == 0 ? nothing : Matrix{Float64}(As)
+    B = length(Br) == 0 ? nothing : Matrix{Float64}(Br)
+    mo = B === nothing ? m : div(m * size(B, 1), size(B, 2))
+    no = A === nothing ? n : div(n, size(A, 2)) * size(A, 1)
+    v = CuArray{Float64}(undef, mo, no)
+    GC.@preserve A B check(ccall((:sem_abu, libsem), Cint,
+        (Ptr{Cdouble}, Cint, Cint, Ptr{Cdouble}, Cint, Cint, CuPtr{Cdouble}, Cint, Cint,
+         CuPtr{Cdouble}, Ptr{Cvoid}),
+        A === nothing ? C_NULL : pointer(A), A === nothing ? 0 : size(A, 1), A === nothing ? 0 : size(A, 2),
+        B === nothing ? C_NULL : pointer(B), B === nothing ? 0 : size(B, 1), B === nothing ? 0 : size(B, 2),
+        pointer(u), m, n, pointer(v), stream()))
+    return v
+end
+
+# ---- lapl(u,msh), lapl(u,ν,msh), mass, hlmz, gatherScatter, mask
+function lapl(u::CuArray{Float64,2}, msh::Mesh)
+    out = similar(u)
+    check(ccall((:sem_lapl, libsem), Cint, (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(msh), pointer(u), pointer(out), 0, stream()))
+    return out
+end
+
+function lapl(u::CuArray{Float64,2}, ν::CuArray{Float64,2}, msh::Mesh)
+    out = similar(u)
+    check(ccall((:sem_lapl_nu, libsem), Cint,
+                (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(msh), pointer(ν), pointer(u), pointer(out), 0, stream()))
+    return out
+end
+
+function mass(u::CuArray{Float64,2}, msh::Mesh)
+    out = similar(u)
+    check(ccall((:sem_mass, libsem), Cint, (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(msh), pointer(u), pointer(out), 0, stream()))
+    return out
+end
+
+function hlmz(u::CuArray{Float64,2}, ν::Number, k::Number, msh::Mesh)
+    out = similar(u)
+    check(ccall((:sem_hlmz, libsem), Cint,
+                (Ptr{Cvoid}, CuPtr{Cdouble}, Cdouble, Cdouble, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(msh), CU_NULL, ν, k, pointer(u), pointer(out), 0, stream()))
+    return out
+end
+
+function hlmz(u::CuArray{Float64,2}, ν::CuArray{Float64,2}, k::Number, msh::Mesh)
+    out = similar(u)
+    check(ccall((:sem_hlmz, libsem), Cint,
+                (Ptr{Cvoid}, CuPtr{Cdouble}, Cdouble, Cdouble, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(msh), pointer(ν), 1.0, k, pointer(u), pointer(out), 0, stream()))
+    return out
+end
+
+function gatherScatter(u::CuArray{Float64,2}, msh::Mesh)
+    out = similar(u)
+    check(ccall((:sem_gather_scatter, libsem), Cint, (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ptr{Cvoid}),
+                handle(msh), pointer(u), pointer(out), stream()))
+    return out
+end
+
+function mask(u::CuArray{Float64,2}, M::CuArray{Float64,2})
+    out = similar(u)
+    check(ccall((:sem_mask, libsem), Cint, (CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Int64, Ptr{Cvoid}),
+                pointer(M), pointer(u), pointer(out), length(u), stream()))
+    return out
+end
+
+# ---- fused operator objects accepted by pcg (callable, so opA * u works
+# through Base.:*(op::Function, x) of src/SpectralElements.jl:21)
+struct HelmholtzOp <: Function
+    msh::Mesh
+    ν::Float64
+    k::Float64
+    bc::Vector{Char}
+end
+function (op::HelmholtzOp)(u::CuArray{Float64,2})
+    set_bc!(op.msh, op.bc)
+    out = similar(u)
+    check(ccall((:sem_hlmz, libsem), Cint,
+                (Ptr{Cvoid}, CuPtr{Cdouble}, Cdouble, Cdouble, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(op.msh), CU_NULL, op.ν, op.k, pointer(u), pointer(out), SEM_GS | SEM_MASK, stream()))
+    return out
+end
+
+struct Jacobi <: Function
+    op::HelmholtzOp
+end
+
+# ---- pcg(b,opA;opM,mult,ifv,tol,maxiter) (src/pcg.jl:16-60) on the device
+function pcg(b::CuArray{Float64,2}, opA::HelmholtzOp; opM=x -> x, mult=nothing, ifv=false,
+             tol=1e-8, maxiter=length(b), precision=SEM_F64_DF)
+    opM isa Jacobi || opM === identity || opM isa Function && !(opM isa HelmholtzOp) ||
+        throw(ArgumentError("opM must be x->x or SEMB200.Jacobi(opA)"))
+    set_bc!(opA.msh, opA.bc)
+    x = similar(b)
+    o = Ref(PcgOpts(opA.ν, CU_NULL, opA.k, opM isa Jacobi ? 1 : 0, precision, tol, maxiter,
+                    1e-4, 6, 0, mult === nothing ? 1 : 0))
+    info = Ref(SolveInfo())
+    st = ccall((:sem_pcg, libsem), Cint,
+               (Ptr{Cvoid}, Ref{PcgOpts}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ref{SolveInfo}, Ptr{Cvoid}),
+               handle(opA.msh), o, pointer(b), pointer(x), info, stream())
+    if st == SEM_ERR_NOT_CONVERGED
+        println("warning: res:", info[].res_inf)
+        return x
+    end
+    check(st)
+    ifv && println("PCG iter: ", info[].iters, ", res: ", info[].res_inf)
+    return x
+end
+
+pcg(b::CuArray, opA::Function; kw...) =
+    throw(ArgumentError("pcg on CuArrays takes a SEMB200 operator object; closures are not run on the host"))
+
+function pcg!(x::CuArray{Float64,2}, b::CuArray{Float64,2}, opA::HelmholtzOp; kw...)
+    x .= pcg(b, opA; kw...)
+    return
+end
+
+end # module

@@ -1,0 +1,22 @@
+"""semgb300 — host-side mirror of SpectralElements.jl's operator/solve API over
+libsem_b200.so (GB300, sm_103a).
+
+Names and argument meanings follow the reference: ``Mesh``, ``generateMask``,
+``ABu``, ``lapl``, ``mass``, ``hlmz``, ``gatherScatter``, ``mask``, ``pcg``,
+``pcg_`` (pcg!), ``Diffusion``.  Fields are CUDA float64 tensors in the
+reference's column-major local layout.
+"""
+from ._lib import (SEM_F32, SEM_F64, SEM_F64_DF, SEM_GS, SEM_MASK, SEM_MIXED, NotConverged,  # noqa: F401
+                   SemError, build, load)
+from .host import bdfExtK, derivMat, fixU, gausslobatto, interpMat, ndgrid, semmesh, semq_index  # noqa: F401
+from .mesh import Mesh, QQt, as_local, generateMask, local_empty  # noqa: F401
+from .ops import ABu, gatherScatter, hlmz, lapl, mask, mass  # noqa: F401
+from .solver import (Diffusion, HelmholtzOp, Jacobi, TimeStepper, identity,  # noqa: F401
+                     linsolve_varcoef, pcg, pcg_)
+
+__all__ = ["Mesh", "QQt", "generateMask", "ABu", "lapl", "mass", "hlmz", "gatherScatter", "mask",
+           "pcg", "pcg_", "HelmholtzOp", "Jacobi", "identity", "Diffusion", "TimeStepper",
+           "linsolve_varcoef", "gausslobatto", "derivMat", "interpMat", "semmesh", "ndgrid",
+           "semq_index", "bdfExtK", "fixU", "as_local", "local_empty", "build", "load",
+           "SemError", "NotConverged", "SEM_F64", "SEM_F64_DF", "SEM_F32", "SEM_MIXED",
+           "SEM_GS", "SEM_MASK"]

@@ -1,0 +1,188 @@
+"""Parity of the device operators (through libsem_b200's C ABI) with the oracle.
+
+Tolerances: relative L2 <= 1e-12 for FP64 operator applies (both the native
+FP64 and the double-float arithmetic); bit-exact for masks, multiplicities
+and gather-scatter of summed copies (the same summation order as the oracle).
+"""
+import numpy as np
+import pytest
+
+import sem_oracle as O
+from _helpers import host, meshes, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+CASES = [
+    # n, Ex, Ey, periodic, bc, deform amplitude
+    (9, 8, 8, (False, False), "DDDD", 0.1),
+    (9, 17, 13, (False, False), "DNDN", 0.05),
+    (5, 3, 2, (True, False), "DDDD", 0.05),
+    (4, 1, 1, (True, True), "NNNN", 0.0),
+    (2, 9, 5, (False, True), "DDNN", 0.05),
+    (3, 20, 11, (False, False), "NDDN", 0.05),
+    (8, 10, 9, (True, True), "DDDD", 0.0),
+    (12, 5, 7, (False, False), "DDDD", 0.05),
+    (13, 3, 4, (True, False), "NNDD", 0.05),
+    (16, 4, 3, (False, False), "DDDD", 0.05),
+    (17, 3, 5, (False, True), "DDDD", 0.05),
+    (6, 25, 1, (False, False), "DDDD", 0.05),
+    (7, 1, 19, (False, False), "DDDD", 0.05),
+]
+
+
+def _ids(c):
+    return f"n{c[0]}_{c[1]}x{c[2]}_p{int(c[3][0])}{int(c[3][1])}_{c[4]}"
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+@pytest.mark.parametrize("prec", ["F64", "DF"])
+def test_fused_operators(gpu, case, prec):
+    import semgb300 as S
+    n, Ex, Ey, per, bc, amp = case
+    mo, md = meshes(n, Ex, Ey, per, bc, amp, precision=getattr(S, "SEM_" + ("F64" if prec == "F64" else "F64_DF")))
+    M = O.generateMask(list(bc), mo)
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-1, 1, mo.shape)
+    nu = rng.uniform(0.5, 2.0, mo.shape)
+    ud = S.as_local(u)
+    # lapl(u, msh)
+    assert rel_l2(host(S.lapl(ud, md)), O.lapl(u, mo)) < TOL
+    # lapl(u, nu, msh) = nu .* lapl
+    assert rel_l2(host(S.lapl(ud, S.as_local(nu), md)), O.lapl(u, mo, nu)) < TOL
+    # hlmz(u, nu, k, msh)
+    assert rel_l2(host(S.hlmz(ud, 1e-2, 1.0, md)), O.hlmz(u, 1e-2, 1.0, mo)) < TOL
+    # opLHS: mask(QQ'(hlmz)) fused
+    ref = O.mask(O.gatherScatter(O.hlmz(u, 1e-2, 1.0, mo), mo), M)
+    got = host(S.HelmholtzOp(md, 1e-2, 1.0)(ud))
+    assert rel_l2(got, ref) < TOL
+    # every copy of a global node carries the same value
+    np.testing.assert_array_equal(got, O.gatherScatter(got, mo) * mo.mult)
+    # variable coefficient folded into G: D'(nu G)D
+    ref = O.mask(O.gatherScatter(O.laplace(u, mo.Dr, mo.Ds, nu * mo.G11, nu * mo.G12, nu * mo.G22), mo), M)
+    got = host(S.HelmholtzOp(md, 1.0, 0.0, nu_field=S.as_local(nu))(ud))
+    assert rel_l2(got, ref) < TOL
+    # functional lapl(u, M, [], [], QQtx, QQty, Dr, Ds, G11, G12, G22, mult)
+    Md = S.generateMask(list(bc), md)
+    got = host(S.lapl(ud, Md, [], [], md.QQtx, md.QQty, md.Dr, md.Ds, S.as_local(mo.G11),
+                      S.as_local(mo.G12), S.as_local(mo.G22), md.mult))
+    ref = O.mask(O.gatherScatter(O.lapl(u, mo), mo), M)
+    assert rel_l2(got, ref) < TOL
+    # block-diagonal kron(I, Dr) accepted as in examples/p2d_explicit.jl:28; no QQ', no mask
+    got = host(S.lapl(ud, [], [], [], [], [], np.kron(np.eye(Ex), mo.Dr), np.kron(np.eye(Ey), mo.Ds),
+                      S.as_local(mo.G11), S.as_local(mo.G12), S.as_local(mo.G22), md.mult))
+    assert rel_l2(got, O.lapl(u, mo)) < TOL
+
+
+@pytest.mark.parametrize("case", CASES[:6], ids=_ids)
+def test_structured_kernels_bit_exact(gpu, case):
+    import semgb300 as S
+    n, Ex, Ey, per, bc, amp = case
+    mo, md = meshes(n, Ex, Ey, per, bc, amp)
+    M = O.generateMask(list(bc), mo)
+    rng = np.random.default_rng(4)
+    u = rng.uniform(-1, 1, mo.shape)
+    ud = S.as_local(u)
+    np.testing.assert_array_equal(host(S.gatherScatter(ud, md)),
+                                  O.gatherScatter_index(u, mo.l2gx, mo.nxg, mo.l2gy, mo.nyg))
+    np.testing.assert_array_equal(host(S.gatherScatter(ud, md.QQtx, md.QQty)), O.gatherScatter(u, mo))
+    Md = S.generateMask(list(bc), md)
+    np.testing.assert_array_equal(host(Md), M)
+    np.testing.assert_array_equal(host(S.mask(ud, Md)), O.mask(u, M))
+    np.testing.assert_array_equal(host(S.mask(ud, [])), u)
+    np.testing.assert_array_equal(host(md.mult), mo.mult)
+    np.testing.assert_array_equal(host(S.mass(ud, md)), O.mass(u, mo))
+    mf = host(md.field("mask"))
+    np.testing.assert_array_equal(mf, M.astype(float))
+    # functional mass(u, M, B, [], [], QQtx, QQty, mult)
+    got = host(S.mass(ud, Md, S.as_local(mo.B), [], [], md.QQtx, md.QQty, md.mult))
+    ref = O.mask(O.gatherScatter(mo.B * u, mo), M)
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n,Ex,Ey,per", [(9, 8, 8, (False, False)), (5, 7, 3, (True, False)),
+                                         (17, 3, 2, (False, True))])
+def test_device_geometry(gpu, n, Ex, Ey, per):
+    import semgb300 as S
+    mo = O.Mesh(n, n, Ex, Ey, per, O.sin_deform(0.1))
+    md = S.Mesh(n, n, Ex, Ey, per, O.sin_deform(0.1))
+    np.testing.assert_array_equal(host(md.x), mo.x)
+    for k in ("Jac", "rx", "ry", "sx", "sy", "B", "G11", "G12", "G22", "Bi", "Jaci"):
+        assert rel_l2(host(getattr(md, k)), getattr(mo, k)) < 1e-12, k
+
+
+@pytest.mark.parametrize("shape_u,As,Br", [
+    ((18, 27), (9, 9), (9, 9)),
+    ((18, 27), None, (9, 9)),
+    ((18, 27), (9, 9), None),
+    ((12, 10), (3, 5), (7, 4)),
+    ((8, 6), (4, 2), None),
+    ((6, 4), None, (3, 4)),  # reshape(u, 4, :) spans columns
+    ((64, 96), (32, 32), (32, 32)),
+])
+def test_abu(gpu, shape_u, As, Br):
+    import semgb300 as S
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal(shape_u)
+    A = None if As is None else rng.standard_normal(As)
+    B = None if Br is None else rng.standard_normal(Br)
+    got = host(S.ABu(A, B, S.as_local(u)))
+    assert rel_l2(got, O.ABu(A, B, u)) < 1e-14
+
+
+def test_abu_rejects_large_blocks(gpu):
+    import semgb300 as S
+    u = S.as_local(np.ones((66, 66)))
+    with pytest.raises(S.SemError):
+        S.ABu(None, np.eye(33), u)
+
+
+def test_full_size_properties_cfg2(gpu):
+    """256x256 elements, N=8: F64 vs double-float, C-oracle parity, symmetry,
+    linearity (size-independent properties at the benchmark size)."""
+    import sem_oracle_c as C
+    import semgb300 as S
+    import torch
+    mo, md = meshes(9, 256, 256, (False, False), "DDDD", 0.05)
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-1, 1, mo.shape)
+    ud = S.as_local(u)
+    op = S.HelmholtzOp(md, 1e-2, 1.0)
+    md.set_precision(S.SEM_F64_DF)
+    a_df = host(op(ud))
+    md.set_precision(S.SEM_F64)
+    a_64 = host(op(ud))
+    assert rel_l2(a_df, a_64) < TOL
+    ref = C.apply(C.grid(9, 256, 256, (False, False), "DDDD"), mo.Dr, mo.Ds, mo.G11, mo.G12,
+                  mo.G22, mo.B, u, nu=1e-2, k=1.0)
+    assert rel_l2(a_64, ref) < TOL
+    assert rel_l2(a_df, ref) < TOL
+    md.set_precision(S.SEM_F64_DF)
+    # symmetry <v, A u>_mult == <u, A v>_mult on continuous masked fields
+    Md = S.generateMask(["D"] * 4, md)
+    cont = lambda w: S.mask(md.mult * S.gatherScatter(w, md), Md)  # noqa: E731
+    uc = cont(ud)
+    vc = cont(S.as_local(rng.uniform(-1, 1, mo.shape)))
+    s1 = torch.sum(vc * op(uc) * md.mult).item()
+    s2 = torch.sum(uc * op(vc) * md.mult).item()
+    assert abs(s1 - s2) < 1e-11 * abs(s1)
+    # linearity
+    lhs = op(2.5 * uc - 0.75 * vc)
+    rhs = 2.5 * op(uc) - 0.75 * op(vc)
+    assert (torch.linalg.norm(lhs - rhs) / torch.linalg.norm(rhs)).item() < 1e-13
+
+
+def test_errors(gpu):
+    import semgb300 as S
+    mo, md = meshes(5, 3, 3)
+    u = S.as_local(np.ones(mo.shape))
+    lib = S.load()
+    st = lib.sem_lapl(md.handle, u.data_ptr(), u.data_ptr(), 0, None)
+    assert st == 1 and b"alias" in lib.sem_last_error()
+    md.set_bc(None)
+    with pytest.raises(S.SemError):
+        lib_st = lib.sem_mask_bc(md.handle, u.data_ptr(), S.local_empty(*mo.shape).data_ptr(), None)
+        S._lib.check(lib_st)
+    with pytest.raises(ValueError):
+        S.lapl(S.as_local(np.ones((5, 5))), md)

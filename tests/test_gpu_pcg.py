@@ -1,0 +1,135 @@
+"""PCG on the device against the oracle's restatement of src/pcg.jl:16-60.
+
+The reference loop is reproduced exactly (absolute Inf-norm tolerance,
+zero initial guess, mult-weighted dots, maxiter = length(b)); iteration
+counts agree to within 2 (summation order changes the last digits of the
+dot products), solutions agree to the solver tolerance.
+"""
+import numpy as np
+import pytest
+
+import sem_oracle as O
+from _helpers import host, meshes, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _poisson_rhs(mo, M):
+    ut = np.sin(np.pi * mo.x) * np.sin(np.pi * mo.y)
+    f = 2 * np.pi ** 2 * ut
+    return ut, O.gatherScatter(O.mask(O.mass(f, mo), M), mo)
+
+
+@pytest.mark.parametrize("prec", ["F64", "DF"])
+def test_poisson_cfg1_jacobi(gpu, prec):
+    import semgb300 as S
+    mo, md = meshes(9, 8, 8, (False, False), "DDDD", 0.1,
+                    precision=S.SEM_F64 if prec == "F64" else S.SEM_F64_DF)
+    M = O.generateMask(["D"] * 4, mo)
+    ut, b = _poisson_rhs(mo, M)
+    tol = 1e-10 * np.abs(b).max()
+    d = O.jacobi_diag(mo, 1.0, 0.0, M)
+    info_o = {}
+    x_o = O.pcg(b, lambda v: O.mask(O.gatherScatter(O.lapl(v, mo), mo), M), opM=lambda r: r / d,
+                mult=mo.mult, tol=tol, info=info_o)
+    op = S.HelmholtzOp(md, 1.0, 0.0)
+    jac = S.Jacobi(op)
+    np.testing.assert_allclose(host(jac.diag()), d, rtol=1e-13)
+    info = {}
+    x = host(S.pcg(S.as_local(b), op, opM=jac, mult=md.mult, tol=tol, info=info))
+    assert info["converged"] and abs(info["iters"] - info_o["iters"]) <= 2, (info, info_o)
+    assert np.abs(x - x_o).max() < 1e-10
+    assert np.abs(x - ut).max() < 1e-8
+    assert info["res_inf"] <= tol
+
+
+def test_helmholtz_cfg2_shape_vs_c_oracle(gpu):
+    """nu=1e-2, lambda=1 Helmholtz, Jacobi PCG to 1e-8 relative on 32x32, N=8."""
+    import sem_oracle_c as C
+    import semgb300 as S
+    mo, md = meshes(9, 32, 32, (False, False), "DDDD", 0.05)
+    M = O.generateMask(["D"] * 4, mo)
+    rng = np.random.default_rng(2)
+    f = np.zeros(mo.shape)
+    for _ in range(16):
+        kx, ky = rng.integers(1, 9, size=2)
+        f += rng.standard_normal() / (kx ** 2 + ky ** 2) * np.sin(kx * np.pi * mo.x) * np.sin(ky * np.pi * mo.y)
+    b = O.gatherScatter(O.mask(O.mass(f, mo), M), mo)
+    tol = 1e-8 * np.abs(b).max()
+    d = O.jacobi_diag(mo, 1e-2, 1.0, M)
+    g = C.grid(9, 32, 32, (False, False), "DDDD")
+    x_c, it_c, res_c = C.pcg(g, mo.Dr, mo.Ds, mo.G11, mo.G12, mo.G22, mo.B, b, nu=1e-2, k=1.0, d=d, tol=tol)
+    op = S.HelmholtzOp(md, 1e-2, 1.0)
+    info = {}
+    x = host(S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info))
+    assert info["converged"] and abs(info["iters"] - it_c) <= 2, (info, it_c)
+    assert rel_l2(x, x_c) < 1e-8
+    # mixed precision reaches the same tolerance; error against the FP64 solution stated
+    info_m = {}
+    xm = host(S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info_m,
+                    precision=S.SEM_MIXED))
+    assert info_m["converged"] and info_m["outer"] <= 6, info_m
+    assert info_m["res_inf"] <= tol
+    assert rel_l2(xm, x_c) < 1e-7
+
+
+def test_unweighted_default_and_identity_precond(gpu):
+    import semgb300 as S
+    mo, md = meshes(5, 4, 3, (False, False), "DDDD", 0.05)
+    M = O.generateMask(["D"] * 4, mo)
+    ut, b = _poisson_rhs(mo, M)
+    info_o = {}
+    x_o = O.pcg(b, lambda v: O.mask(O.gatherScatter(O.hlmz(v, 0.5, 2.0, mo), mo), M), tol=1e-9,
+                info=info_o)
+    op = S.HelmholtzOp(md, 0.5, 2.0)
+    info = {}
+    x = host(S.pcg(S.as_local(b), op, tol=1e-9, info=info))
+    assert abs(info["iters"] - info_o["iters"]) <= 2
+    assert np.abs(x - x_o).max() < 1e-8
+
+
+def test_maxiter_warns_and_returns_x(gpu, capsys):
+    import semgb300 as S
+    mo, md = meshes(9, 8, 8, (False, False), "DDDD", 0.1)
+    M = O.generateMask(["D"] * 4, mo)
+    _, b = _poisson_rhs(mo, M)
+    info_o = {}
+    x_o = O.pcg(b, lambda v: O.mask(O.gatherScatter(O.lapl(v, mo), mo), M), mult=mo.mult,
+                tol=1e-30, maxiter=7, info=info_o)
+    op = S.HelmholtzOp(md, 1.0, 0.0)
+    info = {}
+    x = host(S.pcg(S.as_local(b), op, mult=md.mult, tol=1e-30, maxiter=7, info=info))
+    assert "warning: res:" in capsys.readouterr().out
+    assert info["iters"] == 7 and not info["converged"]
+    assert rel_l2(x, x_o) < 1e-12
+    # pcg! writes into x
+    y = md.empty()
+    S.pcg_(y, S.as_local(b), op, mult=md.mult, tol=1e-30, maxiter=7)
+    assert rel_l2(host(y), x_o) < 1e-12
+
+
+def test_nan_is_reported(gpu):
+    import semgb300 as S
+    mo, md = meshes(5, 3, 3)
+    b = np.ones(mo.shape)
+    b[4, 4] = np.nan
+    op = S.HelmholtzOp(md, 1.0, 1.0)
+    with pytest.raises(S.SemError) as e:
+        S.pcg(S.as_local(b), op, mult=md.mult)
+    assert e.value.status == 3
+
+
+def test_zero_rhs_returns_zero(gpu):
+    import semgb300 as S
+    mo, md = meshes(5, 3, 3)
+    op = S.HelmholtzOp(md, 1.0, 1.0)
+    info = {}
+    x = host(S.pcg(S.as_local(np.zeros(mo.shape)), op, mult=md.mult, info=info))
+    assert info["iters"] == 0 and not x.any()
+
+
+def test_rejects_host_closures(gpu):
+    import semgb300 as S
+    mo, md = meshes(5, 3, 3)
+    with pytest.raises(TypeError):
+        S.pcg(S.as_local(np.ones(mo.shape)), lambda v: v)

@@ -1,0 +1,84 @@
+"""Host-side logic of the product (no GPU): set-up numerics against the oracle,
+and the C ABI library's exports."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import sem_oracle as O
+from semgb300 import _lib, host
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("n", range(2, 18))
+def test_gll_and_derivmat_match_oracle(n):
+    z, w = host.gausslobatto(n)
+    zo, wo = O.gausslobatto(n)
+    np.testing.assert_allclose(z, zo, rtol=0, atol=4e-16)
+    np.testing.assert_allclose(w, wo, rtol=4e-16, atol=0)
+    D, Do = host.derivMat(zo), O.derivMat(zo)
+    np.testing.assert_allclose(D, Do, rtol=1e-13, atol=1e-13 * np.abs(Do).max())
+
+
+def test_interp_semmesh_semq_bdf():
+    xi, _ = O.gausslobatto(7)
+    xo = np.linspace(-1, 1, 11)
+    np.testing.assert_allclose(host.interpMat(xo, xi), O.interpMat(xo, xi), rtol=1e-13, atol=1e-14)
+    for E, n in ((3, 4), (5, 9)):
+        z, w = host.semmesh(E, n)
+        zo, wo = O.semmesh(E, n)
+        np.testing.assert_allclose(z, zo, rtol=0, atol=1e-15)
+        np.testing.assert_allclose(w, wo, rtol=1e-15)
+        for per in (False, True):
+            g, ng = host.semq_index(E, n, per)
+            go, ngo = O.semq_index(E, n, per)
+            np.testing.assert_array_equal(g, go)
+            assert ng == ngo
+    for t, k in (([0.0] * 4, 3), ([0.1, 0.0], 1), ([0.3, 0.2, 0.1, 0.0], 3), ([0.2, 0.1, 0.0, 0.0], 3)):
+        a, b = host.bdfExtK(t, k)
+        ao, bo = O.bdfExtK(t, k)
+        np.testing.assert_allclose(a, ao, rtol=1e-13)
+        np.testing.assert_allclose(b, bo, rtol=1e-13)
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "sem_b200.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(sem_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = _header_functions()
+    assert "sem_pcg" in names and "sem_lapl" in names
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+    assert lib.sem_abi_version() == 1
+
+
+def test_argument_validation_needs_no_gpu():
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.sem_mesh_create(None, ctypes.byref(h)) == _lib.SEM_ERR_BAD_ARG
+    assert b"NULL" in lib.sem_last_error()
+    d = _lib.MeshDesc()
+    d.nr, d.ns, d.Ex, d.Ey = 9, 7, 2, 2
+    assert lib.sem_mesh_create(ctypes.byref(d), ctypes.byref(h)) == _lib.SEM_ERR_UNSUPPORTED
+    d.nr, d.ns = 1, 1
+    assert lib.sem_mesh_create(ctypes.byref(d), ctypes.byref(h)) == _lib.SEM_ERR_BAD_ARG
+    assert lib.sem_mask(None, None, None, -1, None) == _lib.SEM_ERR_BAD_ARG
+    a = np.zeros(4)
+    assert lib.sem_abu(None, 0, 0, None, 0, 0, a.ctypes.data, 2, 2, a.ctypes.data, None) == _lib.SEM_ERR_BAD_ARG
+
+
+def test_product_has_no_oracle_imports():
+    pkg = os.path.join(ROOT, "spectralelements.jl_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".jl")):
+                txt = open(os.path.join(dirpath, f)).read()
+                assert "sem_oracle" not in txt and "oracle/" not in txt, f
