@@ -55,6 +55,24 @@ static unsigned op_mode(const sem_mesh* m, unsigned flags) {
   return mode;
 }
 
+int upload_line_info(sem_mesh* m) {
+  const int64_t NX = m->g.NX, NY = m->g.NY;
+  if (!m->info) SEM_CUDA(cudaMalloc(&m->info, (size_t)(NX + NY)));
+  unsigned char* h = (unsigned char*)std::malloc((size_t)(NX + NY));
+  const unsigned t = m->g.topo;
+  const bool bc = m->has_bc;
+  for (int64_t r = 0; r < NX; ++r)
+    h[r] = line_info(r, m->g.n, m->g.Ex, (t & M_PERX) != 0, bc && (t & M_DXMIN), bc && (t & M_DXMAX));
+  for (int64_t c = 0; c < NY; ++c)
+    h[NX + c] = line_info(c, m->g.n, m->g.Ey, (t & M_PERY) != 0, bc && (t & M_DYMIN), bc && (t & M_DYMAX));
+  cudaError_t e = cudaMemcpy(m->info, h, (size_t)(NX + NY), cudaMemcpyHostToDevice);
+  std::free(h);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMemcpy(line info)");
+  m->g.rinfo = m->info;
+  m->g.cinfo = m->info + NX;
+  return SEM_OK;
+}
+
 }  // namespace sem
 
 using namespace sem;
@@ -137,6 +155,7 @@ int sem_mesh_create(const sem_mesh_desc* d, sem_mesh_t** out) {
     if (st == SEM_OK && (e = cudaStreamSynchronize(0)) != cudaSuccess)
       st = cuda_error(e, "geometry kernel");
   }
+  if (st == SEM_OK) st = upload_line_info(m);
   if (st != SEM_OK) {
     sem_mesh_destroy(m);
     return st;
@@ -150,6 +169,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (m->x) cudaFree(m->x);
   if (m->G11_f) cudaFree(m->G11_f);
   if (m->ws) cudaFree(m->ws);
+  if (m->info) cudaFree(m->info);
   if (m->ops) free_operator_set(m->ops);
   std::free(m->Dr_h);
   std::free(m->Ds_h);
@@ -164,12 +184,12 @@ int sem_mesh_set_bc(sem_mesh_t* m, const char* bc) {
   m->g.topo &= ~(M_DXMIN | M_DXMAX | M_DYMIN | M_DYMAX);
   if (!bc) {
     m->has_bc = false;
-    return SEM_OK;
+    return upload_line_info(m);
   }
   if (!valid_bc(bc)) return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
   m->g.topo |= bc_bits(bc);
   m->has_bc = true;
-  return SEM_OK;
+  return upload_line_info(m);
 }
 
 int sem_mesh_set_precision(sem_mesh_t* m, int precision) {
@@ -322,6 +342,7 @@ int sem_lapl_geom(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y
   OperatorSet* ops = nullptr;
   SEM_CHECK(make_operator_set(Dr, Ds, nr, &ops));
   Grid g;
+  std::memset(&g, 0, sizeof(g));
   g.n = nr;
   g.Ex = Ex;
   g.Ey = Ey;

@@ -214,6 +214,8 @@ int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cuda
 
 }  // namespace sem
 
+using sem::cuda_error;
+
 extern "C" {
 
 int sem_timing_enable(int on) {

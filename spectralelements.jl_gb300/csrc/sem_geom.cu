@@ -87,14 +87,10 @@ __global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, long 
     b[i] = (float)a[i];
 }
 
-__global__ void k_maskfield(double* __restrict__ out, Grid g, int has_bc) {
-  const long long total = g.NX * g.NY;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long c = idx / g.NX;
-    const long long r = idx - c * g.NX;
-    out[idx] = (!has_bc || mask_keep(r, c, g.NX, g.NY, g.topo)) ? 1.0 : 0.0;
-  }
+__global__ void k_maskfield(double* __restrict__ out, Grid g) {
+  for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
+    out[idx] = ((g.rinfo[r] | g.cinfo[c]) & L_ZERO) ? 0.0 : 1.0;
+  });
 }
 
 void fill_geom_args(GeomArgs& a, const sem_mesh* m) {
@@ -155,7 +151,7 @@ int export_field(const sem_mesh* m, int which, double* out, cudaStream_t s) {
     case SEM_FIELD_MULT:
       return launch_mult(m->g, out, s);
     case SEM_FIELD_MASK:
-      k_maskfield<<<blocks_for(m->g.NX * m->g.NY), 256, 0, s>>>(out, m->g, m->has_bc ? 1 : 0);
+      k_maskfield<<<blocks_for(m->g.NX * m->g.NY), 256, 0, s>>>(out, m->g);
       SEM_CUDA(cudaGetLastError());
       return SEM_OK;
     case SEM_FIELD_JAC:

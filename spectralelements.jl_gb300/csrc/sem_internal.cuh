@@ -51,12 +51,46 @@ enum : unsigned {
   M_MULT1 = 1u << 12,  // solver dots without the SEM multiplicity weights
 };
 
+// per-row / per-column structure bits (device tables of a mesh handle)
+enum : unsigned char {
+  L_LEFT = 1,    // partner copy is the previous row/column
+  L_RIGHT = 2,   // partner copy is the next row/column
+  L_WRAPE = 4,   // partner copy is the last row/column (periodic wrap)
+  L_WRAPS = 8,   // partner copy is the first row/column (periodic wrap)
+  L_ZERO = 16,   // Dirichlet row/column under the handle's bc
+};
+constexpr unsigned char L_COPY2 = L_LEFT | L_RIGHT | L_WRAPE | L_WRAPS;
+
 struct Grid {
   int n;        // GLL points per direction (nr == ns)
   int Ex, Ey;
   int64_t NX, NY;  // local rows n*Ex, local columns n*Ey
   unsigned topo;   // M_PERX | M_PERY | M_D* bits
+  const unsigned char* rinfo;  // device, NX entries of L_* bits (may be NULL off-handle)
+  const unsigned char* cinfo;  // device, NY entries
 };
+
+// host: L_* bits of local line l (row or column) of a direction with E
+// elements of n points; zero_first/zero_last mark Dirichlet ends
+inline unsigned char line_info(int64_t l, int n, int E, bool per, bool zero_first, bool zero_last) {
+  const int64_t NL = (int64_t)n * E;
+  const int64_t e = l / n;
+  const int i = (int)(l - e * n);
+  unsigned char b = 0;
+  if (i == 0) b |= e > 0 ? L_LEFT : (per ? L_WRAPE : 0);
+  if (i == n - 1) b |= e < E - 1 ? L_RIGHT : (per ? L_WRAPS : 0);
+  if (!per && ((zero_first && l == 0) || (zero_last && l == NL - 1))) b |= L_ZERO;
+  return b;
+}
+
+// partner line of l under the L_* bits, or -1
+__host__ __device__ inline int64_t line_partner(int64_t l, unsigned char b, int64_t NL) {
+  if (b & L_LEFT) return l - 1;
+  if (b & L_RIGHT) return l + 1;
+  if (b & L_WRAPE) return NL - 1;
+  if (b & L_WRAPS) return 0;
+  return -1;
+}
 
 // mask value of local point (r, c) under the topology bits
 __host__ __device__ inline bool mask_keep(int64_t r, int64_t c, int64_t NX, int64_t NY,
@@ -137,6 +171,7 @@ struct sem_mesh {
   // solver workspace (lazily created)
   void* ws;
   size_t ws_bytes;
+  unsigned char* info;     // device L_* tables: NX row entries then NY column entries
 };
 
 namespace sem {
@@ -179,4 +214,24 @@ int launch_abu(const double* As, int ma, int na, const double* Br, int mb, int n
                const double* u, int m, int n, double* v, cudaStream_t s);
 
 unsigned topo_bits(const Grid& g);
+int upload_line_info(sem_mesh* m);
+
+// Visit every local point (r, c) of g with a block-uniform loop (all threads
+// of a block run the same number of trips, so block reductions may follow):
+// blocks walk chunks of blockDim.x consecutive rows of one column.
+template <class F>
+__device__ __forceinline__ void for_each_point(const Grid& g, F&& f) {
+  const unsigned NX = (unsigned)g.NX, NY = (unsigned)g.NY;
+  const unsigned nrc = (NX + blockDim.x - 1) / blockDim.x;
+  const unsigned total = nrc * NY;
+  for (unsigned b = blockIdx.x; b < total; b += gridDim.x) {
+    const unsigned c = b / nrc;
+    const unsigned r = (b - c * nrc) * blockDim.x + threadIdx.x;
+    if (r < NX) f(r, c, (long long)r + (long long)c * NX);
+  }
+}
+
+__device__ __forceinline__ int copies_at(const Grid& g, unsigned r, unsigned c) {
+  return ((g.rinfo[r] & L_COPY2) ? 2 : 1) * ((g.cinfo[c] & L_COPY2) ? 2 : 1);
+}
 }  // namespace sem

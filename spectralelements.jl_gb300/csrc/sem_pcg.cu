@@ -35,12 +35,9 @@ struct Scalars {
   int k, maxiter, done, converged, nan;
 };
 
-__device__ __forceinline__ double mult_at(long long idx, const Grid& g) {
+__device__ __forceinline__ double mult_at(unsigned r, unsigned c, const Grid& g) {
   if (g.topo & M_MULT1) return 1.0;
-  const long long c = idx / g.NX;
-  const long long r = idx - c * g.NX;
-  const int cc = copies_1d(r, g.n, g.Ex, (g.topo & M_PERX) != 0) *
-                 copies_1d(c, g.n, g.Ey, (g.topo & M_PERY) != 0);
+  const int cc = copies_at(g, r, c);
   return cc == 1 ? 1.0 : (cc == 2 ? 0.5 : 0.25);
 }
 
@@ -103,18 +100,16 @@ __device__ __forceinline__ void final_reduce(const double* part, int nparts,
 template <class T, class TB>
 __global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
                        T* __restrict__ p, const T* __restrict__ dinv, double* part, Grid g) {
-  const long long L = g.NX * g.NY;
   double t = 0.0, rm = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
-       i += (long long)gridDim.x * blockDim.x) {
+  for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     const T ri = (T)b[i];
     x[i] = (T)0;
     p[i] = (T)0;
     r[i] = ri;
     const T h = dinv ? ri * dinv[i] : ri;
-    t += (double)ri * (double)h * mult_at(i, g);
+    t += (double)ri * (double)h * mult_at(rr, cc, g);
     rm = nanmax(rm, fabs((double)ri));
-  }
+  });
   double v[2] = {t, rm};
   const bool mx[2] = {false, true};
   block_reduce<2>(v, mx, part);
@@ -155,11 +150,10 @@ template <class T>
 __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, double* part,
                           const Scalars* sc, Grid g) {
   if (sc->done) return;
-  const long long L = g.NX * g.NY;
   double s = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
-       i += (long long)gridDim.x * blockDim.x)
-    s += (double)p[i] * (double)Ap[i] * mult_at(i, g);
+  for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
+    s += (double)p[i] * (double)Ap[i] * mult_at(rr, cc, g);
+  });
   double v[1] = {s};
   const bool mx[1] = {false};
   block_reduce<1>(v, mx, part);
@@ -182,18 +176,16 @@ __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restri
                          const T* __restrict__ Ap, const T* __restrict__ dinv, double* part,
                          const Scalars* sc, Grid g) {
   if (sc->done) return;
-  const long long L = g.NX * g.NY;
   const T alpha = (T)sc->alpha;
   double t = 0.0, rm = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
-       i += (long long)gridDim.x * blockDim.x) {
+  for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     x[i] = x[i] + alpha * p[i];
     const T ri = r[i] - alpha * Ap[i];
     r[i] = ri;
     const T h = dinv ? ri * dinv[i] : ri;
-    t += (double)ri * (double)h * mult_at(i, g);
+    t += (double)ri * (double)h * mult_at(rr, cc, g);
     rm = nanmax(rm, fabs((double)ri));
-  }
+  });
   double v[2] = {t, rm};
   const bool mx[2] = {false, true};
   block_reduce<2>(v, mx, part);
@@ -255,26 +247,17 @@ __global__ void k_diag_local(const __grid_constant__ DiagArgs a, const double* _
 
 // dinv = keep ? 1/d : 1 (masked entries of the diagonal are set to 1)
 template <class T>
-__global__ void k_diag_inv(const double* __restrict__ d, T* __restrict__ dinv, Grid g,
-                           unsigned topo, int has_mask) {
-  const long long L = g.NX * g.NY;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < L;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long c = idx / g.NX;
-    const long long r = idx - c * g.NX;
-    const bool keep = !has_mask || mask_keep(r, c, g.NX, g.NY, topo);
+__global__ void k_diag_inv(const double* __restrict__ d, T* __restrict__ dinv, Grid g) {
+  for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
+    const bool keep = !((g.rinfo[r] | g.cinfo[c]) & L_ZERO);
     dinv[idx] = keep ? (T)(1.0 / d[idx]) : (T)1;
-  }
+  });
 }
 
-__global__ void k_diag_mask(double* __restrict__ d, Grid g, unsigned topo) {
-  const long long L = g.NX * g.NY;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < L;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long c = idx / g.NX;
-    const long long r = idx - c * g.NX;
-    if (!mask_keep(r, c, g.NX, g.NY, topo)) d[idx] = 1.0;
-  }
+__global__ void k_diag_mask(double* __restrict__ d, Grid g) {
+  for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
+    if ((g.rinfo[r] | g.cinfo[c]) & L_ZERO) d[idx] = 1.0;
+  });
 }
 
 // r = b - Ax, max|r| partials (outer FP64 residual of the mixed solver)
@@ -476,7 +459,7 @@ int sem_jacobi_diag(sem_mesh_t* m, const double* nu_field, double nu, double k, 
   SEM_CHECK(get_ws(m, false, w));
   SEM_CHECK(diag_build(m, nu_field, nu, k, diag, w.d, s));
   if (m->has_bc) {
-    k_diag_mask<<<nblocks(m->g.NX * m->g.NY) * 4, kRT, 0, s>>>(diag, m->g, m->g.topo);
+    k_diag_mask<<<nblocks(m->g.NX * m->g.NY) * 4, kRT, 0, s>>>(diag, m->g);
     SEM_CUDA(cudaGetLastError());
   }
   return SEM_OK;
@@ -526,9 +509,9 @@ int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
   if (o->mult_ones) gv.topo |= M_MULT1;
   if (jac) {
     SEM_CHECK(diag_build(m, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
-    k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, m->g, m->g.topo, m->has_bc ? 1 : 0);
+    k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, m->g);
     if (prec == SEM_MIXED)
-      k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, m->g, m->g.topo, m->has_bc ? 1 : 0);
+      k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, m->g);
     SEM_CUDA(cudaGetLastError());
   }
   Scalars res;

@@ -17,63 +17,40 @@ inline unsigned grid_for(long long n, int threads = kThreads, long long cap = 15
   return (unsigned)b;
 }
 
-// partner of local row r under direct-stiffness summation, or -1
-__device__ __forceinline__ long long partner(long long r, int n, int E, long long NX, bool per) {
-  const long long e = r / n;
-  const int i = (int)(r - e * n);
-  if (i == 0) {
-    if (e > 0) return r - 1;
-    if (per) return NX - 1;
-  }
-  if (i == n - 1) {
-    if (e < E - 1) return r + 1;
-    if (per) return 0;
-  }
-  return -1;
-}
-
 // QQ' u: x sums in increasing row order, then y sums in increasing column
 // order, so every copy of a global node receives bit-identical values
 // (src/gatherScatter.jl:8-16 applies QQtx then QQty).
 __global__ void k_gather_scatter(const double* __restrict__ u, double* __restrict__ out, Grid g,
                                  unsigned mode) {
-  const long long total = g.NX * g.NY;
-  const bool perx = (mode & M_PERX) != 0, pery = (mode & M_PERY) != 0;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long c = idx / g.NX;
-    const long long r = idx - c * g.NX;
-    const long long pr = partner(r, g.n, g.Ex, g.NX, perx);
-    const long long pc = partner(c, g.n, g.Ey, g.NY, pery);
+  const long long NX = g.NX;
+  for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
+    const unsigned char rb = g.rinfo[r], cb = g.cinfo[c];
+    const long long pr = line_partner(r, rb, g.NX);
+    const long long pc = line_partner(c, cb, g.NY);
     const long long r0 = (pr >= 0 && pr < r) ? pr : r;
-    const long long r1 = (pr >= 0 && pr < r) ? r : pr;
+    const long long r1 = (pr >= 0 && pr < r) ? (long long)r : pr;
     auto xsum = [&](long long cc) {
-      double s = u[r0 + cc * g.NX];
-      if (r1 >= 0) s += u[r1 + cc * g.NX];
+      double s = u[r0 + cc * NX];
+      if (r1 >= 0) s += u[r1 + cc * NX];
       return s;
     };
     double v;
     if (pc < 0) {
       v = xsum(c);
     } else {
-      const long long c0 = pc < c ? pc : c, c1 = pc < c ? c : pc;
+      const long long c0 = pc < c ? pc : (long long)c, c1 = pc < c ? (long long)c : pc;
       v = xsum(c0) + xsum(c1);
     }
-    if ((mode & M_MASK) && !mask_keep(r, c, g.NX, g.NY, mode)) v = v * 0.0;
+    if ((mode & M_MASK) && ((rb | cb) & L_ZERO)) v = v * 0.0;
     out[idx] = v;
-  }
+  });
 }
 
-__global__ void k_mask_bc(const double* __restrict__ u, double* __restrict__ out, Grid g,
-                          unsigned topo) {
-  const long long total = g.NX * g.NY;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long c = idx / g.NX;
-    const long long r = idx - c * g.NX;
+__global__ void k_mask_bc(const double* __restrict__ u, double* __restrict__ out, Grid g) {
+  for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
     const double v = u[idx];
-    out[idx] = mask_keep(r, c, g.NX, g.NY, topo) ? v : v * 0.0;
-  }
+    out[idx] = ((g.rinfo[r] | g.cinfo[c]) & L_ZERO) ? v * 0.0 : v;
+  });
 }
 
 __global__ void k_mask_array(const double* __restrict__ M, const double* __restrict__ u,
@@ -92,16 +69,10 @@ __global__ void k_mass(const double* __restrict__ B, const double* __restrict__ 
 
 // mult = 1 ./ QQ'(ones) (src/mesh.jl:94-96): 1 / (copies_x * copies_y)
 __global__ void k_mult(double* __restrict__ out, Grid g) {
-  const long long total = g.NX * g.NY;
-  const bool perx = (g.topo & M_PERX) != 0, pery = (g.topo & M_PERY) != 0;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long c = idx / g.NX;
-    const long long r = idx - c * g.NX;
-    const double cx = copies_1d(r, g.n, g.Ex, perx);
-    const double cy = copies_1d(c, g.n, g.Ey, pery);
-    out[idx] = 1.0 / (cx * cy);
-  }
+  for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
+    const int cc = copies_at(g, r, c);
+    out[idx] = cc == 1 ? 1.0 : (cc == 2 ? 0.5 : 0.25);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -195,13 +166,15 @@ unsigned topo_bits(const Grid& g) { return g.topo; }
 
 int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode,
                           cudaStream_t s) {
+  if (!g.rinfo) return set_error(SEM_ERR_BAD_ARG, "gather-scatter needs a mesh handle");
   k_gather_scatter<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(u, out, g, mode);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
 }
 
 int launch_mask_bc(const Grid& g, const double* u, double* out, unsigned topo, cudaStream_t s) {
-  k_mask_bc<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(u, out, g, topo);
+  (void)topo;
+  k_mask_bc<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(u, out, g);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
 }

@@ -118,7 +118,7 @@ def test_device_geometry(gpu, n, Ex, Ey, per):
     ((18, 27), (9, 9), None),
     ((12, 10), (3, 5), (7, 4)),
     ((8, 6), (4, 2), None),
-    ((6, 4), None, (3, 4)),  # reshape(u, 4, :) spans columns
+    ((6, 4), None, (2, 4)),  # reshape(u, 4, :) spans columns
     ((64, 96), (32, 32), (32, 32)),
 ])
 def test_abu(gpu, shape_u, As, Br):

@@ -50,8 +50,14 @@ def _header_functions():
     return sorted(set(re.findall(r"\b(sem_[a-z0-9_]+)\s*\(", src)))
 
 
-def test_library_exports_every_declared_symbol():
-    lib = _lib.load()
+@pytest.fixture(scope="module")
+def built():
+    _lib.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = built
     names = _header_functions()
     assert "sem_pcg" in names and "sem_lapl" in names
     for name in names:
@@ -60,8 +66,8 @@ def test_library_exports_every_declared_symbol():
     assert lib.sem_abi_version() == 1
 
 
-def test_argument_validation_needs_no_gpu():
-    lib = _lib.load()
+def test_argument_validation_needs_no_gpu(built):
+    lib = built
     h = ctypes.c_void_p()
     assert lib.sem_mesh_create(None, ctypes.byref(h)) == _lib.SEM_ERR_BAD_ARG
     assert b"NULL" in lib.sem_last_error()
