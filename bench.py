@@ -155,6 +155,8 @@ def run_ours(args, rank, world, local_rank):
     sampler.start()
 
     msh = S.Mesh(N_ORDER + 1, N_ORDER + 1, E_X, E_Y, (False, False), sin_deform(AMP), bc="DDDD")
+    tune = {name: msh.autotune(prec) for name, prec in
+            (("f64_df", S.SEM_F64_DF), ("f64", S.SEM_F64), ("f32", S.SEM_F32))}
     nx, ny = msh.shape
     L = nx * ny
     G = unique_dof(N_ORDER + 1, E_X, E_Y)
@@ -263,7 +265,8 @@ def run_ours(args, rank, world, local_rank):
                    "arith": "double-float (FP32 pairs) with FP64 storage; rel-L2 vs native FP64 "
                             f"{rel:.2e}",
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "autotune": tune},
         "roofline": roofline, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clocks,
         "f64_native_apply": {"ms": t64, "GDOF/s": G / (t64 * 1e-3) / 1e9},
     }
@@ -335,6 +338,8 @@ def bench_pcg(S, msh, stream):
         "mixed_over_fp64": dt64 / dtm}
     # cfg1 / cfg3: Poisson 8x8, N=8, amp 0.1, exact solution sin(pi x) sin(pi y), 1e-10
     m1 = S.Mesh(9, 9, 8, 8, (False, False), sin_deform(0.1), bc="DDDD")
+    m1.autotune(S.SEM_F64_DF)
+    m1.autotune(S.SEM_F32)
     ut = torch.sin(np.pi * m1.x) * torch.sin(np.pi * m1.y)
     f1 = 2 * np.pi ** 2 * ut
     M1 = S.generateMask("DDDD", m1)
@@ -369,12 +374,13 @@ def bench_sweep(S, stream):
     res = {}
     for N, E in ((4, 500), (8, 256), (12, 167), (16, 125)):
         m = S.Mesh(N + 1, N + 1, E, E, (False, False), sin_deform(AMP), bc="DDDD")
+        tv = m.autotune()
         u = S.as_local(torch.rand(m.shape, dtype=torch.float64, device="cuda") * 2 - 1)
         op = S.HelmholtzOp(m, NU, LAM)
         ms = time_apply(lambda: op(u), stream, 10)
         G = unique_dof(N + 1, E, E)
         L = (N + 1) ** 2 * E * E
-        res[f"N{N}_E{E}"] = {"GDOF/s": G / (ms * 1e-3) / 1e9, "ms": ms,
+        res[f"N{N}_E{E}"] = {"GDOF/s": G / (ms * 1e-3) / 1e9, "ms": ms, "variant": tv["chosen"],
                              "GB/s_alg": BYTES_PER_LOCAL * L / (ms * 1e-3) / 1e9}
         del m
     return res

@@ -93,6 +93,15 @@ int sem_mesh_destroy(sem_mesh_t* mesh);
 int sem_mesh_set_bc(sem_mesh_t* mesh, const char* bc);
 /* select the arithmetic of the fused FP64 operators (SEM_F64 or SEM_F64_DF) */
 int sem_mesh_set_precision(sem_mesh_t* mesh, int precision);
+/* autotuner (no counterpart in the reference): time every variant of the fused
+ * element-operator kernel (direct loads / cp.async-staged inputs) on this mesh,
+ * running mask(QQ'(hlmz)) on scratch fields in the given precision (SEM_F64,
+ * SEM_F64_DF or SEM_F32), and keep the fastest for all later calls of that
+ * precision.  ms_out (nullable) receives one time per variant; chosen
+ * (nullable) the variant kept.  Synchronous. */
+int sem_mesh_autotune(sem_mesh_t* mesh, int precision, double* ms_out, int* chosen);
+/* pin a kernel variant (0 = direct loads, 1 = staged) for one precision */
+int sem_mesh_set_variant(sem_mesh_t* mesh, int precision, int variant);
 /* copy one geometry field (enum sem_field) into a caller device buffer */
 int sem_mesh_field(sem_mesh_t* mesh, int which, double* out, sem_stream_t stream);
 /* sizes: local rows (nr*Ex), local columns (ns*Ey) */

@@ -200,6 +200,74 @@ int sem_mesh_set_precision(sem_mesh_t* m, int precision) {
   return SEM_OK;
 }
 
+int sem_mesh_set_variant(sem_mesh_t* m, int precision, int variant) {
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  if (precision < SEM_F64 || precision > SEM_F32) return set_error(SEM_ERR_BAD_ARG, "bad precision");
+  if (variant < 0 || variant >= kVariants) return set_error(SEM_ERR_BAD_ARG, "bad variant");
+  m->variant[precision] = variant;
+  return SEM_OK;
+}
+
+int sem_mesh_autotune(sem_mesh_t* m, int precision, double* ms_out, int* chosen) {
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  if (precision < SEM_F64 || precision > SEM_F32) return set_error(SEM_ERR_BAD_ARG, "bad precision");
+  SEM_CHECK(check_device(m));
+  cudaStream_t s = nullptr;
+  SEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const long long L = m->g.NX * m->g.NY;
+  const bool f32 = precision == SEM_F32;
+  if (f32) SEM_CHECK(ensure_f32_geometry(m, s));
+  void* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = SEM_OK;
+  double best = 1e30;
+  int bestv = 0;
+  cudaError_t e = cudaMalloc(&out, (size_t)L * (f32 ? 4 : 8));
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) st = cuda_error(e, "autotune set-up");
+  ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
+  c.u = f32 ? (const void*)m->G11_f : (const void*)m->x;  // any smooth non-zero field
+  c.out = out;
+  c.G11 = f32 ? (const void*)m->G11_f : (const void*)m->G11;
+  c.G12 = f32 ? (const void*)m->G12_f : (const void*)m->G12;
+  c.G22 = f32 ? (const void*)m->G22_f : (const void*)m->G22;
+  c.B = f32 ? (const void*)m->B_f : (const void*)m->B;
+  c.nu_s = 0.5;
+  c.k_s = 1.0;
+  c.mode = m->g.topo | M_STIFF | M_MASS | M_GS | (m->has_bc ? M_MASK : 0u);
+  c.precision = precision;
+  for (int v = 0; v < kVariants && st == SEM_OK; ++v) {
+    c.variant = v;
+    for (int w = 0; w < 2 && st == SEM_OK; ++w) st = launch_apply(m->g, m->ops, c, s);
+    if (st != SEM_OK) break;
+    if ((e = cudaEventRecord(e0, s)) != cudaSuccess) { st = cuda_error(e, "event"); break; }
+    for (int r = 0; r < 5 && st == SEM_OK; ++r) st = launch_apply(m->g, m->ops, c, s);
+    if (st != SEM_OK) break;
+    float ms = 0.f;
+    if ((e = cudaEventRecord(e1, s)) != cudaSuccess || (e = cudaEventSynchronize(e1)) != cudaSuccess ||
+        (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) {
+      st = cuda_error(e, "autotune timing");
+      break;
+    }
+    const double t = ms / 5.0;
+    if (ms_out) ms_out[v] = t;
+    if (t < best) {
+      best = t;
+      bestv = v;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (out) cudaFree(out);
+  cudaStreamDestroy(s);
+  if (st != SEM_OK) return st;
+  m->variant[precision] = bestv;
+  if (chosen) *chosen = bestv;
+  return SEM_OK;
+}
+
 int sem_mesh_field(sem_mesh_t* m, int which, double* out, sem_stream_t stream) {
   if (!m || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
   SEM_CHECK(check_device(m));
@@ -255,6 +323,7 @@ static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, con
   c.mode = mode | (nu ? M_NU : 0u);
   c.precision = m->precision;
   c.skip = nullptr;
+  c.variant = m->variant[m->precision];
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 
@@ -297,6 +366,7 @@ int sem_varcoef(sem_mesh_t* m, const double* nu_field, double k, const double* u
   c.k_s = k;
   c.mode = mode;
   c.precision = m->precision;
+  c.variant = m->variant[m->precision];
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 

@@ -5,12 +5,11 @@
 #include <utility>
 #include <vector>
 
-#include "sem_apply_kernels.cuh"
+#include "sem_apply_launch.cuh"
 
 namespace sem {
 
 // ---- event timing of the fused kernel launches (instrumentation)
-namespace {
 std::mutex g_tmu;
 bool g_timing = false;
 std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_pool;  // recycled event pairs
@@ -30,15 +29,18 @@ std::pair<cudaEvent_t, cudaEvent_t>* timing_slot() {
   }
   return &g_pool[g_used++];
 }
-}  // namespace
 
-struct OperatorSet {
-  int n;
-  // even-odd coefficients in double for Dr, Dr', Ds, Ds' (index 0..3); each
-  // block holds A (m*m), C (m*m), cm (m), mr (m)
-  std::vector<double> eo[4];
-  std::vector<double> Dr, Ds;  // dense, column-major
-};
+size_t max_smem_optin() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 48 * 1024;
+  if (!cached[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) v = 48 * 1024;
+    cached[dev] = v;
+  }
+  return (size_t)cached[dev];
+}
 
 bool is_centro_antisymmetric(const double* D, int n, double rel_tol) {
   double mx = 0.0;
@@ -92,77 +94,6 @@ int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** o
 
 void free_operator_set(OperatorSet* o) { delete o; }
 
-template <class P, int N>
-static void fill_eo(EOCoef<N, typename P::v>& c, const std::vector<double>& src) {
-  constexpr int M = N / 2;
-  const double* A = src.data();
-  const double* C = A + M * M;
-  const double* cm = C + M * M;
-  const double* mr = cm + M;
-  for (int i = 0; i < M; ++i)
-    for (int k = 0; k < M; ++k) {
-      c.A[i][k] = P::from_double(A[i * M + k]);
-      c.Cc[i][k] = P::from_double(C[i * M + k]);
-    }
-  for (int i = 0; i < M; ++i) {
-    c.cm[i] = P::from_double(cm[i]);
-    c.mr[i] = P::from_double(mr[i]);
-  }
-}
-
-template <class P, int N>
-static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
-                          cudaStream_t s) {
-  typedef TileShape<N> TS;
-  typedef typename P::io io;
-  ApplyArgs<P, N> a;
-  std::memset(&a, 0, sizeof(a));
-  a.u = static_cast<const io*>(c.u);
-  a.out = static_cast<io*>(c.out);
-  a.G11 = static_cast<const io*>(c.G11);
-  a.G12 = static_cast<const io*>(c.G12);
-  a.G22 = static_cast<const io*>(c.G22);
-  a.B = static_cast<const io*>(c.B);
-  a.nu = static_cast<const io*>(c.nu);
-  a.nu_s = P::from_double(c.nu_s);
-  a.k_s = P::from_double(c.k_s);
-  a.Ex = g.Ex;
-  a.Ey = g.Ey;
-  a.NX = g.NX;
-  a.mode = c.mode;
-  a.skip = c.skip;
-  fill_eo<P, N>(a.Dr, ops->eo[0]);
-  fill_eo<P, N>(a.Drt, ops->eo[1]);
-  fill_eo<P, N>(a.Ds, ops->eo[2]);
-  fill_eo<P, N>(a.Dst, ops->eo[3]);
-  const size_t smem = 2ull * TS::TX * TS::TY * TS::ES * sizeof(typename P::v);
-  auto kern = k_apply<P, N, TS::TX, TS::TY>;
-  if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
-  auto* ev = timing_slot();
-  if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
-  kern<<<grid, TS::THREADS, smem, s>>>(a);
-  SEM_CUDA(cudaGetLastError());
-  if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
-  return SEM_OK;
-}
-
-template <class P>
-static int launch_apply_p(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
-                          cudaStream_t s) {
-  switch (g.n) {
-#define SEM_CASE(NN) \
-  case NN:           \
-    return launch_apply_n<P, NN>(g, ops, c, s);
-    SEM_CASE(2) SEM_CASE(3) SEM_CASE(4) SEM_CASE(5) SEM_CASE(6) SEM_CASE(7) SEM_CASE(8)
-    SEM_CASE(9) SEM_CASE(10) SEM_CASE(11) SEM_CASE(12) SEM_CASE(13) SEM_CASE(14)
-    SEM_CASE(15) SEM_CASE(16) SEM_CASE(17)
-#undef SEM_CASE
-    default:
-      return set_error(SEM_ERR_UNSUPPORTED, "no fused kernel for n = %d", g.n);
-  }
-}
-
 // tile shape of the fused kernel for a given n (host mirror of TileShape)
 static void tile_of(int n, int* TX, int* TY) {
   *TX = 8;
@@ -201,11 +132,11 @@ int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s) {
   int st;
   if (c.precision == SEM_F64)
-    st = launch_apply_p<PF64>(g, ops, c, s);
+    st = launch_apply_f64(g, ops, c, s);
   else if (c.precision == SEM_F64_DF)
-    st = launch_apply_p<PDF>(g, ops, c, s);
+    st = launch_apply_df(g, ops, c, s);
   else if (c.precision == SEM_F32)
-    st = launch_apply_p<PF32>(g, ops, c, s);
+    st = launch_apply_f32(g, ops, c, s);
   else
     return set_error(SEM_ERR_BAD_ARG, "unknown precision %d", c.precision);
   if (st != SEM_OK) return st;

@@ -45,6 +45,7 @@ struct ApplyArgs {
   long long NX;
   unsigned mode;
   const int* skip;
+  int slot_g, slot_b, slot_nu;  // staged-variant shared-memory slots (-1: not staged)
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
 
@@ -57,6 +58,30 @@ struct TileShape {
   static constexpr int THREADS = TX * TY * N;
 };
 
+// resident blocks per SM requested from the register allocator: the
+// double-float kernels are latency bound, so up to n = 9 they trade a few
+// spilled registers for a third resident block
+template <class P, int N, bool STAGE>
+struct MinBlocks {
+  static constexpr int value =
+      STAGE ? (N <= 9 ? 2 : 1)
+            : ((P::kPrecision == SEM_F64_DF) ? (N <= 9 ? 3 : (N <= 12 ? 2 : 1))
+                                              : (N <= 10 ? 3 : (N <= 12 ? 2 : 1)));
+};
+
+// asynchronous global -> shared copies (LDGSTS); each thread later reads only
+// the entries it copied itself, so cp.async.wait_all is the only fence needed
+template <class IO>
+__device__ __forceinline__ void cp_async(IO* dst_smem, const IO* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  if (sizeof(IO) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // y = D x for a centro-antisymmetric D given in even-odd form
 template <class P, int N>
 __device__ __forceinline__ void eo_apply(const EOCoef<N, typename P::v>& D,
@@ -66,8 +91,8 @@ __device__ __forceinline__ void eo_apply(const EOCoef<N, typename P::v>& D,
   V e[M], o[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    e[k] = P::add(x[k], x[N - 1 - k]);
-    o[k] = P::sub(x[k], x[N - 1 - k]);
+    e[k] = P::add_u(x[k], x[N - 1 - k]);
+    o[k] = P::sub_u(x[k], x[N - 1 - k]);
   }
 #pragma unroll
   for (int i = 0; i < M; ++i) {
@@ -78,14 +103,14 @@ __device__ __forceinline__ void eo_apply(const EOCoef<N, typename P::v>& D,
 #pragma unroll
     for (int k = 1; k < M; ++k) t = P::fma(D.Cc[i][k], e[k], t);
     if (N & 1) t = P::fma(D.cm[i], x[M], t);
-    y[i] = P::add(s, t);
-    y[N - 1 - i] = P::sub(s, t);
+    y[i] = P::add_u(s, t);
+    y[N - 1 - i] = P::sub_u(s, t);
   }
   if (N & 1) {
     V s = P::mul(D.mr[0], o[0]);
 #pragma unroll
     for (int k = 1; k < M; ++k) s = P::fma(D.mr[k], o[k], s);
-    y[M] = P::fin(s);
+    y[M] = s;
   }
 }
 
@@ -96,16 +121,18 @@ __host__ __device__ inline bool xcross_row(int ex, int i, int n, int Ex, int TX,
   return false;
 }
 
-template <class P, int N, int TX, int TY>
-__global__ void __launch_bounds__(TX* TY* N)
+template <class P, int N, int TX, int TY, bool STAGE>
+__global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     k_apply(const __grid_constant__ ApplyArgs<P, N> a) {
   typedef typename P::v V;
   typedef typename P::io IO;
   constexpr int SP = N | 1;
   constexpr int ES = N * SP;
+  constexpr int TE = TX * TY * ES;  // entries of one tile-sized buffer
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* S1 = reinterpret_cast<V*>(smem_raw);
-  V* S2 = S1 + TX * TY * ES;
+  V* S2 = S1 + TE;
+  IO* R = reinterpret_cast<IO*>(S2 + TE);  // staged raw inputs (STAGE): slot * TE + ...
 
   if (a.skip && *a.skip) return;
   const int t = threadIdx.x;
@@ -122,6 +149,30 @@ __global__ void __launch_bounds__(TX* TY* N)
   const bool stiff = (mode & M_STIFF) != 0;
   V* s1 = S1 + elem * ES;
   V* s2 = S2 + elem * ES;
+  const int rofs = elem * ES + lane;  // this thread's row inside a staged slot (+ j*SP)
+
+  // ---- staged variant: issue every later global read of this row now
+  if (STAGE) {
+    if (valid) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const long long gi = base + (long long)j * NX;
+        if (a.slot_g >= 0) {
+          cp_async(R + (a.slot_g + 0) * TE + rofs + j * SP, a.G11 + gi);
+          cp_async(R + (a.slot_g + 1) * TE + rofs + j * SP, a.G12 + gi);
+          cp_async(R + (a.slot_g + 2) * TE + rofs + j * SP, a.G22 + gi);
+        }
+        if (a.slot_b >= 0) cp_async(R + a.slot_b * TE + rofs + j * SP, a.B + gi);
+        if (a.slot_nu >= 0) cp_async(R + a.slot_nu * TE + rofs + j * SP, a.nu + gi);
+      }
+    }
+    cp_async_commit();
+  }
+  auto ldx = [&](const IO* gsrc, int slot, int j) -> V {
+    if (!valid) return P::zero();
+    if (STAGE && slot >= 0) return P::cvt(R[slot * TE + rofs + j * SP]);
+    return P::ld(gsrc + base + (long long)j * NX);
+  };
 
   // ---- A: row `lane` of u; y-direction derivative
   V u[N];
@@ -146,22 +197,22 @@ __global__ void __launch_bounds__(TX* TY* N)
     }
     __syncthreads();
     // ---- C: row `lane`; metric terms, transposed y-derivative
+    if (STAGE) cp_async_wait_all();
     V os[N];
     {
       V ws[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        const long long gi = base + (long long)j * NX;
-        V g11 = valid ? P::ld(a.G11 + gi) : P::zero();
-        V g12 = valid ? P::ld(a.G12 + gi) : P::zero();
-        V g22 = valid ? P::ld(a.G22 + gi) : P::zero();
+        V g11 = ldx(a.G11, a.slot_g, j);
+        V g12 = ldx(a.G12, a.slot_g < 0 ? -1 : a.slot_g + 1, j);
+        V g22 = ldx(a.G22, a.slot_g < 0 ? -1 : a.slot_g + 2, j);
         V ur = s2[j * SP + lane];
-        V wr = P::fin(P::fma(g11, ur, P::mul(g12, us[j])));
-        ws[j] = P::fin(P::fma(g12, ur, P::mul(g22, us[j])));
+        V wr = P::fma(g11, ur, P::mul(g12, us[j]));
+        ws[j] = P::fma(g12, ur, P::mul(g22, us[j]));
         if (mode & M_NUG) {
-          V nu = valid ? P::ld(a.nu + gi) : P::zero();
-          wr = P::fin(P::mul(nu, wr));
-          ws[j] = P::fin(P::mul(nu, ws[j]));
+          V nu = ldx(a.nu, a.slot_nu, j);
+          wr = P::mul(nu, wr);
+          ws[j] = P::mul(nu, ws[j]);
         }
         s1[j * SP + lane] = wr;
       }
@@ -184,7 +235,7 @@ __global__ void __launch_bounds__(TX* TY* N)
     if (mode & M_NU) {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        V nu = valid ? P::ld(a.nu + base + (long long)j * NX) : P::zero();
+        V nu = ldx(a.nu, a.slot_nu, j);
         res[j] = P::fin(P::mul(nu, res[j]));
       }
     } else {
@@ -196,10 +247,11 @@ __global__ void __launch_bounds__(TX* TY* N)
     for (int j = 0; j < N; ++j) res[j] = P::zero();
   }
   if (mode & M_MASS) {
+    if (STAGE && !stiff) cp_async_wait_all();
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      V b = valid ? P::ld(a.B + base + (long long)j * NX) : P::zero();
-      V kb = P::fin(P::mul(a.k_s, b));
+      V b = ldx(a.B, a.slot_b, j);
+      V kb = P::mul(a.k_s, b);
       res[j] = P::fin(P::fma(kb, u[j], res[j]));
     }
   }
@@ -245,7 +297,7 @@ __global__ void __launch_bounds__(TX* TY* N)
     IO val = P::st(res[j]);
     if (!raw && (mode & M_MASK)) {
       const long long col = (long long)ey * N + j;
-      if (!mask_keep(row, col, NX, NY, mode)) val = val * (IO)0;
+      if (!mask_keep(row, col, NX, NY, mode)) val = masked_zero(val);
     }
     a.out[base + (long long)j * NX] = val;
   }
@@ -290,8 +342,8 @@ __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
       const IO s = out[rl + c * f.NX] + out[rr + c * f.NX];
       IO sl = s, sr = s;
       if (msk) {
-        if (!mask_keep(rl, c, f.NX, f.NY, f.mode)) sl = s * (IO)0;
-        if (!mask_keep(rr, c, f.NX, f.NY, f.mode)) sr = s * (IO)0;
+        if (!mask_keep(rl, c, f.NX, f.NY, f.mode)) sl = masked_zero(s);
+        if (!mask_keep(rr, c, f.NX, f.NY, f.mode)) sr = masked_zero(s);
       }
       out[rl + c * f.NX] = sl;
       out[rr + c * f.NX] = sr;
@@ -308,8 +360,8 @@ __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
       const IO s = out[r + cl * f.NX] + out[r + cr * f.NX];
       IO sl = s, sr = s;
       if (msk) {
-        if (!mask_keep(r, cl, f.NX, f.NY, f.mode)) sl = s * (IO)0;
-        if (!mask_keep(r, cr, f.NX, f.NY, f.mode)) sr = s * (IO)0;
+        if (!mask_keep(r, cl, f.NX, f.NY, f.mode)) sl = masked_zero(s);
+        if (!mask_keep(r, cr, f.NX, f.NY, f.mode)) sr = masked_zero(s);
       }
       out[r + cl * f.NX] = sl;
       out[r + cr * f.NX] = sr;
@@ -330,7 +382,7 @@ __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
       for (int u = 0; u < 2; ++u)
         for (int v = 0; v < 2; ++v) {
           IO val = s;
-          if (msk && !mask_keep(rs[u], cs[v], f.NX, f.NY, f.mode)) val = s * (IO)0;
+          if (msk && !mask_keep(rs[u], cs[v], f.NX, f.NY, f.mode)) val = masked_zero(s);
           out[rs[u] + cs[v] * f.NX] = val;
         }
     }

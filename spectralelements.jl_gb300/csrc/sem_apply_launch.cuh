@@ -1,0 +1,124 @@
+// Launch templates of the fused element-operator kernel, instantiated once per
+// arithmetic policy in sem_apply_{f64,df,f32}.cu (parallel compilation).
+#pragma once
+
+#include <cstring>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "sem_apply_kernels.cuh"
+
+namespace sem {
+
+struct OperatorSet {
+  int n;
+  // even-odd coefficients in double for Dr, Dr', Ds, Ds' (index 0..3); each
+  // block holds A (m*m), C (m*m), cm (m), mr (m)
+  std::vector<double> eo[4];
+  std::vector<double> Dr, Ds;  // dense, column-major
+};
+
+std::pair<cudaEvent_t, cudaEvent_t>* timing_slot();
+size_t max_smem_optin();
+int launch_apply_f64(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
+int launch_apply_df(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
+int launch_apply_f32(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
+
+template <class P, int N>
+static void fill_eo(EOCoef<N, typename P::v>& c, const std::vector<double>& src) {
+  constexpr int M = N / 2;
+  const double* A = src.data();
+  const double* C = A + M * M;
+  const double* cm = C + M * M;
+  const double* mr = cm + M;
+  for (int i = 0; i < M; ++i)
+    for (int k = 0; k < M; ++k) {
+      c.A[i][k] = P::from_double(A[i * M + k]);
+      c.Cc[i][k] = P::from_double(C[i * M + k]);
+    }
+  for (int i = 0; i < M; ++i) {
+    c.cm[i] = P::from_double(cm[i]);
+    c.mr[i] = P::from_double(mr[i]);
+  }
+}
+
+template <class P, int N, bool STAGE>
+static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                          cudaStream_t s) {
+  typedef TileShape<N> TS;
+  typedef typename P::io io;
+  ApplyArgs<P, N> a;
+  std::memset(&a, 0, sizeof(a));
+  a.u = static_cast<const io*>(c.u);
+  a.out = static_cast<io*>(c.out);
+  a.G11 = static_cast<const io*>(c.G11);
+  a.G12 = static_cast<const io*>(c.G12);
+  a.G22 = static_cast<const io*>(c.G22);
+  a.B = static_cast<const io*>(c.B);
+  a.nu = static_cast<const io*>(c.nu);
+  a.nu_s = P::from_double(c.nu_s);
+  a.k_s = P::from_double(c.k_s);
+  a.Ex = g.Ex;
+  a.Ey = g.Ey;
+  a.NX = g.NX;
+  a.mode = c.mode;
+  a.skip = c.skip;
+  int nslot = 0;
+  a.slot_g = a.slot_b = a.slot_nu = -1;
+  if (STAGE) {
+    if (c.mode & M_STIFF) {
+      a.slot_g = nslot;
+      nslot += 3;
+    }
+    if (c.mode & M_MASS) a.slot_b = nslot++;
+    if (c.mode & (M_NU | M_NUG)) a.slot_nu = nslot++;
+  }
+  fill_eo<P, N>(a.Dr, ops->eo[0]);
+  fill_eo<P, N>(a.Drt, ops->eo[1]);
+  fill_eo<P, N>(a.Ds, ops->eo[2]);
+  fill_eo<P, N>(a.Dst, ops->eo[3]);
+  const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
+  const size_t smem = 2 * te * sizeof(typename P::v) + nslot * te * sizeof(io);
+  auto kern = k_apply<P, N, TS::TX, TS::TY, STAGE>;
+  if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
+  auto* ev = timing_slot();
+  if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
+  kern<<<grid, TS::THREADS, smem, s>>>(a);
+  SEM_CUDA(cudaGetLastError());
+  if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
+  return SEM_OK;
+}
+
+template <class P, int N>
+static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                          cudaStream_t s) {
+  if (c.variant == 1) {
+    typedef TileShape<N> TS;
+    const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
+    const int nslot = ((c.mode & M_STIFF) ? 3 : 0) + ((c.mode & M_MASS) ? 1 : 0) +
+                      ((c.mode & (M_NU | M_NUG)) ? 1 : 0);
+    const size_t smem = 2 * te * sizeof(typename P::v) + nslot * te * sizeof(typename P::io);
+    if (smem <= max_smem_optin()) return launch_apply_v<P, N, true>(g, ops, c, s);
+  }
+  return launch_apply_v<P, N, false>(g, ops, c, s);
+}
+
+template <class P>
+static int launch_apply_p(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                          cudaStream_t s) {
+  switch (g.n) {
+#define SEM_CASE(NN) \
+  case NN:           \
+    return launch_apply_n<P, NN>(g, ops, c, s);
+    SEM_CASE(2) SEM_CASE(3) SEM_CASE(4) SEM_CASE(5) SEM_CASE(6) SEM_CASE(7) SEM_CASE(8)
+    SEM_CASE(9) SEM_CASE(10) SEM_CASE(11) SEM_CASE(12) SEM_CASE(13) SEM_CASE(14)
+    SEM_CASE(15) SEM_CASE(16) SEM_CASE(17)
+#undef SEM_CASE
+    default:
+      return set_error(SEM_ERR_UNSUPPORTED, "no fused kernel for n = %d", g.n);
+  }
+}
+
+}  // namespace sem

@@ -41,6 +41,12 @@ __device__ __forceinline__ df df_add(df a, df b) {
   return fast_two_sum(s.h, e);
 }
 
+// unnormalised sum (no final renormalisation; l may reach a few ulp(h))
+__device__ __forceinline__ df df_add_u(df a, df b) {
+  df s = two_sum(a.h, b.h);
+  return {s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l))};
+}
+
 __device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
 
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
@@ -65,25 +71,65 @@ __device__ __forceinline__ df df_fma_u(df a, df b, df c) {
   return {s.h, __fadd_rn(s.l, __fadd_rn(pe, c.l))};
 }
 
+// GB300 runs every FP64 instruction, conversions included, at 1/64 of the FP32
+// rate, so the conversions below use integer operations only (plus one FP32
+// subtraction and, on the way out, one FP64 addition).
+//
 // double -> (h, l): h keeps the leading 24 significand bits (truncated), l the
-// next 23, both extracted with integer operations so the FP64 pipe stays idle.
-// Exponents outside [2^-103, 2^127) take the conversion instructions instead.
+// next 23; |x| in [2^-103, 2^128).  Outside that range: smaller magnitudes keep
+// h only (normal floats) or flush to a signed zero (below 2^-126, far below any
+// field value of this code's workloads), larger ones and Inf map to a signed
+// Inf and NaN stays NaN.
 __device__ __forceinline__ df d2df(double x) {
   const unsigned lo = (unsigned)__double2loint(x);
   const unsigned hi = (unsigned)__double2hiint(x);
   const unsigned ed = (hi >> 20) & 0x7ffu;
-  if (ed - 920u < 231u) {
-    const unsigned hb = (__funnelshift_l(lo, hi, 3) + 0x40000000u) | (hi & 0x80000000u);
-    const unsigned pb = (hb & 0xff800000u) - 0x0B800000u;
-    const unsigned fb = pb | ((lo >> 6) & 0x007fffffu);
-    return {__uint_as_float(hb), __fsub_rn(__uint_as_float(fb), __uint_as_float(pb))};
+  const unsigned sg = hi & 0x80000000u;
+  const unsigned hb = (__funnelshift_l(lo, hi, 3) + 0x40000000u) | sg;  // valid for ed in [897, 1150]
+  const unsigned pb = (hb & 0xff800000u) - 0x0B800000u;
+  const unsigned fb = pb | ((lo >> 6) & 0x007fffffu);
+  float h = __uint_as_float(hb);
+  float l = __fsub_rn(__uint_as_float(fb), __uint_as_float(pb));
+  if (ed - 920u >= 231u) {  // rare: out of the split range (selects, no FP64 instruction)
+    const bool nan = ed == 0x7ffu && (((hi & 0xfffffu) | lo) != 0u);
+    const unsigned big = sg | 0x7f800000u | (nan ? 0x00400000u : 0u);
+    h = __uint_as_float(ed > 1150u ? big : (ed >= 897u ? hb : sg));
+    l = 0.0f;
   }
-  const float h = __double2float_rz(x);
-  const float l = __double2float_rn(x - (double)h);
   return {h, l};
 }
 
-__device__ __forceinline__ double df2d(df a) { return (double)a.h + (double)a.l; }
+// exact float -> double by bit manipulation (subnormal floats flush to zero)
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned ef = (b >> 23) & 0xffu;
+  const unsigned sg = b & 0x80000000u;
+  unsigned hi = sg | ((ef + 896u) << 20) | ((b & 0x007fffffu) >> 3);
+  unsigned lo = b << 29;
+  if (ef == 0u) {
+    hi = sg;
+    lo = 0u;
+  } else if (ef == 0xffu) {
+    hi = sg | 0x7ff00000u | ((b & 0x007fffffu) ? 0x00080000u : 0u);
+    lo = 0u;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ double df2d(df a) { return __dadd_rn(f2d_bits(a.h), f2d_bits(a.l)); }
+
+// M .* v for M = 0 (src/mask.jl:14): a signed zero, NaN for Inf/NaN inputs,
+// without an FP64 multiply
+__device__ __forceinline__ double masked_zero(double v) {
+  const long long b = __double_as_longlong(v);
+  const bool special = ((b >> 52) & 0x7ff) == 0x7ff;
+  return special ? __longlong_as_double(0x7ff8000000000000LL)
+                 : __longlong_as_double(b & (long long)0x8000000000000000ULL);
+}
+__device__ __forceinline__ float masked_zero(float v) {
+  const unsigned b = __float_as_uint(v);
+  return ((b >> 23) & 0xffu) == 0xffu ? __uint_as_float(0x7fc00000u) : __uint_as_float(b & 0x80000000u);
+}
 
 // ---------------------------------------------------------------------------
 // policies
@@ -93,10 +139,13 @@ struct PF64 {
   typedef double v;
   static constexpr int kPrecision = SEM_F64;
   static __device__ __forceinline__ v ld(const io* p) { return __ldg(p); }
+  static __device__ __forceinline__ v cvt(io x) { return x; }
   static __device__ __forceinline__ io st(v a) { return a; }
   static __device__ __forceinline__ v zero() { return 0.0; }
   static __device__ __forceinline__ v add(v a, v b) { return a + b; }
   static __device__ __forceinline__ v sub(v a, v b) { return a - b; }
+  static __device__ __forceinline__ v add_u(v a, v b) { return a + b; }
+  static __device__ __forceinline__ v sub_u(v a, v b) { return a - b; }
   static __device__ __forceinline__ v mul(v a, v b) { return a * b; }
   static __device__ __forceinline__ v fma(v a, v b, v c) { return __fma_rn(a, b, c); }
   static __device__ __forceinline__ v fin(v a) { return a; }
@@ -108,10 +157,13 @@ struct PF32 {
   typedef float v;
   static constexpr int kPrecision = SEM_F32;
   static __device__ __forceinline__ v ld(const io* p) { return __ldg(p); }
+  static __device__ __forceinline__ v cvt(io x) { return x; }
   static __device__ __forceinline__ io st(v a) { return a; }
   static __device__ __forceinline__ v zero() { return 0.0f; }
   static __device__ __forceinline__ v add(v a, v b) { return a + b; }
   static __device__ __forceinline__ v sub(v a, v b) { return a - b; }
+  static __device__ __forceinline__ v add_u(v a, v b) { return a + b; }
+  static __device__ __forceinline__ v sub_u(v a, v b) { return a - b; }
   static __device__ __forceinline__ v mul(v a, v b) { return a * b; }
   static __device__ __forceinline__ v fma(v a, v b, v c) { return __fmaf_rn(a, b, c); }
   static __device__ __forceinline__ v fin(v a) { return a; }
@@ -123,10 +175,13 @@ struct PDF {
   typedef df v;
   static constexpr int kPrecision = SEM_F64_DF;
   static __device__ __forceinline__ v ld(const io* p) { return d2df(__ldg(p)); }
+  static __device__ __forceinline__ v cvt(io x) { return d2df(x); }
   static __device__ __forceinline__ io st(v a) { return df2d(a); }
   static __device__ __forceinline__ v zero() { return {0.0f, 0.0f}; }
   static __device__ __forceinline__ v add(v a, v b) { return df_add(a, b); }
   static __device__ __forceinline__ v sub(v a, v b) { return df_sub(a, b); }
+  static __device__ __forceinline__ v add_u(v a, v b) { return df_add_u(a, b); }
+  static __device__ __forceinline__ v sub_u(v a, v b) { return df_add_u(a, df_neg(b)); }
   static __device__ __forceinline__ v mul(v a, v b) { return df_mul_u(a, b); }
   static __device__ __forceinline__ v fma(v a, v b, v c) { return df_fma_u(a, b, c); }
   static __device__ __forceinline__ v fin(v a) { return df_norm(a); }

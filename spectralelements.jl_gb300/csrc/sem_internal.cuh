@@ -172,6 +172,7 @@ struct sem_mesh {
   void* ws;
   size_t ws_bytes;
   unsigned char* info;     // device L_* tables: NX row entries then NY column entries
+  int variant[4];          // autotuned kernel variant per precision (SEM_F64, SEM_F64_DF, SEM_F32)
 };
 
 namespace sem {
@@ -198,7 +199,10 @@ struct ApplyCall {
   unsigned mode;   // M_* bits (topology bits included)
   int precision;   // SEM_F64, SEM_F64_DF, SEM_F32
   const int* skip; // device flag: when non-zero the launch does nothing (solver loops)
+  int variant;     // kernel variant: 0 = direct loads, 1 = cp.async-staged inputs
 };
+
+constexpr int kVariants = 2;
 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
 int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned mode, int precision,

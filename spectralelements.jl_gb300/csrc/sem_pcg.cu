@@ -423,6 +423,7 @@ int run_cg(sem_mesh* m, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, co
   }
   if (k == 0.0) c.mode &= ~M_MASS;
   c.precision = op_precision;
+  c.variant = m->variant[op_precision];
   c.skip = &w.sc->done;
   const unsigned nb = nblocks(L);
   for (;;) {
@@ -555,6 +556,7 @@ int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
     c.k_s = o->k;
     c.mode = m->g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (m->has_bc ? M_MASK : 0u);
     c.precision = m->precision;
+    c.variant = m->variant[m->precision];
     bool nan = rmax != rmax;
     while (!(rmax <= o->tol) && !nan && outer < max_outer) {
       ++outer;

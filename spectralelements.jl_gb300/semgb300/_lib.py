@@ -25,7 +25,8 @@ INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
-SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu"]
+SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
+           "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu"]
 
 
 class SemError(RuntimeError):
@@ -122,6 +123,8 @@ SIGNATURES = {
     "sem_mesh_destroy": (_I, [_P]),
     "sem_mesh_set_bc": (_I, [_P, ctypes.c_char_p]),
     "sem_mesh_set_precision": (_I, [_P, _I]),
+    "sem_mesh_autotune": (_I, [_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
+    "sem_mesh_set_variant": (_I, [_P, _I, _I]),
     "sem_mesh_field": (_I, [_P, _I, _P, _P]),
     "sem_mesh_dims": (_I, [_P, ctypes.POINTER(_L), ctypes.POINTER(_L)]),
     "sem_last_error": (ctypes.c_char_p, []),

@@ -184,6 +184,19 @@ class Mesh:
         _lib.check(self._lib.sem_mesh_set_precision(self._h, int(precision)))
         self.precision = int(precision)
 
+    def autotune(self, precision=None):
+        """Time the fused-kernel variants on this mesh and keep the fastest
+        (per precision); returns {variant: ms}."""
+        prec = self.precision if precision is None else int(precision)
+        ms = (ctypes.c_double * 2)()
+        ch = ctypes.c_int()
+        _lib.check(self._lib.sem_mesh_autotune(self._h, prec, ms, ctypes.byref(ch)))
+        return {"chosen": ch.value, "ms": list(ms)}
+
+    def set_variant(self, variant, precision=None):
+        prec = self.precision if precision is None else int(precision)
+        _lib.check(self._lib.sem_mesh_set_variant(self._h, prec, int(variant)))
+
     @property
     def shape(self):
         return (self.nr * self.Ex, self.ns * self.Ey)
