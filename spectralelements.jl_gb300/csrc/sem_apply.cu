@@ -71,22 +71,31 @@ void eo_from_dense(const double* D, int n, bool transpose, double* A, double* C,
   }
 }
 
-int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** out) {
+int init_operator_set(const double* Dr, const double* Ds, int n, OperatorSet* o) {
   if (n < 2 || n > kMaxN) return set_error(SEM_ERR_UNSUPPORTED, "fused operators serve 2 <= n <= %d GLL points, got %d", kMaxN, n);
   if (!is_centro_antisymmetric(Dr, n, 1e-12) || !is_centro_antisymmetric(Ds, n, 1e-12))
     return set_error(SEM_ERR_UNSUPPORTED,
                      "derivative matrices must be centro-antisymmetric (GLL derivative "
                      "matrices are); a general matrix is served by sem_abu");
-  OperatorSet* o = new OperatorSet;
+  std::memset(o, 0, sizeof(*o));
   o->n = n;
-  o->Dr.assign(Dr, Dr + n * n);
-  o->Ds.assign(Ds, Ds + n * n);
+  std::memcpy(o->Dr, Dr, sizeof(double) * n * n);
+  std::memcpy(o->Ds, Ds, sizeof(double) * n * n);
   const int m = n / 2;
   for (int b = 0; b < 4; ++b) {
-    o->eo[b].assign(2 * m * m + 2 * m, 0.0);
     const double* D = b < 2 ? Dr : Ds;
-    double* p = o->eo[b].data();
+    double* p = o->eo[b];
     eo_from_dense(D, n, (b & 1) != 0, p, p + m * m, p + 2 * m * m, p + 2 * m * m + m);
+  }
+  return SEM_OK;
+}
+
+int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** out) {
+  OperatorSet* o = new OperatorSet;
+  const int st = init_operator_set(Dr, Ds, n, o);
+  if (st != SEM_OK) {
+    delete o;
+    return st;
   }
   *out = o;
   return SEM_OK;

@@ -11,14 +11,6 @@
 
 namespace sem {
 
-struct OperatorSet {
-  int n;
-  // even-odd coefficients in double for Dr, Dr', Ds, Ds' (index 0..3); each
-  // block holds A (m*m), C (m*m), cm (m), mr (m)
-  std::vector<double> eo[4];
-  std::vector<double> Dr, Ds;  // dense, column-major
-};
-
 std::pair<cudaEvent_t, cudaEvent_t>* timing_slot();
 size_t max_smem_optin();
 int launch_apply_f64(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
@@ -26,9 +18,9 @@ int launch_apply_df(const Grid& g, const OperatorSet* ops, const ApplyCall& c, c
 int launch_apply_f32(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
 
 template <class P, int N>
-static void fill_eo(EOCoef<N, typename P::v>& c, const std::vector<double>& src) {
+static void fill_eo(EOCoef<N, typename P::v>& c, const double* src) {
   constexpr int M = N / 2;
-  const double* A = src.data();
+  const double* A = src;
   const double* C = A + M * M;
   const double* cm = C + M * M;
   const double* mr = cm + M;

@@ -72,7 +72,7 @@ struct Grid {
 
 // host: L_* bits of local line l (row or column) of a direction with E
 // elements of n points; zero_first/zero_last mark Dirichlet ends
-inline unsigned char line_info(int64_t l, int n, int E, bool per, bool zero_first, bool zero_last) {
+__host__ __device__ inline unsigned char line_info(int64_t l, int n, int E, bool per, bool zero_first, bool zero_last) {
   const int64_t NL = (int64_t)n * E;
   const int64_t e = l / n;
   const int i = (int)(l - e * n);
@@ -150,7 +150,16 @@ void eo_from_dense(const double* D, int n, bool transpose, double* A, double* C,
 // ---------------------------------------------------------------------------
 // the mesh handle
 // ---------------------------------------------------------------------------
-struct OperatorSet;  // cached kernel coefficient blocks (sem_apply.cu)
+// coefficient blocks of the fused kernels for one pair of derivative matrices
+// (fixed size, no heap storage: it can live on the stack of a call)
+struct OperatorSet {
+  int n;
+  // even-odd coefficients in double for Dr, Dr', Ds, Ds' (index 0..3); each
+  // block holds A (m*m), C (m*m), cm (m), mr (m) with m = n/2
+  double eo[4][2 * (kMaxN / 2) * (kMaxN / 2) + 2 * (kMaxN / 2)];
+  double Dr[kMaxN * kMaxN], Ds[kMaxN * kMaxN];  // dense, column-major
+};
+int init_operator_set(const double* Dr, const double* Ds, int n, OperatorSet* o);
 
 }  // namespace sem
 

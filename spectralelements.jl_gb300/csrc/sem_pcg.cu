@@ -19,6 +19,7 @@
 // r = b - A x recomputed in FP64 after every inner FP32 CG solve.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "sem_internal.cuh"
@@ -374,47 +375,75 @@ int get_ws(sem_mesh* m, bool mixed, WS& w) {
   return SEM_OK;
 }
 
-int diag_build(sem_mesh* m, const double* nu_field, double nu, double k, double* d, double* tmp,
-               cudaStream_t s) {
+// the operator a solve works on: grid, coefficient set and geometry, from a
+// mesh handle or from caller-owned arrays
+struct OpCtx {
+  Grid g;
+  const OperatorSet* ops;
+  bool has_bc;
+  const double *G11, *G12, *G22, *B;
+  const float *G11f, *G12f, *G22f, *Bf;
+  const int* variant;  // per precision
+};
+
+OpCtx ctx_of(const sem_mesh* m) {
+  OpCtx cx;
+  cx.g = m->g;
+  cx.ops = m->ops;
+  cx.has_bc = m->has_bc;
+  cx.G11 = m->G11;
+  cx.G12 = m->G12;
+  cx.G22 = m->G22;
+  cx.B = m->B;
+  cx.G11f = m->G11_f;
+  cx.G12f = m->G12_f;
+  cx.G22f = m->G22_f;
+  cx.Bf = m->B_f;
+  cx.variant = m->variant;
+  return cx;
+}
+
+int diag_build(const OpCtx& cx, const double* nu_field, double nu, double k, double* d,
+               double* tmp, cudaStream_t s) {
   DiagArgs a;
   std::memset(&a, 0, sizeof(a));
-  const int n = m->g.n;
-  std::memcpy(a.Dr, m->Dr_h, sizeof(double) * n * n);
-  std::memcpy(a.Ds, m->Ds_h, sizeof(double) * n * n);
+  const int n = cx.g.n;
+  std::memcpy(a.Dr, cx.ops->Dr, sizeof(double) * n * n);
+  std::memcpy(a.Ds, cx.ops->Ds, sizeof(double) * n * n);
   a.nu = nu_field ? 1.0 : nu;
   a.k = k;
-  const long long L = m->g.NX * m->g.NY;
-  k_diag_local<<<nblocks(L) * 4, kRT, 0, s>>>(a, m->G11, m->G12, m->G22, m->B, nu_field, tmp, m->g);
+  const long long L = cx.g.NX * cx.g.NY;
+  k_diag_local<<<nblocks(L) * 4, kRT, 0, s>>>(a, cx.G11, cx.G12, cx.G22, cx.B, nu_field, tmp, cx.g);
   SEM_CUDA(cudaGetLastError());
-  SEM_CHECK(launch_gather_scatter(m->g, tmp, d, m->g.topo, s));
+  SEM_CHECK(launch_gather_scatter(cx.g, tmp, d, cx.g.topo, s));
   return SEM_OK;
 }
 
 // run CG iterations until done; T = double (F64/DF operator) or float (F32)
 template <class T>
-int run_cg(sem_mesh* m, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, const T* dinv,
+int run_cg(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, const T* dinv,
            int op_precision, const double* nu_field, double nu, double k, int check_every,
            Scalars* out, cudaStream_t s) {
-  const long long L = m->g.NX * m->g.NY;
+  const long long L = cx.g.NX * cx.g.NY;
   ApplyCall c;
   std::memset(&c, 0, sizeof(c));
   c.u = p;
   c.out = Ap;
   if (op_precision == SEM_F32) {
-    c.G11 = m->G11_f;
-    c.G12 = m->G12_f;
-    c.G22 = m->G22_f;
-    c.B = m->B_f;
+    c.G11 = cx.G11f;
+    c.G12 = cx.G12f;
+    c.G22 = cx.G22f;
+    c.B = cx.Bf;
   } else {
-    c.G11 = m->G11;
-    c.G12 = m->G12;
-    c.G22 = m->G22;
-    c.B = m->B;
+    c.G11 = cx.G11;
+    c.G12 = cx.G12;
+    c.G22 = cx.G22;
+    c.B = cx.B;
   }
   c.nu = nullptr;
   c.nu_s = nu_field ? 1.0 : nu;
   c.k_s = k;
-  c.mode = m->g.topo | M_STIFF | M_MASS | M_GS | (m->has_bc ? M_MASK : 0u);
+  c.mode = cx.g.topo | M_STIFF | M_MASS | M_GS | (cx.has_bc ? M_MASK : 0u);
   if (nu_field) {
     if (op_precision == SEM_F32)
       return set_error(SEM_ERR_UNSUPPORTED, "a nu field is not served by the FP32 inner solve");
@@ -423,13 +452,13 @@ int run_cg(sem_mesh* m, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, co
   }
   if (k == 0.0) c.mode &= ~M_MASS;
   c.precision = op_precision;
-  c.variant = m->variant[op_precision];
+  c.variant = cx.variant[op_precision];
   c.skip = &w.sc->done;
   const unsigned nb = nblocks(L);
   for (;;) {
     for (int it = 0; it < check_every; ++it) {
       k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
-      SEM_CHECK(launch_apply(m->g, m->ops, c, s));
+      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
       k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
       k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
       k_update<T><<<nb, kRT, 0, s>>>(x, r, p, Ap, dinv, w.part, w.sc, gv);
@@ -443,6 +472,122 @@ int run_cg(sem_mesh* m, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, co
   *out = *w.sc_h;
   return SEM_OK;
 }
+
+// argument checks shared by the solver entry points
+int pcg_check(const sem_pcg_opts* o, const double* b, double* x) {
+  if (!o || !b || !x) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (b == x) return set_error(SEM_ERR_BAD_ARG, "x must not alias b");
+  if (o->precond != SEM_PRECOND_NONE && o->precond != SEM_PRECOND_JACOBI)
+    return set_error(SEM_ERR_BAD_ARG, "unknown preconditioner %d", o->precond);
+  const int prec = o->precision;
+  if (prec != SEM_F64 && prec != SEM_F64_DF && prec != SEM_MIXED)
+    return set_error(SEM_ERR_BAD_ARG, "precision must be SEM_F64, SEM_F64_DF or SEM_MIXED");
+  return SEM_OK;
+}
+
+// pcg (src/pcg.jl:16-60) on an operator context with workspace w; the mixed
+// path needs the mesh handle m (FP32 geometry copies)
+int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, const double* b,
+             double* x, sem_solve_info* info, cudaStream_t s) {
+  const int prec = o->precision;
+  OpCtx cx = cx0;
+  const long long L = cx.g.NX * cx.g.NY;
+  const int maxiter = o->maxiter > 0 ? o->maxiter : (int)(L > 2147483647LL ? 2147483647LL : L);
+  int check_every = o->check_every > 0 ? o->check_every : (L < 200000 ? 64 : 16);
+  const unsigned nb = nblocks(L);
+  const bool jac = o->precond == SEM_PRECOND_JACOBI;
+  Grid gv = cx.g;
+  if (o->mult_ones) gv.topo |= M_MULT1;
+  if (jac) {
+    SEM_CHECK(diag_build(cx, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
+    k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, cx.g);
+    if (prec == SEM_MIXED)
+      k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, cx.g);
+    SEM_CUDA(cudaGetLastError());
+  }
+  Scalars res;
+  std::memset(&res, 0, sizeof(res));
+  int outer = 0;
+  double res0 = 0.0;
+  if (prec != SEM_MIXED) {
+    k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
+    k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
+    SEM_CUDA(cudaGetLastError());
+    SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    SEM_CUDA(cudaStreamSynchronize(s));
+    res0 = w.sc_h->rmax;
+    res = *w.sc_h;
+    if (!w.sc_h->done)
+      SEM_CHECK(run_cg<double>(cx, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
+                               o->nu, o->k, check_every, &res, s));
+  } else {
+    if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED does not take a nu field");
+    if (!m) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED needs a mesh handle");
+    SEM_CHECK(ensure_f32_geometry(m, s));
+    cx = ctx_of(m);
+    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 6;
+    // x = 0, r = b
+    k_zero<<<nb, kRT, 0, s>>>(x, L);
+    k_residual<<<nb, kRT, 0, s>>>(b, x, w.r, w.part, L);  // r = b - 0
+    k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
+    SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SEM_CUDA(cudaStreamSynchronize(s));
+    double rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
+    res0 = rmax;
+    int total_it = 0;
+    ApplyCall c;
+    std::memset(&c, 0, sizeof(c));
+    c.u = x;
+    c.out = w.Ap;
+    c.G11 = cx.G11;
+    c.G12 = cx.G12;
+    c.G22 = cx.G22;
+    c.B = cx.B;
+    c.nu_s = o->nu;
+    c.k_s = o->k;
+    c.mode = cx.g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (cx.has_bc ? M_MASK : 0u);
+    c.precision = m->precision;
+    c.variant = cx.variant[m->precision];
+    bool nan = rmax != rmax;
+    while (!(rmax <= o->tol) && !nan && outer < max_outer) {
+      ++outer;
+      // inner FP32 CG on A d = r to inner_tol * |r|_inf
+      k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, w.p32, jac ? w.dinv32 : nullptr, w.part, gv);
+      k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
+      SEM_CUDA(cudaGetLastError());
+      Scalars ir;
+      SEM_CHECK(run_cg<float>(cx, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
+                              nullptr, o->nu, o->k, check_every, &ir, s));
+      total_it += ir.k;
+      k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
+      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
+      k_residual<<<nb, kRT, 0, s>>>(b, w.Ap, w.r, w.part, L);
+      k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
+      SEM_CUDA(cudaGetLastError());
+      SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
+      SEM_CUDA(cudaStreamSynchronize(s));
+      rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
+      nan = rmax != rmax;
+    }
+    res.k = total_it;
+    res.rmax = rmax;
+    res.nan = nan;
+    res.converged = rmax <= o->tol;
+  }
+  if (info) {
+    info->iters = res.k;
+    info->outer = outer;
+    info->res_inf = res.rmax;
+    info->res0_inf = res0;
+    info->converged = res.converged;
+  }
+  if (res.nan) return set_error(SEM_ERR_NAN, "NaN/Inf in the residual after %d iterations", res.k);
+  if (!res.converged)
+    return set_error(SEM_ERR_NOT_CONVERGED, "warning: res: %.17g after %d iterations", res.rmax, res.k);
+  return SEM_OK;
+}
+
 
 }  // namespace
 
@@ -458,7 +603,7 @@ int sem_jacobi_diag(sem_mesh_t* m, const double* nu_field, double nu, double k, 
   cudaStream_t s = (cudaStream_t)stream;
   WS w;
   SEM_CHECK(get_ws(m, false, w));
-  SEM_CHECK(diag_build(m, nu_field, nu, k, diag, w.d, s));
+  SEM_CHECK(diag_build(ctx_of(m), nu_field, nu, k, diag, w.d, s));
   if (m->has_bc) {
     k_diag_mask<<<nblocks(m->g.NX * m->g.NY) * 4, kRT, 0, s>>>(diag, m->g);
     SEM_CUDA(cudaGetLastError());
@@ -491,109 +636,11 @@ int sem_adjoint_grad(sem_mesh_t* m, const double* lam, const double* u, double* 
 
 int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
             sem_solve_info* info, sem_stream_t stream) {
-  if (!m || !o || !b || !x) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
-  if (b == x) return set_error(SEM_ERR_BAD_ARG, "x must not alias b");
-  if (o->precond != SEM_PRECOND_NONE && o->precond != SEM_PRECOND_JACOBI)
-    return set_error(SEM_ERR_BAD_ARG, "unknown preconditioner %d", o->precond);
-  const int prec = o->precision;
-  if (prec != SEM_F64 && prec != SEM_F64_DF && prec != SEM_MIXED)
-    return set_error(SEM_ERR_BAD_ARG, "precision must be SEM_F64, SEM_F64_DF or SEM_MIXED");
-  cudaStream_t s = (cudaStream_t)stream;
-  const long long L = m->g.NX * m->g.NY;
-  const int maxiter = o->maxiter > 0 ? o->maxiter : (int)(L > 2147483647LL ? 2147483647LL : L);
-  int check_every = o->check_every > 0 ? o->check_every : (L < 200000 ? 64 : 16);
+  if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
+  SEM_CHECK(pcg_check(o, b, x));
   WS w;
-  SEM_CHECK(get_ws(m, prec == SEM_MIXED, w));
-  const unsigned nb = nblocks(L);
-  const bool jac = o->precond == SEM_PRECOND_JACOBI;
-  Grid gv = m->g;
-  if (o->mult_ones) gv.topo |= M_MULT1;
-  if (jac) {
-    SEM_CHECK(diag_build(m, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
-    k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, m->g);
-    if (prec == SEM_MIXED)
-      k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, m->g);
-    SEM_CUDA(cudaGetLastError());
-  }
-  Scalars res;
-  std::memset(&res, 0, sizeof(res));
-  int outer = 0;
-  double res0 = 0.0;
-  if (prec != SEM_MIXED) {
-    k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
-    k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
-    SEM_CUDA(cudaGetLastError());
-    SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-    SEM_CUDA(cudaStreamSynchronize(s));
-    res0 = w.sc_h->rmax;
-    res = *w.sc_h;
-    if (!w.sc_h->done)
-      SEM_CHECK(run_cg<double>(m, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
-                               o->nu, o->k, check_every, &res, s));
-  } else {
-    if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED does not take a nu field");
-    SEM_CHECK(ensure_f32_geometry(m, s));
-    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
-    const int max_outer = o->max_outer > 0 ? o->max_outer : 6;
-    // x = 0, r = b
-    k_zero<<<nb, kRT, 0, s>>>(x, L);
-    k_residual<<<nb, kRT, 0, s>>>(b, x, w.r, w.part, L);  // r = b - 0
-    k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
-    SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
-    SEM_CUDA(cudaStreamSynchronize(s));
-    double rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
-    res0 = rmax;
-    int total_it = 0;
-    ApplyCall c;
-    std::memset(&c, 0, sizeof(c));
-    c.u = x;
-    c.out = w.Ap;
-    c.G11 = m->G11;
-    c.G12 = m->G12;
-    c.G22 = m->G22;
-    c.B = m->B;
-    c.nu_s = o->nu;
-    c.k_s = o->k;
-    c.mode = m->g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (m->has_bc ? M_MASK : 0u);
-    c.precision = m->precision;
-    c.variant = m->variant[m->precision];
-    bool nan = rmax != rmax;
-    while (!(rmax <= o->tol) && !nan && outer < max_outer) {
-      ++outer;
-      // inner FP32 CG on A d = r to inner_tol * |r|_inf
-      k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, w.p32, jac ? w.dinv32 : nullptr, w.part, gv);
-      k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
-      SEM_CUDA(cudaGetLastError());
-      Scalars ir;
-      SEM_CHECK(run_cg<float>(m, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
-                              nullptr, o->nu, o->k, check_every, &ir, s));
-      total_it += ir.k;
-      k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
-      SEM_CHECK(launch_apply(m->g, m->ops, c, s));
-      k_residual<<<nb, kRT, 0, s>>>(b, w.Ap, w.r, w.part, L);
-      k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
-      SEM_CUDA(cudaGetLastError());
-      SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
-      SEM_CUDA(cudaStreamSynchronize(s));
-      rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
-      nan = rmax != rmax;
-    }
-    res.k = total_it;
-    res.rmax = rmax;
-    res.nan = nan;
-    res.converged = rmax <= o->tol;
-  }
-  if (info) {
-    info->iters = res.k;
-    info->outer = outer;
-    info->res_inf = res.rmax;
-    info->res0_inf = res0;
-    info->converged = res.converged;
-  }
-  if (res.nan) return set_error(SEM_ERR_NAN, "NaN/Inf in the residual after %d iterations", res.k);
-  if (!res.converged)
-    return set_error(SEM_ERR_NOT_CONVERGED, "warning: res: %.17g after %d iterations", res.rmax, res.k);
-  return SEM_OK;
+  SEM_CHECK(get_ws(m, o->precision == SEM_MIXED, w));
+  return pcg_core(ctx_of(m), w, m, o, b, x, info, (cudaStream_t)stream);
 }
 
 }  // extern "C"
