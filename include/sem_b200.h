@@ -182,6 +182,32 @@ typedef struct {
 int sem_pcg(sem_mesh_t* mesh, const sem_pcg_opts* opts, const double* b, double* x,
             sem_solve_info* info, sem_stream_t stream);
 
+/* ---- allocation-free solve (no counterpart in the reference).
+ * For callers that may not allocate device memory while they run, such as an
+ * application's allocation-free real-time loop, a memory manager that owns
+ * every device byte, or a plug-in that may not grow the process's device
+ * footprint.  It is the same solve as sem_pcg (opA = mask(QQ'(hlmz)), SEM_F64
+ * or SEM_F64_DF, Jacobi or no preconditioner). The mesh is described by
+ * arguments instead of a handle: nr = ns, host Dr/Ds, and DEVICE G11, G12,
+ * G22, B in the local layout.  All scratch vectors live in one fixed
+ * file-scope device array sized for SEM_NOALLOC_MAX_LOCAL local DOF, about
+ * 12.9 MB, which every GPU that loads the library holds until the process
+ * exits.  The call allocates nothing: no cudaMalloc, cudaFree, pinned host
+ * memory or library allocator.  Larger meshes are rejected with
+ * SEM_ERR_BAD_ARG.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) once for that device.  Make that first call
+ *    before any stream capture.
+ *  - Every call reuses the same array and overwrites the part it needs, so
+ *    calls whose GPU work overlaps (two streams, two host threads) race and
+ *    corrupt each other's results; serialise them.
+ *  - Like sem_pcg it synchronises the stream to read the convergence flag. */
+#define SEM_NOALLOC_MAX_LOCAL 262144
+int sem_pcg_noalloc(int nr, int Ex, int Ey, int periodic_x, int periodic_y, const char* bc,
+                    const double* Dr, const double* Ds, const double* G11, const double* G12,
+                    const double* G22, const double* B, const sem_pcg_opts* opts,
+                    const double* b, double* x, sem_solve_info* info, sem_stream_t stream);
+
 /* Jacobi diagonal of mask(QQ'(hlmz)) with masked entries set to 1 (new: the
  * reference has no Jacobi preconditioner; derived from src/lapl.jl:70-81) */
 int sem_jacobi_diag(sem_mesh_t* mesh, const double* nu_field, double nu, double k,

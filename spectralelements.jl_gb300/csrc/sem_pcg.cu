@@ -644,3 +644,141 @@ int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free solve.
+//
+// Some callers cannot call cudaMalloc while they run: code inside an
+// allocation-free region of a host application (a real-time loop, a memory
+// manager that owns every device byte, a plug-in that may not grow the
+// process's device footprint).  sem_pcg_noalloc serves them: the caller
+// passes the geometry, b and x, and every scratch vector of the solve lives in
+// the file-scope device array below.  Its size is fixed at build time, so
+// every GPU that loads this library holds it until the process exits.
+// ---------------------------------------------------------------------------
+namespace sem {
+namespace {
+
+constexpr long long kNoAllocMaxLocal = SEM_NOALLOC_MAX_LOCAL;
+constexpr size_t kNoAllocVec = (size_t)kNoAllocMaxLocal * sizeof(double);     // 256-multiple
+constexpr size_t kNoAllocInfo = (((size_t)kNoAllocMaxLocal + 1) + 255) & ~(size_t)255;
+constexpr size_t kNoAllocPart = ((sizeof(double) * kRB * 4) + 255) & ~(size_t)255;
+constexpr size_t kNoAllocBytes = 6 * kNoAllocVec + kNoAllocInfo + kNoAllocPart + 256 + 256;
+
+}  // namespace
+}  // namespace sem
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sem::kNoAllocBytes];
+
+namespace sem {
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+// device address of the scratch array for the current device, looked up once
+// per device (the array's host-side name is not a device address)
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  SEM_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(SEM_ERR_UNSUPPORTED, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return SEM_OK;
+}
+
+__global__ void k_line_info(unsigned char* rinfo, unsigned char* cinfo, Grid g, int has_bc) {
+  const unsigned t = g.topo;
+  const long long tot = g.NX + g.NY;
+  for (long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x; l < tot;
+       l += (long long)gridDim.x * blockDim.x) {
+    if (l < g.NX)
+      rinfo[l] = line_info(l, g.n, g.Ex, (t & M_PERX) != 0, has_bc && (t & M_DXMIN), has_bc && (t & M_DXMAX));
+    else
+      cinfo[l - g.NX] = line_info(l - g.NX, g.n, g.Ey, (t & M_PERY) != 0, has_bc && (t & M_DYMIN),
+                                  has_bc && (t & M_DYMAX));
+  }
+}
+
+}  // namespace
+}  // namespace sem
+
+extern "C" int sem_pcg_noalloc(int nr, int Ex, int Ey, int periodic_x, int periodic_y,
+                               const char* bc, const double* Dr, const double* Ds,
+                               const double* G11, const double* G12, const double* G22,
+                               const double* B, const sem_pcg_opts* o, const double* b, double* x,
+                               sem_solve_info* info, sem_stream_t stream) {
+  using namespace sem;
+  SEM_CHECK(pcg_check(o, b, x));
+  if (nr < 2 || Ex < 1 || Ey < 1) return set_error(SEM_ERR_BAD_ARG, "bad sizes nr=%d Ex=%d Ey=%d", nr, Ex, Ey);
+  if (!Dr || !Ds || !G11 || !G12 || !G22 || !B) return set_error(SEM_ERR_BAD_ARG, "NULL geometry");
+  if (bc && !(bc[0] && bc[1] && bc[2] && bc[3]))
+    return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
+  if (bc)
+    for (int i = 0; i < 4; ++i)
+      if (bc[i] != 'D' && bc[i] != 'N') return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
+  if (o->precision == SEM_MIXED)
+    return set_error(SEM_ERR_UNSUPPORTED, "the allocation-free solve serves SEM_F64 and SEM_F64_DF");
+  const long long NX = (long long)nr * Ex, NY = (long long)nr * Ey;
+  if (NX * NY > kNoAllocMaxLocal)
+    return set_error(SEM_ERR_BAD_ARG,
+                     "the allocation-free solve holds at most %lld local DOF in its fixed scratch "
+                     "array; this mesh has %lld (use sem_pcg)",
+                     kNoAllocMaxLocal, NX * NY);
+  OperatorSet ops;
+  SEM_CHECK(init_operator_set(Dr, Ds, nr, &ops));
+  void* base = nullptr;
+  SEM_CHECK(noalloc_scratch(&base));
+  cudaStream_t s = (cudaStream_t)stream;
+  char* p = static_cast<char*>(base);
+  WS w;
+  std::memset(&w, 0, sizeof(w));
+  w.r = (double*)p; p += kNoAllocVec;
+  w.p = (double*)p; p += kNoAllocVec;
+  w.Ap = (double*)p; p += kNoAllocVec;
+  w.dinv = (double*)p; p += kNoAllocVec;
+  w.d = (double*)p; p += kNoAllocVec;
+  w.x64tmp = (double*)p; p += kNoAllocVec;
+  unsigned char* info_tab = (unsigned char*)p; p += kNoAllocInfo;
+  w.part = (double*)p; p += kNoAllocPart;
+  w.sc = (Scalars*)p; p += 256;
+  w.dmax = (double*)p;
+  Scalars host_sc[2];
+  w.sc_h = host_sc;  // pageable host copy: read back with a plain copy, no pinned allocation
+  Grid g;
+  std::memset(&g, 0, sizeof(g));
+  g.n = nr;
+  g.Ex = Ex;
+  g.Ey = Ey;
+  g.NX = NX;
+  g.NY = NY;
+  g.topo = (periodic_x ? M_PERX : 0u) | (periodic_y ? M_PERY : 0u);
+  if (bc) {
+    if (bc[0] == 'D') g.topo |= M_DXMIN;
+    if (bc[1] == 'D') g.topo |= M_DXMAX;
+    if (bc[2] == 'D') g.topo |= M_DYMIN;
+    if (bc[3] == 'D') g.topo |= M_DYMAX;
+  }
+  g.rinfo = info_tab;
+  g.cinfo = info_tab + NX;
+  k_line_info<<<nblocks(NX + NY), kRT, 0, s>>>(info_tab, info_tab + NX, g, bc ? 1 : 0);
+  SEM_CUDA(cudaGetLastError());
+  static const int kDirect[4] = {0, 0, 0, 0};
+  OpCtx cx;
+  std::memset(&cx, 0, sizeof(cx));
+  cx.g = g;
+  cx.ops = &ops;
+  cx.has_bc = bc != nullptr;
+  cx.G11 = G11;
+  cx.G12 = G12;
+  cx.G22 = G22;
+  cx.B = B;
+  cx.variant = kDirect;
+  return pcg_core(cx, w, nullptr, o, b, x, info, s);
+}

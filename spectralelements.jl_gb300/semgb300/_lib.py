@@ -141,6 +141,8 @@ SIGNATURES = {
     "sem_lapl_geom": (_I, [_I, _I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P, _P,
                            _U, _I, _P]),
     "sem_pcg": (_I, [_P, ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
+    "sem_pcg_noalloc": (_I, [_I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P,
+                             ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
     "sem_jacobi_diag": (_I, [_P, _P, _D, _D, _P, _P]),
     "sem_adjoint_grad": (_I, [_P, _P, _P, _P, _U, _P]),
     "sem_timing_enable": (_I, [_I]),
