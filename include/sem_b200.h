@@ -208,6 +208,25 @@ int sem_pcg_noalloc(int nr, int Ex, int Ey, int periodic_x, int periodic_y, cons
                     const double* G22, const double* B, const sem_pcg_opts* opts,
                     const double* b, double* x, sem_solve_info* info, sem_stream_t stream);
 
+/* ---- batched solves (no counterpart in the reference, which solves one
+ * system at a time): many independent pcg solves of opA = mask(QQ'(hlmz))
+ * on meshes of different sizes and orders (2 <= n <= 11) in ONE persistent
+ * launch of thread-block clusters that pull problems from a device work queue.
+ * sem_batch_create takes the mesh handles (their bc sets the mask), one nu and
+ * one k per problem and the preconditioner; it allocates the per-problem
+ * workspace and the Jacobi diagonals.  sem_batch_pcg solves all problems:
+ * b[i], x[i] device fields, tol[i] absolute Inf-norm tolerances, maxiter[i]
+ * (NULL or <= 0: length(b)), precision SEM_F64_DF or SEM_MIXED (inner_tol,
+ * max_outer as in sem_pcg_opts; <= 0 picks 1e-4 and 6); info[i] per problem.
+ * Synchronous; returns SEM_ERR_NOT_CONVERGED if any problem reached maxiter. */
+typedef struct sem_batch sem_batch_t;
+int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* k, int count,
+                     int precond, sem_batch_t** out);
+int sem_batch_destroy(sem_batch_t* batch);
+int sem_batch_pcg(sem_batch_t* batch, const double* const* b, double* const* x, const double* tol,
+                  const int* maxiter, int precision, double inner_tol, int max_outer,
+                  sem_solve_info* info, sem_stream_t stream);
+
 /* Jacobi diagonal of mask(QQ'(hlmz)) with masked entries set to 1 (new: the
  * reference has no Jacobi preconditioner; derived from src/lapl.jl:70-81) */
 int sem_jacobi_diag(sem_mesh_t* mesh, const double* nu_field, double nu, double k,

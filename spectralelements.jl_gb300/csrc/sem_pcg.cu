@@ -22,13 +22,14 @@
 #include <mutex>
 #include <vector>
 
+#include "sem_arith.cuh"
 #include "sem_internal.cuh"
 
 namespace sem {
 
 namespace {
 
-constexpr int kRB = 304;  // reduction grid (fixed: deterministic sums)
+constexpr int kRB = 1216;  // reduction grid, 8 blocks per SM (fixed: deterministic sums)
 constexpr int kRT = 256;
 
 struct Scalars {
@@ -97,21 +98,85 @@ __device__ __forceinline__ void final_reduce(const double* part, int nparts,
   for (int q = 0; q < NV; ++q) res[q] = sh[q][0];
 }
 
+// Per-thread accumulators of the vector kernels.  GB300 runs FP64 at 1/64 of
+// the FP32 rate, so for FP64 vectors the products and sums of the dots are
+// formed in double-float on the FP32 pipe and max|r| is an integer maximum of
+// the magnitude bits (NaN patterns order above Inf, so a NaN propagates); only
+// the x and r updates stay native FP64 FMAs.  FP32 vectors accumulate in FP32
+// (the inner solve of the mixed-precision CG).
+template <class T>
+struct Acc;
+
+template <>
+struct Acc<double> {
+  df s = {0.0f, 0.0f};
+  unsigned long long mx = 0ull;
+  // s += a * b * m with m an exact power of two
+  __device__ __forceinline__ void prod(double a, double b, double m) {
+    df p = df_mul_u(d2df(a), d2df(b));
+    const float mf = (float)m;
+    p.h *= mf;
+    p.l *= mf;
+    s = df_add_u(s, p);
+  }
+  // s += a * (a * d) * m  (the Jacobi-weighted residual dot r.h.mult)
+  __device__ __forceinline__ void rhr(double a, double d, double m) {
+    const df ad = d2df(a);
+    df h = df_mul_u(ad, d2df(d));
+    const float mf = (float)m;
+    h.h *= mf;
+    h.l *= mf;
+    s = df_fma_u(ad, h, s);
+  }
+  __device__ __forceinline__ void amax(double a) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+    mx = b > mx ? b : mx;
+  }
+  __device__ __forceinline__ double sum() const { return df2d(df_norm(s)); }
+  __device__ __forceinline__ double max() const { return __longlong_as_double((long long)mx); }
+};
+
+template <>
+struct Acc<float> {
+  float s = 0.0f;
+  unsigned mx = 0u;
+  __device__ __forceinline__ void prod(float a, float b, double m) { s = __fmaf_rn(a * (float)m, b, s); }
+  __device__ __forceinline__ void rhr(float a, float d, double m) { s = __fmaf_rn(a, a * d * (float)m, s); }
+  __device__ __forceinline__ void amax(float a) {
+    const unsigned b = __float_as_uint(a) & 0x7fffffffu;
+    mx = b > mx ? b : mx;
+  }
+  __device__ __forceinline__ double sum() const { return (double)s; }
+  __device__ __forceinline__ double max() const { return (double)__uint_as_float(mx); }
+};
+
+// p = h + beta p_old with h = r .* dinv
+__device__ __forceinline__ double pdir_value(double r, double d, double beta, double p, bool jac) {
+  const df rd = d2df(r);
+  const df h = jac ? df_mul_u(rd, d2df(d)) : rd;
+  return df2d(df_fma_u(d2df(beta), d2df(p), h));
+}
+__device__ __forceinline__ float pdir_value(float r, float d, float beta, float p, bool jac) {
+  return __fmaf_rn(beta, p, jac ? r * d : r);
+}
+
 // x = 0, r = b (converted), p = 0; partials of t = r.h.mult and max|r|
 template <class T, class TB>
 __global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
                        T* __restrict__ p, const T* __restrict__ dinv, double* part, Grid g) {
-  double t = 0.0, rm = 0.0;
+  Acc<T> acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     const T ri = (T)b[i];
     x[i] = (T)0;
     p[i] = (T)0;
     r[i] = ri;
-    const T h = dinv ? ri * dinv[i] : ri;
-    t += (double)ri * (double)h * mult_at(rr, cc, g);
-    rm = nanmax(rm, fabs((double)ri));
+    if (dinv)
+      acc.rhr(ri, dinv[i], mult_at(rr, cc, g));
+    else
+      acc.prod(ri, ri, mult_at(rr, cc, g));
+    acc.amax(ri);
   });
-  double v[2] = {t, rm};
+  double v[2] = {acc.sum(), acc.max()};
   const bool mx[2] = {false, true};
   block_reduce<2>(v, mx, part);
 }
@@ -140,22 +205,21 @@ __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* _
                        const Scalars* sc, long long L) {
   if (sc->done) return;
   const T beta = (T)sc->beta;
+  const bool jac = dinv != nullptr;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
-       i += (long long)gridDim.x * blockDim.x) {
-    const T h = dinv ? r[i] * dinv[i] : r[i];
-    p[i] = h + beta * p[i];
-  }
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = pdir_value(r[i], jac ? dinv[i] : (T)1, beta, p[i], jac);
 }
 
 template <class T>
 __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, double* part,
                           const Scalars* sc, Grid g) {
   if (sc->done) return;
-  double s = 0.0;
+  Acc<T> acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
-    s += (double)p[i] * (double)Ap[i] * mult_at(rr, cc, g);
+    acc.prod(p[i], Ap[i], mult_at(rr, cc, g));
   });
-  double v[1] = {s};
+  double v[1] = {acc.sum()};
   const bool mx[1] = {false};
   block_reduce<1>(v, mx, part);
 }
@@ -178,16 +242,18 @@ __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restri
                          const Scalars* sc, Grid g) {
   if (sc->done) return;
   const T alpha = (T)sc->alpha;
-  double t = 0.0, rm = 0.0;
+  Acc<T> acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     x[i] = x[i] + alpha * p[i];
     const T ri = r[i] - alpha * Ap[i];
     r[i] = ri;
-    const T h = dinv ? ri * dinv[i] : ri;
-    t += (double)ri * (double)h * mult_at(rr, cc, g);
-    rm = nanmax(rm, fabs((double)ri));
+    if (dinv)
+      acc.rhr(ri, dinv[i], mult_at(rr, cc, g));
+    else
+      acc.prod(ri, ri, mult_at(rr, cc, g));
+    acc.amax(ri);
   });
-  double v[2] = {t, rm};
+  double v[2] = {acc.sum(), acc.max()};
   const bool mx[2] = {false, true};
   block_reduce<2>(v, mx, part);
 }
@@ -590,6 +656,16 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
 
 
 }  // namespace
+
+// Jacobi inverse diagonal of a mesh's mask(QQ'(hlmz(., nu, k))) into dinv
+// (tmp: one scratch field); used by the batched solver's set-up
+int batch_diag(sem_mesh* m, double nu, double k, double* dinv, double* tmp, cudaStream_t s) {
+  const OpCtx cx = ctx_of(m);
+  SEM_CHECK(diag_build(cx, nullptr, nu, k, dinv, tmp, s));
+  k_diag_inv<double><<<nblocks(m->g.NX * m->g.NY) * 4, kRT, 0, s>>>(dinv, dinv, m->g);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
 
 }  // namespace sem
 

@@ -11,8 +11,8 @@ from ._lib import (SEM_F32, SEM_F64, SEM_F64_DF, SEM_GS, SEM_MASK, SEM_MIXED, No
 from .host import bdfExtK, derivMat, fixU, gausslobatto, interpMat, ndgrid, semmesh, semq_index  # noqa: F401
 from .mesh import Mesh, QQt, as_local, generateMask, local_empty  # noqa: F401
 from .ops import ABu, gatherScatter, hlmz, lapl, mask, mass  # noqa: F401
-from .solver import (Diffusion, HelmholtzOp, Jacobi, TimeStepper, identity,  # noqa: F401
-                     linsolve_varcoef, pcg, pcg_)
+from .solver import (BatchSolver, Diffusion, HelmholtzOp, Jacobi, TimeStepper, identity,  # noqa: F401
+                     linsolve_varcoef, pcg, pcg_, transient_varcoef)
 
 __all__ = ["Mesh", "QQt", "generateMask", "ABu", "lapl", "mass", "hlmz", "gatherScatter", "mask",
            "pcg", "pcg_", "HelmholtzOp", "Jacobi", "identity", "Diffusion", "TimeStepper",

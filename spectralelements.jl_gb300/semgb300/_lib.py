@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
-           "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu"]
+           "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
+           "sem_batch_kb.cu", "sem_batch_kc.cu"]
 
 
 class SemError(RuntimeError):
@@ -143,6 +144,12 @@ SIGNATURES = {
     "sem_pcg": (_I, [_P, ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
     "sem_pcg_noalloc": (_I, [_I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P,
                              ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
+    "sem_batch_create": (_I, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(_D),
+                              ctypes.POINTER(_D), _I, _I, ctypes.POINTER(ctypes.c_void_p)]),
+    "sem_batch_destroy": (_I, [_P]),
+    "sem_batch_pcg": (_I, [_P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                           ctypes.POINTER(_D), ctypes.POINTER(_I), _I, _D, _I,
+                           ctypes.POINTER(SolveInfo), _P]),
     "sem_jacobi_diag": (_I, [_P, _P, _D, _D, _P, _P]),
     "sem_adjoint_grad": (_I, [_P, _P, _P, _P, _U, _P]),
     "sem_timing_enable": (_I, [_I]),

@@ -138,6 +138,59 @@ def pcg(b, opA, opM=None, mult=None, ifv=False, tol=1e-8, maxiter=None, *, preci
     return x
 
 
+class BatchSolver:
+    """Many independent pcg solves of mask(QQ'(hlmz(., nu_i, k_i))) on meshes of
+    different sizes and orders (n <= 11), run by persistent cluster launches
+    (``sem_batch_create`` / ``sem_batch_pcg``)."""
+
+    def __init__(self, meshes, nus, ks, jacobi=True):
+        lib = _lib.load()
+        self.meshes = list(meshes)
+        n = len(self.meshes)
+        H = (ctypes.c_void_p * n)(*[m.handle.value for m in self.meshes])
+        nu = (ctypes.c_double * n)(*[float(v) for v in nus])
+        k = (ctypes.c_double * n)(*[float(v) for v in ks])
+        h = ctypes.c_void_p()
+        _lib.check(lib.sem_batch_create(H, nu, k, n,
+                                        _lib.SEM_PRECOND_JACOBI if jacobi else _lib.SEM_PRECOND_NONE,
+                                        ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.sem_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, bs, tols, precision=_lib.SEM_F64_DF, maxiter=None, xs=None, inner_tol=1e-4,
+              max_outer=6, infos=None):
+        """Solve every problem; returns the list of solutions.  ``infos`` (a list)
+        receives one dict per problem.  Raises NotConverged (after filling
+        ``infos``) if any problem reached maxiter."""
+        n = len(self.meshes)
+        bs = [as_local(b) for b in bs]
+        if xs is None:
+            xs = [m.empty() for m in self.meshes]
+        B = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+        X = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+        T = (ctypes.c_double * n)(*[float(t) for t in tols])
+        M = None if maxiter is None else (ctypes.c_int * n)(*[int(v) for v in maxiter])
+        info = (_lib.SolveInfo * n)()
+        st = self._lib.sem_batch_pcg(self._h, B, X, T, M, int(precision), float(inner_tol),
+                                     int(max_outer), info, stream_ptr())
+        if infos is not None:
+            infos[:] = [dict(iters=i.iters, outer=i.outer, res_inf=i.res_inf, converged=bool(i.converged))
+                        for i in info]
+        _lib.check(st)
+        return xs
+
+
 def pcg_(x, b, opA, **kw):
     """pcg!(x, b, opA; ...) (src/pcg.jl:64-79): x .= pcg(b, opA; ...)."""
     y = pcg(b, opA, **kw)
@@ -179,6 +232,92 @@ def linsolve_varcoef(nu, b, msh: Mesh, **kw):
     """Differentiable solve of -div(nu grad u) = f (b = mask(QQ'(B f))) w.r.t.
     the nodal nu, the pattern of ``linsolve`` + ``@adjoint`` (src/adjoint.jl)."""
     return _VarCoefSolve.apply(nu, b, msh, kw)
+
+
+def _mass_gs_mask(msh, v, scale):
+    """mask(QQ'(scale * B v)) on the device."""
+    lib = _lib.load()
+    out = msh.empty()
+    _lib.check(lib.sem_mass(msh.handle, as_local(v).data_ptr(), out.data_ptr(),
+                            _lib.SEM_GS | (_lib.SEM_MASK if msh.bc else 0), stream_ptr()))
+    return out if scale == 1.0 else out * scale
+
+
+def _step_solve(msh, nu, dt, rhs, kw):
+    op = HelmholtzOp(msh, 1.0, 1.0 / dt, nu_field=nu)
+    return pcg(rhs, op, opM=Jacobi(op), mult=msh.mult, **kw)
+
+
+class _TransientVarCoef(torch.autograd.Function):
+    """Implicit Euler for du/dt = div(nu grad u) + f with nu folded into G:
+    (K(nu) + B/dt) u_n = B u_{n-1}/dt + B f, assembled as mask(QQ'(.)), for
+    n = 1..nsteps; returns u_nsteps.  Forward states are kept every
+    ``checkpoint_every`` steps; backward recomputes each segment from its
+    checkpoint and runs the discrete adjoint backwards in time:
+    (K + B/dt) lam_T = mask(QQ'(u_bar)), (K + B/dt) lam_n = mask(QQ'(B lam_{n+1}/dt)),
+    dJ/dnu = sum_n -G:(grad lam_n)(grad u_n) per local copy."""
+
+    @staticmethod
+    def forward(ctx, nu, u0, f, msh, dt, nsteps, every, kw):
+        nu = nu.detach()
+        bf = _mass_gs_mask(msh, f, 1.0)
+        u = as_local(u0).clone(memory_format=torch.preserve_format)
+        ckpt = {0: u}
+        for n in range(1, nsteps + 1):
+            rhs = _mass_gs_mask(msh, u, 1.0 / dt) + bf
+            u = _step_solve(msh, nu, dt, rhs, kw)
+            if every and n % every == 0 and n < nsteps:
+                ckpt[n] = u
+        ctx.save_for_backward(nu)
+        ctx.msh, ctx.dt, ctx.nsteps, ctx.every, ctx.kw = msh, dt, nsteps, every, kw
+        ctx.ckpt, ctx.bf, ctx.uT = ckpt, bf, u
+        ctx.recomputed_steps = 0
+        return u
+
+    @staticmethod
+    def backward(ctx, ubar):
+        (nu,) = ctx.saved_tensors
+        msh, dt, T, every, kw = ctx.msh, ctx.dt, ctx.nsteps, ctx.every, ctx.kw
+        lib = _lib.load()
+        from .ops import gatherScatter, mask
+        M = generateMask(msh.bc, msh) if msh.bc else []
+        grad = torch.zeros_like(nu)
+        starts = sorted(ctx.ckpt)
+        lam = None
+        n = T
+        for s in reversed(starts):
+            # recompute u_{s+1} .. u_{min(next checkpoint, T)} from the checkpoint at s
+            stop = min(T, s + every) if every else T
+            seg = {}
+            u = ctx.ckpt[s]
+            for m in range(s + 1, stop + 1):
+                if m == T:
+                    u = ctx.uT
+                else:
+                    rhs = _mass_gs_mask(msh, u, 1.0 / dt) + ctx.bf
+                    u = _step_solve(msh, nu, dt, rhs, kw)
+                    ctx.recomputed_steps += 1
+                seg[m] = u
+            for m in range(stop, s, -1):
+                if m == T:
+                    rhs = gatherScatter(mask(as_local(ubar), M), msh)
+                else:
+                    rhs = _mass_gs_mask(msh, lam, 1.0 / dt)
+                lam = _step_solve(msh, nu, dt, rhs, kw)
+                g = msh.empty()
+                _lib.check(lib.sem_adjoint_grad(msh.handle, lam.data_ptr(), seg[m].data_ptr(),
+                                                g.data_ptr(), 0, stream_ptr()))
+                grad += g
+                n = m
+        assert n == 1
+        return grad, None, None, None, None, None, None, None
+
+
+def transient_varcoef(nu, u0, f, msh: Mesh, dt, nsteps, checkpoint_every=20, **kw):
+    """Differentiable implicit-Euler run of the variable-coefficient diffusion
+    (``Diffusion`` with k=1 and nu folded into G), checkpointing every
+    ``checkpoint_every`` steps; returns the final state."""
+    return _TransientVarCoef.apply(nu, u0, f, msh, dt, nsteps, checkpoint_every, kw)
 
 
 # ---------------------------------------------------------------------------

@@ -1,0 +1,161 @@
+"""Adjoint gradients of J(nu) = 1/2 sum B (u - u_target)^2 with respect to a
+nodal, G-folded diffusivity nu (the linsolve + @adjoint pattern of
+src/adjoint.jl:5-24, examples/semPS.jl:157-192), checked against the oracle's
+exact discrete adjoint and against central finite differences (h = 1e-6), for
+the steady problem and for implicit-Euler time stepping with checkpoints.
+"""
+import numpy as np
+import pytest
+
+import sem_oracle as O
+from _helpers import host, meshes, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def gaussian_field(mo, seed, sigma=0.5, nk=8):
+    """Seeded random field sum_{kx,ky<=8} c k^-2 (cos|sin)(...), normalised to std sigma."""
+    rng = np.random.default_rng(seed)
+    g = np.zeros(mo.shape)
+    for kx in range(1, nk + 1):
+        for ky in range(1, nk + 1):
+            a, b = rng.standard_normal(2) / (kx * kx + ky * ky)
+            ph = rng.uniform(0, 2 * np.pi)
+            g += a * np.cos(np.pi * (kx * mo.x + ky * mo.y) + ph) + b * np.sin(np.pi * (kx * mo.x - ky * mo.y))
+    return sigma * (g - g.mean()) / g.std()
+
+
+def oracle_varcoef_solve(mo, M, nu, rhs, k=0.0, tol=1e-13):
+    G = (nu * mo.G11, nu * mo.G12, nu * mo.G22)
+    A = lambda v: O.mask(O.gatherScatter(O.laplace(v, mo.Dr, mo.Ds, *G) + k * mo.B * v, mo), M)  # noqa: E731
+    d = O.jacobi_diag(mo, 1.0, k, M, G=G)
+    return O.pcg(rhs, A, opM=lambda r: r / d, mult=mo.mult, tol=tol)
+
+
+def test_steady_adjoint_matches_oracle_and_fd(gpu):
+    import torch
+
+    import semgb300 as S
+    mo, md = meshes(9, 10, 10, (False, False), "DDDD", 0.05)
+    M = O.generateMask(["D"] * 4, mo)
+    nu = np.exp(gaussian_field(mo, 5))
+    ut = 0.05 * gaussian_field(mo, 6)
+    b = O.gatherScatter(O.mask(O.mass(np.ones(mo.shape), mo), M), mo)
+    tol = 1e-12 * np.abs(b).max()
+    bd = S.as_local(b)
+    Bd = md.B
+
+    def J_dev(nu_np):
+        u = S.linsolve_varcoef(S.as_local(nu_np), bd, md, tol=tol)
+        return 0.5 * torch.sum(Bd * (u - S.as_local(ut)) ** 2).item()
+
+    nu_t = S.as_local(nu).requires_grad_(True)
+    u = S.linsolve_varcoef(nu_t, bd, md, tol=tol)
+    J = 0.5 * torch.sum(Bd * (u - S.as_local(ut)) ** 2)
+    J.backward()
+    g = host(nu_t.grad)
+
+    # oracle: exact discrete adjoint  A lam = mask(QQ'(B (u - ut))), g = -G:(grad lam)(grad u)
+    u_o = oracle_varcoef_solve(mo, M, nu, b, tol=tol)
+    assert rel_l2(host(u), u_o) < 1e-10
+    rhs_adj = O.mask(O.gatherScatter(mo.B * (u_o - ut), mo), M)
+    lam = oracle_varcoef_solve(mo, M, nu, rhs_adj, tol=1e-12 * np.abs(rhs_adj).max())
+    g_o = O.grad_dot(lam, u_o, mo)
+    assert rel_l2(g, g_o) < 1e-8
+
+    # central finite differences along continuous directions; the J evaluations
+    # run native FP64 operators, so that rounding (amplified by 1/h) stays well
+    # below the 1e-5 tolerance
+    md.set_precision(S.SEM_F64)
+    rng = np.random.default_rng(7)
+    for _ in range(4):
+        delta = mo.mult * O.gatherScatter(rng.standard_normal(mo.shape), mo)
+        h = 1e-6
+        fd = (J_dev(nu + h * delta) - J_dev(nu - h * delta)) / (2 * h)
+        ad = float(np.sum(g * delta))
+        assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-14, (fd, ad)
+
+    # the right-hand side examples/semPS.jl:184-186 uses for the adjoint solve,
+    # mult .* QQ'(mask(u_bar)), averages the copies instead of summing them; its
+    # gradient misses the finite differences where the exact one matches them
+    rhs_ps = mo.mult * O.gatherScatter(O.mask(mo.B * (u_o - ut), M), mo)
+    lam_ps = oracle_varcoef_solve(mo, M, nu, rhs_ps, tol=1e-12 * np.abs(rhs_ps).max())
+    g_ps = O.grad_dot(lam_ps, u_o, mo)
+    assert rel_l2(g_ps, g_o) > 1e-3
+
+
+def test_transient_adjoint_with_checkpoints(gpu):
+    import torch
+
+    import semgb300 as S
+    mo, md = meshes(7, 6, 6, (False, False), "DDDD", 0.05)
+    M = O.generateMask(["D"] * 4, mo)
+    nu = np.exp(gaussian_field(mo, 5))
+    ut = 0.05 * gaussian_field(mo, 6)
+    u0 = O.mask(np.sin(np.pi * mo.x) * np.sin(np.pi * mo.y), M)
+    f = np.ones(mo.shape)
+    dt, T, every = 1e-3, 12, 4
+    tol = 1e-13
+
+    # oracle time loop: (K + B/dt) u_n = B u_{n-1}/dt + B f, assembled
+    bf = O.gatherScatter(O.mask(mo.B * f, M), mo)
+    u_o = u0.copy()
+    for _ in range(T):
+        rhs = O.gatherScatter(O.mask(mo.B * u_o / dt, M), mo) + bf
+        u_o = oracle_varcoef_solve(mo, M, nu, rhs, k=1.0 / dt, tol=tol)
+
+    def J_dev(nu_np):
+        u = S.transient_varcoef(S.as_local(nu_np), S.as_local(u0), S.as_local(f), md, dt, T, every, tol=tol)
+        return 0.5 * torch.sum(md.B * (u - S.as_local(ut)) ** 2).item()
+
+    nu_t = S.as_local(nu).requires_grad_(True)
+    uT = S.transient_varcoef(nu_t, S.as_local(u0), S.as_local(f), md, dt, T, every, tol=tol)
+    assert rel_l2(host(uT), u_o) < 1e-10
+    J = 0.5 * torch.sum(md.B * (uT - S.as_local(ut)) ** 2)
+    J.backward()
+    g = host(nu_t.grad)
+    assert np.isfinite(g).all() and np.abs(g).max() > 0
+    md.set_precision(S.SEM_F64)  # FD evaluations in native FP64 (see the steady test)
+    rng = np.random.default_rng(8)
+    for _ in range(2):
+        delta = mo.mult * O.gatherScatter(rng.standard_normal(mo.shape), mo)
+        h = 1e-6
+        fd = (J_dev(nu + h * delta) - J_dev(nu - h * delta)) / (2 * h)
+        ad = float(np.sum(g * delta))
+        assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-16, (fd, ad)
+
+
+def test_diffusion_driver_matches_oracle(gpu):
+    """Diffusion(bc, msh; Ti, Tf, dt, k) stepping (src/diffusion.jl:51-137) with
+    the manufactured solution of examples/d2d.jl:13-33, against the oracle's
+    restatement of opLHS/makeRHS and against the exact solution."""
+    import semgb300 as S
+    n, E = 9, 4
+    mo, md = meshes(n, E, E, (False, False), "DDDD", 0.0)
+    kx = ky = kt = 2.0
+    nu = 1.0
+
+    def ut(x, y, t):
+        return np.sin(kx * np.pi * x) * np.sin(ky * np.pi * y) * np.cos(kt * np.pi * t)
+
+    def forcing(x, y, t):
+        return (ut(x, y, t) * ((kx ** 2 + ky ** 2) * np.pi ** 2 * nu)
+                - np.sin(kx * np.pi * x) * np.sin(ky * np.pi * y) * np.sin(kt * np.pi * t) * (kt * np.pi))
+
+    dt, steps, k = 1e-3, 10, 1
+    dfn = S.Diffusion("DDDD", md, Ti=0.0, Tf=steps * dt, dt=dt, k=k, nu=nu)
+    x, y = host(md.x), host(md.y)
+    dfn.u.copy_(S.as_local(ut(x, y, 0.0)))
+    M = O.generateMask(["D"] * 4, mo)
+    u_o = ut(mo.x, mo.y, 0.0)
+    t = 0.0
+    for _ in range(steps):
+        dfn.evolve(setForcing=lambda fdev, xx, yy, tt: fdev.copy_(S.as_local(forcing(x, y, tt))), tol=1e-12)
+        t += dt
+        a, bb = O.bdfExtK([t, t - dt], k=1)
+        rhs = O.diffusion_makeRHS(mo, nu, forcing(mo.x, mo.y, t), np.zeros(mo.shape), [u_o], bb, M)
+        d = O.jacobi_diag(mo, nu, bb[0], M)
+        u_o = O.pcg(rhs, lambda v: O.diffusion_opLHS(v, mo, nu, bb[0], M), opM=lambda r: r / d,
+                    mult=mo.mult, tol=1e-12)
+    assert rel_l2(host(dfn.u), u_o) < 1e-9
+    assert np.abs(host(dfn.u) - ut(x, y, t)).max() < 5e-3  # implicit Euler, dt = 1e-3
