@@ -273,6 +273,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_extras:
         result["pcg"] = bench_pcg(S, msh, stream)
         result["sweep"] = bench_sweep(S, stream)
+        result["batch"] = bench_batch(S)
     sampler.stop()
     if rank == 0 and world == 1 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -363,6 +364,71 @@ def bench_pcg(S, msh, stream):
                    "res_inf": info["res_inf"], "tol_rel": tolr,
                    "err_vs_exact_inf": (x - ut).abs().max().item()}
     out["cfg1_cfg3_poisson_8x8_n8"] = r
+    return out
+
+
+def bench_batch(S):
+    """cfg4: 512 independent Helmholtz problems (seed 4): Ex, Ey ~ U{4..64},
+    N ~ U{4,6,8,10}, nu log-uniform in [1e-3, 1], lambda ~ U[0, 10], deformation
+    amplitude 0.05, forcing 2 pi^2 sin(pi x) sin(pi y), Dirichlet, Jacobi, tol
+    1e-8 relative; one persistent launch per order.  Also cfg1/cfg3 (one
+    8x8 N=8 Poisson problem) through the same persistent kernel."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(4)
+    meshes, nus, lams, bs, tols = [], [], [], [], []
+    for _ in range(512):
+        Ex, Ey = (int(v) for v in rng.integers(4, 65, size=2))
+        N = int(rng.choice([4, 6, 8, 10]))
+        nus.append(float(10 ** rng.uniform(-3, 0)))
+        lams.append(float(rng.uniform(0, 10)))
+        m = S.Mesh(N + 1, N + 1, Ex, Ey, (False, False), sin_deform(0.05), bc="DDDD")
+        f = 2 * np.pi ** 2 * torch.sin(np.pi * m.x) * torch.sin(np.pi * m.y)
+        M = S.generateMask("DDDD", m)
+        b = S.gatherScatter(S.mask(S.mass(f, m), M), m)
+        meshes.append(m)
+        bs.append(b)
+        tols.append(1e-8 * b.abs().max().item())
+    local = sum(m.shape[0] * m.shape[1] for m in meshes)
+    solver = S.BatchSolver(meshes, nus, lams, jacobi=True)
+    out = {"problems": 512, "local_dof": local}
+    xs = {}
+    for name, prec in (("fp64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED)):
+        infos = []
+        solver.solve(bs, tols, precision=prec, infos=infos)  # warm
+        torch.cuda.synchronize()
+        t = time.time()
+        xs[name] = solver.solve(bs, tols, precision=prec, infos=infos)
+        torch.cuda.synchronize()
+        dt = time.time() - t
+        it = [i["iters"] for i in infos]
+        out[name] = {"batch_s": dt, "solves_per_s": 512 / dt, "converged": sum(i["converged"] for i in infos),
+                     "iters_max": max(it), "iters_mean": float(np.mean(it))}
+    errs = [(torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() for a, b in zip(xs["mixed"], xs["fp64"])]
+    out["mixed"]["rel_l2_vs_fp64_max"] = max(errs)
+    out["mixed_over_fp64"] = out["fp64"]["batch_s"] / out["mixed"]["batch_s"]
+    del solver, meshes, bs, xs
+    # cfg1 / cfg3 through the persistent kernel (one cluster, one problem)
+    m1 = S.Mesh(9, 9, 8, 8, (False, False), sin_deform(0.1), bc="DDDD")
+    ut = torch.sin(np.pi * m1.x) * torch.sin(np.pi * m1.y)
+    M1 = S.generateMask("DDDD", m1)
+    b1 = S.gatherScatter(S.mask(S.mass(2 * np.pi ** 2 * ut, m1), M1), m1)
+    one = S.BatchSolver([m1], [1.0], [0.0], jacobi=True)
+    res = {}
+    for name, prec, tolr in (("cfg1_fp64", S.SEM_F64_DF, 1e-10), ("cfg3_mixed", S.SEM_MIXED, 1e-10)):
+        tol1 = [tolr * b1.abs().max().item()]
+        infos = []
+        one.solve([b1], tol1, precision=prec, infos=infos)
+        torch.cuda.synchronize()
+        reps = 50
+        t = time.time()
+        for _ in range(reps):
+            x = one.solve([b1], tol1, precision=prec, infos=infos)[0]
+        torch.cuda.synchronize()
+        dt = (time.time() - t) / reps
+        res[name] = {"solves_per_s": 1 / dt, "iters": infos[0]["iters"], "outer": infos[0]["outer"],
+                     "err_vs_exact_inf": (x - ut).abs().max().item()}
+    out["cfg1_cfg3_persistent"] = res
     return out
 
 
