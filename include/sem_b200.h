@@ -93,14 +93,24 @@ int sem_mesh_destroy(sem_mesh_t* mesh);
 int sem_mesh_set_bc(sem_mesh_t* mesh, const char* bc);
 /* select the arithmetic of the fused FP64 operators (SEM_F64 or SEM_F64_DF) */
 int sem_mesh_set_precision(sem_mesh_t* mesh, int precision);
+/* number of fused element-operator kernel variants:
+ *   0  two shared-memory line buffers, every input read directly;
+ *   1  as 0, with the geometry, B and nu fields staged by cp.async;
+ *   2  one in-place line buffer, u kept in shared memory for the mass term;
+ *      for SEM_F64_DF the geometry is read pre-split into float pairs (the
+ *      mesh then holds 4 more fields of NX*NY*8 bytes);
+ *   3  as 2, with G11, G12, G22 staged by cp.async.
+ * All variants compute the same operations in the same order: their results
+ * are bit-identical. */
+#define SEM_VARIANTS 4
 /* autotuner (no counterpart in the reference): time every variant of the fused
- * element-operator kernel (direct loads / cp.async-staged inputs) on this mesh,
- * running mask(QQ'(hlmz)) on scratch fields in the given precision (SEM_F64,
- * SEM_F64_DF or SEM_F32), and keep the fastest for all later calls of that
- * precision.  ms_out (nullable) receives one time per variant; chosen
- * (nullable) the variant kept.  Synchronous. */
+ * element-operator kernel on this mesh, running mask(QQ'(hlmz)) on scratch
+ * fields in the given precision (SEM_F64, SEM_F64_DF or SEM_F32), and keep the
+ * fastest for all later calls of that precision.  ms_out (nullable) receives
+ * SEM_VARIANTS times, one per variant; chosen (nullable) the variant kept.
+ * Synchronous. */
 int sem_mesh_autotune(sem_mesh_t* mesh, int precision, double* ms_out, int* chosen);
-/* pin a kernel variant (0 = direct loads, 1 = staged) for one precision */
+/* pin a kernel variant (0 .. SEM_VARIANTS-1) for one precision; synchronous */
 int sem_mesh_set_variant(sem_mesh_t* mesh, int precision, int variant);
 /* copy one geometry field (enum sem_field) into a caller device buffer */
 int sem_mesh_field(sem_mesh_t* mesh, int which, double* out, sem_stream_t stream);

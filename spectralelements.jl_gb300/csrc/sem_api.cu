@@ -168,6 +168,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (!m) return SEM_OK;
   if (m->x) cudaFree(m->x);
   if (m->G11_f) cudaFree(m->G11_f);
+  if (m->Gdf) cudaFree(m->Gdf);
   if (m->ws) cudaFree(m->ws);
   if (m->info) cudaFree(m->info);
   if (m->ops) free_operator_set(m->ops);
@@ -204,6 +205,11 @@ int sem_mesh_set_variant(sem_mesh_t* m, int precision, int variant) {
   if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
   if (precision < SEM_F64 || precision > SEM_F32) return set_error(SEM_ERR_BAD_ARG, "bad precision");
   if (variant < 0 || variant >= kVariants) return set_error(SEM_ERR_BAD_ARG, "bad variant");
+  if (precision == SEM_F64_DF && variant >= 2) {
+    SEM_CHECK(check_device(m));
+    SEM_CHECK(ensure_df_geometry(m, nullptr));
+    SEM_CUDA(cudaStreamSynchronize(nullptr));  // later launches may use any stream
+  }
   m->variant[precision] = variant;
   return SEM_OK;
 }
@@ -217,6 +223,7 @@ int sem_mesh_autotune(sem_mesh_t* m, int precision, double* ms_out, int* chosen)
   const long long L = m->g.NX * m->g.NY;
   const bool f32 = precision == SEM_F32;
   if (f32) SEM_CHECK(ensure_f32_geometry(m, s));
+  if (precision == SEM_F64_DF) SEM_CHECK(ensure_df_geometry(m, s));
   void* out = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int st = SEM_OK;
@@ -234,6 +241,7 @@ int sem_mesh_autotune(sem_mesh_t* m, int precision, double* ms_out, int* chosen)
   c.G12 = f32 ? (const void*)m->G12_f : (const void*)m->G12;
   c.G22 = f32 ? (const void*)m->G22_f : (const void*)m->G22;
   c.B = f32 ? (const void*)m->B_f : (const void*)m->B;
+  c.Gdf = m->Gdf;
   c.nu_s = 0.5;
   c.k_s = 1.0;
   c.mode = m->g.topo | M_STIFF | M_MASS | M_GS | (m->has_bc ? M_MASK : 0u);
@@ -324,6 +332,7 @@ static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, con
   c.precision = m->precision;
   c.skip = nullptr;
   c.variant = m->variant[m->precision];
+  c.Gdf = m->Gdf;
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 
@@ -367,6 +376,7 @@ int sem_varcoef(sem_mesh_t* m, const double* nu_field, double k, const double* u
   c.mode = mode;
   c.precision = m->precision;
   c.variant = m->variant[m->precision];
+  c.Gdf = m->Gdf;
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 

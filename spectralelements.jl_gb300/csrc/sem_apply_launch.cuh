@@ -7,6 +7,7 @@
 #include <utility>
 #include <vector>
 
+#include "sem_apply2.cuh"
 #include "sem_apply_kernels.cuh"
 
 namespace sem {
@@ -83,9 +84,69 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   return SEM_OK;
 }
 
+template <class P, int N, bool STAGE>
+static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                           cudaStream_t s) {
+  typedef TileShape<N> TS;
+  typedef typename P::io io;
+  typedef typename GeoT<P>::type gt;
+  Apply2Args<P, N> a;
+  std::memset(&a, 0, sizeof(a));
+  a.u = static_cast<const io*>(c.u);
+  a.out = static_cast<io*>(c.out);
+  if (P::kPrecision == SEM_F64_DF) {
+    const long long L = g.NX * g.NY;
+    const gt* G = static_cast<const gt*>(c.Gdf);
+    a.G11 = G;
+    a.G12 = G + L;
+    a.G22 = G + 2 * L;
+    a.B = G + 3 * L;
+  } else {
+    a.G11 = static_cast<const gt*>(c.G11);
+    a.G12 = static_cast<const gt*>(c.G12);
+    a.G22 = static_cast<const gt*>(c.G22);
+    a.B = static_cast<const gt*>(c.B);
+  }
+  a.nu = static_cast<const io*>(c.nu);
+  a.nu_s = P::from_double(c.nu_s);
+  a.k_s = P::from_double(c.k_s);
+  a.Ex = g.Ex;
+  a.Ey = g.Ey;
+  a.NX = g.NX;
+  a.mode = c.mode;
+  a.skip = c.skip;
+  fill_eo<P, N>(a.Dr, ops->eo[0]);
+  fill_eo<P, N>(a.Drt, ops->eo[1]);
+  fill_eo<P, N>(a.Ds, ops->eo[2]);
+  fill_eo<P, N>(a.Dst, ops->eo[3]);
+  const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
+  const size_t smem = 2 * te * sizeof(typename P::v) + (STAGE ? 3 * te * sizeof(gt) : 0);
+  auto kern = k_apply2<P, N, TS::TX, TS::TY, STAGE>;
+  if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
+  auto* ev = timing_slot();
+  if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
+  kern<<<grid, TS::THREADS, smem, s>>>(a);
+  SEM_CUDA(cudaGetLastError());
+  if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
+  return SEM_OK;
+}
+
+// variant 0: k_apply, direct loads; 1: k_apply, cp.async-staged inputs;
+// 2: k_apply2, direct loads; 3: k_apply2, cp.async-staged metric terms.
+// Variants 2 and 3 of the double-float policy read the pre-split geometry
+// (ApplyCall::Gdf) and run as variant 0 when the call carries none; a staged
+// variant whose shared memory exceeds the opt-in limit runs unstaged.
 template <class P, int N>
 static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
                           cudaStream_t s) {
+  if (c.variant >= 2 && (P::kPrecision != SEM_F64_DF || c.Gdf)) {
+    typedef TileShape<N> TS;
+    const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
+    const size_t smem = 2 * te * sizeof(typename P::v) + 3 * te * sizeof(typename GeoT<P>::type);
+    if (c.variant == 3 && smem <= max_smem_optin()) return launch_apply_v2<P, N, true>(g, ops, c, s);
+    return launch_apply_v2<P, N, false>(g, ops, c, s);
+  }
   if (c.variant == 1) {
     typedef TileShape<N> TS;
     const size_t te = (size_t)TS::TX * TS::TY * TS::ES;

@@ -3,6 +3,7 @@
 // (src/jac.jl:24-40, src/mesh.jl:111-123).
 #include <cstring>
 
+#include "sem_arith.cuh"
 #include "sem_internal.cuh"
 
 namespace sem {
@@ -85,6 +86,13 @@ __global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, long 
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
        i += (long long)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
+}
+
+// the same split the double-float loads perform (d2df), done once
+__global__ void k_d2df(const double* __restrict__ a, df* __restrict__ b, long long len) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = d2df(a[i]);
 }
 
 __global__ void k_maskfield(double* __restrict__ out, Grid g) {
@@ -187,6 +195,20 @@ int ensure_f32_geometry(sem_mesh* m, cudaStream_t s) {
   k_d2f<<<blocks_for(len), 256, 0, s>>>(m->G12, m->G12_f, len);
   k_d2f<<<blocks_for(len), 256, 0, s>>>(m->G22, m->G22_f, len);
   k_d2f<<<blocks_for(len), 256, 0, s>>>(m->B, m->B_f, len);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int ensure_df_geometry(sem_mesh* m, cudaStream_t s) {
+  if (m->Gdf) return SEM_OK;
+  const long long len = m->g.NX * m->g.NY;
+  df* p = nullptr;
+  SEM_CUDA(cudaMalloc(&p, 4 * sizeof(df) * (size_t)len));
+  m->Gdf = p;
+  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->G11, p, len);
+  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->G12, p + len, len);
+  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->G22, p + 2 * len, len);
+  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->B, p + 3 * len, len);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
 }

@@ -176,6 +176,9 @@ struct sem_mesh {
   double *x, *y, *B, *G11, *G12, *G22;
   // FP32 copies for the mixed-precision inner solve (lazily created)
   float *B_f, *G11_f, *G12_f, *G22_f;
+  // G11, G12, G22, B split into double-float pairs by d2df (lazily created,
+  // read by the double-float kernel variants 2 and 3)
+  sem::df* Gdf;
   sem::OperatorSet* ops;   // coefficient blocks for the kernels
   // solver workspace (lazily created)
   void* ws;
@@ -190,6 +193,7 @@ namespace sem {
 int build_geometry(sem_mesh* m, const double* x_h, const double* y_h, cudaStream_t s);
 int export_field(const sem_mesh* m, int which, double* out, cudaStream_t s);
 int ensure_f32_geometry(sem_mesh* m, cudaStream_t s);
+int ensure_df_geometry(sem_mesh* m, cudaStream_t s);
 
 // operator coefficients (sem_apply.cu)
 int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** out);
@@ -208,10 +212,11 @@ struct ApplyCall {
   unsigned mode;   // M_* bits (topology bits included)
   int precision;   // SEM_F64, SEM_F64_DF, SEM_F32
   const int* skip; // device flag: when non-zero the launch does nothing (solver loops)
-  int variant;     // kernel variant: 0 = direct loads, 1 = cp.async-staged inputs
+  int variant;     // kernel variant 0..kVariants-1 (launch_apply_n in sem_apply_launch.cuh)
+  const void* Gdf; // G11, G12, G22, B split into double-float pairs (4 blocks of NX*NY), or NULL
 };
 
-constexpr int kVariants = 2;
+constexpr int kVariants = SEM_VARIANTS;
 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
 int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned mode, int precision,

@@ -449,6 +449,7 @@ struct OpCtx {
   bool has_bc;
   const double *G11, *G12, *G22, *B;
   const float *G11f, *G12f, *G22f, *Bf;
+  const void* Gdf;     // double-float split geometry (or NULL)
   const int* variant;  // per precision
 };
 
@@ -465,6 +466,7 @@ OpCtx ctx_of(const sem_mesh* m) {
   cx.G12f = m->G12_f;
   cx.G22f = m->G22_f;
   cx.Bf = m->B_f;
+  cx.Gdf = m->Gdf;
   cx.variant = m->variant;
   return cx;
 }
@@ -519,6 +521,7 @@ int run_cg(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap
   if (k == 0.0) c.mode &= ~M_MASS;
   c.precision = op_precision;
   c.variant = cx.variant[op_precision];
+  c.Gdf = cx.Gdf;
   c.skip = &w.sc->done;
   const unsigned nb = nblocks(L);
   for (;;) {
@@ -615,6 +618,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     c.mode = cx.g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (cx.has_bc ? M_MASK : 0u);
     c.precision = m->precision;
     c.variant = cx.variant[m->precision];
+    c.Gdf = cx.Gdf;
     bool nan = rmax != rmax;
     while (!(rmax <= o->tol) && !nan && outer < max_outer) {
       ++outer;

@@ -188,7 +188,7 @@ class Mesh:
         """Time the fused-kernel variants on this mesh and keep the fastest
         (per precision); returns {variant: ms}."""
         prec = self.precision if precision is None else int(precision)
-        ms = (ctypes.c_double * 2)()
+        ms = (ctypes.c_double * _lib.SEM_VARIANTS)()
         ch = ctypes.c_int()
         _lib.check(self._lib.sem_mesh_autotune(self._h, prec, ms, ctypes.byref(ch)))
         return {"chosen": ch.value, "ms": list(ms)}

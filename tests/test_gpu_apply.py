@@ -38,10 +38,12 @@ def _ids(c):
 
 @pytest.mark.parametrize("case", CASES, ids=_ids)
 @pytest.mark.parametrize("prec", ["F64", "DF"])
-def test_fused_operators(gpu, case, prec):
+@pytest.mark.parametrize("variant", [0, 2])
+def test_fused_operators(gpu, case, prec, variant):
     import semgb300 as S
     n, Ex, Ey, per, bc, amp = case
     mo, md = meshes(n, Ex, Ey, per, bc, amp, precision=getattr(S, "SEM_" + ("F64" if prec == "F64" else "F64_DF")))
+    md.set_variant(variant)
     M = O.generateMask(list(bc), mo)
     rng = np.random.default_rng(3)
     u = rng.uniform(-1, 1, mo.shape)
@@ -73,6 +75,56 @@ def test_fused_operators(gpu, case, prec):
     got = host(S.lapl(ud, [], [], [], [], [], np.kron(np.eye(Ex), mo.Dr), np.kron(np.eye(Ey), mo.Ds),
                       S.as_local(mo.G11), S.as_local(mo.G12), S.as_local(mo.G22), md.mult))
     assert rel_l2(got, O.lapl(u, mo)) < TOL
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+def test_kernel_variants_bit_identical(gpu, case):
+    """Every fused-kernel variant computes the same operations in the same
+    order, so its output is bit-identical to variant 0 (FP64, double-float,
+    and the FP32 operator through the mixed-precision solve)."""
+    import semgb300 as S
+    import torch
+    n, Ex, Ey, per, bc, amp = case
+    mo, md = meshes(n, Ex, Ey, per, bc, amp)
+    rng = np.random.default_rng(5)
+    ud = S.as_local(rng.uniform(-1, 1, mo.shape))
+    nu = S.as_local(rng.uniform(0.5, 2.0, mo.shape))
+    for prec in (S.SEM_F64, S.SEM_F64_DF):
+        md.set_precision(prec)
+        outs = []
+        for v in range(S._lib.SEM_VARIANTS):
+            md.set_variant(v)
+            outs.append([host(S.lapl(ud, md)), host(S.lapl(ud, nu, md)), host(S.mass(ud, md)),
+                         host(S.HelmholtzOp(md, 1e-2, 1.0)(ud)),
+                         host(S.HelmholtzOp(md, 1.0, 0.5, nu_field=nu)(ud))])
+        for v in range(1, len(outs)):
+            for a, b in zip(outs[0], outs[v]):
+                np.testing.assert_array_equal(a, b)
+    # FP32 inner operator: identical mixed-precision solves for every variant
+    md.set_precision(S.SEM_F64_DF)
+    md.set_variant(0)
+    M = O.generateMask(list(bc), mo)
+    b = S.as_local(O.mask(O.gatherScatter(mo.B * rng.standard_normal(mo.shape), mo), M))
+    op = S.HelmholtzOp(md, 0.5, 1.0)
+    tol = 1e-10 * float(torch.max(torch.abs(b)))
+    xs = []
+    for v in range(S._lib.SEM_VARIANTS):
+        md.set_variant(v, S.SEM_F32)
+        info = {}
+        xs.append((host(S.pcg(b, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info,
+                              precision=S.SEM_MIXED)), info["iters"]))
+    for x, it in xs[1:]:
+        assert it == xs[0][1]
+        np.testing.assert_array_equal(x, xs[0][0])
+
+
+def test_autotune_reports_every_variant(gpu):
+    import semgb300 as S
+    _, md = meshes(8, 40, 30, (False, False), "DDDD", 0.05)
+    for prec in (S.SEM_F64, S.SEM_F64_DF, S.SEM_F32):
+        t = md.autotune(prec)
+        assert len(t["ms"]) == S._lib.SEM_VARIANTS and all(m > 0 for m in t["ms"]), t
+        assert t["ms"][t["chosen"]] == min(t["ms"])
 
 
 @pytest.mark.parametrize("case", CASES[:6], ids=_ids)

@@ -66,6 +66,13 @@ def test_library_exports_every_declared_symbol(built):
     assert lib.sem_abi_version() == 1
 
 
+def test_header_constants_match_binding():
+    src = open(os.path.join(ROOT, "include", "sem_b200.h")).read()
+    defines = dict(re.findall(r"#define\s+(SEM_[A-Z_]+)\s+(\d+)", src))
+    assert int(defines["SEM_VARIANTS"]) == _lib.SEM_VARIANTS
+    assert int(defines["SEM_NOALLOC_MAX_LOCAL"]) > 0
+
+
 def test_argument_validation_needs_no_gpu(built):
     lib = built
     h = ctypes.c_void_p()
