@@ -245,15 +245,14 @@ def run_ours(args, rank, world, local_rank):
 
     peak, peak_kind = load_peaks()
     variant = tune["f64_df"]["chosen"]
-    kname = "k_apply2" if variant >= 2 else "k_apply"
-    staged = variant % 2 == 1
+    kname = ("k_apply", "k_apply", "k_apply2", "k_apply2", "k_apply3")[variant]
+    ktempl = "<PDF,9,8,3>" if variant == 4 else f"<PDF,9,8,3,{'true' if variant % 2 else 'false'}>"
     bytes_launch = BYTES_PER_LOCAL * L
     achieved = bytes_launch / (kernel_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": profiled_traffic(f"{kname}_hlmz_df_256x256_n8.md"),
-                "kernel": f"{kname}<PDF,9,8,3,{'true' if staged else 'false'}> (fused element operator, "
-                          f"double-float, autotuned variant {variant})",
+                "kernel": f"{kname}{ktempl} (fused element operator, double-float, autotuned variant {variant})",
                 "kernel_ms": kernel_ms, "kernel_launches_timed": kn.value,
                 "algorithmic_bytes_per_launch": bytes_launch,
                 "flops_per_launch": (8 * 9 ** 3 + 7 * 9 ** 2) * E_X * E_Y,

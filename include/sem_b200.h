@@ -99,10 +99,12 @@ int sem_mesh_set_precision(sem_mesh_t* mesh, int precision);
  *   2  one in-place line buffer, u kept in shared memory for the mass term;
  *      for SEM_F64_DF the geometry is read pre-split into float pairs (the
  *      mesh then holds 4 more fields of NX*NY*8 bytes);
- *   3  as 2, with G11, G12, G22 staged by cp.async.
+ *   3  as 2, with G11, G12, G22 staged by cp.async;
+ *   4  as 2, in a persistent grid whose CTAs prefetch the next element tile's
+ *      inputs (cp.async) while they compute the current one.
  * All variants compute the same operations in the same order: their results
  * are bit-identical. */
-#define SEM_VARIANTS 4
+#define SEM_VARIANTS 5
 /* autotuner (no counterpart in the reference): time every variant of the fused
  * element-operator kernel on this mesh, running mask(QQ'(hlmz)) on scratch
  * fields in the given precision (SEM_F64, SEM_F64_DF or SEM_F32), and keep the

@@ -169,6 +169,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (m->x) cudaFree(m->x);
   if (m->G11_f) cudaFree(m->G11_f);
   if (m->Gdf) cudaFree(m->Gdf);
+  free_graph_cache(m);
   if (m->ws) cudaFree(m->ws);
   if (m->info) cudaFree(m->info);
   if (m->ops) free_operator_set(m->ops);

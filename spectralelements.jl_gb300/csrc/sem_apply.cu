@@ -1,4 +1,5 @@
 // Host side of the fused operator kernels: coefficient sets and launches.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -28,6 +29,11 @@ std::pair<cudaEvent_t, cudaEvent_t>* timing_slot() {
     g_pool.emplace_back(a, b);
   }
   return &g_pool[g_used++];
+}
+
+bool timing_enabled() {
+  std::lock_guard<std::mutex> lk(g_tmu);
+  return g_timing;
 }
 
 size_t max_smem_optin() {
@@ -103,21 +109,27 @@ int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** o
 
 void free_operator_set(OperatorSet* o) { delete o; }
 
-// tile shape of the fused kernel for a given n (host mirror of TileShape)
-static void tile_of(int n, int* TX, int* TY) {
-  *TX = 8;
-  *TY = n <= 4 ? 8 : (n <= 8 ? 4 : (n <= 12 ? 3 : 2));
+int num_sms() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cached[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 152;
+    cached[dev] = v;
+  }
+  return cached[dev];
 }
 
-int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned mode,
-                     int precision, const int* skip, cudaStream_t s) {
-  (void)ops;
+int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
+                     int TY, cudaStream_t s) {
   if (!(mode & M_GS)) return SEM_OK;
   FixArgs f;
   f.n = g.n;
   f.Ex = g.Ex;
   f.Ey = g.Ey;
-  tile_of(g.n, &f.TX, &f.TY);
+  f.TX = TX;
+  f.TY = TY;
   f.NX = g.NX;
   f.NY = g.NY;
   f.mode = mode;
@@ -125,31 +137,35 @@ int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned 
   const bool perx = (mode & M_PERX) != 0, pery = (mode & M_PERY) != 0;
   f.nxi = (g.Ex - 1) / f.TX + (perx ? 1 : 0);
   f.nyi = (g.Ey - 1) / f.TY + (pery ? 1 : 0);
-  const long long total = f.nxi * f.NY + f.nyi * f.NX + f.nxi * f.nyi;
-  if (total == 0) return SEM_OK;
+  const long long nI = f.nxi + f.nyi + (f.nxi * f.nyi > 0 ? 1 : 0);
+  if (nI == 0) return SEM_OK;
   const int threads = 256;
-  long long blocks = (total + threads - 1) / threads;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  long long along = std::max(std::max(f.NX, f.NY), f.nxi * f.nyi);
+  long long bx = (along + threads - 1) / threads;
+  if (bx > 64) bx = 64;
+  const dim3 grid((unsigned)bx, (unsigned)std::min(nI, 65535LL));
   if (precision == SEM_F32)
-    k_dss_fixup<float><<<(unsigned)blocks, threads, 0, s>>>(static_cast<float*>(out), f);
+    k_dss_fixup<float><<<grid, threads, 0, s>>>(static_cast<float*>(out), f);
   else
-    k_dss_fixup<double><<<(unsigned)blocks, threads, 0, s>>>(static_cast<double*>(out), f);
+    k_dss_fixup<double><<<grid, threads, 0, s>>>(static_cast<double*>(out), f);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
 }
 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s) {
   int st;
+  int tile[2] = {0, 0};
+  const bool hi = g.n >= 10;
   if (c.precision == SEM_F64)
-    st = launch_apply_f64(g, ops, c, s);
+    st = hi ? launch_apply_f64_hi(g, ops, c, s, tile) : launch_apply_f64_lo(g, ops, c, s, tile);
   else if (c.precision == SEM_F64_DF)
-    st = launch_apply_df(g, ops, c, s);
+    st = hi ? launch_apply_df_hi(g, ops, c, s, tile) : launch_apply_df_lo(g, ops, c, s, tile);
   else if (c.precision == SEM_F32)
-    st = launch_apply_f32(g, ops, c, s);
+    st = hi ? launch_apply_f32_hi(g, ops, c, s, tile) : launch_apply_f32_lo(g, ops, c, s, tile);
   else
     return set_error(SEM_ERR_BAD_ARG, "unknown precision %d", c.precision);
   if (st != SEM_OK) return st;
-  return launch_dss_fixup(g, ops, c.out, c.mode, c.precision, c.skip, s);
+  return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s);
 }
 
 }  // namespace sem

@@ -56,8 +56,17 @@ struct Apply2Args {
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
 
+// resident blocks per SM asked of the register allocator: without the
+// register copy of u the double-float kernel fits four blocks (72 registers,
+// no spills) up to n = 9
+template <class P, int N, bool STAGE>
+struct MinBlocks2 {
+  static constexpr int value =
+      (!STAGE && P::kPrecision == SEM_F64_DF && N <= 9) ? 4 : MinBlocks<P, N, STAGE>::value;
+};
+
 template <class P, int N, int TX, int TY, bool STAGE>
-__global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
+__global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
     k_apply2(const __grid_constant__ Apply2Args<P, N> a) {
   typedef typename P::v V;
   typedef typename P::io IO;
@@ -189,51 +198,9 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     }
   }
 
-  const bool gs = (mode & M_GS) != 0;
-  const bool perx = (mode & M_PERX) != 0;
-  const bool pery = (mode & M_PERY) != 0;
-  if (gs) {
-    // x pairs inside the tile: every thread stores its own row, then reads the
-    // neighbour element's edge row
-#pragma unroll
-    for (int j = 0; j < N; ++j) s1[j * SP + lane] = res[j];
-    __syncthreads();
-    if (lane == N - 1 && exl + 1 < TX && ex + 1 < a.Ex) {
-      const V* nb = S1 + (elem + 1) * ES;
-#pragma unroll
-      for (int j = 0; j < N; ++j) res[j] = P::add(res[j], nb[j * SP]);
-    }
-    if (lane == 0 && exl > 0) {
-      const V* nb = S1 + (elem - 1) * ES;
-#pragma unroll
-      for (int j = 0; j < N; ++j) res[j] = P::add(nb[j * SP + N - 1], res[j]);
-    }
-    // y pairs inside the tile through s0 (u is no longer needed)
-    s0[lane] = res[0];
-    s0[(N - 1) * SP + lane] = res[N - 1];
-    __syncthreads();
-    if (eyl + 1 < TY && ey + 1 < a.Ey) res[N - 1] = P::add(res[N - 1], S0[(elem + TX) * ES + lane]);
-    if (eyl > 0) res[0] = P::add(S0[(elem - TX) * ES + (N - 1) * SP + lane], res[0]);
-  }
-  if (!valid) return;
-
-  const bool xc = gs && xcross_row(ex, lane, N, a.Ex, TX, perx);
-  const long long row = (long long)ex * N + lane;
-  const long long NY = (long long)a.Ey * N;
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-    bool raw = xc;
-    if (gs) {
-      if (j == 0 && eyl == 0 && (ey > 0 || pery)) raw = true;
-      if (j == N - 1 && (eyl == TY - 1 || ey == a.Ey - 1) && (ey < a.Ey - 1 || pery)) raw = true;
-    }
-    IO val = P::st(res[j]);
-    if (!raw && (mode & M_MASK)) {
-      const long long col = (long long)ey * N + j;
-      if (!mask_keep(row, col, NX, NY, mode)) val = masked_zero(val);
-    }
-    a.out[base + (long long)j * NX] = val;
-  }
+  static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
+  tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
+                               ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
 }
 
 }  // namespace sem

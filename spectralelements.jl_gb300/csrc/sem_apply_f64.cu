@@ -1,8 +1,9 @@
-// Fused element-operator kernels, PF64 arithmetic (all n from 2 to 17).
+// Fused element-operator kernels, native FP64 arithmetic, n = 2..9.
 #include "sem_apply_launch.cuh"
 
 namespace sem {
-int launch_apply_f64(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s) {
-  return launch_apply_p<PF64>(g, ops, c, s);
+int launch_apply_f64_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s,
+                        int* tile) {
+  return launch_apply_range<PF64, 2, 9>(g, ops, c, s, tile);
 }
 }  // namespace sem

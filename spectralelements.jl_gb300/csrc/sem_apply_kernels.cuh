@@ -121,6 +121,75 @@ __host__ __device__ inline bool xcross_row(int ex, int i, int n, int Ex, int TX,
   return false;
 }
 
+// QQ' inside the tile, the mask, and the store of one thread's row.  Each
+// local value is first rounded to the storage type; the copies of a node are
+// then summed in storage arithmetic, x pairs before y pairs, so every node
+// gets exactly the sums of k_gather_scatter on the rounded values, whatever
+// the tile shape.  A row on a cross-tile x interface takes no in-tile y pair:
+// k_dss_fixup finishes its corners in the same x-first order.  Points with
+// copies in another tile are stored unsummed and unmasked.  X1 and X0 are
+// two tile-sized shared buffers free for reuse; every thread of the block
+// calls this (it holds barriers).
+template <class P, int N, int TX, int TY>
+__device__ __forceinline__ void tile_dss_store(const typename P::v (&res)[N], typename P::io* X1,
+                                               typename P::io* X0, int elem, int lane, int ex,
+                                               int ey, bool valid, long long base, int Ex, int Ey,
+                                               long long NX, unsigned mode, typename P::io* out) {
+  typedef typename P::io IO;
+  constexpr int SP = N | 1;
+  constexpr int ES = N * SP;
+  const int exl = elem % TX;
+  const int eyl = elem / TX;
+  const bool gs = (mode & M_GS) != 0;
+  const bool perx = (mode & M_PERX) != 0;
+  const bool pery = (mode & M_PERY) != 0;
+  IO rv[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) rv[j] = P::st(res[j]);
+  const bool xrow = gs && xcross_row(ex, lane, N, Ex, TX, perx);
+  if (gs) {
+    // x pairs inside the tile: row n-1 of element exl with row 0 of exl+1
+    IO* x1 = X1 + elem * ES;
+#pragma unroll
+    for (int j = 0; j < N; ++j) x1[j * SP + lane] = rv[j];
+    __syncthreads();
+    if (lane == N - 1 && exl + 1 < TX && ex + 1 < Ex) {
+      const IO* nb = X1 + (elem + 1) * ES;
+#pragma unroll
+      for (int j = 0; j < N; ++j) rv[j] = io_add(rv[j], nb[j * SP]);
+    }
+    if (lane == 0 && exl > 0) {
+      const IO* nb = X1 + (elem - 1) * ES;
+#pragma unroll
+      for (int j = 0; j < N; ++j) rv[j] = io_add(nb[j * SP + N - 1], rv[j]);
+    }
+    // y pairs inside the tile: column n-1 of element eyl with column 0 of eyl+1
+    IO* x0 = X0 + elem * ES;
+    x0[lane] = rv[0];
+    x0[(N - 1) * SP + lane] = rv[N - 1];
+    __syncthreads();
+    if (!xrow && eyl + 1 < TY && ey + 1 < Ey) rv[N - 1] = io_add(rv[N - 1], X0[(elem + TX) * ES + lane]);
+    if (!xrow && eyl > 0) rv[0] = io_add(X0[(elem - TX) * ES + (N - 1) * SP + lane], rv[0]);
+  }
+  if (!valid) return;
+  const long long row = (long long)ex * N + lane;
+  const long long NY = (long long)Ey * N;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    bool raw = xrow;
+    if (gs) {
+      if (j == 0 && eyl == 0 && (ey > 0 || pery)) raw = true;
+      if (j == N - 1 && (eyl == TY - 1 || ey == Ey - 1) && (ey < Ey - 1 || pery)) raw = true;
+    }
+    IO val = rv[j];
+    if (!raw && (mode & M_MASK)) {
+      const long long col = (long long)ey * N + j;
+      if (!mask_keep(row, col, NX, NY, mode)) val = masked_zero(val);
+    }
+    out[base + (long long)j * NX] = val;
+  }
+}
+
 template <class P, int N, int TX, int TY, bool STAGE>
 __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     k_apply(const __grid_constant__ ApplyArgs<P, N> a) {
@@ -256,56 +325,19 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     }
   }
 
-  const bool gs = (mode & M_GS) != 0;
-  const bool perx = (mode & M_PERX) != 0;
-  const bool pery = (mode & M_PERY) != 0;
-  if (gs) {
-    // x pairs inside the tile: row n-1 of element exl with row 0 of exl+1
-    if (!stiff) __syncthreads();
-#pragma unroll
-    for (int j = 0; j < N; ++j) s1[j * SP + lane] = res[j];
-    __syncthreads();
-    if (lane == N - 1 && exl + 1 < TX && ex + 1 < a.Ex) {
-      const V* nb = S1 + (elem + 1) * ES;
-#pragma unroll
-      for (int j = 0; j < N; ++j) res[j] = P::add(res[j], nb[j * SP]);
-    }
-    if (lane == 0 && exl > 0) {
-      const V* nb = S1 + (elem - 1) * ES;
-#pragma unroll
-      for (int j = 0; j < N; ++j) res[j] = P::add(nb[j * SP + N - 1], res[j]);
-    }
-    // y pairs inside the tile: column n-1 of element eyl with column 0 of eyl+1
-    s2[lane] = res[0];
-    s2[(N - 1) * SP + lane] = res[N - 1];
-    __syncthreads();
-    if (eyl + 1 < TY && ey + 1 < a.Ey) res[N - 1] = P::add(res[N - 1], S2[(elem + TX) * ES + lane]);
-    if (eyl > 0) res[0] = P::add(S2[(elem - TX) * ES + (N - 1) * SP + lane], res[0]);
-  }
-  if (!valid) return;
-
-  const bool xc = gs && xcross_row(ex, lane, N, a.Ex, TX, perx);
-  const long long row = (long long)ex * N + lane;
-  const long long NY = (long long)a.Ey * N;
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-    bool raw = xc;
-    if (gs) {
-      if (j == 0 && eyl == 0 && (ey > 0 || pery)) raw = true;
-      if (j == N - 1 && (eyl == TY - 1 || ey == a.Ey - 1) && (ey < a.Ey - 1 || pery)) raw = true;
-    }
-    IO val = P::st(res[j]);
-    if (!raw && (mode & M_MASK)) {
-      const long long col = (long long)ey * N + j;
-      if (!mask_keep(row, col, NX, NY, mode)) val = masked_zero(val);
-    }
-    a.out[base + (long long)j * NX] = val;
-  }
+  static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
+  tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S2), elem, lane,
+                               ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
 }
 
 // Finishes QQ' (and the mask) at the points whose copies sit in different
 // tiles: x interfaces every TX elements (+ the periodic wrap), y interfaces
-// every TY elements (+ wrap), and the corners where both meet.
+// every TY elements (+ wrap), and the corners on them.  Every node with four
+// copies is summed x pairs first, ((rl,cl) + (rr,cl)) + ((rl,cr) + (rr,cr)),
+// the order the in-tile pass and k_gather_scatter use, so the result does not
+// depend on the tile shape.  blockIdx.y walks the interfaces (x interfaces,
+// then y interfaces, then one row for the corners of two cross-tile
+// interfaces), blockIdx.x/threadIdx.x the points along one interface.
 struct FixArgs {
   int n, Ex, Ey, TX, TY;
   long long NX, NY;
@@ -319,72 +351,78 @@ __host__ __device__ inline long long fix_iface(long long q, int T, bool per) {
 }
 
 template <class IO>
+__device__ __forceinline__ void fix_store(IO* out, long long r, long long c, IO s, const FixArgs& f,
+                                          bool msk) {
+  if (msk && !mask_keep(r, c, f.NX, f.NY, f.mode)) s = masked_zero(s);
+  out[r + c * f.NX] = s;
+}
+
+template <class IO>
 __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
   if (f.skip && *f.skip) return;
   const bool perx = (f.mode & M_PERX) != 0;
   const bool pery = (f.mode & M_PERY) != 0;
   const bool msk = (f.mode & M_MASK) != 0;
-  const long long nX = f.nxi * f.NY;
-  const long long nY = f.nyi * f.NX;
-  const long long nC = f.nxi * f.nyi;
-  const long long total = nX + nY + nC;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    if (idx < nX) {
-      const long long q = idx / f.NY;
-      const long long c = idx - q * f.NY;
-      const long long ey = c / f.n;
-      const int j = (int)(c - ey * f.n);
-      if (xcross_row((int)ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner
+  const long long ncorner = f.nxi * f.nyi;
+  const long long nI = f.nxi + f.nyi + (ncorner > 0 ? 1 : 0);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned n = (unsigned)f.n;
+  for (long long q = blockIdx.y; q < nI; q += gridDim.y) {
+    if (q < f.nxi) {
+      // x interface q: rows rl | rr, every column c
       const long long a = fix_iface(q, f.TX, perx);
       const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
       const long long rr = a * f.n;
-      const IO s = out[rl + c * f.NX] + out[rr + c * f.NX];
-      IO sl = s, sr = s;
-      if (msk) {
-        if (!mask_keep(rl, c, f.NX, f.NY, f.mode)) sl = masked_zero(s);
-        if (!mask_keep(rr, c, f.NX, f.NY, f.mode)) sr = masked_zero(s);
-      }
-      out[rl + c * f.NX] = sl;
-      out[rr + c * f.NX] = sr;
-    } else if (idx < nX + nY) {
-      const long long id2 = idx - nX;
-      const long long q = id2 / f.NX;
-      const long long r = id2 - q * f.NX;
-      const long long ex = r / f.n;
-      const int i = (int)(r - ex * f.n);
-      if (xcross_row((int)ex, i, f.n, f.Ex, f.TX, perx)) continue;  // corner
-      const long long b = fix_iface(q, f.TY, pery);
-      const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
-      const long long cr = b * f.n;
-      const IO s = out[r + cl * f.NX] + out[r + cr * f.NX];
-      IO sl = s, sr = s;
-      if (msk) {
-        if (!mask_keep(r, cl, f.NX, f.NY, f.mode)) sl = masked_zero(s);
-        if (!mask_keep(r, cr, f.NX, f.NY, f.mode)) sr = masked_zero(s);
-      }
-      out[r + cl * f.NX] = sl;
-      out[r + cr * f.NX] = sr;
-    } else {
-      const long long id3 = idx - nX - nY;
-      const long long q = id3 / f.nyi;
-      const long long p = id3 - q * f.nyi;
-      const long long a = fix_iface(q, f.TX, perx);
-      const long long b = fix_iface(p, f.TY, pery);
-      const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
-      const long long rr = a * f.n;
-      const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
-      const long long cr = b * f.n;
-      const IO s = (out[rl + cl * f.NX] + out[rr + cl * f.NX]) +
-                   (out[rl + cr * f.NX] + out[rr + cr * f.NX]);
-      const long long rs[2] = {rl, rr};
-      const long long cs[2] = {cl, cr};
-      for (int u = 0; u < 2; ++u)
-        for (int v = 0; v < 2; ++v) {
-          IO val = s;
-          if (msk && !mask_keep(rs[u], cs[v], f.NX, f.NY, f.mode)) val = masked_zero(s);
-          out[rs[u] + cs[v] * f.NX] = val;
+      for (long long c = first; c < f.NY; c += stride) {
+        const int ey = (int)((unsigned long long)c / n);
+        const int j = (int)(c - (long long)ey * f.n);
+        if (xcross_row(ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner of two cross-tile interfaces
+        if (j == 0 && ey > 0) continue;                            // in-tile y pair, done from column c-1
+        if (j == f.n - 1 && ey + 1 < f.Ey) {
+          // in-tile y interface: four copies
+          const long long c2 = c + 1;
+          const IO s = (out[rl + c * f.NX] + out[rr + c * f.NX]) + (out[rl + c2 * f.NX] + out[rr + c2 * f.NX]);
+          fix_store(out, rl, c, s, f, msk);
+          fix_store(out, rr, c, s, f, msk);
+          fix_store(out, rl, c2, s, f, msk);
+          fix_store(out, rr, c2, s, f, msk);
+          continue;
         }
+        const IO s = out[rl + c * f.NX] + out[rr + c * f.NX];
+        fix_store(out, rl, c, s, f, msk);
+        fix_store(out, rr, c, s, f, msk);
+      }
+    } else if (q < f.nxi + f.nyi) {
+      // y interface: columns cl | cr, every row r (rows on cross-tile x
+      // interfaces are corners)
+      const long long b = fix_iface(q - f.nxi, f.TY, pery);
+      const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
+      const long long cr = b * f.n;
+      for (long long r = first; r < f.NX; r += stride) {
+        const int ex = (int)((unsigned long long)r / n);
+        const int i = (int)(r - (long long)ex * f.n);
+        if (xcross_row(ex, i, f.n, f.Ex, f.TX, perx)) continue;
+        const IO s = out[r + cl * f.NX] + out[r + cr * f.NX];
+        fix_store(out, r, cl, s, f, msk);
+        fix_store(out, r, cr, s, f, msk);
+      }
+    } else {
+      for (long long id = first; id < ncorner; id += stride) {
+        const long long qx = id / f.nyi;
+        const long long qy = id - qx * f.nyi;
+        const long long a = fix_iface(qx, f.TX, perx);
+        const long long b = fix_iface(qy, f.TY, pery);
+        const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
+        const long long rr = a * f.n;
+        const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
+        const long long cr = b * f.n;
+        const IO s = (out[rl + cl * f.NX] + out[rr + cl * f.NX]) + (out[rl + cr * f.NX] + out[rr + cr * f.NX]);
+        fix_store(out, rl, cl, s, f, msk);
+        fix_store(out, rr, cl, s, f, msk);
+        fix_store(out, rl, cr, s, f, msk);
+        fix_store(out, rr, cr, s, f, msk);
+      }
     }
   }
 }

@@ -8,15 +8,22 @@
 #include <vector>
 
 #include "sem_apply2.cuh"
+#include "sem_apply3.cuh"
 #include "sem_apply_kernels.cuh"
 
 namespace sem {
 
 std::pair<cudaEvent_t, cudaEvent_t>* timing_slot();
 size_t max_smem_optin();
-int launch_apply_f64(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
-int launch_apply_df(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
-int launch_apply_f32(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
+int num_sms();
+// per-policy launchers, one translation unit each for n <= 9 and n >= 10; tile
+// receives the element tile (TX, TY) of the launched kernel for k_dss_fixup
+int launch_apply_f64_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
+int launch_apply_f64_hi(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
+int launch_apply_df_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
+int launch_apply_df_hi(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
+int launch_apply_f32_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
+int launch_apply_f32_hi(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
 
 template <class P, int N>
 static void fill_eo(EOCoef<N, typename P::v>& c, const double* src) {
@@ -84,13 +91,10 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   return SEM_OK;
 }
 
-template <class P, int N, bool STAGE>
-static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
-                           cudaStream_t s) {
-  typedef TileShape<N> TS;
+template <class P, int N>
+static void fill_args2(Apply2Args<P, N>& a, const Grid& g, const OperatorSet* ops, const ApplyCall& c) {
   typedef typename P::io io;
   typedef typename GeoT<P>::type gt;
-  Apply2Args<P, N> a;
   std::memset(&a, 0, sizeof(a));
   a.u = static_cast<const io*>(c.u);
   a.out = static_cast<io*>(c.out);
@@ -119,6 +123,15 @@ static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCal
   fill_eo<P, N>(a.Drt, ops->eo[1]);
   fill_eo<P, N>(a.Ds, ops->eo[2]);
   fill_eo<P, N>(a.Dst, ops->eo[3]);
+}
+
+template <class P, int N, bool STAGE>
+static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                           cudaStream_t s) {
+  typedef TileShape<N> TS;
+  typedef typename GeoT<P>::type gt;
+  Apply2Args<P, N> a;
+  fill_args2<P, N>(a, g, ops, c);
   const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
   const size_t smem = 2 * te * sizeof(typename P::v) + (STAGE ? 3 * te * sizeof(gt) : 0);
   auto kern = k_apply2<P, N, TS::TX, TS::TY, STAGE>;
@@ -132,23 +145,63 @@ static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCal
   return SEM_OK;
 }
 
+// persistent prefetching kernel: grid = resident CTAs, balanced so that every
+// CTA walks the same number of tiles (up to one)
+template <class P, int N>
+static int launch_apply_v3(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                           cudaStream_t s) {
+  typedef PTile<N> TS;
+  typedef typename GeoT<P>::type gt;
+  Apply2Args<P, N> a;
+  fill_args2<P, N>(a, g, ops, c);
+  const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
+  const size_t smem = 2 * te * sizeof(typename P::v) +
+                      (size_t)N * TS::THREADS * (4 * sizeof(gt) + sizeof(typename P::io));
+  auto kern = k_apply3<P, N, TS::TX, TS::TY>;
+  if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  SEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TS::THREADS, smem));
+  if (per_sm < 1) return set_error(SEM_ERR_UNSUPPORTED, "persistent operator kernel does not fit an SM (n = %d)", N);
+  const int tiles_x = (g.Ex + TS::TX - 1) / TS::TX;
+  const int tiles_y = (g.Ey + TS::TY - 1) / TS::TY;
+  const long long tiles = (long long)tiles_x * tiles_y;
+  if (tiles > 2147483647LL) return set_error(SEM_ERR_UNSUPPORTED, "too many element tiles");
+  const long long slots = (long long)per_sm * num_sms();
+  const long long rounds = (tiles + slots - 1) / slots;
+  const long long grid = (tiles + rounds - 1) / rounds;
+  auto* ev = timing_slot();
+  if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
+  kern<<<(unsigned)grid, TS::THREADS, smem, s>>>(a, tiles_x, (int)tiles);
+  SEM_CUDA(cudaGetLastError());
+  if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
+  return SEM_OK;
+}
+
 // variant 0: k_apply, direct loads; 1: k_apply, cp.async-staged inputs;
-// 2: k_apply2, direct loads; 3: k_apply2, cp.async-staged metric terms.
-// Variants 2 and 3 of the double-float policy read the pre-split geometry
+// 2: k_apply2, direct loads; 3: k_apply2, cp.async-staged metric terms;
+// 4: k_apply3, persistent CTAs prefetching the next tile.
+// Variants 2-4 of the double-float policy read the pre-split geometry
 // (ApplyCall::Gdf) and run as variant 0 when the call carries none; a staged
 // variant whose shared memory exceeds the opt-in limit runs unstaged.
 template <class P, int N>
 static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
-                          cudaStream_t s) {
-  if (c.variant >= 2 && (P::kPrecision != SEM_F64_DF || c.Gdf)) {
-    typedef TileShape<N> TS;
+                          cudaStream_t s, int* tile) {
+  const bool geo_ok = P::kPrecision != SEM_F64_DF || c.Gdf;
+  if (c.variant == 4 && geo_ok) {
+    tile[0] = PTile<N>::TX;
+    tile[1] = PTile<N>::TY;
+    return launch_apply_v3<P, N>(g, ops, c, s);
+  }
+  typedef TileShape<N> TS;
+  tile[0] = TS::TX;
+  tile[1] = TS::TY;
+  if (c.variant >= 2 && geo_ok) {
     const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
     const size_t smem = 2 * te * sizeof(typename P::v) + 3 * te * sizeof(typename GeoT<P>::type);
     if (c.variant == 3 && smem <= max_smem_optin()) return launch_apply_v2<P, N, true>(g, ops, c, s);
     return launch_apply_v2<P, N, false>(g, ops, c, s);
   }
   if (c.variant == 1) {
-    typedef TileShape<N> TS;
     const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
     const int nslot = ((c.mode & M_STIFF) ? 3 : 0) + ((c.mode & M_MASS) ? 1 : 0) +
                       ((c.mode & (M_NU | M_NUG)) ? 1 : 0);
@@ -158,20 +211,23 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
   return launch_apply_v<P, N, false>(g, ops, c, s);
 }
 
-template <class P>
-static int launch_apply_p(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
-                          cudaStream_t s) {
+// the orders LO..HI of one policy (one translation unit)
+template <class P, int LO, int HI>
+static int launch_apply_range(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
+                              cudaStream_t s, int* tile) {
   switch (g.n) {
-#define SEM_CASE(NN) \
-  case NN:           \
-    return launch_apply_n<P, NN>(g, ops, c, s);
+#define SEM_CASE(NN)                                                            \
+  case NN:                                                                      \
+    if constexpr (NN >= LO && NN <= HI) return launch_apply_n<P, NN>(g, ops, c, s, tile); \
+    break;
     SEM_CASE(2) SEM_CASE(3) SEM_CASE(4) SEM_CASE(5) SEM_CASE(6) SEM_CASE(7) SEM_CASE(8)
     SEM_CASE(9) SEM_CASE(10) SEM_CASE(11) SEM_CASE(12) SEM_CASE(13) SEM_CASE(14)
     SEM_CASE(15) SEM_CASE(16) SEM_CASE(17)
 #undef SEM_CASE
     default:
-      return set_error(SEM_ERR_UNSUPPORTED, "no fused kernel for n = %d", g.n);
+      break;
   }
+  return set_error(SEM_ERR_UNSUPPORTED, "no fused kernel for n = %d", g.n);
 }
 
 }  // namespace sem

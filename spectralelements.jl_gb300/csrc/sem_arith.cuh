@@ -131,6 +131,10 @@ __device__ __forceinline__ float masked_zero(float v) {
   return ((b >> 23) & 0xffu) == 0xffu ? __uint_as_float(0x7fc00000u) : __uint_as_float(b & 0x80000000u);
 }
 
+// correctly rounded sums of stored values (never contracted into an FMA)
+__device__ __forceinline__ double io_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float io_add(float a, float b) { return __fadd_rn(a, b); }
+
 // ---------------------------------------------------------------------------
 // policies
 // ---------------------------------------------------------------------------

@@ -185,6 +185,7 @@ struct sem_mesh {
   size_t ws_bytes;
   unsigned char* info;     // device L_* tables: NX row entries then NY column entries
   int variant[4];          // autotuned kernel variant per precision (SEM_F64, SEM_F64_DF, SEM_F32)
+  void* graphs;            // CUDA graphs of the CG iteration chunks (sem_pcg.cu), or NULL
 };
 
 namespace sem {
@@ -219,8 +220,10 @@ struct ApplyCall {
 constexpr int kVariants = SEM_VARIANTS;
 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
-int launch_dss_fixup(const Grid& g, const OperatorSet* ops, void* out, unsigned mode, int precision,
-                     const int* skip, cudaStream_t s);
+bool timing_enabled();                 // sem_timing_enable state (sem_apply.cu)
+void free_graph_cache(sem_mesh* m);    // sem_pcg.cu
+int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
+                     int TY, cudaStream_t s);
 
 // elementwise / structured kernels (sem_vec.cu)
 int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode, cudaStream_t s);

@@ -487,12 +487,119 @@ int diag_build(const OpCtx& cx, const double* nu_field, double nu, double k, dou
   return SEM_OK;
 }
 
-// run CG iterations until done; T = double (F64/DF operator) or float (F32)
+// one chunk of CG iterations (src/pcg.jl:36-55) followed by the copy of the
+// device scalars to the host; every kernel returns at once when the device
+// "done" flag is set, so iterations past convergence cost only launch slots
 template <class T>
-int run_cg(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap, const T* dinv,
-           int op_precision, const double* nu_field, double nu, double k, int check_every,
-           Scalars* out, cudaStream_t s) {
+int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap,
+                  const T* dinv, const ApplyCall& c, int check_every, cudaStream_t s) {
   const long long L = cx.g.NX * cx.g.NY;
+  const unsigned nb = nblocks(L);
+  for (int it = 0; it < check_every; ++it) {
+    k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
+    SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
+    k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
+    k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+    k_update<T><<<nb, kRT, 0, s>>>(x, r, p, Ap, dinv, w.part, w.sc, gv);
+    k_scal_beta<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+  }
+  SEM_CUDA(cudaGetLastError());
+  SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  return SEM_OK;
+}
+
+// ---- CUDA graphs of the iteration chunks
+// A mesh handle keeps one instantiated graph per vector type (FP64/DF and the
+// FP32 inner solve), keyed by every argument the captured launches bake in.
+// A solve with the same key replays it; a different key re-captures and
+// updates the executable graph in place (cudaGraphExecUpdate), or
+// re-instantiates it when the topology changed.
+struct GraphKey {
+  const void* ptr[10];
+  ApplyCall c;
+  Grid g, gv;
+  const OperatorSet* ops;
+  int check_every;
+  int tsize;
+};
+struct GraphEntry {
+  bool valid;
+  GraphKey key;
+  cudaGraphExec_t exec;
+};
+struct GraphCache {
+  cudaStream_t cap;  // private capture stream
+  GraphEntry e[2];
+};
+
+template <class T>
+int chunk_graph(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap,
+                const T* dinv, const ApplyCall& c, int check_every, cudaGraphExec_t* out) {
+  GraphKey key;
+  std::memset(&key, 0, sizeof(key));  // padding bytes take part in the comparison
+  const void* ptrs[10] = {x, r, p, Ap, dinv, w.sc, w.part, w.sc_h, cx.g.rinfo, cx.g.cinfo};
+  std::memcpy(key.ptr, ptrs, sizeof(ptrs));
+  key.c = c;
+  key.g = cx.g;
+  key.gv = gv;
+  key.ops = cx.ops;
+  key.check_every = check_every;
+  key.tsize = (int)sizeof(T);
+  GraphCache* gc = static_cast<GraphCache*>(m->graphs);
+  if (!gc) {
+    gc = new GraphCache;
+    std::memset(gc, 0, sizeof(*gc));
+    const cudaError_t e = cudaStreamCreateWithFlags(&gc->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete gc;
+      return cuda_error(e, "cudaStreamCreate(capture)");
+    }
+    m->graphs = gc;
+  }
+  GraphEntry& ent = gc->e[sizeof(T) == 4 ? 1 : 0];
+  if (ent.valid && std::memcmp(&ent.key, &key, sizeof(key)) == 0) {
+    *out = ent.exec;
+    return SEM_OK;
+  }
+  SEM_CUDA(cudaStreamBeginCapture(gc->cap, cudaStreamCaptureModeThreadLocal));
+  const int st = enqueue_chunk<T>(cx, gv, w, x, r, p, Ap, dinv, c, check_every, gc->cap);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(gc->cap, &graph);
+  if (st != SEM_OK || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return st != SEM_OK ? st : cuda_error(ce, "cudaStreamEndCapture");
+  }
+  bool ok = false;
+  if (ent.valid) {
+    cudaGraphExecUpdateResultInfo info;
+    ok = cudaGraphExecUpdate(ent.exec, graph, &info) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(ent.exec);
+      ent.valid = false;
+    }
+  }
+  if (!ok) {
+    const cudaError_t ie = cudaGraphInstantiate(&ent.exec, graph, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return cuda_error(ie, "cudaGraphInstantiate");
+    }
+  }
+  cudaGraphDestroy(graph);
+  ent.valid = true;
+  ent.key = key;
+  *out = ent.exec;
+  return SEM_OK;
+}
+
+// run CG iterations until done; T = double (F64/DF operator) or float (F32).
+// With a mesh handle (m non-NULL) and kernel timing off, each chunk is one
+// graph launch; otherwise the chunk's kernels are launched one by one.
+template <class T>
+int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap,
+           const T* dinv, int op_precision, const double* nu_field, double nu, double k,
+           int check_every, Scalars* out, cudaStream_t s) {
   ApplyCall c;
   std::memset(&c, 0, sizeof(c));
   c.u = p;
@@ -523,18 +630,14 @@ int run_cg(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p, T* Ap
   c.variant = cx.variant[op_precision];
   c.Gdf = cx.Gdf;
   c.skip = &w.sc->done;
-  const unsigned nb = nblocks(L);
+  cudaGraphExec_t exec = nullptr;
+  if (m && !timing_enabled())
+    SEM_CHECK(chunk_graph<T>(m, cx, gv, w, x, r, p, Ap, dinv, c, check_every, &exec));
   for (;;) {
-    for (int it = 0; it < check_every; ++it) {
-      k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
-      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
-      k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
-      k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
-      k_update<T><<<nb, kRT, 0, s>>>(x, r, p, Ap, dinv, w.part, w.sc, gv);
-      k_scal_beta<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
-    }
-    SEM_CUDA(cudaGetLastError());
-    SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    if (exec)
+      SEM_CUDA(cudaGraphLaunch(exec, s));
+    else
+      SEM_CHECK(enqueue_chunk<T>(cx, gv, w, x, r, p, Ap, dinv, c, check_every, s));
     SEM_CUDA(cudaStreamSynchronize(s));
     if (w.sc_h->done) break;
   }
@@ -587,7 +690,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     res0 = w.sc_h->rmax;
     res = *w.sc_h;
     if (!w.sc_h->done)
-      SEM_CHECK(run_cg<double>(cx, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
+      SEM_CHECK(run_cg<double>(m, cx, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
                                o->nu, o->k, check_every, &res, s));
   } else {
     if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED does not take a nu field");
@@ -627,7 +730,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
       SEM_CUDA(cudaGetLastError());
       Scalars ir;
-      SEM_CHECK(run_cg<float>(cx, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
+      SEM_CHECK(run_cg<float>(m, cx, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
                               nullptr, o->nu, o->k, check_every, &ir, s));
       total_it += ir.k;
       k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
@@ -660,6 +763,17 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
 
 
 }  // namespace
+
+void free_graph_cache(sem_mesh* m) {
+  GraphCache* gc = static_cast<GraphCache*>(m->graphs);
+  if (!gc) return;
+  for (GraphEntry& e : gc->e)
+    if (e.valid) cudaGraphExecDestroy(e.exec);
+  if (gc->cap) cudaStreamDestroy(gc->cap);
+  delete gc;
+  m->graphs = nullptr;
+}
+
 
 // Jacobi inverse diagonal of a mesh's mask(QQ'(hlmz(., nu, k))) into dinv
 // (tmp: one scratch field); used by the batched solver's set-up

@@ -38,7 +38,7 @@ def _ids(c):
 
 @pytest.mark.parametrize("case", CASES, ids=_ids)
 @pytest.mark.parametrize("prec", ["F64", "DF"])
-@pytest.mark.parametrize("variant", [0, 2])
+@pytest.mark.parametrize("variant", [0, 2, 4])
 def test_fused_operators(gpu, case, prec, variant):
     import semgb300 as S
     n, Ex, Ey, per, bc, amp = case
@@ -100,6 +100,11 @@ def test_kernel_variants_bit_identical(gpu, case):
         for v in range(1, len(outs)):
             for a, b in zip(outs[0], outs[v]):
                 np.testing.assert_array_equal(a, b)
+        # the fused QQ' and mask sum every node in the order of the standalone
+        # gatherScatter: fused == mask(gatherScatter(hlmz(u)))
+        Md = S.generateMask(list(bc), md)
+        unfused = host(S.mask(S.gatherScatter(S.hlmz(ud, 1e-2, 1.0, md), md), Md))
+        np.testing.assert_array_equal(outs[0][3], unfused)
     # FP32 inner operator: identical mixed-precision solves for every variant
     md.set_precision(S.SEM_F64_DF)
     md.set_variant(0)
