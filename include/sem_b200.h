@@ -101,10 +101,14 @@ int sem_mesh_set_precision(sem_mesh_t* mesh, int precision);
  *      mesh then holds 4 more fields of NX*NY*8 bytes);
  *   3  as 2, with G11, G12, G22 staged by cp.async;
  *   4  as 2, in a persistent grid whose CTAs prefetch the next element tile's
- *      inputs (cp.async) while they compute the current one.
+ *      inputs (cp.async) while they compute the current one;
+ *   5  as 2, with the cross-tile QQ' finished inside the same launch (the
+ *      last CTA to reach a tile edge or corner sums its copies; the mesh
+ *      holds 3 arrival counters per element tile).  Fused calls on one mesh
+ *      handle must then not run concurrently on the GPU.
  * All variants compute the same operations in the same order: their results
  * are bit-identical. */
-#define SEM_VARIANTS 5
+#define SEM_VARIANTS 6
 /* autotuner (no counterpart in the reference): time every variant of the fused
  * element-operator kernel on this mesh, running mask(QQ'(hlmz)) on scratch
  * fields in the given precision (SEM_F64, SEM_F64_DF or SEM_F32), and keep the

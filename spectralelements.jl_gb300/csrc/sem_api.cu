@@ -169,6 +169,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (m->x) cudaFree(m->x);
   if (m->G11_f) cudaFree(m->G11_f);
   if (m->Gdf) cudaFree(m->Gdf);
+  if (m->fix_ctr) cudaFree(m->fix_ctr);
   free_graph_cache(m);
   if (m->ws) cudaFree(m->ws);
   if (m->info) cudaFree(m->info);
@@ -206,9 +207,10 @@ int sem_mesh_set_variant(sem_mesh_t* m, int precision, int variant) {
   if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
   if (precision < SEM_F64 || precision > SEM_F32) return set_error(SEM_ERR_BAD_ARG, "bad precision");
   if (variant < 0 || variant >= kVariants) return set_error(SEM_ERR_BAD_ARG, "bad variant");
-  if (precision == SEM_F64_DF && variant >= 2) {
+  if ((precision == SEM_F64_DF && variant >= 2) || variant == 5) {
     SEM_CHECK(check_device(m));
-    SEM_CHECK(ensure_df_geometry(m, nullptr));
+    if (precision == SEM_F64_DF) SEM_CHECK(ensure_df_geometry(m, nullptr));
+    if (variant == 5) SEM_CHECK(ensure_fix_counters(m));
     SEM_CUDA(cudaStreamSynchronize(nullptr));  // later launches may use any stream
   }
   m->variant[precision] = variant;
@@ -225,6 +227,7 @@ int sem_mesh_autotune(sem_mesh_t* m, int precision, double* ms_out, int* chosen)
   const bool f32 = precision == SEM_F32;
   if (f32) SEM_CHECK(ensure_f32_geometry(m, s));
   if (precision == SEM_F64_DF) SEM_CHECK(ensure_df_geometry(m, s));
+  SEM_CHECK(ensure_fix_counters(m));
   void* out = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int st = SEM_OK;
@@ -243,6 +246,7 @@ int sem_mesh_autotune(sem_mesh_t* m, int precision, double* ms_out, int* chosen)
   c.G22 = f32 ? (const void*)m->G22_f : (const void*)m->G22;
   c.B = f32 ? (const void*)m->B_f : (const void*)m->B;
   c.Gdf = m->Gdf;
+  c.ctr = m->fix_ctr;
   c.nu_s = 0.5;
   c.k_s = 1.0;
   c.mode = m->g.topo | M_STIFF | M_MASS | M_GS | (m->has_bc ? M_MASK : 0u);
@@ -320,6 +324,7 @@ static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, con
     return set_error(SEM_ERR_BAD_ARG, "output must not alias an input of a fused operator");
   SEM_CHECK(check_device(m));
   ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
   c.u = u;
   c.out = out;
   c.G11 = m->G11;
@@ -334,6 +339,7 @@ static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, con
   c.skip = nullptr;
   c.variant = m->variant[m->precision];
   c.Gdf = m->Gdf;
+  c.ctr = m->fix_ctr;
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 
@@ -378,6 +384,7 @@ int sem_varcoef(sem_mesh_t* m, const double* nu_field, double k, const double* u
   c.precision = m->precision;
   c.variant = m->variant[m->precision];
   c.Gdf = m->Gdf;
+  c.ctr = m->fix_ctr;
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 

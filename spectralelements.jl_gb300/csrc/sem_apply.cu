@@ -165,7 +165,30 @@ int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cuda
   else
     return set_error(SEM_ERR_BAD_ARG, "unknown precision %d", c.precision);
   if (st != SEM_OK) return st;
+  if (tile[0] == 0) return SEM_OK;  // completed inside the kernel
   return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s);
+}
+
+long long cg_apply_parts(const Grid& g) {
+  int tx = 1, ty = 1;
+  tile_shape(g.n, &tx, &ty);
+  return (long long)((g.Ex + tx - 1) / tx) * ((g.Ey + ty - 1) / ty);
+}
+
+int ensure_fix_counters(sem_mesh* m) {
+  if (m->fix_ctr) return SEM_OK;
+  int tx = 1, ty = 1;
+  tile_shape(m->g.n, &tx, &ty);
+  const long long tiles = (long long)((m->g.Ex + tx - 1) / tx) * ((m->g.Ey + ty - 1) / ty);
+  unsigned* p = nullptr;
+  SEM_CUDA(cudaMalloc(&p, sizeof(unsigned) * 3 * (size_t)tiles));
+  const cudaError_t e = cudaMemset(p, 0, sizeof(unsigned) * 3 * (size_t)tiles);
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    return cuda_error(e, "cudaMemset(interface counters)");
+  }
+  m->fix_ctr = p;
+  return SEM_OK;
 }
 
 }  // namespace sem

@@ -53,8 +53,108 @@ struct Apply2Args {
   long long NX;
   unsigned mode;
   const int* skip;
+  unsigned* ctr;          // interface arrival counters (in-kernel completion), or NULL
+  int tiles_x, tiles_y;   // element tiles of the launch (in-kernel completion)
+  // CG-fused launch: u = p = dinv .* r + beta p_old is formed here (p read and
+  // written in place) and every CTA stores its share of p . A p in dpart
+  const io* r;
+  const io* dinv;
+  io* p;
+  const double* beta;
+  df* dpart;
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
+
+// one term of the CG denominator p . A p, formed in double-float
+__device__ __forceinline__ df dot_term(df a, df b) { return df_mul_u(a, b); }
+__device__ __forceinline__ df dot_term(double a, double b) { return df_mul_u(d2df(a), d2df(b)); }
+__device__ __forceinline__ df dot_term(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+
+// In-kernel completion of the cross-tile QQ' (kernel variant 5).  Every tile
+// edge and every tile corner on a cross-tile interface has an arrival counter
+// (three per tile: the edge to its right, the edge above it, their corner).
+// A CTA that has stored its tile counts itself in at the counters of the up to
+// four edges and four corners it touches; the CTA that arrives last at an edge
+// (second of two) or corner (fourth of four) sums its copies, with the
+// operations and order of k_dss_fixup, so the result is bit-identical to a
+// separate fixup launch.  Counters are never reset: an edge completes when its
+// count is odd after the increment, a corner when it is 3 mod 4, so every
+// launch that runs to its end leaves them consistent for the next.  Stores are
+// made device-visible (__threadfence) before the arrival, and the last arriver
+// reads the other tiles' copies from L2.  Needs two distinct tiles across every
+// periodic direction (tiles_x >= 2 if x is periodic, likewise y).
+template <class IO, int TX, int TY>
+__device__ __forceinline__ void finish_tile_interfaces(IO* out, int n, int Ex, int Ey, long long NX,
+                                                       unsigned mode, unsigned* ctr, int tiles_x,
+                                                       int tiles_y, int bx, int by) {
+  __shared__ int s_last[8];
+  __shared__ long long s_a[8], s_b[8];
+  const bool perx = (mode & M_PERX) != 0, pery = (mode & M_PERY) != 0;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    const int k = threadIdx.x;
+    const int lx = (bx + tiles_x - 1) % tiles_x, ly = (by + tiles_y - 1) % tiles_y;
+    const bool left = bx > 0 || perx, right = bx + 1 < tiles_x || perx;
+    const bool below = by > 0 || pery, above = by + 1 < tiles_y || pery;
+    // segment k: 0 left edge, 1 right edge, 2 lower edge, 3 upper edge,
+    // 4..7 corners lower-left, lower-right, upper-left, upper-right
+    int tx = bx, ty = by, kind = 0;
+    bool exists = false;
+    switch (k) {
+      case 0: tx = lx; kind = 0; exists = left; break;
+      case 1: kind = 0; exists = right; break;
+      case 2: ty = ly; kind = 1; exists = below; break;
+      case 3: kind = 1; exists = above; break;
+      case 4: tx = lx; ty = ly; kind = 2; exists = left && below; break;
+      case 5: ty = ly; kind = 2; exists = right && below; break;
+      case 6: tx = lx; kind = 2; exists = left && above; break;
+      default: kind = 2; exists = right && above; break;
+    }
+    int last = 0;
+    if (exists) {
+      const unsigned old = atomicAdd(ctr + 3 * ((long long)ty * tiles_x + tx) + kind, 1u);
+      last = kind == 2 ? ((old & 3u) == 3u) : ((old & 1u) == 1u);
+      if (last) __threadfence();
+    }
+    // interface element indices right of / above the owner tile (0: the wrap)
+    const long long a = (long long)(tx + 1) * TX >= Ex ? 0 : (long long)(tx + 1) * TX;
+    const long long b = (long long)(ty + 1) * TY >= Ey ? 0 : (long long)(ty + 1) * TY;
+    s_last[k] = last ? kind + 1 : 0;
+    s_a[k] = kind == 1 ? (long long)tx : a;  // y edge: owner tile column
+    s_b[k] = kind == 0 ? (long long)ty : b;  // x edge: owner tile row
+  }
+  __syncthreads();
+  FixArgs f;
+  f.n = n;
+  f.Ex = Ex;
+  f.Ey = Ey;
+  f.TX = TX;
+  f.TY = TY;
+  f.NX = NX;
+  f.NY = (long long)Ey * n;
+  f.mode = mode;
+  f.skip = nullptr;
+  f.nxi = f.nyi = 0;
+  auto none = [](long long, long long, IO) {};
+  for (int k = 0; k < 8; ++k) {
+    const int kind = s_last[k] - 1;
+    if (kind == 0) {
+      const long long ty = s_b[k];
+      const long long c1 = ((ty + 1) * TY < Ey ? (ty + 1) * TY : (long long)Ey) * n;
+      fix_xline(out, f, s_a[k], ty * TY * n + threadIdx.x, c1, (long long)blockDim.x, none);
+    } else if (kind == 1) {
+      const long long tx = s_a[k];
+      const long long r1 = ((tx + 1) * TX < Ex ? (tx + 1) * TX : (long long)Ex) * n;
+      fix_yline(out, f, s_b[k], tx * TX * n + threadIdx.x, r1, (long long)blockDim.x, none);
+    } else if (kind == 2 && threadIdx.x == (k - 4) * (blockDim.x / 4)) {
+      fix_corner(out, f, s_a[k], s_b[k], none);
+    }
+  }
+}
 
 // resident blocks per SM asked of the register allocator: without the
 // register copy of u the double-float kernel fits four blocks (72 registers,
@@ -65,7 +165,14 @@ struct MinBlocks2 {
       (!STAGE && P::kPrecision == SEM_F64_DF && N <= 9) ? 4 : MinBlocks<P, N, STAGE>::value;
 };
 
-template <class P, int N, int TX, int TY, bool STAGE>
+// CG: the launch is one CG iteration's operator application (src/pcg.jl:40-47):
+// it forms the direction p from r and the previous p, applies the operator to
+// it and writes each CTA's part of p . A p.  The denominator is summed over the
+// unassembled local products p_i (A_e p)_i, which equals the reference's
+// sum(p .* Ap .* mult) for a continuous, masked p (QQ' is the transpose of the
+// scatter and mask zeroes p where it zeroes Ap), so the cross-tile completion
+// does not enter it and the sum is deterministic.
+template <class P, int N, int TX, int TY, bool STAGE, bool FUSE = false, bool CG = false>
 __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
     k_apply2(const __grid_constant__ Apply2Args<P, N> a) {
   typedef typename P::v V;
@@ -118,10 +225,26 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   V res[N];
   {
     V u[N];
+    if constexpr (CG) {
+      const IO beta = (IO)*a.beta;
+      const bool jac = a.dinv != nullptr;
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
-      s0[j * SP + lane] = u[j];
+      for (int j = 0; j < N; ++j) {
+        IO pn = (IO)0;
+        if (valid) {
+          const long long gi = base + (long long)j * NX;
+          pn = cg_direction(a.r[gi], jac ? a.dinv[gi] : (IO)1, beta, a.p[gi], jac);
+          a.p[gi] = pn;
+        }
+        u[j] = P::cvt(pn);
+        s0[j * SP + lane] = u[j];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
+        s0[j * SP + lane] = u[j];
+      }
     }
     if (stiff) {
       V us[N];
@@ -198,9 +321,21 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
     }
   }
 
+  if constexpr (CG) {
+    df acc = {0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc = df_add_u(acc, dot_term(s0[j * SP + lane], res[j]));
+    const df tot = block_sum_df(df_norm(acc));
+    if (threadIdx.x == 0) a.dpart[blockIdx.y * gridDim.x + blockIdx.x] = tot;
+  }
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
   tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
                                ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
+  if constexpr (FUSE) {
+    if (mode & M_GS)
+      finish_tile_interfaces<IO, TX, TY>(a.out, N, a.Ex, a.Ey, NX, mode, a.ctr, a.tiles_x, a.tiles_y,
+                                         blockIdx.x, blockIdx.y);
+  }
 }
 
 }  // namespace sem

@@ -127,14 +127,21 @@ __host__ __device__ inline bool xcross_row(int ex, int i, int n, int Ex, int TX,
 // gets exactly the sums of k_gather_scatter on the rounded values, whatever
 // the tile shape.  A row on a cross-tile x interface takes no in-tile y pair:
 // k_dss_fixup finishes its corners in the same x-first order.  Points with
-// copies in another tile are stored unsummed and unmasked.  X1 and X0 are
-// two tile-sized shared buffers free for reuse; every thread of the block
-// calls this (it holds barriers).
-template <class P, int N, int TX, int TY>
+// copies in another tile are stored unsummed and unmasked; finished(j, value)
+// is called for every other point of the row.  X1 and X0 are two tile-sized
+// shared buffers free for reuse; every thread of the block calls this (it
+// holds barriers).
+struct NoFinish {
+  template <class IO>
+  __device__ __forceinline__ void operator()(int, IO) const {}
+};
+
+template <class P, int N, int TX, int TY, class F = NoFinish>
 __device__ __forceinline__ void tile_dss_store(const typename P::v (&res)[N], typename P::io* X1,
                                                typename P::io* X0, int elem, int lane, int ex,
                                                int ey, bool valid, long long base, int Ex, int Ey,
-                                               long long NX, unsigned mode, typename P::io* out) {
+                                               long long NX, unsigned mode, typename P::io* out,
+                                               F&& finished = F()) {
   typedef typename P::io IO;
   constexpr int SP = N | 1;
   constexpr int ES = N * SP;
@@ -182,9 +189,10 @@ __device__ __forceinline__ void tile_dss_store(const typename P::v (&res)[N], ty
       if (j == N - 1 && (eyl == TY - 1 || ey == Ey - 1) && (ey < Ey - 1 || pery)) raw = true;
     }
     IO val = rv[j];
-    if (!raw && (mode & M_MASK)) {
+    if (!raw) {
       const long long col = (long long)ey * N + j;
-      if (!mask_keep(row, col, NX, NY, mode)) val = masked_zero(val);
+      if ((mode & M_MASK) && !mask_keep(row, col, NX, NY, mode)) val = masked_zero(val);
+      finished(j, val);
     }
     out[base + (long long)j * NX] = val;
   }
@@ -351,80 +359,138 @@ __host__ __device__ inline long long fix_iface(long long q, int T, bool per) {
 }
 
 template <class IO>
-__device__ __forceinline__ void fix_store(IO* out, long long r, long long c, IO s, const FixArgs& f,
-                                          bool msk) {
-  if (msk && !mask_keep(r, c, f.NX, f.NY, f.mode)) s = masked_zero(s);
-  out[r + c * f.NX] = s;
+__device__ __forceinline__ IO fix_value(long long r, long long c, IO s, const FixArgs& f, bool msk) {
+  return (msk && !mask_keep(r, c, f.NX, f.NY, f.mode)) ? masked_zero(s) : s;
+}
+
+// Number of interface rows of k_dss_fixup's index space: x interfaces, then
+// y interfaces, then one row for the corners of two cross-tile interfaces.
+__host__ __device__ inline long long fix_rows(const FixArgs& f) {
+  return f.nxi + f.nyi + (f.nxi * f.nyi > 0 ? 1 : 0);
+}
+
+// Loads of values another CTA may have stored during the same launch go to L2
+// (ld.global.cg), never to a possibly stale L1 line.
+template <class IO>
+__device__ __forceinline__ IO fix_ld(const IO* p) {
+  return __ldcg(p);
+}
+
+// The copies on the x interface left of element column a (a == 0: the
+// periodic wrap between the last and the first column), columns c_begin,
+// c_begin + stride, ... below c_end.  Columns on cross-tile y interfaces are
+// corners (fix_corner); on an in-tile y interface the four copies are summed,
+// x pairs first.  done(r, c, value) is called for every copy stored.
+template <class IO, class F>
+__device__ __forceinline__ void fix_xline(IO* out, const FixArgs& f, long long a, long long c_begin,
+                                          long long c_end, long long stride, F&& done) {
+  const bool pery = (f.mode & M_PERY) != 0;
+  const bool msk = (f.mode & M_MASK) != 0;
+  const unsigned n = (unsigned)f.n;
+  const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
+  const long long rr = a * f.n;
+  auto put = [&](long long r, long long c, IO s) {
+    const IO v = fix_value(r, c, s, f, msk);
+    out[r + c * f.NX] = v;
+    done(r, c, v);
+  };
+  for (long long c = c_begin; c < c_end; c += stride) {
+    const int ey = (int)((unsigned long long)c / n);
+    const int j = (int)(c - (long long)ey * f.n);
+    if (xcross_row(ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner of two cross-tile interfaces
+    if (j == 0 && ey > 0) continue;                            // in-tile y pair, done from column c-1
+    if (j == f.n - 1 && ey + 1 < f.Ey) {
+      const long long c2 = c + 1;
+      const IO s = io_add(io_add(fix_ld(out + rl + c * f.NX), fix_ld(out + rr + c * f.NX)),
+                          io_add(fix_ld(out + rl + c2 * f.NX), fix_ld(out + rr + c2 * f.NX)));
+      put(rl, c, s);
+      put(rr, c, s);
+      put(rl, c2, s);
+      put(rr, c2, s);
+      continue;
+    }
+    const IO s = io_add(fix_ld(out + rl + c * f.NX), fix_ld(out + rr + c * f.NX));
+    put(rl, c, s);
+    put(rr, c, s);
+  }
+}
+
+// The copies on the y interface below element row b (b == 0: the wrap), rows
+// r_begin, r_begin + stride, ... below r_end; rows on cross-tile x interfaces
+// are corners.
+template <class IO, class F>
+__device__ __forceinline__ void fix_yline(IO* out, const FixArgs& f, long long b, long long r_begin,
+                                          long long r_end, long long stride, F&& done) {
+  const bool perx = (f.mode & M_PERX) != 0;
+  const bool msk = (f.mode & M_MASK) != 0;
+  const unsigned n = (unsigned)f.n;
+  const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
+  const long long cr = b * f.n;
+  for (long long r = r_begin; r < r_end; r += stride) {
+    const int ex = (int)((unsigned long long)r / n);
+    const int i = (int)(r - (long long)ex * f.n);
+    if (xcross_row(ex, i, f.n, f.Ex, f.TX, perx)) continue;
+    const IO s = io_add(fix_ld(out + r + cl * f.NX), fix_ld(out + r + cr * f.NX));
+    const IO vl = fix_value(r, cl, s, f, msk);
+    const IO vr = fix_value(r, cr, s, f, msk);
+    out[r + cl * f.NX] = vl;
+    out[r + cr * f.NX] = vr;
+    done(r, cl, vl);
+    done(r, cr, vr);
+  }
+}
+
+// The four copies where the cross-tile x interface left of element column a
+// meets the cross-tile y interface below element row b.
+template <class IO, class F>
+__device__ __forceinline__ void fix_corner(IO* out, const FixArgs& f, long long a, long long b, F&& done) {
+  const bool msk = (f.mode & M_MASK) != 0;
+  const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
+  const long long rr = a * f.n;
+  const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
+  const long long cr = b * f.n;
+  const IO s = io_add(io_add(fix_ld(out + rl + cl * f.NX), fix_ld(out + rr + cl * f.NX)),
+                      io_add(fix_ld(out + rl + cr * f.NX), fix_ld(out + rr + cr * f.NX)));
+  const long long rs[2] = {rl, rr};
+  const long long cs[2] = {cl, cr};
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const IO val = fix_value(rs[u], cs[v], s, f, msk);
+      out[rs[u] + cs[v] * f.NX] = val;
+      done(rs[u], cs[v], val);
+    }
+}
+
+// Finishes interface row q of k_dss_fixup's index space at the points first,
+// first + stride, ...
+template <class IO, class F>
+__device__ __forceinline__ void fix_interface(IO* __restrict__ out, const FixArgs& f, long long q,
+                                              long long first, long long stride, F&& done) {
+  const bool perx = (f.mode & M_PERX) != 0;
+  const bool pery = (f.mode & M_PERY) != 0;
+  if (q < f.nxi) {
+    fix_xline(out, f, fix_iface(q, f.TX, perx), first, f.NY, stride, done);
+  } else if (q < f.nxi + f.nyi) {
+    fix_yline(out, f, fix_iface(q - f.nxi, f.TY, pery), first, f.NX, stride, done);
+  } else {
+    for (long long id = first; id < f.nxi * f.nyi; id += stride) {
+      const long long qx = id / f.nyi;
+      const long long qy = id - qx * f.nyi;
+      fix_corner(out, f, fix_iface(qx, f.TX, perx), fix_iface(qy, f.TY, pery), done);
+    }
+  }
 }
 
 template <class IO>
 __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
   if (f.skip && *f.skip) return;
-  const bool perx = (f.mode & M_PERX) != 0;
-  const bool pery = (f.mode & M_PERY) != 0;
-  const bool msk = (f.mode & M_MASK) != 0;
-  const long long ncorner = f.nxi * f.nyi;
-  const long long nI = f.nxi + f.nyi + (ncorner > 0 ? 1 : 0);
+  const long long nI = fix_rows(f);
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned n = (unsigned)f.n;
-  for (long long q = blockIdx.y; q < nI; q += gridDim.y) {
-    if (q < f.nxi) {
-      // x interface q: rows rl | rr, every column c
-      const long long a = fix_iface(q, f.TX, perx);
-      const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
-      const long long rr = a * f.n;
-      for (long long c = first; c < f.NY; c += stride) {
-        const int ey = (int)((unsigned long long)c / n);
-        const int j = (int)(c - (long long)ey * f.n);
-        if (xcross_row(ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner of two cross-tile interfaces
-        if (j == 0 && ey > 0) continue;                            // in-tile y pair, done from column c-1
-        if (j == f.n - 1 && ey + 1 < f.Ey) {
-          // in-tile y interface: four copies
-          const long long c2 = c + 1;
-          const IO s = (out[rl + c * f.NX] + out[rr + c * f.NX]) + (out[rl + c2 * f.NX] + out[rr + c2 * f.NX]);
-          fix_store(out, rl, c, s, f, msk);
-          fix_store(out, rr, c, s, f, msk);
-          fix_store(out, rl, c2, s, f, msk);
-          fix_store(out, rr, c2, s, f, msk);
-          continue;
-        }
-        const IO s = out[rl + c * f.NX] + out[rr + c * f.NX];
-        fix_store(out, rl, c, s, f, msk);
-        fix_store(out, rr, c, s, f, msk);
-      }
-    } else if (q < f.nxi + f.nyi) {
-      // y interface: columns cl | cr, every row r (rows on cross-tile x
-      // interfaces are corners)
-      const long long b = fix_iface(q - f.nxi, f.TY, pery);
-      const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
-      const long long cr = b * f.n;
-      for (long long r = first; r < f.NX; r += stride) {
-        const int ex = (int)((unsigned long long)r / n);
-        const int i = (int)(r - (long long)ex * f.n);
-        if (xcross_row(ex, i, f.n, f.Ex, f.TX, perx)) continue;
-        const IO s = out[r + cl * f.NX] + out[r + cr * f.NX];
-        fix_store(out, r, cl, s, f, msk);
-        fix_store(out, r, cr, s, f, msk);
-      }
-    } else {
-      for (long long id = first; id < ncorner; id += stride) {
-        const long long qx = id / f.nyi;
-        const long long qy = id - qx * f.nyi;
-        const long long a = fix_iface(qx, f.TX, perx);
-        const long long b = fix_iface(qy, f.TY, pery);
-        const long long rl = a == 0 ? f.NX - 1 : a * f.n - 1;
-        const long long rr = a * f.n;
-        const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
-        const long long cr = b * f.n;
-        const IO s = (out[rl + cl * f.NX] + out[rr + cl * f.NX]) + (out[rl + cr * f.NX] + out[rr + cr * f.NX]);
-        fix_store(out, rl, cl, s, f, msk);
-        fix_store(out, rr, cl, s, f, msk);
-        fix_store(out, rl, cr, s, f, msk);
-        fix_store(out, rr, cr, s, f, msk);
-      }
-    }
-  }
+  for (long long q = blockIdx.y; q < nI; q += gridDim.y)
+    fix_interface(out, f, q, first, stride, [](long long, long long, IO) {});
 }
 
 }  // namespace sem

@@ -125,16 +125,29 @@ static void fill_args2(Apply2Args<P, N>& a, const Grid& g, const OperatorSet* op
   fill_eo<P, N>(a.Dst, ops->eo[3]);
 }
 
-template <class P, int N, bool STAGE>
+template <class P, int N, bool STAGE, bool FUSE = false, bool CG = false>
 static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
                            cudaStream_t s) {
   typedef TileShape<N> TS;
   typedef typename GeoT<P>::type gt;
+  typedef typename P::io io;
   Apply2Args<P, N> a;
   fill_args2<P, N>(a, g, ops, c);
+  if (CG) {
+    a.r = static_cast<const io*>(c.cg_r);
+    a.dinv = static_cast<const io*>(c.cg_dinv);
+    a.p = static_cast<io*>(c.cg_p);
+    a.beta = c.cg_beta;
+    a.dpart = static_cast<df*>(c.cg_dpart);
+  }
+  if (FUSE) {
+    a.ctr = c.ctr;
+    a.tiles_x = (g.Ex + TS::TX - 1) / TS::TX;
+    a.tiles_y = (g.Ey + TS::TY - 1) / TS::TY;
+  }
   const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
   const size_t smem = 2 * te * sizeof(typename P::v) + (STAGE ? 3 * te * sizeof(gt) : 0);
-  auto kern = k_apply2<P, N, TS::TX, TS::TY, STAGE>;
+  auto kern = k_apply2<P, N, TS::TX, TS::TY, STAGE, FUSE, CG>;
   if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
   auto* ev = timing_slot();
@@ -179,14 +192,34 @@ static int launch_apply_v3(const Grid& g, const OperatorSet* ops, const ApplyCal
 
 // variant 0: k_apply, direct loads; 1: k_apply, cp.async-staged inputs;
 // 2: k_apply2, direct loads; 3: k_apply2, cp.async-staged metric terms;
-// 4: k_apply3, persistent CTAs prefetching the next tile.
-// Variants 2-4 of the double-float policy read the pre-split geometry
-// (ApplyCall::Gdf) and run as variant 0 when the call carries none; a staged
-// variant whose shared memory exceeds the opt-in limit runs unstaged.
+// 4: k_apply3, persistent CTAs prefetching the next tile; 5: k_apply2 with
+// the cross-tile QQ' completed inside the kernel (tile = {0, 0}: no fixup).
+// Variants 2-5 of the double-float policy read the pre-split geometry
+// (ApplyCall::Gdf) and run as variant 0 when the call carries none; variant 5
+// runs as variant 2 without counters (ApplyCall::ctr) or with a single tile
+// across a periodic direction; a staged variant whose shared memory exceeds
+// the opt-in limit runs unstaged.
 template <class P, int N>
 static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
                           cudaStream_t s, int* tile) {
   const bool geo_ok = P::kPrecision != SEM_F64_DF || c.Gdf;
+  const bool cg = c.cg_p != nullptr;
+  if (cg && !(geo_ok && (c.variant == 2 || c.variant == 5) && (c.mode & M_STIFF)))
+    return set_error(SEM_ERR_UNSUPPORTED, "CG-fused operator launch needs kernel variant 2 or 5");
+  if (c.variant == 5 && geo_ok && c.ctr && (c.mode & M_GS)) {
+    typedef TileShape<N> TS;
+    const bool one_x = (g.Ex + TS::TX - 1) / TS::TX < 2, one_y = (g.Ey + TS::TY - 1) / TS::TY < 2;
+    if (!((c.mode & M_PERX) && one_x) && !((c.mode & M_PERY) && one_y)) {
+      tile[0] = tile[1] = 0;
+      return cg ? launch_apply_v2<P, N, false, true, true>(g, ops, c, s)
+                : launch_apply_v2<P, N, false, true>(g, ops, c, s);
+    }
+  }
+  if (cg) {
+    tile[0] = TileShape<N>::TX;
+    tile[1] = TileShape<N>::TY;
+    return launch_apply_v2<P, N, false, false, true>(g, ops, c, s);
+  }
   if (c.variant == 4 && geo_ok) {
     tile[0] = PTile<N>::TX;
     tile[1] = PTile<N>::TY;
@@ -195,7 +228,7 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
   typedef TileShape<N> TS;
   tile[0] = TS::TX;
   tile[1] = TS::TY;
-  if (c.variant >= 2 && geo_ok) {
+  if (c.variant >= 2 && c.variant != 4 && geo_ok) {
     const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
     const size_t smem = 2 * te * sizeof(typename P::v) + 3 * te * sizeof(typename GeoT<P>::type);
     if (c.variant == 3 && smem <= max_smem_optin()) return launch_apply_v2<P, N, true>(g, ops, c, s);
@@ -209,6 +242,23 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
     if (smem <= max_smem_optin()) return launch_apply_v<P, N, true>(g, ops, c, s);
   }
   return launch_apply_v<P, N, false>(g, ops, c, s);
+}
+
+// element tile (TX, TY) of the non-persistent kernels for n points (host)
+inline void tile_shape(int n, int* tx, int* ty) {
+  switch (n) {
+#define SEM_CASE(NN)            \
+  case NN:                      \
+    *tx = TileShape<NN>::TX;    \
+    *ty = TileShape<NN>::TY;    \
+    return;
+    SEM_CASE(2) SEM_CASE(3) SEM_CASE(4) SEM_CASE(5) SEM_CASE(6) SEM_CASE(7) SEM_CASE(8)
+    SEM_CASE(9) SEM_CASE(10) SEM_CASE(11) SEM_CASE(12) SEM_CASE(13) SEM_CASE(14)
+    SEM_CASE(15) SEM_CASE(16) SEM_CASE(17)
+#undef SEM_CASE
+    default:
+      *tx = *ty = 1;
+  }
 }
 
 // the orders LO..HI of one policy (one translation unit)

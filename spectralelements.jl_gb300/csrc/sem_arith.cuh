@@ -135,6 +135,39 @@ __device__ __forceinline__ float masked_zero(float v) {
 __device__ __forceinline__ double io_add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float io_add(float a, float b) { return __fadd_rn(a, b); }
 
+// CG direction p = h + beta p_old with h = dinv .* r (Jacobi) or r, formed in
+// double-float and rounded once for FP64 vectors, in FP32 for FP32 vectors
+// (src/pcg.jl:40-45)
+__device__ __forceinline__ double cg_direction(double r, double d, double beta, double p, bool jac) {
+  const df rd = d2df(r);
+  const df h = jac ? df_mul_u(rd, d2df(d)) : rd;
+  return df2d(df_fma_u(d2df(beta), d2df(p), h));
+}
+__device__ __forceinline__ float cg_direction(float r, float d, float beta, float p, bool jac) {
+  return __fmaf_rn(beta, p, jac ? r * d : r);
+}
+
+// block-wide double-float sum in a fixed order (warp trees, then the warps in
+// order); the result is valid in thread 0.  Every thread of the block calls it.
+__device__ __forceinline__ df block_sum_df(df x) {
+  __shared__ df warp_sums[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  for (int o = 16; o > 0; o >>= 1) {
+    const df y = {__shfl_down_sync(full, x.h, o), __shfl_down_sync(full, x.l, o)};
+    x = df_add(x, y);
+  }
+  __syncthreads();  // warp_sums may still be read by a previous call
+  if (lane == 0) warp_sums[w] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    x = warp_sums[0];
+    for (int i = 1; i < nw; ++i) x = df_add(x, warp_sums[i]);
+  }
+  return x;
+}
+
 // ---------------------------------------------------------------------------
 // policies
 // ---------------------------------------------------------------------------

@@ -115,10 +115,6 @@ int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* 
     q.topo = m->g.topo | (m->has_bc ? M_MASK : 0u);
     q.nu = nu[i];
     q.k = k[i];
-    q.G11 = m->G11;
-    q.G12 = m->G12;
-    q.G22 = m->G22;
-    q.B = m->B;
     q.r = (double*)take(L * 8);
     q.p = (double*)take(L * 8);
     q.Ap = (double*)take(L * 8);
@@ -129,6 +125,8 @@ int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* 
     q.x32 = (float*)take(L * 4);
     q.dinv32 = (float*)take(L * 4);
     st = ensure_f32_geometry(m, 0);
+    if (st == SEM_OK) st = ensure_df_geometry(m, 0);
+    q.Gdf = m->Gdf;
     q.G11f = m->G11_f;
     q.G12f = m->G12_f;
     q.G22f = m->G22_f;
@@ -216,7 +214,7 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   for (auto& g : b->groups) wtot += g.work;
   int sms = 0;
   SEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-  const int budget = std::max(1, sms / kCluster);  // clusters of one CTA per SM
+  const int budget = std::max(1, sms * kBatchCtasPerSm / kCluster);  // resident clusters
   for (size_t gi = 0; gi < b->groups.size(); ++gi) {
     auto& g = b->groups[gi];
     BatchCommon c;

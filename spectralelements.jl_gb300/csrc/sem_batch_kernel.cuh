@@ -29,15 +29,16 @@
 #include <cstring>
 #include <vector>
 
-#include "sem_apply_kernels.cuh"
+#include "sem_apply2.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace sem {
 
-constexpr int kBT = 256;       // threads per CTA
-constexpr int kCluster = 8;    // CTAs per cluster (portable size)
-constexpr int kBatchMaxN = 11; // GLL points per direction served by the batch kernel
+constexpr int kBT = 256;             // threads per CTA
+constexpr int kCluster = 8;          // CTAs per cluster (portable size)
+constexpr int kBatchMaxN = 11;       // GLL points per direction served by the batch kernel
+constexpr int kBatchCtasPerSm = 2;   // resident CTAs per SM asked of the register allocator
 
 template <int N>
 struct BTile {  // element tile of the batch kernel: TX*TY*N <= kBT
@@ -46,6 +47,9 @@ struct BTile {  // element tile of the batch kernel: TX*TY*N <= kBT
                             (N == 7 ? 6 : (N == 8 ? 4 : (N == 9 ? 4 : (N == 10 ? 5 : 4))))))));
   static constexpr int SP = N | 1;
   static constexpr int ES = N * SP;
+  // element slots of one line buffer: every thread of the CTA owns one (the
+  // threads beyond the tile write into slots no tile thread reads)
+  static constexpr int SLOTS = (kBT + N - 1) / N;
   static_assert(TX * TY * N <= kBT, "tile exceeds the CTA");
 };
 
@@ -55,7 +59,7 @@ struct BProb {
   unsigned topo;  // M_PERX | M_PERY | M_D* | M_MASK
   double nu, k, tol;
   int maxiter;
-  const double *G11, *G12, *G22, *B;
+  const df* Gdf;  // G11, G12, G22, B split into double-float pairs (4 blocks of NX*NY)
   const float *G11f, *G12f, *G22f, *Bf;
   const double* b;
   double* x;
@@ -91,20 +95,21 @@ struct BatchArgs {
   EOCoef<N, float> cf[4];  // the same in FP32 (inner solve)
 };
 
-// ---- per-thread accumulators (see sem_pcg.cu): double-float sums for FP64
-// vectors, FP32 sums for FP32 vectors, integer max of magnitude bits
+// ---- per-thread accumulators: double-float sums (FP32 pipe) and the maximum
+// of |value| as the bit pattern of a non-negative double (NaN sorts last)
 template <class T>
 struct BAcc;
 template <>
 struct BAcc<double> {
   df s = {0.0f, 0.0f};
   unsigned long long mx = 0ull;
-  __device__ __forceinline__ void prod(double a, double b, float m) {
-    df p = df_mul_u(d2df(a), d2df(b));
+  __device__ __forceinline__ void prod_v(df a, double b, float m) {
+    df p = df_mul_u(a, d2df(b));
     p.h *= m;
     p.l *= m;
     s = df_add_u(s, p);
   }
+  __device__ __forceinline__ void prod(double a, double b, float m) { prod_v(d2df(a), b, m); }
   __device__ __forceinline__ void rhr(double a, double d, float m) {
     const df ad = d2df(a);
     df h = df_mul_u(ad, d2df(d));
@@ -116,21 +121,24 @@ struct BAcc<double> {
     const unsigned long long b = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
     mx = b > mx ? b : mx;
   }
-  __device__ __forceinline__ double sum() const { return df2d(df_norm(s)); }
-  __device__ __forceinline__ double max() const { return __longlong_as_double((long long)mx); }
+  __device__ __forceinline__ df sum() const { return df_norm(s); }
+  __device__ __forceinline__ unsigned long long max_bits() const { return mx; }
 };
 template <>
 struct BAcc<float> {
   float s = 0.0f;
   unsigned mx = 0u;
-  __device__ __forceinline__ void prod(float a, float b, float m) { s = __fmaf_rn(a * m, b, s); }
+  __device__ __forceinline__ void prod_v(float a, float b, float m) { s = __fmaf_rn(a * m, b, s); }
+  __device__ __forceinline__ void prod(float a, float b, float m) { prod_v(a, b, m); }
   __device__ __forceinline__ void rhr(float a, float d, float m) { s = __fmaf_rn(a, a * d * m, s); }
   __device__ __forceinline__ void amax(float a) {
     const unsigned b = __float_as_uint(a) & 0x7fffffffu;
     mx = b > mx ? b : mx;
   }
-  __device__ __forceinline__ double sum() const { return (double)s; }
-  __device__ __forceinline__ double max() const { return (double)__uint_as_float(mx); }
+  __device__ __forceinline__ df sum() const { return {s, 0.0f}; }
+  __device__ __forceinline__ unsigned long long max_bits() const {
+    return (unsigned long long)__double_as_longlong((double)__uint_as_float(mx));
+  }
 };
 
 __device__ __forceinline__ double bpdir(double r, double d, double beta, double p, bool jac) {
@@ -142,251 +150,230 @@ __device__ __forceinline__ float bpdir(float r, float d, float beta, float p, bo
   return __fmaf_rn(beta, p, jac ? r * d : r);
 }
 
-__device__ __forceinline__ double bnanmax(double a, double b) { return (b > a || b != b) ? b : a; }
+__device__ __forceinline__ double bits_to_double(unsigned long long b) {
+  return __longlong_as_double((long long)b);
+}
 
 // copies of the node behind local row r of element e (1 or 2)
 __device__ __forceinline__ int bcopies(int e, int i, int n, int E, bool per) {
   return ((i == 0 && (e > 0 || per)) || (i == n - 1 && (e < E - 1 || per))) ? 2 : 1;
 }
+__device__ __forceinline__ float bmult(int cc) { return cc == 1 ? 1.0f : (cc == 2 ? 0.5f : 0.25f); }
 
-// Cluster-wide sum (NV values, is_max selects max) in fixed rank order; every
-// CTA gets the same result.  Calls rotate over three slots (rc counts the
-// calls, identically in every thread of the cluster): a slot is written again
-// only two cluster barriers after its last read, so no CTA overwrites a value
-// another CTA may still be reading.
-template <int NV>
-__device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, double* slots, int& rc,
-                                               double (&v)[NV], const bool (&is_max)[NV]) {
+// shared state of the cluster reductions
+struct BRed {
+  df ws[2][kBT / 32];
+  unsigned long long wm[2][kBT / 32];
+  df slot_s[3][2];
+  unsigned long long slot_m[3][2];
+};
+
+// Cluster-wide sums (NS double-float values) and maxima (NM bit patterns) in a
+// fixed order: warp trees, then the warps of a CTA in order, then the CTAs in
+// rank order, so every CTA gets the same, deterministic result.  All the
+// arithmetic runs on the FP32 pipe.  Calls rotate over three slots (rc counts
+// the calls, identically in every thread of the cluster): a slot is written
+// again only after two more cluster barriers, when no CTA still reads it.
+template <int NS, int NM>
+__device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, BRed& sh, int& rc, df (&s)[NS],
+                                               unsigned long long (&m)[NM]) {
   const int slot = rc % 3;
   ++rc;
-  __shared__ double wsum[NV][kBT / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    double x = v[q];
+  for (int q = 0; q < NS; ++q) {
+    df x = s[q];
     for (int o = 16; o > 0; o >>= 1) {
-      const double y = __shfl_down_sync(0xffffffffu, x, o);
-      x = is_max[q] ? bnanmax(x, y) : x + y;
+      const df y = {__shfl_down_sync(0xffffffffu, x.h, o), __shfl_down_sync(0xffffffffu, x.l, o)};
+      x = df_add(x, y);
     }
-    if (lane == 0) wsum[q][w] = x;
+    if (lane == 0) sh.ws[q][w] = x;
+  }
+#pragma unroll
+  for (int q = 0; q < NM; ++q) {
+    unsigned long long x = m[q];
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long y = __shfl_down_sync(0xffffffffu, x, o);
+      x = y > x ? y : x;
+    }
+    if (lane == 0) sh.wm[q][w] = x;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-      double x = wsum[q][0];
-      for (int i = 1; i < kBT / 32; ++i) x = is_max[q] ? bnanmax(x, wsum[q][i]) : x + wsum[q][i];
-      slots[slot * 4 + q] = x;
+    for (int q = 0; q < NS; ++q) {
+      df x = sh.ws[q][0];
+      for (int i = 1; i < kBT / 32; ++i) x = df_add(x, sh.ws[q][i]);
+      sh.slot_s[slot][q] = x;
+    }
+#pragma unroll
+    for (int q = 0; q < NM; ++q) {
+      unsigned long long x = sh.wm[q][0];
+      for (int i = 1; i < kBT / 32; ++i) x = sh.wm[q][i] > x ? sh.wm[q][i] : x;
+      sh.slot_m[slot][q] = x;
     }
   }
   cl.sync();
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    double x = 0.0;
-    for (int rk = 0; rk < kCluster; ++rk) {
-      const double y = cl.map_shared_rank(slots, rk)[slot * 4 + q];
-      x = is_max[q] ? bnanmax(x, y) : x + y;
+  for (int q = 0; q < NS; ++q) {
+    df x = *cl.map_shared_rank(&sh.slot_s[slot][q], 0);
+    for (int rk = 1; rk < kCluster; ++rk) x = df_add(x, *cl.map_shared_rank(&sh.slot_s[slot][q], rk));
+    s[q] = x;
+  }
+#pragma unroll
+  for (int q = 0; q < NM; ++q) {
+    unsigned long long x = *cl.map_shared_rank(&sh.slot_m[slot][q], 0);
+    for (int rk = 1; rk < kCluster; ++rk) {
+      const unsigned long long y = *cl.map_shared_rank(&sh.slot_m[slot][q], rk);
+      x = y > x ? y : x;
     }
-    v[q] = x;
+    m[q] = x;
   }
 }
 
-// One element tile of the operator mask(QQ'(nu lapl(u) + k B u)), optionally
-// with the CG direction update fused in front: u = p = dinv.*r + beta p_old.
-// Writes Ap (cross-tile points unsummed) and adds u.Ap.mult of the finished
-// points to acc.  All threads of the CTA call it (threads beyond the tile idle).
+// One element tile of the operator mask(QQ'(nu lapl(u) + k B u)) in the
+// phases of k_apply2 (and with its arithmetic, so a tile's Ap equals the
+// single-problem operator's), optionally with the CG direction update fused
+// in front: u = p = dinv.*r + beta p_old.  Writes Ap (cross-tile points
+// unsummed) and adds u.Ap.mult of the finished points to acc.  Every thread
+// of the CTA calls it; S0, S1 and X0 have one element slot per thread.
 template <class P, int N, int TX, int TY>
-__device__ void btile(const BProb& pr, const EOCoef<N, typename P::v>* D, int bx, int by,
+__device__ __noinline__ void btile(const BProb& pr, const EOCoef<N, typename P::v>* D, int bx, int by,
                       const typename P::io* u_src, const typename P::io* r, const typename P::io* dinv,
                       typename P::io beta, typename P::io* p, bool pdir, typename P::io* Ap,
-                      const typename P::io* G11, const typename P::io* G12, const typename P::io* G22,
-                      const typename P::io* B, typename P::v* S1, typename P::v* S2,
-                      BAcc<typename P::io>& acc) {
+                      const typename GeoT<P>::type* Geo, long long L, typename P::v* S0,
+                      typename P::v* S1, typename P::io* X0, BAcc<typename P::io>& acc) {
   typedef typename P::v V;
   typedef typename P::io IO;
+  typedef typename GeoT<P>::type GT;
   constexpr int SP = N | 1, ES = N * SP;
   const int t = threadIdx.x;
-  const bool inside = t < TX * TY * N;
-  const int elem = inside ? t / N : 0;
-  const int lane = inside ? t - elem * N : 0;
+  const int elem = t / N;
+  const int lane = t - elem * N;
+  const bool inside = elem < TX * TY;
   const int exl = elem % TX, eyl = elem / TX;
   const int ex = bx * TX + exl, ey = by * TY + eyl;
   const bool valid = inside && ex < pr.Ex && ey < pr.Ey;
   const long long NX = pr.NX;
   const long long base = (long long)ex * N + lane + (long long)ey * N * NX;
+  V* s0 = S0 + elem * ES;
   V* s1 = S1 + elem * ES;
-  V* s2 = S2 + elem * ES;
-  const unsigned topo = pr.topo;
-  const bool perx = (topo & M_PERX) != 0, pery = (topo & M_PERY) != 0;
+  const GT* G11 = Geo;
+  const GT* G12 = Geo + L;
+  const GT* G22 = Geo + 2 * L;
+  const GT* B = Geo + 3 * L;
   const bool jac = dinv != nullptr;
 
-  V u[N];
-  IO uraw[N];
+  // ---- A: row `lane` of u (the CG direction, formed here in pdir mode)
+  V us[N];
+  {
+    V u[N];
 #pragma unroll
-  for (int j = 0; j < N; ++j) {
-    IO v = 0;
-    if (valid) {
-      const long long gi = base + (long long)j * NX;
-      if (pdir) {
-        v = bpdir(r[gi], jac ? dinv[gi] : (IO)1, beta, p[gi], jac);
-        p[gi] = v;
-      } else {
-        v = u_src[gi];
+    for (int j = 0; j < N; ++j) {
+      IO v = 0;
+      if (valid) {
+        const long long gi = base + (long long)j * NX;
+        if (pdir) {
+          v = bpdir(r[gi], jac ? dinv[gi] : (IO)1, beta, p[gi], jac);
+          p[gi] = v;
+        } else {
+          v = u_src[gi];
+        }
       }
+      u[j] = P::cvt(v);
+      s0[j * SP + lane] = u[j];
+      s1[j * SP + lane] = u[j];
     }
-    uraw[j] = v;
-    u[j] = P::cvt(v);
+    eo_apply<P, N>(D[2], u, us);
   }
-  V us[N], res[N];
-  if (inside)
-#pragma unroll
-    for (int j = 0; j < N; ++j) s1[j * SP + lane] = u[j];
-  eo_apply<P, N>(D[2], u, us);
   __syncthreads();
-  if (inside) {
+  // ---- B: column `lane` in place; x-direction derivative
+  {
     V col[N], ur[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) col[i] = s1[lane * SP + i];
     eo_apply<P, N>(D[0], col, ur);
 #pragma unroll
-    for (int i = 0; i < N; ++i) s2[lane * SP + i] = ur[i];
+    for (int i = 0; i < N; ++i) s1[lane * SP + i] = ur[i];
   }
   __syncthreads();
+  // ---- C: row `lane` in place; metric terms, transposed y-derivative
   V os[N];
   {
     V ws[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       const long long gi = base + (long long)j * NX;
-      V g11 = valid ? P::ld(G11 + gi) : P::zero();
-      V g12 = valid ? P::ld(G12 + gi) : P::zero();
-      V g22 = valid ? P::ld(G22 + gi) : P::zero();
-      V ur = s2[j * SP + lane];
-      const V wr = P::fma(g11, ur, P::mul(g12, us[j]));
-      if (inside) s1[j * SP + lane] = wr;
+      const V g11 = valid ? GeoT<P>::ld(G11 + gi) : P::zero();
+      const V g12 = valid ? GeoT<P>::ld(G12 + gi) : P::zero();
+      const V g22 = valid ? GeoT<P>::ld(G22 + gi) : P::zero();
+      const V ur = s1[j * SP + lane];
+      s1[j * SP + lane] = P::fma(g11, ur, P::mul(g12, us[j]));
       ws[j] = P::fma(g12, ur, P::mul(g22, us[j]));
     }
     eo_apply<P, N>(D[3], ws, os);
   }
   __syncthreads();
-  if (inside) {
+  // ---- D: column `lane` in place; transposed x-derivative
+  {
     V col[N], o[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) col[i] = s1[lane * SP + i];
     eo_apply<P, N>(D[1], col, o);
 #pragma unroll
-    for (int i = 0; i < N; ++i) s2[lane * SP + i] = o[i];
+    for (int i = 0; i < N; ++i) s1[lane * SP + i] = o[i];
   }
   __syncthreads();
+  // ---- E: assemble nu (or + os) + k B u
+  V res[N];
   const V nu = P::cvt((IO)pr.nu);
   const V kk = P::cvt((IO)pr.k);
 #pragma unroll
-  for (int j = 0; j < N; ++j) {
-    res[j] = P::fin(P::mul(nu, P::add(s2[j * SP + lane], os[j])));
-    if (pr.k != 0.0) {
-      V bb = valid ? P::ld(B + base + (long long)j * NX) : P::zero();
-      res[j] = P::fin(P::fma(P::fin(P::mul(kk, bb)), u[j], res[j]));
-    }
-  }
-  // in-tile QQ': x pairs then y pairs
-  __syncthreads();
-  if (inside)
-#pragma unroll
-    for (int j = 0; j < N; ++j) s1[j * SP + lane] = res[j];
-  __syncthreads();
-  if (inside && lane == N - 1 && exl + 1 < TX && ex + 1 < pr.Ex) {
-    const V* nb = S1 + (elem + 1) * ES;
-#pragma unroll
-    for (int j = 0; j < N; ++j) res[j] = P::add(res[j], nb[j * SP]);
-  }
-  if (inside && lane == 0 && exl > 0) {
-    const V* nb = S1 + (elem - 1) * ES;
-#pragma unroll
-    for (int j = 0; j < N; ++j) res[j] = P::add(nb[j * SP + N - 1], res[j]);
-  }
-  if (inside) {
-    s2[lane] = res[0];
-    s2[(N - 1) * SP + lane] = res[N - 1];
-  }
-  __syncthreads();
-  if (inside && eyl + 1 < TY && ey + 1 < pr.Ey) res[N - 1] = P::add(res[N - 1], S2[(elem + TX) * ES + lane]);
-  if (inside && eyl > 0) res[0] = P::add(S2[(elem - TX) * ES + (N - 1) * SP + lane], res[0]);
-  if (valid) {
-    const bool xc = xcross_row(ex, lane, N, pr.Ex, TX, perx);
-    const long long row = (long long)ex * N + lane;
-    const int cx = bcopies(ex, lane, N, pr.Ex, perx);
+  for (int j = 0; j < N; ++j) res[j] = P::fin(P::mul(nu, P::add(s1[j * SP + lane], os[j])));
+  if (pr.k != 0.0) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      bool raw = xc;
-      if (j == 0 && eyl == 0 && (ey > 0 || pery)) raw = true;
-      if (j == N - 1 && (eyl == TY - 1 || ey == pr.Ey - 1) && (ey < pr.Ey - 1 || pery)) raw = true;
-      IO val = P::st(res[j]);
-      if (!raw) {
-        const long long col = (long long)ey * N + j;
-        if ((topo & M_MASK) && !mask_keep(row, col, NX, pr.NY, topo)) val = masked_zero(val);
-        const int cc = cx * bcopies(ey, j, N, pr.Ey, pery);
-        acc.prod(uraw[j], val, cc == 1 ? 1.0f : (cc == 2 ? 0.5f : 0.25f));
-      }
-      Ap[base + (long long)j * NX] = val;
+      const V b = valid ? GeoT<P>::ld(B + base + (long long)j * NX) : P::zero();
+      res[j] = P::fin(P::fma(P::mul(kk, b), s0[j * SP + lane], res[j]));
     }
   }
-  __syncthreads();
+  // ---- in-tile QQ', mask, store; u.Ap.mult of the finished points
+  const bool perx = (pr.topo & M_PERX) != 0, pery = (pr.topo & M_PERY) != 0;
+  const int cx = bcopies(ex, lane, N, pr.Ex, perx);
+  tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), X0, elem, lane, ex, ey, valid, base,
+                               pr.Ex, pr.Ey, NX, pr.topo | M_GS, Ap, [&](int j, IO val) {
+                                 acc.prod_v(s0[j * SP + lane], val, bmult(cx * bcopies(ey, j, N, pr.Ey, pery)));
+                               });
+  __syncthreads();  // the next tile overwrites the line buffers
 }
 
-// cross-tile QQ' completion, work split over the whole cluster; adds
-// p.Ap.mult of every copy it finishes
+// cross-tile QQ' completion (the interface rows of k_dss_fixup), work split
+// over the whole cluster; adds p.Ap.mult of every copy it finishes
 template <class IO, int TX, int TY>
-__device__ void bfixup(const BProb& pr, int n, IO* __restrict__ Ap, const IO* __restrict__ p,
+__device__ __noinline__ void bfixup(const BProb& pr, int n, IO* __restrict__ Ap, const IO* __restrict__ p,
                        int rank, BAcc<IO>& acc) {
-  const unsigned topo = pr.topo;
-  const bool perx = (topo & M_PERX) != 0, pery = (topo & M_PERY) != 0;
-  const bool msk = (topo & M_MASK) != 0;
-  const long long NX = pr.NX, NY = pr.NY;
-  const long long nxi = (pr.Ex - 1) / TX + (perx ? 1 : 0);
-  const long long nyi = (pr.Ey - 1) / TY + (pery ? 1 : 0);
-  const long long nX = nxi * NY, nY = nyi * NX, nC = nxi * nyi;
-  const long long total = nX + nY + nC;
-  auto fin = [&](long long r, long long c, IO s, float m) {
-    IO v = s;
-    if (msk && !mask_keep(r, c, NX, NY, topo)) v = masked_zero(s);
-    Ap[r + c * NX] = v;
-    acc.prod(p[r + c * NX], v, m);
-  };
-  for (long long idx = (long long)rank * kBT + threadIdx.x; idx < total; idx += (long long)kCluster * kBT) {
-    if (idx < nX) {
-      const long long q = idx / NY, c = idx - q * NY;
-      const long long ey = c / n;
-      const int j = (int)(c - ey * n);
-      if (xcross_row((int)ey, j, n, pr.Ey, TY, pery)) continue;
-      const long long aa = fix_iface(q, TX, perx);
-      const long long rl = aa == 0 ? NX - 1 : aa * n - 1, rr = aa * n;
-      const IO s = Ap[rl + c * NX] + Ap[rr + c * NX];
-      const float m = 0.5f / (float)bcopies((int)ey, j, n, pr.Ey, pery);
-      fin(rl, c, s, m);
-      fin(rr, c, s, m);
-    } else if (idx < nX + nY) {
-      const long long id2 = idx - nX, q = id2 / NX, r = id2 - q * NX;
-      const long long ex = r / n;
-      const int i = (int)(r - ex * n);
-      if (xcross_row((int)ex, i, n, pr.Ex, TX, perx)) continue;
-      const long long bb = fix_iface(q, TY, pery);
-      const long long cl = bb == 0 ? NY - 1 : bb * n - 1, cr = bb * n;
-      const IO s = Ap[r + cl * NX] + Ap[r + cr * NX];
-      const float m = 0.5f / (float)bcopies((int)ex, i, n, pr.Ex, perx);
-      fin(r, cl, s, m);
-      fin(r, cr, s, m);
-    } else {
-      const long long id3 = idx - nX - nY, q = id3 / nyi, pp = id3 - q * nyi;
-      const long long aa = fix_iface(q, TX, perx), bb = fix_iface(pp, TY, pery);
-      const long long rl = aa == 0 ? NX - 1 : aa * n - 1, rr = aa * n;
-      const long long cl = bb == 0 ? NY - 1 : bb * n - 1, cr = bb * n;
-      const IO s = (Ap[rl + cl * NX] + Ap[rr + cl * NX]) + (Ap[rl + cr * NX] + Ap[rr + cr * NX]);
-      fin(rl, cl, s, 0.25f);
-      fin(rr, cl, s, 0.25f);
-      fin(rl, cr, s, 0.25f);
-      fin(rr, cr, s, 0.25f);
-    }
-  }
+  FixArgs f;
+  f.n = n;
+  f.Ex = pr.Ex;
+  f.Ey = pr.Ey;
+  f.TX = TX;
+  f.TY = TY;
+  f.NX = pr.NX;
+  f.NY = pr.NY;
+  f.mode = pr.topo | M_GS;
+  f.skip = nullptr;
+  const bool perx = (pr.topo & M_PERX) != 0, pery = (pr.topo & M_PERY) != 0;
+  f.nxi = (pr.Ex - 1) / TX + (perx ? 1 : 0);
+  f.nyi = (pr.Ey - 1) / TY + (pery ? 1 : 0);
+  const long long nI = fix_rows(f);
+  const long long first = (long long)rank * kBT + threadIdx.x;
+  const unsigned un = (unsigned)n;
+  for (long long q = 0; q < nI; ++q)
+    fix_interface(Ap, f, q, first, (long long)kCluster * kBT, [&](long long r, long long c, IO v) {
+      const int ex = (int)((unsigned)r / un), ey = (int)((unsigned)c / un);
+      const int cc = bcopies(ex, (int)r - ex * n, n, pr.Ex, perx) * bcopies(ey, (int)c - ey * n, n, pr.Ey, pery);
+      acc.prod(p[r + c * pr.NX], v, bmult(cc));
+    });
 }
 
 // run `f(row, col, idx, mult)` over the points of this CTA's tiles
@@ -412,15 +399,34 @@ __device__ __forceinline__ void own_points(const BProb& pr, int rank, F&& f) {
   }
 }
 
+// shared-memory line buffers of one CTA
+template <int N>
+struct BBuf {
+  df* S0;
+  df* S1;
+  double* X0;
+  __device__ BBuf(unsigned char* smem) {
+    constexpr size_t E = (size_t)BTile<N>::SLOTS * BTile<N>::ES;
+    S0 = reinterpret_cast<df*>(smem);
+    S1 = S0 + E;
+    X0 = reinterpret_cast<double*>(S1 + E);
+  }
+  template <class P>
+  __device__ typename P::v* s0() const { return reinterpret_cast<typename P::v*>(S0); }
+  template <class P>
+  __device__ typename P::v* s1() const { return reinterpret_cast<typename P::v*>(S1); }
+  template <class P>
+  __device__ typename P::io* x0() const { return reinterpret_cast<typename P::io*>(X0); }
+};
+
 // CG on A y = rhs (P: PDF for FP64 vectors, PF32 for the FP32 inner solve).
 // rhs is read as double (b or the FP64 residual) and converted.
 template <class P, int N>
 __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int rank,
                     const double* rhs, typename P::io* y, typename P::io* r, typename P::io* p,
-                    typename P::io* Ap, const typename P::io* dinv, const typename P::io* G11,
-                    const typename P::io* G12, const typename P::io* G22, const typename P::io* B,
-                    double tol, int maxiter, double* slots, int& rc, typename P::v* S1, typename P::v* S2,
-                    int& iters, double& rmax_out, bool& nan_out) {
+                    typename P::io* Ap, const typename P::io* dinv, const typename GeoT<P>::type* Geo,
+                    double tol, int maxiter, BRed& red, int& rc, const BBuf<N>& buf, int& iters,
+                    double& rmax_out, bool& nan_out) {
   typedef typename P::io IO;
   typedef BTile<N> T;
   const EOCoef<N, typename P::v>* D;
@@ -429,6 +435,7 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
   else
     D = a.cdf;
   const bool jac = dinv != nullptr;
+  const long long L = pr.NX * pr.NY;
   const int ntx = (pr.Ex + T::TX - 1) / T::TX, nty = (pr.Ey + T::TY - 1) / T::TY;
   // init: y = 0, r = rhs, p = 0; t = r.h.mult, max|r|
   BAcc<IO> acc;
@@ -443,10 +450,10 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
       acc.prod(ri, ri, m);
     acc.amax(ri);
   });
-  double v2[2] = {acc.sum(), acc.max()};
-  const bool mx2[2] = {false, true};
-  cluster_reduce<2>(cl, slots, rc, v2, mx2);
-  double t = v2[0], rmax = v2[1];
+  df s1[1] = {acc.sum()};
+  unsigned long long m1[1] = {acc.max_bits()};
+  cluster_reduce<1, 1>(cl, red, rc, s1, m1);
+  double t = df2d(s1[0]), rmax = bits_to_double(m1[0]);
   double tprev = 1.0;
   int k = 0;
   bool nan = rmax != rmax;
@@ -456,15 +463,16 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
     BAcc<IO> dot;
     for (int tile = rank; tile < ntx * nty; tile += kCluster) {
       const int by = tile / ntx, bx = tile - by * ntx;
-      btile<P, N, T::TX, T::TY>(pr, D, bx, by, nullptr, r, dinv, (IO)beta, p, true, Ap, G11, G12,
-                                G22, B, S1, S2, dot);
+      btile<P, N, T::TX, T::TY>(pr, D, bx, by, nullptr, r, dinv, (IO)beta, p, true, Ap, Geo, L,
+                                buf.template s0<P>(), buf.template s1<P>(), buf.template x0<P>(), dot);
     }
     cl.sync();
     bfixup<IO, T::TX, T::TY>(pr, N, Ap, p, rank, dot);
-    double v1[1] = {dot.sum()};
-    const bool mx1[1] = {false};
-    cluster_reduce<1>(cl, slots, rc, v1, mx1);
-    const double alpha = t / v1[0];
+    df s2[1] = {dot.sum()};
+    unsigned long long m0[1] = {0ull};
+    cluster_reduce<1, 1>(cl, red, rc, s2, m0);
+    const double pap = df2d(s2[0]);
+    const double alpha = t / pap;
     ++k;
     BAcc<IO> up;
     own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float m) {
@@ -477,11 +485,12 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
         up.prod(ri, ri, m);
       up.amax(ri);
     });
-    double w2[2] = {up.sum(), up.max()};
-    cluster_reduce<2>(cl, slots, rc, w2, mx2);
+    df s3[1] = {up.sum()};
+    unsigned long long m3[1] = {up.max_bits()};
+    cluster_reduce<1, 1>(cl, red, rc, s3, m3);
     tprev = t;
-    t = w2[0];
-    rmax = w2[1];
+    t = df2d(s3[0]);
+    rmax = bits_to_double(m3[0]);
     nan = (rmax != rmax) || (alpha != alpha);
     done = !(rmax > tol) || k >= maxiter || nan;
   }
@@ -493,15 +502,15 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
 // Ax (FP64, double-float operator) then r = b - Ax and max|r| over the cluster
 template <int N>
 __device__ double bresidual(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int rank,
-                            double* slots, int& rc, df* S1, df* S2) {
+                            BRed& red, int& rc, const BBuf<N>& buf) {
   typedef BTile<N> T;
-  const EOCoef<N, df>* D = a.cdf;
+  const long long L = pr.NX * pr.NY;
   const int ntx = (pr.Ex + T::TX - 1) / T::TX, nty = (pr.Ey + T::TY - 1) / T::TY;
   BAcc<double> unused;
   for (int tile = rank; tile < ntx * nty; tile += kCluster) {
     const int by = tile / ntx, bx = tile - by * ntx;
-    btile<PDF, N, T::TX, T::TY>(pr, D, bx, by, pr.x, nullptr, nullptr, 0.0, nullptr, false, pr.Ap,
-                                pr.G11, pr.G12, pr.G22, pr.B, S1, S2, unused);
+    btile<PDF, N, T::TX, T::TY>(pr, a.cdf, bx, by, pr.x, nullptr, nullptr, 0.0, nullptr, false, pr.Ap,
+                                pr.Gdf, L, buf.S0, buf.S1, buf.X0, unused);
   }
   cl.sync();
   bfixup<double, T::TX, T::TY>(pr, N, pr.Ap, pr.x, rank, unused);
@@ -512,26 +521,24 @@ __device__ double bresidual(const BatchArgs<N>& a, BProb& pr, cg::cluster_group&
     pr.r[i] = v;
     acc.amax(v);
   });
-  double v1[1] = {acc.max()};
-  const bool mx1[1] = {true};
-  cluster_reduce<1>(cl, slots, rc, v1, mx1);
-  return v1[0];
+  df s0[1] = {{0.0f, 0.0f}};
+  unsigned long long m1[1] = {acc.max_bits()};
+  cluster_reduce<1, 1>(cl, red, rc, s0, m1);
+  return bits_to_double(m1[0]);
 }
 
 template <int N>
-__device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int rank,
-                       double* slots, int& rc, unsigned char* smem) {
+__device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int rank, BRed& red,
+                       int& rc, const BBuf<N>& buf) {
   typedef BTile<N> T;
-  df* S1 = reinterpret_cast<df*>(smem);
-  df* S2 = S1 + T::TX * T::TY * T::ES;
   const bool jac = a.jacobi != 0;
   const int maxiter = pr.maxiter;
   if (a.precision != SEM_MIXED) {
     int it = 0;
     double rmax = 0.0;
     bool nan = false;
-    bcg<PDF, N>(a, pr, cl, rank, pr.b, pr.x, pr.r, pr.p, pr.Ap, jac ? pr.dinv : nullptr, pr.G11,
-                pr.G12, pr.G22, pr.B, pr.tol, maxiter, slots, rc, S1, S2, it, rmax, nan);
+    bcg<PDF, N>(a, pr, cl, rank, pr.b, pr.x, pr.r, pr.p, pr.Ap, jac ? pr.dinv : nullptr, pr.Gdf, pr.tol,
+                maxiter, red, rc, buf, it, rmax, nan);
     if (rank == 0 && threadIdx.x == 0) {
       pr.iters = it;
       pr.outer = 0;
@@ -541,8 +548,6 @@ __device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, 
     }
     return;
   }
-  float* F1 = reinterpret_cast<float*>(smem);
-  float* F2 = F1 + T::TX * T::TY * T::ES;
   // FP64 defect correction around the FP32 inner CG: x = 0, r = b
   BAcc<double> acc;
   own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float) {
@@ -550,25 +555,26 @@ __device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, 
     pr.r[i] = pr.b[i];
     acc.amax(pr.b[i]);
   });
-  double v1[1] = {acc.max()};
-  const bool mx1[1] = {true};
-  cluster_reduce<1>(cl, slots, rc, v1, mx1);
-  double rmax = v1[0];
+  df s0[1] = {{0.0f, 0.0f}};
+  unsigned long long m1[1] = {acc.max_bits()};
+  cluster_reduce<1, 1>(cl, red, rc, s0, m1);
+  double rmax = bits_to_double(m1[0]);
   const double res0 = rmax;
   int outer = 0, total = 0;
   bool nan = rmax != rmax;
+  // the FP32 geometry blocks are contiguous (G11, G12, G22, B)
+  const float* Gf = pr.G11f;
   while (!(rmax <= pr.tol) && !nan && outer < a.max_outer) {
     ++outer;
     int it = 0;
     double rin = 0.0;
     bool nin = false;
-    bcg<PF32, N>(a, pr, cl, rank, pr.r, pr.x32, pr.r32, pr.p32, pr.Ap32, jac ? pr.dinv32 : nullptr,
-                 pr.G11f, pr.G12f, pr.G22f, pr.Bf, a.inner_tol * rmax, maxiter, slots, rc, F1, F2, it,
-                 rin, nin);
+    bcg<PF32, N>(a, pr, cl, rank, pr.r, pr.x32, pr.r32, pr.p32, pr.Ap32, jac ? pr.dinv32 : nullptr, Gf,
+                 a.inner_tol * rmax, maxiter, red, rc, buf, it, rin, nin);
     total += it;
     own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float) { pr.x[i] += (double)pr.x32[i]; });
     cl.sync();
-    rmax = bresidual<N>(a, pr, cl, rank, slots, rc, S1, S2);
+    rmax = bresidual<N>(a, pr, cl, rank, red, rc, buf);
     nan = rmax != rmax;
   }
   if (rank == 0 && threadIdx.x == 0) {
@@ -582,21 +588,22 @@ __device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, 
 }
 
 template <int N>
-__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kBT, 1)
+__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kBT, kBatchCtasPerSm)
     k_batch_pcg(const __grid_constant__ BatchArgs<N> a) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double slots[3 * 4];
+  __shared__ BRed red;
   int rc = 0;
   __shared__ int s_pid;
+  const BBuf<N> buf(smem);
   for (;;) {
     if (rank == 0 && threadIdx.x == 0) s_pid = atomicAdd(a.queue, 1);
     cl.sync();
     const int pid = *cl.map_shared_rank(&s_pid, 0);
     cl.sync();  // every CTA has read s_pid before rank 0 may overwrite it
     if (pid >= a.count) return;
-    bsolve<N>(a, a.probs[pid], cl, rank, slots, rc, smem);
+    bsolve<N>(a, a.probs[pid], cl, rank, red, rc, buf);
     cl.sync();  // the problem's results are written before the next one starts
   }
 }
@@ -635,7 +642,7 @@ int launch_batch_order(const BatchCommon& c, const OperatorSet& ops, cudaStream_
     }
   }
   typedef BTile<N> T;
-  const size_t smem = 2 * (size_t)T::TX * T::TY * T::ES * sizeof(df);
+  const size_t smem = (size_t)T::SLOTS * T::ES * (2 * sizeof(df) + sizeof(double));
   SEM_CUDA(cudaFuncSetAttribute(k_batch_pcg<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int nclusters = c.clusters;
   if (nclusters <= 0) {

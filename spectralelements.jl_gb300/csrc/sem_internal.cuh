@@ -186,6 +186,7 @@ struct sem_mesh {
   unsigned char* info;     // device L_* tables: NX row entries then NY column entries
   int variant[4];          // autotuned kernel variant per precision (SEM_F64, SEM_F64_DF, SEM_F32)
   void* graphs;            // CUDA graphs of the CG iteration chunks (sem_pcg.cu), or NULL
+  unsigned* fix_ctr;       // interface arrival counters of kernel variant 5 (3 per tile), or NULL
 };
 
 namespace sem {
@@ -195,6 +196,7 @@ int build_geometry(sem_mesh* m, const double* x_h, const double* y_h, cudaStream
 int export_field(const sem_mesh* m, int which, double* out, cudaStream_t s);
 int ensure_f32_geometry(sem_mesh* m, cudaStream_t s);
 int ensure_df_geometry(sem_mesh* m, cudaStream_t s);
+int ensure_fix_counters(sem_mesh* m);  // sem_apply.cu
 
 // operator coefficients (sem_apply.cu)
 int make_operator_set(const double* Dr, const double* Ds, int n, OperatorSet** out);
@@ -215,7 +217,18 @@ struct ApplyCall {
   const int* skip; // device flag: when non-zero the launch does nothing (solver loops)
   int variant;     // kernel variant 0..kVariants-1 (launch_apply_n in sem_apply_launch.cuh)
   const void* Gdf; // G11, G12, G22, B split into double-float pairs (4 blocks of NX*NY), or NULL
+  unsigned* ctr;   // interface arrival counters of the mesh (variant 5), or NULL
+  // CG-fused launch (variants 2 and 5; cg_p non-NULL): u = p = dinv.*r + beta p
+  // formed in the kernel, per-CTA parts of p.Ap written to cg_dpart
+  const void* cg_r;
+  const void* cg_dinv;
+  void* cg_p;
+  const double* cg_beta;
+  void* cg_dpart;
 };
+
+// number of CTAs (element tiles) of a CG-fused operator launch on grid g
+long long cg_apply_parts(const Grid& g);
 
 constexpr int kVariants = SEM_VARIANTS;
 

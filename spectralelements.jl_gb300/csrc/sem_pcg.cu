@@ -151,15 +151,6 @@ struct Acc<float> {
 };
 
 // p = h + beta p_old with h = r .* dinv
-__device__ __forceinline__ double pdir_value(double r, double d, double beta, double p, bool jac) {
-  const df rd = d2df(r);
-  const df h = jac ? df_mul_u(rd, d2df(d)) : rd;
-  return df2d(df_fma_u(d2df(beta), d2df(p), h));
-}
-__device__ __forceinline__ float pdir_value(float r, float d, float beta, float p, bool jac) {
-  return __fmaf_rn(beta, p, jac ? r * d : r);
-}
-
 // x = 0, r = b (converted), p = 0; partials of t = r.h.mult and max|r|
 template <class T, class TB>
 __global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
@@ -208,7 +199,7 @@ __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* _
   const bool jac = dinv != nullptr;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
        i += (long long)gridDim.x * blockDim.x)
-    p[i] = pdir_value(r[i], jac ? dinv[i] : (T)1, beta, p[i], jac);
+    p[i] = cg_direction(r[i], jac ? dinv[i] : (T)1, beta, p[i], jac);
 }
 
 template <class T>
@@ -222,6 +213,21 @@ __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, dou
   double v[1] = {acc.sum()};
   const bool mx[1] = {false};
   block_reduce<1>(v, mx, part);
+}
+
+// alpha = t / (p . A p) from the per-CTA double-float parts of a CG-fused
+// operator launch, summed in a fixed order (one block)
+__global__ void k_scal_alpha_df(const df* part, long long np, Scalars* sc) {
+  if (sc->done) return;
+  df x = {0.0f, 0.0f};
+  for (long long i = threadIdx.x; i < np; i += blockDim.x) x = df_add(x, part[i]);
+  x = block_sum_df(x);
+  if (threadIdx.x == 0) {
+    const double pap = df2d(x);
+    sc->pAp = pap;
+    sc->alpha = sc->t / pap;
+    sc->k += 1;
+  }
 }
 
 __global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
@@ -402,6 +408,8 @@ struct WS {
   double *r, *p, *Ap, *dinv, *d, *x64tmp;  // FP64 vectors
   float *r32, *p32, *Ap32, *x32, *dinv32;   // FP32 vectors (mixed)
   double* part;
+  df* dpart;             // per-CTA parts of p.Ap of CG-fused operator launches
+  long long dpart_n;
   Scalars* sc;
   double* dmax;
   Scalars* sc_h;  // pinned host mirror
@@ -411,7 +419,9 @@ int get_ws(sem_mesh* m, bool mixed, WS& w) {
   const long long L = m->g.NX * m->g.NY;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t v64 = al(sizeof(double) * L), v32 = al(sizeof(float) * L);
-  const size_t need = 6 * v64 + 5 * v32 + al(sizeof(double) * kRB * 4) + al(sizeof(Scalars)) + al(sizeof(double));
+  const long long np = cg_apply_parts(m->g);
+  const size_t need = 6 * v64 + 5 * v32 + al(sizeof(double) * kRB * 4) + al(sizeof(df) * np) +
+                      al(sizeof(Scalars)) + al(sizeof(double));
   if (m->ws_bytes < need) {
     if (m->ws) cudaFree(m->ws);
     m->ws = nullptr;
@@ -433,6 +443,8 @@ int get_ws(sem_mesh* m, bool mixed, WS& w) {
   w.x32 = (float*)p; p += v32;
   w.dinv32 = (float*)p; p += v32;
   w.part = (double*)p; p += al(sizeof(double) * kRB * 4);
+  w.dpart = (df*)p; p += al(sizeof(df) * np);
+  w.dpart_n = np;
   w.sc = (Scalars*)p; p += al(sizeof(Scalars));
   w.dmax = (double*)p;
   static thread_local Scalars* host = nullptr;
@@ -450,6 +462,7 @@ struct OpCtx {
   const double *G11, *G12, *G22, *B;
   const float *G11f, *G12f, *G22f, *Bf;
   const void* Gdf;     // double-float split geometry (or NULL)
+  unsigned* ctr;       // interface arrival counters (or NULL)
   const int* variant;  // per precision
 };
 
@@ -467,6 +480,7 @@ OpCtx ctx_of(const sem_mesh* m) {
   cx.G22f = m->G22_f;
   cx.Bf = m->B_f;
   cx.Gdf = m->Gdf;
+  cx.ctr = m->fix_ctr;
   cx.variant = m->variant;
   return cx;
 }
@@ -495,11 +509,17 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
                   const T* dinv, const ApplyCall& c, int check_every, cudaStream_t s) {
   const long long L = cx.g.NX * cx.g.NY;
   const unsigned nb = nblocks(L);
+  const bool fused = c.cg_p != nullptr;  // direction and p.Ap inside the operator launch
   for (int it = 0; it < check_every; ++it) {
-    k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
-    SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
-    k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
-    k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+    if (fused) {
+      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
+      k_scal_alpha_df<<<1, kRT, 0, s>>>(w.dpart, cg_apply_parts(cx.g), w.sc);
+    } else {
+      k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
+      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
+      k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
+      k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+    }
     k_update<T><<<nb, kRT, 0, s>>>(x, r, p, Ap, dinv, w.part, w.sc, gv);
     k_scal_beta<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
   }
@@ -629,7 +649,18 @@ int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r
   c.precision = op_precision;
   c.variant = cx.variant[op_precision];
   c.Gdf = cx.Gdf;
+  c.ctr = cx.ctr;
   c.skip = &w.sc->done;
+  // CG-fused operator launches with the kernels that provide them (variants 2
+  // and 5; double-float arithmetic also needs the pre-split geometry)
+  if ((c.variant == 2 || c.variant == 5) && (op_precision != SEM_F64_DF || c.Gdf) && w.dpart &&
+      cg_apply_parts(cx.g) <= w.dpart_n) {
+    c.cg_r = r;
+    c.cg_dinv = dinv;
+    c.cg_p = p;
+    c.cg_beta = &w.sc->beta;
+    c.cg_dpart = w.dpart;
+  }
   cudaGraphExec_t exec = nullptr;
   if (m && !timing_enabled())
     SEM_CHECK(chunk_graph<T>(m, cx, gv, w, x, r, p, Ap, dinv, c, check_every, &exec));
@@ -722,6 +753,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     c.precision = m->precision;
     c.variant = cx.variant[m->precision];
     c.Gdf = cx.Gdf;
+    c.ctr = cx.ctr;
     bool nan = rmax != rmax;
     while (!(rmax <= o->tol) && !nan && outer < max_outer) {
       ++outer;

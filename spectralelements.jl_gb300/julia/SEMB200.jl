@@ -14,7 +14,8 @@
 module SEMB200
 
 using CUDA
-import SpectralElements: ABu, lapl, mass, hlmz, gatherScatter, mask, pcg, pcg!, Mesh
+import ChainRulesCore
+import SpectralElements: ABu, lapl, mass, hlmz, gatherScatter, mask, pcg, pcg!, Mesh, generateMask
 
 const libsem = get(ENV, "SEM_B200_LIB", joinpath(@__DIR__, "..", "lib", "libsem_b200.so"))
 
@@ -70,6 +71,17 @@ end
 
 set_bc!(msh::Mesh, bc::Vector{Char}) =
     check(ccall((:sem_mesh_set_bc, libsem), Cint, (Ptr{Cvoid}, Cstring), handle(msh), String(bc)))
+
+# ---- kernel-variant autotuner (no counterpart in the reference): times every
+# variant of the fused element operator on this mesh and keeps the fastest
+const SEM_VARIANTS = 6
+function autotune!(msh::Mesh; precision=SEM_F64_DF)
+    ms = zeros(Cdouble, SEM_VARIANTS)
+    chosen = Ref{Cint}(0)
+    check(ccall((:sem_mesh_autotune, libsem), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ref{Cint}),
+                handle(msh), precision, ms, chosen))
+    return (chosen=Int(chosen[]), ms=ms)
+end
 
 # ---- ABu(As,Br,u) (src/ABu.jl:9-37); [] = identity
 function ABu(As::AbstractArray, Br::AbstractArray, u::CuArray{Float64,2})
@@ -190,6 +202,73 @@ pcg(b::CuArray, opA::Function; kw...) =
 function pcg!(x::CuArray{Float64,2}, b::CuArray{Float64,2}, opA::HelmholtzOp; kw...)
     x .= pcg(b, opA; kw...)
     return
+end
+
+# ---- batched solves: many independent Diffusion-type systems (different
+# element counts, orders, ν and k) in one persistent launch per order
+mutable struct BatchSolver
+    ptr::Ptr{Cvoid}
+    meshes::Vector{Mesh}
+end
+function BatchSolver(meshes::Vector{<:Mesh}, ν::Vector{Float64}, k::Vector{Float64},
+                     bc::Vector{Char}; jacobi::Bool=true)
+    hs = Ptr{Cvoid}[handle(m) for m in meshes]
+    foreach(m -> set_bc!(m, bc), meshes)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:sem_batch_create, libsem), Cint,
+                (Ptr{Ptr{Cvoid}}, Ptr{Cdouble}, Ptr{Cdouble}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                hs, ν, k, length(meshes), jacobi ? 1 : 0, out))
+    b = BatchSolver(out[], collect(meshes))
+    finalizer(x -> ccall((:sem_batch_destroy, libsem), Cint, (Ptr{Cvoid},), x.ptr), b)
+    return b
+end
+function solve(bs::BatchSolver, rhs::Vector{<:CuArray{Float64,2}}, tol::Vector{Float64};
+               precision=SEM_F64_DF, inner_tol=1e-4, max_outer=6)
+    xs = [similar(r) for r in rhs]
+    bp = CuPtr{Cdouble}[pointer(r) for r in rhs]
+    xp = CuPtr{Cdouble}[pointer(x) for x in xs]
+    info = [SolveInfo() for _ in rhs]
+    st = ccall((:sem_batch_pcg, libsem), Cint,
+               (Ptr{Cvoid}, Ptr{CuPtr{Cdouble}}, Ptr{CuPtr{Cdouble}}, Ptr{Cdouble}, Ptr{Cint}, Cint,
+                Cdouble, Cint, Ptr{SolveInfo}, Ptr{Cvoid}),
+               bs.ptr, bp, xp, tol, C_NULL, precision, inner_tol, max_outer, info, stream())
+    st == SEM_ERR_NOT_CONVERGED && println("warning: some batched solves reached maxiter")
+    st == SEM_ERR_NOT_CONVERGED || check(st)
+    return xs, info
+end
+
+# ---- differentiable solve of -div(ν grad u) = f with ν folded into G
+# (examples/semPS.jl:163-165), the pattern of linsolve + @adjoint in
+# src/adjoint.jl:5-24 as a ChainRulesCore rrule: the pullback solves the
+# adjoint system for λ and returns the per-local-copy gradient
+# -G:(grad λ)(grad u) (sem_adjoint_grad).
+function varcoef_solve(ν::CuArray{Float64,2}, b::CuArray{Float64,2}, msh::Mesh, bc::Vector{Char};
+                       tol=1e-10)
+    set_bc!(msh, bc)
+    x = similar(b)
+    o = Ref(PcgOpts(1.0, pointer(ν), 0.0, 1, SEM_F64_DF, tol, 0, 1e-4, 6, 0, 0))
+    info = Ref(SolveInfo())
+    check(ccall((:sem_pcg, libsem), Cint,
+                (Ptr{Cvoid}, Ref{PcgOpts}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ref{SolveInfo}, Ptr{Cvoid}),
+                handle(msh), o, pointer(b), pointer(x), info, stream()))
+    return x
+end
+
+function ChainRulesCore.rrule(::typeof(varcoef_solve), ν::CuArray{Float64,2}, b::CuArray{Float64,2},
+                              msh::Mesh, bc::Vector{Char}; tol=1e-10)
+    u = varcoef_solve(ν, b, msh, bc; tol=tol)
+    function varcoef_solve_pullback(ū)
+        rhs = gatherScatter(mask(CuArray{Float64,2}(ChainRulesCore.unthunk(ū)),
+                                 CuArray(Float64.(generateMask(bc, msh)))), msh)
+        λ = varcoef_solve(ν, rhs, msh, bc; tol=tol)
+        g = similar(u)
+        check(ccall((:sem_adjoint_grad, libsem), Cint,
+                    (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                    handle(msh), pointer(λ), pointer(u), pointer(g), 0, stream()))
+        return ChainRulesCore.NoTangent(), g, ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(),
+               ChainRulesCore.NoTangent()
+    end
+    return u, varcoef_solve_pullback
 end
 
 end # module

@@ -47,7 +47,7 @@ SEM_OK, SEM_ERR_BAD_ARG, SEM_ERR_NOT_CONVERGED, SEM_ERR_NAN, SEM_ERR_TIMEOUT, SE
 SEM_GS, SEM_MASK = 1, 2
 SEM_F64, SEM_F64_DF, SEM_F32, SEM_MIXED = 0, 1, 2, 3
 SEM_PRECOND_NONE, SEM_PRECOND_JACOBI = 0, 1
-SEM_VARIANTS = 5  # fused element-operator kernel variants (include/sem_b200.h)
+SEM_VARIANTS = 6  # fused element-operator kernel variants (include/sem_b200.h)
 FIELDS = {"x": 0, "y": 1, "Jac": 2, "Jaci": 3, "rx": 4, "ry": 5, "sx": 6, "sy": 7, "B": 8,
           "Bi": 9, "G11": 10, "G12": 11, "G22": 12, "mult": 13, "mask": 14}
 

@@ -38,7 +38,7 @@ def _ids(c):
 
 @pytest.mark.parametrize("case", CASES, ids=_ids)
 @pytest.mark.parametrize("prec", ["F64", "DF"])
-@pytest.mark.parametrize("variant", [0, 2, 4])
+@pytest.mark.parametrize("variant", [0, 2, 4, 5])
 def test_fused_operators(gpu, case, prec, variant):
     import semgb300 as S
     n, Ex, Ey, per, bc, amp = case
@@ -100,12 +100,21 @@ def test_kernel_variants_bit_identical(gpu, case):
         for v in range(1, len(outs)):
             for a, b in zip(outs[0], outs[v]):
                 np.testing.assert_array_equal(a, b)
+        # in-kernel completion (variant 5) over many launches: the arrival
+        # counters stay consistent from launch to launch
+        md.set_variant(5)
+        op = S.HelmholtzOp(md, 1e-2, 1.0)
+        for _ in range(25):
+            np.testing.assert_array_equal(host(op(ud)), outs[0][3])
         # the fused QQ' and mask sum every node in the order of the standalone
         # gatherScatter: fused == mask(gatherScatter(hlmz(u)))
         Md = S.generateMask(list(bc), md)
         unfused = host(S.mask(S.gatherScatter(S.hlmz(ud, 1e-2, 1.0, md), md), Md))
         np.testing.assert_array_equal(outs[0][3], unfused)
     # FP32 inner operator: identical mixed-precision solves for every variant
+    # of one CG form.  Variants 2 and 5 run the CG-fused operator launch, whose
+    # p.Ap is summed over the unassembled products: their solves agree with
+    # each other bit for bit and with the other variants' to the tolerance.
     md.set_precision(S.SEM_F64_DF)
     md.set_variant(0)
     M = O.generateMask(list(bc), mo)
@@ -118,9 +127,13 @@ def test_kernel_variants_bit_identical(gpu, case):
         info = {}
         xs.append((host(S.pcg(b, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info,
                               precision=S.SEM_MIXED)), info["iters"]))
-    for x, it in xs[1:]:
-        assert it == xs[0][1]
-        np.testing.assert_array_equal(x, xs[0][0])
+    fused = (2, 5)
+    for v, (x, it) in enumerate(xs):
+        ref_x, ref_it = xs[fused[0]] if v in fused else xs[0]
+        assert it == ref_it, (v, it, ref_it)
+        np.testing.assert_array_equal(x, ref_x)
+    assert abs(xs[2][1] - xs[0][1]) <= max(2, xs[0][1] // 100)
+    assert rel_l2(xs[2][0], xs[0][0]) < 1e-6
 
 
 def test_autotune_reports_every_variant(gpu):

@@ -51,7 +51,8 @@ def test_batch_matches_single_solves(gpu, precision):
     for (x, inf, (x_ref, it_ref, mo, M, b, nu, lam)) in zip(xs, infos, refs):
         assert inf["converged"] and inf["res_inf"] <= max(tols), inf
         if precision == "DF":
-            assert abs(inf["iters"] - it_ref) <= 2, (inf, it_ref)
+            # same iteration within 1 % (the dot products are summed in another order)
+            assert abs(inf["iters"] - it_ref) <= max(2, it_ref // 100), (inf, it_ref)
         assert rel_l2(host(x), x_ref) < 1e-7, (inf, it_ref)
         # residual against the oracle's operator
         r = b - O.mask(O.gatherScatter(O.hlmz(host(x), nu, lam, mo), mo), M)

@@ -20,11 +20,12 @@ def _poisson_rhs(mo, M):
     return ut, O.gatherScatter(O.mask(O.mass(f, mo), M), mo)
 
 
-@pytest.mark.parametrize("prec", ["F64", "DF"])
-def test_poisson_cfg1_jacobi(gpu, prec):
+@pytest.mark.parametrize("prec,variant", [("F64", 0), ("DF", 0), ("DF", 5)])
+def test_poisson_cfg1_jacobi(gpu, prec, variant):
     import semgb300 as S
     mo, md = meshes(9, 8, 8, (False, False), "DDDD", 0.1,
                     precision=S.SEM_F64 if prec == "F64" else S.SEM_F64_DF)
+    md.set_variant(variant)
     M = O.generateMask(["D"] * 4, mo)
     ut, b = _poisson_rhs(mo, M)
     tol = 1e-10 * np.abs(b).max()
