@@ -277,6 +277,7 @@ def run_ours(args, rank, world, local_rank):
         result["pcg"] = bench_pcg(S, msh, stream)
         result["sweep"] = bench_sweep(S, stream)
         result["batch"] = bench_batch(S)
+        result["adjoint"] = bench_adjoint(S, args.fd_directions)
     sampler.stop()
     if rank == 0 and world == 1 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -435,6 +436,104 @@ def bench_batch(S):
     return out
 
 
+def gaussian_field(x, y, seed, sigma=0.5, nk=8):
+    """Seeded smooth random field: sum over kx, ky <= nk of N(0,1) k^-2
+    cos/sin modes with random phases, normalised to standard deviation sigma."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    g = np.zeros(x.shape)
+    for kx in range(1, nk + 1):
+        for ky in range(1, nk + 1):
+            a, b = rng.standard_normal(2) / (kx * kx + ky * ky)
+            ph = rng.uniform(0, 2 * np.pi)
+            g += a * np.cos(np.pi * (kx * x + ky * y) + ph) + b * np.sin(np.pi * (kx * x - ky * y))
+    return sigma * (g - g.mean()) / g.std()
+
+
+def bench_adjoint(S, fd_directions):
+    """cfg5: steady -div(nu grad u) = 1 on 128x128 elements, N=8, Dirichlet,
+    nu = exp(g) (seed 5), J = 1/2 sum B (u - u_target)^2 (u_target seed 6);
+    gradient w.r.t. the nodal nu by the adjoint solve (autograd function over
+    sem_pcg + sem_adjoint_grad), checked by central differences (h = 1e-6,
+    continuous random directions, seed 7; native FP64 J evaluations); then 200
+    implicit-Euler steps (dt = 1e-3) forward and backward with checkpoints
+    every 20 steps."""
+    import numpy as np
+    import torch
+    msh = S.Mesh(9, 9, 128, 128, (False, False), sin_deform(0.05), bc="DDDD")
+    x = msh.x.cpu().numpy()
+    y = msh.y.cpu().numpy()
+    nu = torch.from_numpy(np.exp(gaussian_field(x, y, 5))).cuda()
+    nu = S.as_local(nu)
+    ut = S.as_local(torch.from_numpy(0.05 * gaussian_field(x, y, 6)).cuda())
+    M = S.generateMask("DDDD", msh)
+    b = S.gatherScatter(S.mask(S.mass(torch.ones_like(msh.x), msh), M), msh)
+    tol = 1e-12 * b.abs().max().item()
+    B = msh.B
+    out = {"mesh": "128x128 elements, N=8", "tol_rel": 1e-12}
+
+    def gradient():
+        nu_t = nu.clone().requires_grad_(True)
+        u = S.linsolve_varcoef(nu_t, b, msh, tol=tol)
+        J = 0.5 * torch.sum(B * (u - ut) ** 2)
+        J.backward()
+        return J.item(), nu_t.grad
+
+    gradient()  # warm
+    torch.cuda.synchronize()
+    t = time.time()
+    J0, g = gradient()
+    torch.cuda.synchronize()
+    out["gradient_s"] = time.time() - t
+    out["J"] = J0
+    # central finite differences along continuous directions
+    msh.set_precision(S.SEM_F64)
+
+    def J_of(nu_v):
+        u = S.linsolve_varcoef(nu_v, b, msh, tol=tol)
+        return 0.5 * torch.sum(B * (u - ut) ** 2).item()
+
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    errs = []
+    h = 1e-6
+    t = time.time()
+    for _ in range(fd_directions):
+        delta = msh.mult * S.gatherScatter(S.as_local(torch.randn(msh.shape, generator=gen, device="cuda",
+                                                                  dtype=torch.float64)), msh)
+        fd = (J_of(nu + h * delta) - J_of(nu - h * delta)) / (2 * h)
+        ad = torch.sum(g * delta).item()
+        errs.append(abs(fd - ad) / abs(ad))
+    out["fd"] = {"directions": fd_directions, "h": h, "max_rel_err": max(errs),
+                 "median_rel_err": float(np.median(errs)), "s": time.time() - t}
+    msh.set_precision(S.SEM_F64_DF)
+    # transient: 200 implicit-Euler steps with checkpoints every 20
+    u0 = S.mask(torch.sin(np.pi * msh.x) * torch.sin(np.pi * msh.y), M)
+    f = torch.ones_like(msh.x)
+    dt, steps, every = 1e-3, 200, 20
+    nu_t = nu.clone().requires_grad_(True)
+    # tolerance relative to the first step's right-hand side B u0 / dt + B f
+    rhs0 = S.gatherScatter(S.mask(S.mass(u0, msh), M), msh) / dt + b
+    tol_t = 1e-10 * rhs0.abs().max().item()
+    torch.cuda.synchronize()
+    t = time.time()
+    uT = S.transient_varcoef(nu_t, u0, f, msh, dt, steps, every, tol=tol_t)
+    torch.cuda.synchronize()
+    t_fwd = time.time() - t
+    J = 0.5 * torch.sum(B * (uT - ut) ** 2)
+    t = time.time()
+    J.backward()
+    torch.cuda.synchronize()
+    t_bwd = time.time() - t
+    # CG iterations of the first step's solve (each step is a cold-started CG)
+    op1 = S.HelmholtzOp(msh, 1.0, 1.0 / dt, nu_field=nu)
+    info1 = {}
+    S.pcg(rhs0, op1, opM=S.Jacobi(op1), mult=msh.mult, tol=tol_t, info=info1)
+    out["transient"] = {"steps": steps, "dt": dt, "checkpoint_every": every, "forward_s": t_fwd,
+                        "backward_s": t_bwd, "first_step_iters": info1["iters"],
+                        "grad_finite": bool(torch.isfinite(nu_t.grad).all().item())}
+    return out
+
+
 def bench_sweep(S, stream):
     """Apply GDOF/s across orders at ~4M unique DOF (double-float, L2-resident
     inputs larger than L2)."""
@@ -547,6 +646,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG and order-sweep extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--fd-directions", type=int, default=8,
+                    help="finite-difference directions of the adjoint check (the config names 32)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -185,7 +185,17 @@ typedef struct {
   int max_outer;         /* SEM_MIXED: defect-correction sweeps (6)          */
   int check_every;       /* iterations between convergence reads (0 = auto) */
   int mult_ones;         /* 1: unweighted dots, pcg's default mult=ones(size(b)) */
+  int path;              /* enum sem_pcg_path                                */
 } sem_pcg_opts;
+
+/* how sem_pcg runs the iterations (no counterpart in the reference):
+ * CHUNKED replays chunks of check_every iterations as CUDA graphs over the
+ * whole GPU; SMALL runs the whole solve in one launch of one thread-block
+ * cluster with one thread per point (meshes of at most SEM_SMALL_MAX_LOCAL
+ * local DOF, 2 <= n <= 11, scalar nu, SEM_F64_DF or SEM_MIXED); AUTO takes
+ * SMALL where it applies. */
+enum sem_pcg_path { SEM_PATH_AUTO = 0, SEM_PATH_CHUNKED = 1, SEM_PATH_SMALL = 2 };
+#define SEM_SMALL_MAX_LOCAL 100000
 
 typedef struct {
   int iters;        /* CG iterations (inner iterations summed for MIXED) */

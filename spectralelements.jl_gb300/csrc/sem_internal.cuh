@@ -230,6 +230,34 @@ struct ApplyCall {
 // number of CTAs (element tiles) of a CG-fused operator launch on grid g
 long long cg_apply_parts(const Grid& g);
 
+// Problem description of the single-launch small-mesh PCG (sem_small.cu),
+// filled by the host and read and updated by the kernel.
+struct SmallProb {
+  int n, Ex, Ey;
+  long long NX, NY;
+  const unsigned char* rinfo;  // L_* bits of the local rows and columns
+  const unsigned char* cinfo;
+  bool has_bc;
+  int jacobi;
+  int mult_ones;  // 1: unweighted dots
+  double nu, k, tol;
+  int maxiter;
+  int precision;  // SEM_F64_DF (or SEM_F64: same vectors, double-float operator) or SEM_MIXED
+  double inner_tol;
+  int max_outer;
+  const double* b;
+  double* x;
+  double *r, *p, *raw, *dinv;
+  float *r32, *p32, *raw32, *x32, *dinv32;
+  const df* Gdf;   // G11, G12, G22, B split into double-float pairs (4 blocks of NX*NY)
+  const float* Gf; // G11, G12, G22, B in FP32 (4 blocks)
+  // results
+  int iters, outer, converged, nan;
+  double res_inf, res0_inf;
+};
+
+int launch_small_pcg(SmallProb* dev, const OperatorSet& ops, int n, cudaStream_t s);  // sem_small.cu
+
 constexpr int kVariants = SEM_VARIANTS;
 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);

@@ -410,6 +410,7 @@ struct WS {
   double* part;
   df* dpart;             // per-CTA parts of p.Ap of CG-fused operator launches
   long long dpart_n;
+  SmallProb* small;      // problem record of the single-launch small-mesh solver
   Scalars* sc;
   double* dmax;
   Scalars* sc_h;  // pinned host mirror
@@ -421,7 +422,7 @@ int get_ws(sem_mesh* m, bool mixed, WS& w) {
   const size_t v64 = al(sizeof(double) * L), v32 = al(sizeof(float) * L);
   const long long np = cg_apply_parts(m->g);
   const size_t need = 6 * v64 + 5 * v32 + al(sizeof(double) * kRB * 4) + al(sizeof(df) * np) +
-                      al(sizeof(Scalars)) + al(sizeof(double));
+                      al(sizeof(SmallProb)) + al(sizeof(Scalars)) + al(sizeof(double));
   if (m->ws_bytes < need) {
     if (m->ws) cudaFree(m->ws);
     m->ws = nullptr;
@@ -445,6 +446,7 @@ int get_ws(sem_mesh* m, bool mixed, WS& w) {
   w.part = (double*)p; p += al(sizeof(double) * kRB * 4);
   w.dpart = (df*)p; p += al(sizeof(df) * np);
   w.dpart_n = np;
+  w.small = (SmallProb*)p; p += al(sizeof(SmallProb));
   w.sc = (Scalars*)p; p += al(sizeof(Scalars));
   w.dmax = (double*)p;
   static thread_local Scalars* host = nullptr;
@@ -652,9 +654,11 @@ int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r
   c.ctr = cx.ctr;
   c.skip = &w.sc->done;
   // CG-fused operator launches with the kernels that provide them (variants 2
-  // and 5; double-float arithmetic also needs the pre-split geometry)
+  // and 5; double-float arithmetic also needs the pre-split geometry).  Their
+  // unassembled p.Ap equals the mult-weighted dot only: unweighted dots
+  // (mult = ones) keep the separate passes.
   if ((c.variant == 2 || c.variant == 5) && (op_precision != SEM_F64_DF || c.Gdf) && w.dpart &&
-      cg_apply_parts(cx.g) <= w.dpart_n) {
+      cg_apply_parts(cx.g) <= w.dpart_n && !(gv.topo & M_MULT1)) {
     c.cg_r = r;
     c.cg_dinv = dinv;
     c.cg_p = p;
@@ -712,7 +716,59 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
   std::memset(&res, 0, sizeof(res));
   int outer = 0;
   double res0 = 0.0;
-  if (prec != SEM_MIXED) {
+  const bool small_ok = m && w.small && L <= SEM_SMALL_MAX_LOCAL && cx.g.n <= 11 && !o->nu_field &&
+                        (prec == SEM_F64_DF || prec == SEM_MIXED);
+  if (o->path == SEM_PATH_SMALL && !small_ok)
+    return set_error(SEM_ERR_UNSUPPORTED,
+                     "the small-mesh path serves meshes of at most %d local DOF, n <= 11, scalar nu, "
+                     "SEM_F64_DF or SEM_MIXED", SEM_SMALL_MAX_LOCAL);
+  if (small_ok && o->path != SEM_PATH_CHUNKED) {
+    // the whole solve in one cluster launch
+    SEM_CHECK(ensure_df_geometry(m, s));
+    if (prec == SEM_MIXED) SEM_CHECK(ensure_f32_geometry(m, s));
+    SmallProb sp;
+    std::memset(&sp, 0, sizeof(sp));
+    sp.n = cx.g.n;
+    sp.Ex = cx.g.Ex;
+    sp.Ey = cx.g.Ey;
+    sp.NX = cx.g.NX;
+    sp.NY = cx.g.NY;
+    sp.rinfo = cx.g.rinfo;
+    sp.cinfo = cx.g.cinfo;
+    sp.has_bc = cx.has_bc;
+    sp.jacobi = jac ? 1 : 0;
+    sp.mult_ones = o->mult_ones ? 1 : 0;
+    sp.nu = o->nu;
+    sp.k = o->k;
+    sp.tol = o->tol;
+    sp.maxiter = maxiter;
+    sp.precision = prec;
+    sp.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+    sp.max_outer = o->max_outer > 0 ? o->max_outer : 6;
+    sp.b = b;
+    sp.x = x;
+    sp.r = w.r;
+    sp.p = w.p;
+    sp.raw = w.x64tmp;
+    sp.dinv = w.dinv;
+    sp.r32 = w.r32;
+    sp.p32 = w.p32;
+    sp.raw32 = w.Ap32;
+    sp.x32 = w.x32;
+    sp.dinv32 = w.dinv32;
+    sp.Gdf = m->Gdf;
+    sp.Gf = m->G11_f;
+    SEM_CUDA(cudaMemcpyAsync(w.small, &sp, sizeof(sp), cudaMemcpyHostToDevice, s));
+    SEM_CHECK(launch_small_pcg(w.small, *cx.ops, cx.g.n, s));
+    SEM_CUDA(cudaMemcpyAsync(&sp, w.small, sizeof(sp), cudaMemcpyDeviceToHost, s));
+    SEM_CUDA(cudaStreamSynchronize(s));
+    res.k = sp.iters;
+    res.rmax = sp.res_inf;
+    res.nan = sp.nan;
+    res.converged = sp.converged;
+    outer = sp.outer;
+    res0 = sp.res0_inf;
+  } else if (prec != SEM_MIXED) {
     k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
     k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
     SEM_CUDA(cudaGetLastError());

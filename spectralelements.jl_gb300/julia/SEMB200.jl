@@ -39,7 +39,7 @@ end
 struct PcgOpts
     nu::Cdouble; nu_field::CuPtr{Cdouble}; k::Cdouble
     precond::Cint; precision::Cint; tol::Cdouble; maxiter::Cint
-    inner_tol::Cdouble; max_outer::Cint; check_every::Cint; mult_ones::Cint
+    inner_tol::Cdouble; max_outer::Cint; check_every::Cint; mult_ones::Cint; path::Cint
 end
 
 mutable struct SolveInfo
@@ -182,7 +182,7 @@ function pcg(b::CuArray{Float64,2}, opA::HelmholtzOp; opM=x -> x, mult=nothing, 
     set_bc!(opA.msh, opA.bc)
     x = similar(b)
     o = Ref(PcgOpts(opA.ν, CU_NULL, opA.k, opM isa Jacobi ? 1 : 0, precision, tol, maxiter,
-                    1e-4, 6, 0, mult === nothing ? 1 : 0))
+                    1e-4, 6, 0, mult === nothing ? 1 : 0, 0))
     info = Ref(SolveInfo())
     st = ccall((:sem_pcg, libsem), Cint,
                (Ptr{Cvoid}, Ref{PcgOpts}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ref{SolveInfo}, Ptr{Cvoid}),
@@ -246,7 +246,7 @@ function varcoef_solve(ν::CuArray{Float64,2}, b::CuArray{Float64,2}, msh::Mesh,
                        tol=1e-10)
     set_bc!(msh, bc)
     x = similar(b)
-    o = Ref(PcgOpts(1.0, pointer(ν), 0.0, 1, SEM_F64_DF, tol, 0, 1e-4, 6, 0, 0))
+    o = Ref(PcgOpts(1.0, pointer(ν), 0.0, 1, SEM_F64_DF, tol, 0, 1e-4, 6, 0, 0, 0))
     info = Ref(SolveInfo())
     check(ccall((:sem_pcg, libsem), Cint,
                 (Ptr{Cvoid}, Ref{PcgOpts}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ref{SolveInfo}, Ptr{Cvoid}),

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu"]
 
 
 class SemError(RuntimeError):
@@ -47,6 +47,8 @@ SEM_OK, SEM_ERR_BAD_ARG, SEM_ERR_NOT_CONVERGED, SEM_ERR_NAN, SEM_ERR_TIMEOUT, SE
 SEM_GS, SEM_MASK = 1, 2
 SEM_F64, SEM_F64_DF, SEM_F32, SEM_MIXED = 0, 1, 2, 3
 SEM_PRECOND_NONE, SEM_PRECOND_JACOBI = 0, 1
+SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL = 0, 1, 2
+SEM_SMALL_MAX_LOCAL = 100000  # include/sem_b200.h
 SEM_VARIANTS = 6  # fused element-operator kernel variants (include/sem_b200.h)
 FIELDS = {"x": 0, "y": 1, "Jac": 2, "Jaci": 3, "rx": 4, "ry": 5, "sx": 6, "sy": 7, "B": 8,
           "Bi": 9, "G11": 10, "G12": 11, "G22": 12, "mult": 13, "mask": 14}
@@ -101,7 +103,7 @@ class PcgOpts(ctypes.Structure):
                 ("precond", ctypes.c_int), ("precision", ctypes.c_int), ("tol", ctypes.c_double),
                 ("maxiter", ctypes.c_int), ("inner_tol", ctypes.c_double),
                 ("max_outer", ctypes.c_int), ("check_every", ctypes.c_int),
-                ("mult_ones", ctypes.c_int)]
+                ("mult_ones", ctypes.c_int), ("path", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):

@@ -82,14 +82,16 @@ def identity(x):
 
 
 def pcg(b, opA, opM=None, mult=None, ifv=False, tol=1e-8, maxiter=None, *, precision=None,
-        inner_tol=1e-4, max_outer=6, info=None, x=None):
+        inner_tol=1e-4, max_outer=6, info=None, x=None, path=0):
     """Left-preconditioned CG with mult-weighted dots (src/pcg.jl:16-60).
 
     tol is the absolute Inf-norm of the residual and maxiter defaults to
     length(b), as in the reference.  On reaching maxiter the reference's
     warning is printed and x is returned.  ``precision``: SEM_F64,
     SEM_F64_DF (default: the mesh's) or SEM_MIXED.  ``info`` (dict) receives
-    iterations, outer sweeps and residuals.
+    iterations, outer sweeps and residuals.  ``path``: SEM_PATH_AUTO (0),
+    SEM_PATH_CHUNKED (graph-replayed chunks over the GPU) or SEM_PATH_SMALL
+    (the whole solve in one cluster launch, small meshes).
     """
     if not isinstance(opA, HelmholtzOp):
         raise TypeError("pcg on the device takes an operator built by this package "
@@ -117,6 +119,7 @@ def pcg(b, opA, opM=None, mult=None, ifv=False, tol=1e-8, maxiter=None, *, preci
     o.inner_tol = float(inner_tol)
     o.max_outer = int(max_outer)
     o.check_every = 0
+    o.path = int(path)
     if mult is None:
         o.mult_ones = 1
     else:

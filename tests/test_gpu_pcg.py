@@ -74,9 +74,15 @@ def test_helmholtz_cfg2_shape_vs_c_oracle(gpu):
     assert rel_l2(xm, x_c) < 1e-7
 
 
-def test_unweighted_default_and_identity_precond(gpu):
+@pytest.mark.parametrize("path,variant", [(0, 0), (1, 0), (1, 2), (1, 5), (2, 0)])
+def test_unweighted_default_and_identity_precond(gpu, path, variant):
+    """pcg's default mult = ones (unweighted dots) and opM = identity, on every
+    solver path: the small-mesh launch, the chunked launches, and the chunked
+    launches with the CG-fused kernel variants (which must not use their
+    unassembled p.Ap for unweighted dots)."""
     import semgb300 as S
     mo, md = meshes(5, 4, 3, (False, False), "DDDD", 0.05)
+    md.set_variant(variant)
     M = O.generateMask(["D"] * 4, mo)
     ut, b = _poisson_rhs(mo, M)
     info_o = {}
@@ -84,7 +90,7 @@ def test_unweighted_default_and_identity_precond(gpu):
                 info=info_o)
     op = S.HelmholtzOp(md, 0.5, 2.0)
     info = {}
-    x = host(S.pcg(S.as_local(b), op, tol=1e-9, info=info))
+    x = host(S.pcg(S.as_local(b), op, tol=1e-9, info=info, path=path))
     assert abs(info["iters"] - info_o["iters"]) <= 2
     assert np.abs(x - x_o).max() < 1e-8
 
@@ -155,7 +161,8 @@ def test_graph_replay_matches_direct_launches(gpu, precision):
         lib.sem_timing_enable(timing)
         try:
             info = {}
-            x = host(S.pcg(bd, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info, precision=prec))
+            x = host(S.pcg(bd, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info, precision=prec,
+                           path=S.SEM_PATH_CHUNKED))
         finally:
             lib.sem_timing_enable(0)
             lib.sem_timing_read(None, None)
@@ -165,9 +172,76 @@ def test_graph_replay_matches_direct_launches(gpu, precision):
         np.testing.assert_array_equal(x, runs[0][0])
     # pcg! into a fixed buffer twice: same graph replayed
     y = md.empty()
-    S.pcg_(y, bd, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=prec)
+    S.pcg_(y, bd, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=prec, path=S.SEM_PATH_CHUNKED)
     y1 = host(y).copy()
     y.zero_()
-    S.pcg_(y, bd, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=prec)
+    S.pcg_(y, bd, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=prec, path=S.SEM_PATH_CHUNKED)
     np.testing.assert_array_equal(host(y), y1)
     np.testing.assert_array_equal(y1, runs[0][0])
+
+
+@pytest.mark.parametrize("case", [
+    (9, 8, 8, (False, False), "DDDD", 0.1, 1.0, 0.0),
+    (5, 7, 3, (True, False), "NNDD", 0.05, 0.5, 2.0),
+    (7, 3, 5, (False, True), "DDNN", 0.05, 1.0, 1.0),
+    (4, 6, 6, (True, True), "NNNN", 0.0, 1.0, 3.0),
+    (11, 4, 3, (False, False), "DNDN", 0.05, 0.2, 0.0),
+    (2, 20, 9, (False, False), "DDDD", 0.05, 1.0, 0.5),
+])
+@pytest.mark.parametrize("precision", ["DF", "MIXED"])
+def test_small_path_matches_chunked_and_oracle(gpu, case, precision):
+    """The single-launch small-mesh solver against the chunked graph path and
+    the oracle: same iterations within 1 %, solutions to the tolerance."""
+    import semgb300 as S
+    n, Ex, Ey, per, bc, amp, nu, lam = case
+    mo, md = meshes(n, Ex, Ey, per, bc, amp)
+    M = O.generateMask(list(bc), mo)
+    rng = np.random.default_rng(n + Ex)
+    b = O.mask(O.gatherScatter(mo.B * rng.standard_normal(mo.shape), mo), M)
+    tol = 1e-10 * np.abs(b).max()
+    op = S.HelmholtzOp(md, nu, lam)
+    prec = S.SEM_F64_DF if precision == "DF" else S.SEM_MIXED
+    res = {}
+    for path in (S.SEM_PATH_SMALL, S.SEM_PATH_CHUNKED):
+        info = {}
+        x = host(S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info,
+                       precision=prec, path=path))
+        assert info["converged"] and info["res_inf"] <= tol, (path, info)
+        res[path] = (x, info)
+    xs, i_s = res[S.SEM_PATH_SMALL]
+    xc, i_c = res[S.SEM_PATH_CHUNKED]
+    if precision == "DF":
+        assert abs(i_s["iters"] - i_c["iters"]) <= max(2, i_c["iters"] // 100), (i_s, i_c)
+    assert rel_l2(xs, xc) < 1e-7
+    # the oracle's residual of the small path's solution
+    r = b - O.mask(O.gatherScatter(O.hlmz(xs, nu, lam, mo), mo), M)
+    assert np.abs(r).max() <= 2 * tol
+    # repeated solves give identical results
+    x2 = host(S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=prec,
+                    path=S.SEM_PATH_SMALL))
+    np.testing.assert_array_equal(x2, xs)
+
+
+def test_small_path_options_and_limits(gpu):
+    import semgb300 as S
+    mo, md = meshes(9, 8, 8, (False, False), "DDDD", 0.1)
+    M = O.generateMask(["D"] * 4, mo)
+    _, b = _poisson_rhs(mo, M)
+    op = S.HelmholtzOp(md, 1.0, 0.0)
+    # unweighted dots, no preconditioner, maxiter reached
+    info_o = {}
+    x_o = O.pcg(b, lambda v: O.mask(O.gatherScatter(O.lapl(v, mo), mo), M), tol=1e-30, maxiter=9,
+                info=info_o)
+    info = {}
+    x = host(S.pcg(S.as_local(b), op, tol=1e-30, maxiter=9, info=info, path=S.SEM_PATH_SMALL))
+    assert info["iters"] == 9 and not info["converged"]
+    assert rel_l2(x, x_o) < 1e-12
+    # a nu field is not served by the small path
+    with pytest.raises(S.SemError):
+        opn = S.HelmholtzOp(md, 1.0, 0.0, nu_field=S.as_local(np.ones(mo.shape)))
+        S.pcg(S.as_local(b), opn, opM=S.Jacobi(opn), mult=md.mult, path=S.SEM_PATH_SMALL)
+    # nor a mesh above the size limit
+    _, big = meshes(9, 40, 40)
+    with pytest.raises(S.SemError):
+        opb = S.HelmholtzOp(big, 1.0, 0.0)
+        S.pcg(S.as_local(np.zeros(big.shape)), opb, mult=big.mult, path=S.SEM_PATH_SMALL)

@@ -26,7 +26,7 @@ def _opts(S, tol, precond, precision):
     o = S._lib.PcgOpts()
     o.nu, o.nu_field, o.k = 1.0, None, 0.0
     o.precond, o.precision, o.tol, o.maxiter = precond, precision, tol, 0
-    o.inner_tol, o.max_outer, o.check_every, o.mult_ones = 1e-4, 6, 0, 0
+    o.inner_tol, o.max_outer, o.check_every, o.mult_ones, o.path = 1e-4, 6, 0, 0, 0
     return o
 
 
@@ -41,11 +41,11 @@ def test_noalloc_solve_matches_pcg_on_two_calls(gpu, precision):
     b = S.as_local(O.gatherScatter(O.mask(O.mass(f, mo), M), mo))
     tol = 1e-10 * b.abs().max().item()
 
-    # the existing entry point on a mesh handle
+    # the existing entry point on a mesh handle, on the same (chunked) path
     op = S.HelmholtzOp(md, 1.0, 0.0)
     ref_info = {}
     x_ref = host(S.pcg(b, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=prec,
-                       info=ref_info))
+                       info=ref_info, path=S.SEM_PATH_CHUNKED))
 
     # the allocation-free entry point on caller-owned geometry
     G11, G12, G22, B = (S.as_local(getattr(mo, k)) for k in ("G11", "G12", "G22", "B"))
