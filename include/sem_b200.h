@@ -55,7 +55,12 @@ enum sem_precision {
   SEM_F64 = 0,    /* native FP64 arithmetic                                  */
   SEM_F64_DF = 1, /* FP64 in/out, double-float (FP32 pair) arithmetic, ~47 bit */
   SEM_F32 = 2,    /* FP32 geometry copy and FP32 arithmetic (solver inner loop) */
-  SEM_MIXED = 3   /* solver only: FP32 inner CG inside FP64 defect correction */
+  SEM_MIXED = 3,  /* solver only: FP32 inner CG inside FP64 defect correction */
+  SEM_MIXED_RR = 4 /* solver only: one FP32 CG whose residual is replaced by the
+                      FP64 residual b - A x (x kept in FP64) whenever it has
+                      fallen by the factor inner_tol (default 0.3) since the
+                      last replacement; the search direction is kept, so the
+                      iteration count stays near that of the FP64 CG */
 };
 
 /* geometry fields that sem_mesh_field can export */
@@ -181,8 +186,8 @@ typedef struct {
   int precision;         /* SEM_F64, SEM_F64_DF or SEM_MIXED                 */
   double tol;            /* absolute Inf-norm tolerance on the residual      */
   int maxiter;           /* <= 0: length(b), as the reference               */
-  double inner_tol;      /* SEM_MIXED: relative inner tolerance (1e-4)      */
-  int max_outer;         /* SEM_MIXED: defect-correction sweeps (6)          */
+  double inner_tol;      /* SEM_MIXED: relative inner tolerance (1e-4); SEM_MIXED_RR: residual drop between replacements (0.3) */
+  int max_outer;         /* SEM_MIXED: defect-correction sweeps (6); SEM_MIXED_RR: replacements (100) */
   int check_every;       /* iterations between convergence reads (0 = auto) */
   int mult_ones;         /* 1: unweighted dots, pcg's default mult=ones(size(b)) */
   int path;              /* enum sem_pcg_path                                */
@@ -192,7 +197,7 @@ typedef struct {
  * CHUNKED replays chunks of check_every iterations as CUDA graphs over the
  * whole GPU; SMALL runs the whole solve in one launch of one thread-block
  * cluster with one thread per point (meshes of at most SEM_SMALL_MAX_LOCAL
- * local DOF, 2 <= n <= 11, scalar nu, SEM_F64_DF or SEM_MIXED); AUTO takes
+ * local DOF, 2 <= n <= 11, scalar nu, SEM_F64_DF, SEM_MIXED or SEM_MIXED_RR); AUTO takes
  * SMALL where it applies. */
 enum sem_pcg_path { SEM_PATH_AUTO = 0, SEM_PATH_CHUNKED = 1, SEM_PATH_SMALL = 2 };
 #define SEM_SMALL_MAX_LOCAL 100000

@@ -192,8 +192,8 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
                   const int* maxiter, int precision, double inner_tol, int max_outer,
                   sem_solve_info* info, sem_stream_t stream) {
   if (!b || !rhs || !x || !tol) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
-  if (precision != SEM_F64_DF && precision != SEM_MIXED)
-    return set_error(SEM_ERR_BAD_ARG, "the batch kernels take SEM_F64_DF or SEM_MIXED");
+  if (precision != SEM_F64_DF && precision != SEM_MIXED && precision != SEM_MIXED_RR)
+    return set_error(SEM_ERR_BAD_ARG, "the batch kernels take SEM_F64_DF, SEM_MIXED or SEM_MIXED_RR");
   cudaStream_t s = (cudaStream_t)stream;
   std::vector<BProb> q(b->count);
   for (int j = 0; j < b->count; ++j) {
@@ -223,8 +223,9 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     c.queue = b->queues + gi;
     c.precision = precision;
     c.jacobi = b->jacobi;
-    c.inner_tol = inner_tol > 0 ? inner_tol : 1e-4;
-    c.max_outer = max_outer > 0 ? max_outer : 6;
+    const bool rr = precision == SEM_MIXED_RR;
+    c.inner_tol = inner_tol > 0 ? inner_tol : (rr ? 0.3 : 1e-4);
+    c.max_outer = max_outer > 0 ? max_outer : (rr ? 100 : 6);
     c.clusters = b->groups.size() == 1 ? 0 : std::max(1, (int)(budget * g.work / wtot + 0.5));
     SEM_CUDA(cudaStreamWaitEvent(g.stream, b->start, 0));
     SEM_CHECK(launch_group(g.n, c, *g.ops, g.stream));

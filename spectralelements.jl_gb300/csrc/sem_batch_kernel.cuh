@@ -527,12 +527,121 @@ __device__ double bresidual(const BatchArgs<N>& a, BProb& pr, cg::cluster_group&
   return bits_to_double(m1[0]);
 }
 
+// SEM_MIXED_RR: one FP32 CG whose residual is replaced by the FP64 b - A x
+// (x += x32 first) whenever it has fallen by the factor inner_tol since the
+// last replacement; p32 and the beta recurrence continue across replacements
+template <int N>
+__device__ void brr(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int rank, BRed& red, int& rc,
+                    const BBuf<N>& buf) {
+  typedef BTile<N> T;
+  const bool jac = a.jacobi != 0;
+  const float* dinv32 = jac ? pr.dinv32 : nullptr;
+  const long long L = pr.NX * pr.NY;
+  const int ntx = (pr.Ex + T::TX - 1) / T::TX, nty = (pr.Ey + T::TY - 1) / T::TY;
+  // x = 0, r = b (FP64)
+  BAcc<double> a0;
+  own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float) {
+    pr.x[i] = 0.0;
+    pr.r[i] = pr.b[i];
+    a0.amax(pr.b[i]);
+  });
+  df z[1] = {{0.0f, 0.0f}};
+  unsigned long long m0[1] = {a0.max_bits()};
+  cluster_reduce<1, 1>(cl, red, rc, z, m0);
+  double rmax64 = bits_to_double(m0[0]);
+  const double res0 = rmax64;
+  // r32 = (float) r, x32 = 0 (p32 = 0 the first time); returns t = r32.h.mult
+  auto load_r32 = [&](bool zero_p) -> double {
+    BAcc<float> acc;
+    own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float m) {
+      const float ri = (float)pr.r[i];
+      pr.r32[i] = ri;
+      pr.x32[i] = 0.0f;
+      if (zero_p) pr.p32[i] = 0.0f;
+      if (jac)
+        acc.rhr(ri, dinv32[i], m);
+      else
+        acc.prod(ri, ri, m);
+    });
+    df s1[1] = {acc.sum()};
+    unsigned long long none[1] = {0ull};
+    cluster_reduce<1, 1>(cl, red, rc, s1, none);
+    return df2d(s1[0]);
+  };
+  double t = load_r32(true);
+  double tprev = 1.0;
+  double thresh = a.inner_tol * rmax64;
+  int k = 0, outer = 0;
+  bool nan = rmax64 != rmax64;
+  bool done = !(rmax64 > pr.tol) || pr.maxiter == 0 || nan;
+  while (!done) {
+    const float beta = k == 0 ? 0.0f : (float)(t / tprev);
+    BAcc<float> dot;
+    for (int tile = rank; tile < ntx * nty; tile += kCluster) {
+      const int by = tile / ntx, bx = tile - by * ntx;
+      btile<PF32, N, T::TX, T::TY>(pr, a.cf, bx, by, nullptr, pr.r32, dinv32, beta, pr.p32, true, pr.Ap32,
+                                   pr.G11f, L, buf.template s0<PF32>(), buf.template s1<PF32>(),
+                                   buf.template x0<PF32>(), dot);
+    }
+    cl.sync();
+    bfixup<float, T::TX, T::TY>(pr, N, pr.Ap32, pr.p32, rank, dot);
+    df s2[1] = {dot.sum()};
+    unsigned long long none[1] = {0ull};
+    cluster_reduce<1, 1>(cl, red, rc, s2, none);
+    const double alpha = t / df2d(s2[0]);
+    const float af = (float)alpha;
+    ++k;
+    BAcc<float> up;
+    own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float m) {
+      pr.x32[i] = pr.x32[i] + af * pr.p32[i];
+      const float ri = pr.r32[i] - af * pr.Ap32[i];
+      pr.r32[i] = ri;
+      if (jac)
+        up.rhr(ri, dinv32[i], m);
+      else
+        up.prod(ri, ri, m);
+      up.amax(ri);
+    });
+    df s3[1] = {up.sum()};
+    unsigned long long m3[1] = {up.max_bits()};
+    cluster_reduce<1, 1>(cl, red, rc, s3, m3);
+    tprev = t;
+    t = df2d(s3[0]);
+    const double rmax32 = bits_to_double(m3[0]);
+    const bool nan32 = (rmax32 != rmax32) || (alpha != alpha);
+    if (!(rmax32 > thresh) || k >= pr.maxiter || nan32) {
+      own_points<N, T::TX, T::TY>(pr, rank, [&](long long i, float) { pr.x[i] += (double)pr.x32[i]; });
+      cl.sync();
+      rmax64 = bresidual<N>(a, pr, cl, rank, red, rc, buf);
+      ++outer;
+      nan = rmax64 != rmax64 || nan32;
+      done = !(rmax64 > pr.tol) || k >= pr.maxiter || nan || outer >= a.max_outer;
+      if (!done) {
+        t = load_r32(false);
+        thresh = a.inner_tol * rmax64;
+      }
+    }
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    pr.iters = k;
+    pr.outer = outer;
+    pr.res_inf = rmax64;
+    pr.res0_inf = res0;
+    pr.nan = nan;
+    pr.converged = !(rmax64 > pr.tol) && !nan;
+  }
+}
+
 template <int N>
 __device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int rank, BRed& red,
                        int& rc, const BBuf<N>& buf) {
   typedef BTile<N> T;
   const bool jac = a.jacobi != 0;
   const int maxiter = pr.maxiter;
+  if (a.precision == SEM_MIXED_RR) {
+    brr<N>(a, pr, cl, rank, red, rc, buf);
+    return;
+  }
   if (a.precision != SEM_MIXED) {
     int it = 0;
     double rmax = 0.0;

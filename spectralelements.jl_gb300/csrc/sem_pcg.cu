@@ -17,6 +17,8 @@
 // mult = 1/(copies) is computed from the local index (1, 1/2 or 1/4).
 // Mixed precision (SEM_MIXED): FP64 defect correction x += A32^{-1} r with
 // r = b - A x recomputed in FP64 after every inner FP32 CG solve.
+// SEM_MIXED_RR: one FP32 CG with residual replacement, r32 <- (float)(b - A x)
+// in FP64 whenever r32 has fallen by inner_tol, keeping the search direction.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -152,6 +154,7 @@ struct Acc<float> {
 
 // p = h + beta p_old with h = r .* dinv
 // x = 0, r = b (converted), p = 0; partials of t = r.h.mult and max|r|
+// (p == NULL: p is kept, the residual replacement of SEM_MIXED_RR)
 template <class T, class TB>
 __global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
                        T* __restrict__ p, const T* __restrict__ dinv, double* part, Grid g) {
@@ -159,7 +162,7 @@ __global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restric
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     const T ri = (T)b[i];
     x[i] = (T)0;
-    p[i] = (T)0;
+    if (p) p[i] = (T)0;
     r[i] = ri;
     if (dinv)
       acc.rhr(ri, dinv[i], mult_at(rr, cc, g));
@@ -188,6 +191,23 @@ __global__ void k_scal_init(const double* part, int np, Scalars* sc, double tol,
     sc->nan = res[1] != res[1];
     sc->converged = !(res[1] > tol) && !sc->nan;
     sc->done = !(res[1] > tol) || maxiter == 0;
+  }
+}
+
+// after a residual replacement: t from the replaced residual, beta with the
+// previous t (the recurrence continues), a new tolerance; k and maxiter stay
+__global__ void k_scal_replace(const double* part, int np, Scalars* sc, double tol) {
+  double res[2];
+  const bool mx[2] = {false, true};
+  final_reduce<2>(part, np, mx, res);
+  if (threadIdx.x == 0) {
+    sc->t = res[0];
+    sc->beta = sc->k > 0 ? res[0] / sc->t_prev : 0.0;
+    sc->rmax = res[1];
+    sc->tol = tol;
+    sc->nan = res[1] != res[1];
+    sc->converged = !(res[1] > tol) && !sc->nan;
+    sc->done = !(res[1] > tol) || sc->k >= sc->maxiter || sc->nan;
   }
 }
 
@@ -687,8 +707,8 @@ int pcg_check(const sem_pcg_opts* o, const double* b, double* x) {
   if (o->precond != SEM_PRECOND_NONE && o->precond != SEM_PRECOND_JACOBI)
     return set_error(SEM_ERR_BAD_ARG, "unknown preconditioner %d", o->precond);
   const int prec = o->precision;
-  if (prec != SEM_F64 && prec != SEM_F64_DF && prec != SEM_MIXED)
-    return set_error(SEM_ERR_BAD_ARG, "precision must be SEM_F64, SEM_F64_DF or SEM_MIXED");
+  if (prec != SEM_F64 && prec != SEM_F64_DF && prec != SEM_MIXED && prec != SEM_MIXED_RR)
+    return set_error(SEM_ERR_BAD_ARG, "precision must be SEM_F64, SEM_F64_DF, SEM_MIXED or SEM_MIXED_RR");
   return SEM_OK;
 }
 
@@ -708,7 +728,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
   if (jac) {
     SEM_CHECK(diag_build(cx, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
     k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, cx.g);
-    if (prec == SEM_MIXED)
+    if (prec == SEM_MIXED || prec == SEM_MIXED_RR)
       k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, cx.g);
     SEM_CUDA(cudaGetLastError());
   }
@@ -717,15 +737,15 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
   int outer = 0;
   double res0 = 0.0;
   const bool small_ok = m && w.small && L <= SEM_SMALL_MAX_LOCAL && cx.g.n <= 11 && !o->nu_field &&
-                        (prec == SEM_F64_DF || prec == SEM_MIXED);
+                        (prec == SEM_F64_DF || prec == SEM_MIXED || prec == SEM_MIXED_RR);
   if (o->path == SEM_PATH_SMALL && !small_ok)
     return set_error(SEM_ERR_UNSUPPORTED,
                      "the small-mesh path serves meshes of at most %d local DOF, n <= 11, scalar nu, "
-                     "SEM_F64_DF or SEM_MIXED", SEM_SMALL_MAX_LOCAL);
+                     "SEM_F64_DF, SEM_MIXED or SEM_MIXED_RR", SEM_SMALL_MAX_LOCAL);
   if (small_ok && o->path != SEM_PATH_CHUNKED) {
     // the whole solve in one cluster launch
     SEM_CHECK(ensure_df_geometry(m, s));
-    if (prec == SEM_MIXED) SEM_CHECK(ensure_f32_geometry(m, s));
+    if (prec != SEM_F64_DF) SEM_CHECK(ensure_f32_geometry(m, s));
     SmallProb sp;
     std::memset(&sp, 0, sizeof(sp));
     sp.n = cx.g.n;
@@ -743,8 +763,9 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     sp.tol = o->tol;
     sp.maxiter = maxiter;
     sp.precision = prec;
-    sp.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
-    sp.max_outer = o->max_outer > 0 ? o->max_outer : 6;
+    const bool rr = prec == SEM_MIXED_RR;
+    sp.inner_tol = o->inner_tol > 0 ? o->inner_tol : (rr ? 0.3 : 1e-4);
+    sp.max_outer = o->max_outer > 0 ? o->max_outer : (rr ? 100 : 6);
     sp.b = b;
     sp.x = x;
     sp.r = w.r;
@@ -768,7 +789,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     res.converged = sp.converged;
     outer = sp.outer;
     res0 = sp.res0_inf;
-  } else if (prec != SEM_MIXED) {
+  } else if (prec != SEM_MIXED && prec != SEM_MIXED_RR) {
     k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
     k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
     SEM_CUDA(cudaGetLastError());
@@ -780,12 +801,16 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       SEM_CHECK(run_cg<double>(m, cx, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
                                o->nu, o->k, check_every, &res, s));
   } else {
-    if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED does not take a nu field");
-    if (!m) return set_error(SEM_ERR_UNSUPPORTED, "SEM_MIXED needs a mesh handle");
+    if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "mixed precision does not take a nu field");
+    if (!m) return set_error(SEM_ERR_UNSUPPORTED, "mixed precision needs a mesh handle");
     SEM_CHECK(ensure_f32_geometry(m, s));
     cx = ctx_of(m);
-    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
-    const int max_outer = o->max_outer > 0 ? o->max_outer : 6;
+    const bool rr = prec == SEM_MIXED_RR;
+    // SEM_MIXED_RR replaces the FP32 residual after every 0.3-fold drop: rarer
+    // replacements let the FP32 recurrence drift (cfg2: 0.3 -> 7,504 iterations,
+    // 0.1 -> 10,365, 0.03 -> 29,513; the FP64 CG takes 6,974)
+    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : (rr ? 0.3 : 1e-4);
+    const int max_outer = o->max_outer > 0 ? o->max_outer : (rr ? 100 : 6);
     // x = 0, r = b
     k_zero<<<nb, kRT, 0, s>>>(x, L);
     k_residual<<<nb, kRT, 0, s>>>(b, x, w.r, w.part, L);  // r = b - 0
@@ -811,7 +836,35 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     c.Gdf = cx.Gdf;
     c.ctr = cx.ctr;
     bool nan = rmax != rmax;
-    while (!(rmax <= o->tol) && !nan && outer < max_outer) {
+    if (rr && !(rmax <= o->tol) && !nan) {
+      // one FP32 CG; its residual is replaced by the FP64 b - A x whenever it
+      // has fallen by inner_tol since the last replacement
+      k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, w.p32, jac ? w.dinv32 : nullptr, w.part, gv);
+      k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
+      SEM_CUDA(cudaGetLastError());
+      for (;;) {
+        Scalars ir;
+        SEM_CHECK(run_cg<float>(m, cx, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
+                                nullptr, o->nu, o->k, check_every, &ir, s));
+        total_it = ir.k;
+        k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
+        SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
+        k_residual<<<nb, kRT, 0, s>>>(b, w.Ap, w.r, w.part, L);
+        k_scal_max<<<1, kRT, 0, s>>>(w.part, (int)nb, w.dmax);
+        SEM_CUDA(cudaGetLastError());
+        SEM_CUDA(cudaMemcpyAsync(&w.sc_h[1], w.dmax, sizeof(double), cudaMemcpyDeviceToHost, s));
+        SEM_CUDA(cudaStreamSynchronize(s));
+        rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
+        nan = rmax != rmax || ir.nan;
+        ++outer;
+        if (rmax <= o->tol || nan || ir.k >= maxiter || outer >= max_outer) break;
+        // replace: r32 = r (FP64 residual), x32 = 0, p32 kept
+        k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, nullptr, jac ? w.dinv32 : nullptr, w.part, gv);
+        k_scal_replace<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax);
+        SEM_CUDA(cudaGetLastError());
+      }
+    }
+    while (!rr && !(rmax <= o->tol) && !nan && outer < max_outer) {
       ++outer;
       // inner FP32 CG on A d = r to inner_tol * |r|_inf
       k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, w.p32, jac ? w.dinv32 : nullptr, w.part, gv);
@@ -921,7 +974,7 @@ int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
   if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
   SEM_CHECK(pcg_check(o, b, x));
   WS w;
-  SEM_CHECK(get_ws(m, o->precision == SEM_MIXED, w));
+  SEM_CHECK(get_ws(m, o->precision == SEM_MIXED || o->precision == SEM_MIXED_RR, w));
   return pcg_core(ctx_of(m), w, m, o, b, x, info, (cudaStream_t)stream);
 }
 
@@ -1005,7 +1058,7 @@ extern "C" int sem_pcg_noalloc(int nr, int Ex, int Ey, int periodic_x, int perio
   if (bc)
     for (int i = 0; i < 4; ++i)
       if (bc[i] != 'D' && bc[i] != 'N') return set_error(SEM_ERR_BAD_ARG, "bc must be 4 chars of 'D'/'N'");
-  if (o->precision == SEM_MIXED)
+  if (o->precision == SEM_MIXED || o->precision == SEM_MIXED_RR)
     return set_error(SEM_ERR_UNSUPPORTED, "the allocation-free solve serves SEM_F64 and SEM_F64_DF");
   const long long NX = (long long)nr * Ex, NY = (long long)nr * Ey;
   if (NX * NY > kNoAllocMaxLocal)

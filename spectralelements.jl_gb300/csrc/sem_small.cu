@@ -18,7 +18,8 @@
 //     reduced over the cluster in distributed shared memory in rank order, so
 //     every CTA takes the same decisions;
 //   * SEM_MIXED runs the FP32 inner CG and the FP64 defect correction of the
-//     mixed-precision solver inside the same launch.
+//     mixed-precision solver inside the same launch, SEM_MIXED_RR its FP32 CG
+//     with FP64 residual replacement.
 //
 // Reference: pcg (src/pcg.jl:16-60), laplace (src/lapl.jl:70-81), hlmz
 // (src/hlmz.jl:12-19), gatherScatter (src/gatherScatter.jl:8-16), mask
@@ -308,6 +309,126 @@ __device__ void small_cg(SmallProb& pr, cg::cluster_group& cl, SmallRed& red, in
   nan_out = nan;
 }
 
+// SEM_MIXED_RR: one FP32 CG (x32, r32, p32) whose residual is replaced by the
+// FP64 residual b - A x (x += x32 first, x in FP64) whenever it has fallen by
+// the factor inner_tol since the last replacement; p32 and the beta
+// recurrence continue across replacements.
+template <int N>
+__device__ void small_rr(SmallProb& pr, cg::cluster_group& cl, SmallRed& red, int& rc, int e0, int e1,
+                         const df (*Ddr)[N], const df (*Dds)[N], const float (*Dfr)[N],
+                         const float (*Dfs)[N], df* Ubuf, df* Wbuf) {
+  const bool jac = pr.jacobi != 0;
+  float* U32 = reinterpret_cast<float*>(Ubuf);
+  float* W32 = reinterpret_cast<float*>(Wbuf);
+  const float* dinv32 = jac ? pr.dinv32 : nullptr;
+  // x = 0, r = b (FP64)
+  unsigned long long mx = 0ull;
+  df z = {0.0f, 0.0f};
+  small_points<N>(pr, e0, e1, [&](long long gi, long long, long long) {
+    pr.x[gi] = 0.0;
+    pr.r[gi] = pr.b[gi];
+    const unsigned long long b = abs_bits(pr.b[gi]);
+    mx = b > mx ? b : mx;
+  });
+  small_reduce(cl, red, rc, z, mx);
+  double rmax64 = __longlong_as_double((long long)mx);
+  const double res0 = rmax64;
+  // r32 = (float) r, x32 = 0 (p32 = 0 the first time); t = r32 . dinv r32 . mult
+  auto load_r32 = [&](bool zero_p) -> double {
+    df sacc = {0.0f, 0.0f};
+    unsigned long long none = 0ull;
+    small_points<N>(pr, e0, e1, [&](long long gi, long long rr, long long cc) {
+      const float ri = (float)pr.r[gi];
+      pr.r32[gi] = ri;
+      pr.x32[gi] = 0.0f;
+      if (zero_p) pr.p32[gi] = 0.0f;
+      sacc = df_add_u(sacc, sq_term(ri, jac ? dinv32[gi] : 1.0f, small_mult(pr, rr, cc)));
+    });
+    sacc = df_norm(sacc);
+    small_reduce(cl, red, rc, sacc, none);
+    return df2d(sacc);
+  };
+  double t = load_r32(true);
+  double tprev = 1.0;
+  double thresh = pr.inner_tol * rmax64;
+  int k = 0, outer = 0;
+  bool nan = rmax64 != rmax64;
+  bool done = !(rmax64 > pr.tol) || pr.maxiter == 0 || nan;
+  while (!done) {
+    const float beta = k == 0 ? 0.0f : (float)(t / tprev);
+    df dot = {0.0f, 0.0f};
+    small_apply<PF32, N>(pr, e0, e1, Dfr, Dfs, U32, W32, nullptr, true, pr.r32, dinv32, beta, pr.p32, pr.Gf,
+                         pr.raw32, dot);
+    unsigned long long none = 0ull;
+    dot = df_norm(dot);
+    small_reduce(cl, red, rc, dot, none);
+    double pap = df2d(dot);
+    if (pr.mult_ones) {
+      df d2 = {0.0f, 0.0f};
+      small_points<N>(pr, e0, e1, [&](long long gi, long long rr, long long cc) {
+        d2 = df_add_u(d2, dot_term(pr.p32[gi], small_gather(pr, pr.raw32, rr, cc)));
+      });
+      d2 = df_norm(d2);
+      small_reduce(cl, red, rc, d2, none);
+      pap = df2d(d2);
+    }
+    const double alpha = t / pap;
+    const float af = (float)alpha;
+    ++k;
+    df s2 = {0.0f, 0.0f};
+    unsigned long long m2 = 0ull;
+    small_points<N>(pr, e0, e1, [&](long long gi, long long rr, long long cc) {
+      const float ap = small_gather(pr, pr.raw32, rr, cc);
+      pr.x32[gi] = pr.x32[gi] + af * pr.p32[gi];
+      const float ri = pr.r32[gi] - af * ap;
+      pr.r32[gi] = ri;
+      s2 = df_add_u(s2, sq_term(ri, jac ? dinv32[gi] : 1.0f, small_mult(pr, rr, cc)));
+      const unsigned long long b = abs_bits(ri);
+      m2 = b > m2 ? b : m2;
+    });
+    s2 = df_norm(s2);
+    small_reduce(cl, red, rc, s2, m2);
+    tprev = t;
+    t = df2d(s2);
+    const double rmax32 = __longlong_as_double((long long)m2);
+    const bool nan32 = (rmax32 != rmax32) || (alpha != alpha);
+    if (!(rmax32 > thresh) || k >= pr.maxiter || nan32) {
+      // replacement: x += x32, r = b - A x in FP64
+      small_points<N>(pr, e0, e1, [&](long long gi, long long, long long) { pr.x[gi] += (double)pr.x32[gi]; });
+      __syncthreads();
+      df unused = {0.0f, 0.0f};
+      small_apply<PDF, N>(pr, e0, e1, Ddr, Dds, Ubuf, Wbuf, pr.x, false, nullptr, nullptr, 0.0, nullptr,
+                          pr.Gdf, pr.raw, unused);
+      cl.sync();
+      unsigned long long m3 = 0ull;
+      small_points<N>(pr, e0, e1, [&](long long gi, long long rr, long long cc) {
+        const double v = pr.b[gi] - small_gather(pr, pr.raw, rr, cc);
+        pr.r[gi] = v;
+        const unsigned long long b = abs_bits(v);
+        m3 = b > m3 ? b : m3;
+      });
+      df z3 = {0.0f, 0.0f};
+      small_reduce(cl, red, rc, z3, m3);
+      rmax64 = __longlong_as_double((long long)m3);
+      ++outer;
+      nan = rmax64 != rmax64 || nan32;
+      done = !(rmax64 > pr.tol) || k >= pr.maxiter || nan || outer >= pr.max_outer;
+      if (!done) {
+        t = load_r32(false);
+        thresh = pr.inner_tol * rmax64;
+      }
+    }
+  }
+  if (cl.block_rank() == 0 && threadIdx.x == 0) {
+    pr.iters = k;
+    pr.outer = outer;
+    pr.res_inf = rmax64;
+    pr.res0_inf = res0;
+    pr.nan = nan;
+    pr.converged = !(rmax64 > pr.tol) && !nan;
+  }
+}
+
 template <int N>
 __global__ void __launch_bounds__(kSmallThreads, 1) k_small_pcg(const __grid_constant__ SmallArgs<N> a) {
   cg::cluster_group cl = cg::this_cluster();
@@ -328,6 +449,11 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_small_pcg(const __grid_con
   int e0, e1;
   small_range(pr, rank, nr, e0, e1);
   const bool jac = pr.jacobi != 0;
+  if (pr.precision == SEM_MIXED_RR) {
+    small_rr<N>(pr, cl, red, rc, e0, e1, Ddf[0], Ddf[1], Df[0], Df[1], Ubuf, Wbuf);
+    cl.sync();  // no CTA exits while another may still read its shared memory
+    return;
+  }
   if (pr.precision != SEM_MIXED) {
     int it = 0;
     double rmax = 0.0;

@@ -26,6 +26,10 @@ const SEM_MASK = Cuint(2)
 const SEM_F64 = Cint(0)
 const SEM_F64_DF = Cint(1)
 const SEM_MIXED = Cint(3)
+const SEM_MIXED_RR = Cint(4)
+const SEM_PATH_AUTO = Cint(0)
+const SEM_PATH_CHUNKED = Cint(1)
+const SEM_PATH_SMALL = Cint(2)
 
 struct MeshDesc
     nr::Cint; ns::Cint; Ex::Cint; Ey::Cint

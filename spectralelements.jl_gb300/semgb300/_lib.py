@@ -45,7 +45,7 @@ class NotConverged(SemError):
 SEM_OK, SEM_ERR_BAD_ARG, SEM_ERR_NOT_CONVERGED, SEM_ERR_NAN, SEM_ERR_TIMEOUT, SEM_ERR_CUDA, \
     SEM_ERR_UNSUPPORTED, SEM_ERR_NO_MEMORY = range(8)
 SEM_GS, SEM_MASK = 1, 2
-SEM_F64, SEM_F64_DF, SEM_F32, SEM_MIXED = 0, 1, 2, 3
+SEM_F64, SEM_F64_DF, SEM_F32, SEM_MIXED, SEM_MIXED_RR = 0, 1, 2, 3, 4
 SEM_PRECOND_NONE, SEM_PRECOND_JACOBI = 0, 1
 SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL = 0, 1, 2
 SEM_SMALL_MAX_LOCAL = 100000  # include/sem_b200.h

@@ -82,13 +82,13 @@ def identity(x):
 
 
 def pcg(b, opA, opM=None, mult=None, ifv=False, tol=1e-8, maxiter=None, *, precision=None,
-        inner_tol=1e-4, max_outer=6, info=None, x=None, path=0):
+        inner_tol=None, max_outer=None, info=None, x=None, path=0):
     """Left-preconditioned CG with mult-weighted dots (src/pcg.jl:16-60).
 
     tol is the absolute Inf-norm of the residual and maxiter defaults to
     length(b), as in the reference.  On reaching maxiter the reference's
     warning is printed and x is returned.  ``precision``: SEM_F64,
-    SEM_F64_DF (default: the mesh's) or SEM_MIXED.  ``info`` (dict) receives
+    SEM_F64_DF (default: the mesh's), SEM_MIXED or SEM_MIXED_RR.  ``info`` (dict) receives
     iterations, outer sweeps and residuals.  ``path``: SEM_PATH_AUTO (0),
     SEM_PATH_CHUNKED (graph-replayed chunks over the GPU) or SEM_PATH_SMALL
     (the whole solve in one cluster launch, small meshes).
@@ -116,8 +116,10 @@ def pcg(b, opA, opM=None, mult=None, ifv=False, tol=1e-8, maxiter=None, *, preci
     o.precision = int(prec)
     o.tol = float(tol)
     o.maxiter = 0 if maxiter is None else int(maxiter)
-    o.inner_tol = float(inner_tol)
-    o.max_outer = int(max_outer)
+    # None: the library's default for the precision (SEM_MIXED: 1e-4 and 6
+    # sweeps; SEM_MIXED_RR: 0.3 and 100 replacements)
+    o.inner_tol = 0.0 if inner_tol is None else float(inner_tol)
+    o.max_outer = 0 if max_outer is None else int(max_outer)
     o.check_every = 0
     o.path = int(path)
     if mult is None:
@@ -171,11 +173,13 @@ class BatchSolver:
         except Exception:
             pass
 
-    def solve(self, bs, tols, precision=_lib.SEM_F64_DF, maxiter=None, xs=None, inner_tol=1e-4,
-              max_outer=6, infos=None):
+    def solve(self, bs, tols, precision=_lib.SEM_F64_DF, maxiter=None, xs=None, inner_tol=None,
+              max_outer=None, infos=None):
         """Solve every problem; returns the list of solutions.  ``infos`` (a list)
         receives one dict per problem.  Raises NotConverged (after filling
-        ``infos``) if any problem reached maxiter."""
+        ``infos``) if any problem reached maxiter.  ``precision``: SEM_F64_DF,
+        SEM_MIXED or SEM_MIXED_RR (inner_tol/max_outer None: the library's
+        defaults for the precision)."""
         n = len(self.meshes)
         bs = [as_local(b) for b in bs]
         if xs is None:
@@ -185,8 +189,9 @@ class BatchSolver:
         T = (ctypes.c_double * n)(*[float(t) for t in tols])
         M = None if maxiter is None else (ctypes.c_int * n)(*[int(v) for v in maxiter])
         info = (_lib.SolveInfo * n)()
-        st = self._lib.sem_batch_pcg(self._h, B, X, T, M, int(precision), float(inner_tol),
-                                     int(max_outer), info, stream_ptr())
+        st = self._lib.sem_batch_pcg(self._h, B, X, T, M, int(precision),
+                                     0.0 if inner_tol is None else float(inner_tol),
+                                     0 if max_outer is None else int(max_outer), info, stream_ptr())
         if infos is not None:
             infos[:] = [dict(iters=i.iters, outer=i.outer, res_inf=i.res_inf, converged=bool(i.converged))
                         for i in info]

@@ -27,7 +27,7 @@ def _rhs(mo, M):
     return O.gatherScatter(O.mask(O.mass(f, mo), M), mo)
 
 
-@pytest.mark.parametrize("precision", ["DF", "MIXED"])
+@pytest.mark.parametrize("precision", ["DF", "MIXED", "MIXED_RR"])
 def test_batch_matches_single_solves(gpu, precision):
     import semgb300 as S
     probs = _problems(11, 14)
@@ -46,7 +46,7 @@ def test_batch_matches_single_solves(gpu, precision):
         refs.append((x_ref, info["iters"], mo, M, b, nu, lam))
     solver = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
     infos = []
-    prec = S.SEM_F64_DF if precision == "DF" else S.SEM_MIXED
+    prec = getattr(S, "SEM_" + ("F64_DF" if precision == "DF" else precision))
     xs = solver.solve(bs, tols, precision=prec, infos=infos)
     for (x, inf, (x_ref, it_ref, mo, M, b, nu, lam)) in zip(xs, infos, refs):
         assert inf["converged"] and inf["res_inf"] <= max(tols), inf

@@ -72,6 +72,14 @@ def test_helmholtz_cfg2_shape_vs_c_oracle(gpu):
     assert info_m["converged"] and info_m["outer"] <= 6, info_m
     assert info_m["res_inf"] <= tol
     assert rel_l2(xm, x_c) < 1e-7
+    # residual replacement: one FP32 CG, FP64 residual swapped in every time the
+    # FP32 residual has fallen by 0.3; the iteration count stays near FP64 CG's
+    info_r = {}
+    xr = host(S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info_r,
+                    precision=S.SEM_MIXED_RR))
+    assert info_r["converged"] and info_r["res_inf"] <= tol, info_r
+    assert info_r["outer"] >= 2 and info_r["iters"] <= 1.5 * it_c, (info_r, it_c)
+    assert rel_l2(xr, x_c) < 1e-7
 
 
 @pytest.mark.parametrize("path,variant", [(0, 0), (1, 0), (1, 2), (1, 5), (2, 0)])
@@ -188,7 +196,7 @@ def test_graph_replay_matches_direct_launches(gpu, precision):
     (11, 4, 3, (False, False), "DNDN", 0.05, 0.2, 0.0),
     (2, 20, 9, (False, False), "DDDD", 0.05, 1.0, 0.5),
 ])
-@pytest.mark.parametrize("precision", ["DF", "MIXED"])
+@pytest.mark.parametrize("precision", ["DF", "MIXED", "MIXED_RR"])
 def test_small_path_matches_chunked_and_oracle(gpu, case, precision):
     """The single-launch small-mesh solver against the chunked graph path and
     the oracle: same iterations within 1 %, solutions to the tolerance."""
@@ -200,7 +208,7 @@ def test_small_path_matches_chunked_and_oracle(gpu, case, precision):
     b = O.mask(O.gatherScatter(mo.B * rng.standard_normal(mo.shape), mo), M)
     tol = 1e-10 * np.abs(b).max()
     op = S.HelmholtzOp(md, nu, lam)
-    prec = S.SEM_F64_DF if precision == "DF" else S.SEM_MIXED
+    prec = getattr(S, "SEM_" + ("F64_DF" if precision == "DF" else precision))
     res = {}
     for path in (S.SEM_PATH_SMALL, S.SEM_PATH_CHUNKED):
         info = {}
