@@ -48,6 +48,19 @@ def sin_deform(amp):
     return deform
 
 
+def replica_throughput(ms_local, units_per_rank, world, device):
+    """Replicas: every rank processes units_per_rank units per step.  Returns
+    (step ms = max over ranks, whole-job units per second)."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * units_per_rank / (ms * 1e-3)
+
+
 def unique_dof(n, Ex, Ey):
     return (Ex * (n - 1) + 1) * (Ey * (n - 1) + 1)
 
@@ -201,12 +214,8 @@ def run_ours(args, rank, world, local_rank):
     kms, kn = ctypes.c_double(), ctypes.c_int()
     lib.sem_timing_read(ctypes.byref(kms), ctypes.byref(kn))
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * G / (ms * 1e-3) / 1e9
+    ms, per_s = replica_throughput(sum(step_ms) / len(step_ms), G, world, dev)
+    value = per_s / 1e9
     kernel_ms = kms.value / max(1, kn.value)
     clocks = sampler.summary(t0, t1)
 
@@ -227,12 +236,8 @@ def run_ours(args, rank, world, local_rank):
         b.synchronize()
         if i >= args.warmup:
             e2e_ms.append(a.elapsed_time(b))
-    e2e_step = sum(e2e_ms) / len(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    e2e = {"value": world * G / (e2e_step * 1e-3) / 1e9, "unit": UNIT,
+    e2e_step, e2e_per_s = replica_throughput(sum(e2e_ms) / len(e2e_ms), G, world, dev)
+    e2e = {"value": e2e_per_s / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L, "ms_per_step": e2e_step,
            "api": "semgb300.HelmholtzOp (sem_hlmz through ctypes), pinned host buffers"}
     # parity of this very output against the F64 arithmetic
@@ -274,10 +279,15 @@ def run_ours(args, rank, world, local_rank):
         "f64_native_apply": {"ms": t64, "GDOF/s": G / (t64 * 1e-3) / 1e9},
     }
     if not args.no_extras:
-        result["pcg"] = bench_pcg(S, msh, stream)
-        result["sweep"] = bench_sweep(S, stream)
-        result["batch"] = bench_batch(S)
-        result["adjoint"] = bench_adjoint(S, args.fd_directions)
+        extras = args.extras.split(",") if args.extras else ["pcg", "sweep", "batch", "adjoint"]
+        if "pcg" in extras:
+            result["pcg"] = bench_pcg(S, msh, stream)
+        if "sweep" in extras:
+            result["sweep"] = bench_sweep(S, stream)
+        if "batch" in extras:
+            result["batch"] = bench_batch(S)
+        if "adjoint" in extras:
+            result["adjoint"] = bench_adjoint(S, args.fd_directions)
     sampler.stop()
     if rank == 0 and world == 1 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -656,6 +666,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG and order-sweep extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--extras", default="",
+                    help="comma-separated subset of pcg,sweep,batch,adjoint (default: all)")
     ap.add_argument("--fd-directions", type=int, default=8,
                     help="finite-difference directions of the adjoint check (the config names 32)")
     args = ap.parse_args()

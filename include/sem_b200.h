@@ -174,6 +174,27 @@ int sem_lapl_geom(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y
                   const double* u, double* out, unsigned flags, int precision,
                   sem_stream_t stream);
 
+/* ---- operators beside the fused path (tensor-product kernel + pointwise
+ * kernels on the device, following the reference's ABu sequences).
+ * Host pointers for the small matrices (column-major), device pointers for
+ * the fields (reference local layout). */
+/* dealiased laplace(u,Jr,Js,Dr,Ds,G11,G12,G22) (src/lapl.jl:83-103): Jr (mr x n)
+ * and Js (ms x n) interpolate an element's n GLL points to mr x ms quadrature
+ * points; G11/G12/G22 are fine-grid fields (mr*Ex x ms*Ey); u, out are
+ * (n*Ex x n*Ey); no QQ', no mask (the functional lapl adds them) */
+int sem_laplace_dealiased(int n, int mr, int ms, int Ex, int Ey, const double* Jr, const double* Js,
+                          const double* Dr, const double* Ds, const double* G11, const double* G12,
+                          const double* G22, const double* u, double* out, sem_stream_t stream);
+/* J'(B .* (J u)) of the functional mass(u,M,B,Jr,Js,QQtx,QQty,mult)
+ * (src/mass.jl:32-50) before QQ' and mask; B fine-grid or NULL ([]) */
+int sem_mass_dealiased(int n, int mr, int ms, int Ex, int Ey, const double* Jr, const double* Js,
+                       const double* B, const double* u, double* out, sem_stream_t stream);
+/* grad(u,msh) (src/grad.jl:16-34): ux = rx Dr u + sx u Ds', uy = ry .. + sy .. */
+int sem_grad(sem_mesh_t* mesh, const double* u, double* ux, double* uy, sem_stream_t stream);
+/* gradᵀ(u,msh) (src/grad.jl:43-63), with the factors as src/grad.jl:55-61
+ * passes them to ABu */
+int sem_grad_t(sem_mesh_t* mesh, const double* u, double* ux, double* uy, sem_stream_t stream);
+
 /* ---- solver: pcg(b,opA;opM,mult,ifv,tol,maxiter) (src/pcg.jl:16-60) with
  * opA = mask(QQ'(hlmz(.,nu,k))) (src/diffusion.jl:36-45) */
 enum sem_precond { SEM_PRECOND_NONE = 0, SEM_PRECOND_JACOBI = 1 };

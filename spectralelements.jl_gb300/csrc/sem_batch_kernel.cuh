@@ -166,6 +166,8 @@ struct BRed {
   unsigned long long wm[2][kBT / 32];
   df slot_s[3][2];
   unsigned long long slot_m[3][2];
+  df res_s[2];
+  unsigned long long res_m[2];
 };
 
 // Cluster-wide sums (NS double-float values) and maxima (NM bit patterns) in a
@@ -214,21 +216,30 @@ __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, BRed& sh, 
     }
   }
   cl.sync();
+  // warp 0 combines the ranks' parts in rank order and shares the result
+  // through shared memory (identical in every CTA)
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int q = 0; q < NS; ++q) {
-    df x = *cl.map_shared_rank(&sh.slot_s[slot][q], 0);
-    for (int rk = 1; rk < kCluster; ++rk) x = df_add(x, *cl.map_shared_rank(&sh.slot_s[slot][q], rk));
-    s[q] = x;
-  }
-#pragma unroll
-  for (int q = 0; q < NM; ++q) {
-    unsigned long long x = *cl.map_shared_rank(&sh.slot_m[slot][q], 0);
-    for (int rk = 1; rk < kCluster; ++rk) {
-      const unsigned long long y = *cl.map_shared_rank(&sh.slot_m[slot][q], rk);
-      x = y > x ? y : x;
+    for (int q = 0; q < NS; ++q) {
+      df x = *cl.map_shared_rank(&sh.slot_s[slot][q], 0);
+      for (int rk = 1; rk < kCluster; ++rk) x = df_add(x, *cl.map_shared_rank(&sh.slot_s[slot][q], rk));
+      sh.res_s[q] = x;
     }
-    m[q] = x;
+#pragma unroll
+    for (int q = 0; q < NM; ++q) {
+      unsigned long long x = *cl.map_shared_rank(&sh.slot_m[slot][q], 0);
+      for (int rk = 1; rk < kCluster; ++rk) {
+        const unsigned long long y = *cl.map_shared_rank(&sh.slot_m[slot][q], rk);
+        x = y > x ? y : x;
+      }
+      sh.res_m[q] = x;
+    }
   }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NS; ++q) s[q] = sh.res_s[q];
+#pragma unroll
+  for (int q = 0; q < NM; ++q) m[q] = sh.res_m[q];
 }
 
 // One element tile of the operator mask(QQ'(nu lapl(u) + k B u)) in the

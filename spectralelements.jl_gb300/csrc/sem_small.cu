@@ -71,16 +71,33 @@ __device__ __forceinline__ void small_reduce(cg::cluster_group& cl, SmallRed& re
     red.slot_m[slot] = x;
   }
   cl.sync();
-  const int nr = (int)cl.num_blocks();
-  df t = *cl.map_shared_rank(&red.slot_s[slot], 0);
-  unsigned long long mm = *cl.map_shared_rank(&red.slot_m[slot], 0);
-  for (int rk = 1; rk < nr; ++rk) {
-    t = df_add(t, *cl.map_shared_rank(&red.slot_s[slot], rk));
-    const unsigned long long y = *cl.map_shared_rank(&red.slot_m[slot], rk);
-    mm = y > mm ? y : mm;
+  // warp 0 combines the CTAs' parts (lane r reads rank r, fixed shuffle tree:
+  // the same order in every CTA) and shares the result through shared memory
+  __shared__ df res_s;
+  __shared__ unsigned long long res_m;
+  if (threadIdx.x < 32) {
+    const int nr = (int)cl.num_blocks();
+    const int lane = threadIdx.x;
+    df t = {0.0f, 0.0f};
+    unsigned long long mm = 0ull;
+    if (lane < nr) {
+      t = *cl.map_shared_rank(&red.slot_s[slot], lane);
+      mm = *cl.map_shared_rank(&red.slot_m[slot], lane);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const df y = {__shfl_down_sync(0xffffffffu, t.h, o), __shfl_down_sync(0xffffffffu, t.l, o)};
+      t = df_add(t, y);
+      const unsigned long long ym = __shfl_down_sync(0xffffffffu, mm, o);
+      mm = ym > mm ? ym : mm;
+    }
+    if (lane == 0) {
+      res_s = t;
+      res_m = mm;
+    }
   }
-  s = t;
-  m = mm;
+  __syncthreads();
+  s = res_s;
+  m = res_m;
 }
 
 // elements [e0, e1) of this CTA

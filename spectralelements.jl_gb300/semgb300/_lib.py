@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu"]
 
 
 class SemError(RuntimeError):
@@ -144,6 +144,10 @@ SIGNATURES = {
     "sem_mask_bc": (_I, [_P, _P, _P, _P]),
     "sem_lapl_geom": (_I, [_I, _I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P, _P,
                            _U, _I, _P]),
+    "sem_laplace_dealiased": (_I, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sem_mass_dealiased": (_I, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "sem_grad": (_I, [_P, _P, _P, _P, _P]),
+    "sem_grad_t": (_I, [_P, _P, _P, _P, _P]),
     "sem_pcg": (_I, [_P, ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
     "sem_pcg_noalloc": (_I, [_I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P,
                              ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),

@@ -101,10 +101,50 @@ def lapl(u, *args):
     raise TypeError("lapl: unsupported signature")
 
 
+def _rect_block_of(J, n, E):
+    """An m x n interpolation matrix, or the diagonal block of kron(I_E, J)."""
+    J = _host_matrix(J)
+    if J.shape[1] == n:
+        return J
+    if J.shape[1] == n * E and J.shape[0] % E == 0:
+        m = J.shape[0] // E
+        blk = J[:m, :n]
+        if np.array_equal(J, np.kron(np.eye(E), blk)):
+            return np.asfortranarray(blk)
+    raise ValueError("interpolation matrix must be m x n or kron(I, J) with an m x n block")
+
+
+def _gs_mask(out, M, QQtx, QQty):
+    if not _empty(QQtx):
+        out = gatherScatter(out, QQtx, QQty)
+    if not _empty(M):
+        out = mask(out, M)
+    return out
+
+
+def _lapl_dealiased(u, M, Jr, Js, QQtx, QQty, Dr, Ds, G11, G12, G22):
+    """Dealiased functional lapl: laplace(u,Jr,Js,Dr,Ds,G11,G12,G22)
+    (src/lapl.jl:83-103) on the device, then QQ' and mask (:54-68)."""
+    lib = _lib.load()
+    u = as_local(u)
+    nx, ny = u.shape
+    n = QQtx.n if isinstance(QQtx, QQt) else _infer_n(Dr, nx)
+    Ex, Ey = nx // n, ny // n
+    Drb, Dsb = _block_of(Dr, n), _block_of(Ds, n)
+    Jrb, Jsb = _rect_block_of(Jr, n, Ex), _rect_block_of(Js, n, Ey)
+    G11, G12, G22 = as_local(G11), as_local(G12), as_local(G22)
+    out = local_empty(nx, ny)
+    _lib.check(lib.sem_laplace_dealiased(n, Jrb.shape[0], Jsb.shape[0], Ex, Ey, Jrb.ctypes.data,
+                                         Jsb.ctypes.data, Drb.ctypes.data, Dsb.ctypes.data,
+                                         G11.data_ptr(), G12.data_ptr(), G22.data_ptr(), u.data_ptr(),
+                                         out.data_ptr(), stream_ptr()))
+    return _gs_mask(out, M, QQtx, QQty)
+
+
 def _lapl_functional(u, M, Jr, Js, QQtx, QQty, Dr, Ds, G11, G12, G22, mult):
     lib = _lib.load()
     if not (_empty(Jr) and _empty(Js)):
-        raise NotImplementedError("dealiased lapl (Jr/Js) is not served by the fused kernel")
+        return _lapl_dealiased(u, M, Jr, Js, QQtx, QQty, Dr, Ds, G11, G12, G22)
     u = as_local(u)
     nx, ny = u.shape
     gs = not _empty(QQtx)
@@ -156,7 +196,24 @@ def mass(u, *args):
     if len(args) == 7:
         M, B, Jr, Js, QQtx, QQty, mult = args
         if not (_empty(Jr) and _empty(Js)):
-            raise NotImplementedError("dealiased mass (Jr/Js) is not served")
+            # J'(B .* (J u)) on the device (src/mass.jl:37-42), then QQ' and mask
+            u = as_local(u)
+            nx, ny = u.shape
+            if isinstance(QQtx, QQt):
+                n = QQtx.n
+            else:
+                # without QQ' the element order comes from an m x n block Jr
+                n = _host_matrix(Jr).shape[1]
+                if n > 32 or nx % n:
+                    raise ValueError("pass Jr as an m x n element block or give the mesh's QQtx")
+            Ex, Ey = nx // n, ny // n
+            Jrb, Jsb = _rect_block_of(Jr, n, Ex), _rect_block_of(Js, n, Ey)
+            Bf = None if _empty(B) else as_local(B)
+            out = local_empty(nx, ny)
+            _lib.check(lib.sem_mass_dealiased(n, Jrb.shape[0], Jsb.shape[0], Ex, Ey, Jrb.ctypes.data,
+                                              Jsb.ctypes.data, None if Bf is None else Bf.data_ptr(),
+                                              u.data_ptr(), out.data_ptr(), stream_ptr()))
+            return _gs_mask(out, M, QQtx, QQty)
         u = as_local(u)
         Bu = u.clone(memory_format=torch.preserve_format) if _empty(B) else mask(u, B)
         if not _empty(QQtx):
@@ -213,3 +270,24 @@ def mask(u, M):
         raise ValueError("mask and field shapes differ")
     _lib.check(lib.sem_mask(Mf.data_ptr(), u.data_ptr(), out.data_ptr(), u.numel(), stream_ptr()))
     return out
+
+
+def grad(u, msh):
+    """grad(u, msh) (src/grad.jl:16-34): (ux, uy) = (rx ur + sx us, ry ur + sy us)
+    with ur = ABu([],Dr,u), us = ABu(Ds,[],u); no continuity across elements."""
+    lib = _lib.load()
+    u = _field(u, msh)
+    ux, uy = msh.empty(), msh.empty()
+    _lib.check(lib.sem_grad(msh.handle, u.data_ptr(), ux.data_ptr(), uy.data_ptr(), stream_ptr()))
+    return ux, uy
+
+
+def gradT(u, msh):
+    """gradᵀ(u, msh) (src/grad.jl:43-63), evaluated as the reference writes it:
+    ux = ABu(Dr',[],rx.*u) + ABu([],Ds',sx.*u), uy likewise with ry, sy.
+    (Python normalises the identifier gradᵀ to gradT.)"""
+    lib = _lib.load()
+    u = _field(u, msh)
+    ux, uy = msh.empty(), msh.empty()
+    _lib.check(lib.sem_grad_t(msh.handle, u.data_ptr(), ux.data_ptr(), uy.data_ptr(), stream_ptr()))
+    return ux, uy
