@@ -250,8 +250,10 @@ def run_ours(args, rank, world, local_rank):
 
     peak, peak_kind = load_peaks()
     variant = tune["f64_df"]["chosen"]
-    kname = ("k_apply", "k_apply", "k_apply2", "k_apply2", "k_apply3")[variant]
-    ktempl = "<PDF,9,8,3>" if variant == 4 else f"<PDF,9,8,3,{'true' if variant % 2 else 'false'}>"
+    kname = ("k_apply", "k_apply", "k_apply2", "k_apply2", "k_apply3", "k_apply2")[variant]
+    ktempl = {0: "<PDF,9,8,3,false>", 1: "<PDF,9,8,3,true>", 2: "<PDF,9,8,3,false,false,false>",
+              3: "<PDF,9,8,3,true,false,false>", 4: "<PDF,9,8,3>",
+              5: "<PDF,9,8,3,false,true,false>"}[variant]
     bytes_launch = BYTES_PER_LOCAL * L
     achieved = bytes_launch / (kernel_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
