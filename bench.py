@@ -281,7 +281,7 @@ def run_ours(args, rank, world, local_rank):
         "f64_native_apply": {"ms": t64, "GDOF/s": G / (t64 * 1e-3) / 1e9},
     }
     if not args.no_extras:
-        extras = args.extras.split(",") if args.extras else ["pcg", "sweep", "batch", "adjoint"]
+        extras = args.extras.split(",") if args.extras else ["pcg", "sweep", "batch", "adjoint", "time"]
         if "pcg" in extras:
             result["pcg"] = bench_pcg(S, msh, stream)
         if "sweep" in extras:
@@ -290,6 +290,8 @@ def run_ours(args, rank, world, local_rank):
             result["batch"] = bench_batch(S)
         if "adjoint" in extras:
             result["adjoint"] = bench_adjoint(S, args.fd_directions)
+        if "time" in extras:
+            result["time"] = bench_time(S)
     sampler.stop()
     if rank == 0 and world == 1 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -389,6 +391,68 @@ def bench_pcg(S, msh, stream):
                    "res_inf": info["res_inf"], "tol_rel": tolr,
                    "err_vs_exact_inf": (x - ut).abs().max().item()}
     out["cfg1_cfg3_poisson_8x8_n8"] = r
+    return out
+
+
+def d2d_problem(S, msh):
+    """examples/d2d.jl:13-33 on msh: u = sin(2 pi x) sin(2 pi y) cos(2 pi t) with
+    its forcing split into two separable modes (spatial field, coefficient of t)."""
+    import numpy as np
+    import torch
+    k = 2.0
+    sp = torch.sin(k * np.pi * msh.x) * torch.sin(k * np.pi * msh.y)
+    modes = [(sp * (2 * k * k * np.pi ** 2), lambda t: float(np.cos(k * np.pi * t))),
+             (sp * (-k * np.pi), lambda t: float(np.sin(k * np.pi * t)))]
+    return sp, modes
+
+
+def bench_time(S):
+    """The Diffusion driver (src/diffusion.jl:81-137): BDF3, dt = 1e-3, the
+    reference's solve (identity preconditioner, mult-weighted dots, absolute
+    tol 1e-8), d2d.jl's manufactured solution.  One sem_bdf_run call for the
+    whole run against the per-step evolve() loop with a setForcing! closure,
+    as the reference's examples drive it."""
+    import numpy as np
+    import torch
+    out = {}
+    for name, E, steps, loop_steps in (("cfg1_mesh_8x8_n8", 8, 1000, 200), ("mesh_64x64_n8", 64, 100, 40)):
+        m = S.Mesh(9, 9, E, E, (False, False), sin_deform(0.1), bc="DDDD")
+        m.autotune(S.SEM_F64_DF)
+        sp, modes = d2d_problem(S, m)
+        r = {"steps": steps, "dt": 1e-3, "order": 3, "tol_abs": 1e-8,
+             "local_dof": int(m.x.numel()), "path": "small (one cluster launch per solve)"
+             if m.x.numel() <= S._lib.SEM_SMALL_MAX_LOCAL else "chunked (CUDA-graph CG chunks)"}
+        # device-resident run
+        d = S.Diffusion("DDDD", m, Ti=0.0, Tf=1.0, dt=1e-3, k=3, nu=1.0)
+        d.u.copy_(sp)
+        d.run(5, forcing=modes)  # warm
+        d = S.Diffusion("DDDD", m, Ti=0.0, Tf=1.0, dt=1e-3, k=3, nu=1.0)
+        d.u.copy_(sp)
+        torch.cuda.synchronize()
+        t = time.time()
+        infos = d.run(steps, forcing=modes)
+        torch.cuda.synchronize()
+        dt_run = time.time() - t
+        err = (d.u - sp * np.cos(2 * np.pi * d.tstep.time[0])).abs().max().item()
+        r["device_run"] = {"steps_per_s": steps / dt_run, "iters_per_step": sum(i["iters"] for i in infos) / steps,
+                           "err_vs_exact_inf": err}
+        # per-step evolve loop (host closure sets f each step)
+        e = S.Diffusion("DDDD", m, Ti=0.0, Tf=1.0, dt=1e-3, k=3, nu=1.0)
+        e.u.copy_(sp)
+        a0, a1 = modes[0][0], modes[1][0]
+
+        def set_f(f, x, y, tt):
+            f.copy_(modes[0][1](tt) * a0 + modes[1][1](tt) * a1)
+        e.evolve(setForcing=set_f)
+        torch.cuda.synchronize()
+        t = time.time()
+        for _ in range(loop_steps):
+            e.evolve(setForcing=set_f)
+        torch.cuda.synchronize()
+        dt_loop = time.time() - t
+        r["evolve_loop"] = {"steps_per_s": loop_steps / dt_loop, "steps": loop_steps}
+        r["run_over_loop"] = (steps / dt_run) / (loop_steps / dt_loop)
+        out[name] = r
     return out
 
 
@@ -631,7 +695,35 @@ def cpu_baseline():
                                      "threads": C.threads(), "ms_per_apply": 1e3 * statistics.median(ts)}
     except Exception as e:  # the C oracle is optional for the baseline line
         out["optimised_c_openmp"] = {"error": str(e)}
+    out["time_loop_cfg1_mesh_8x8_n8"] = cpu_time_loop()
     return out
+
+
+def cpu_time_loop(steps=20):
+    """The Diffusion stepping of src/diffusion.jl:81-106 restated in NumPy
+    (dense QQ', identity preconditioner, mult-weighted dots, tol 1e-8) on the
+    8x8 N=8 mesh with d2d.jl's forcing: BDF3, dt = 1e-3, a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import sem_oracle as O
+    mo = O.Mesh(9, 9, 8, 8, (False, False), O.sin_deform(0.1), dense_qq=True)
+    M = O.generateMask(["D"] * 4, mo)
+    k, dt = 3, 1e-3
+    sp = np.sin(2 * np.pi * mo.x) * np.sin(2 * np.pi * mo.y)
+    u, uh, tt = sp.copy(), [np.zeros(mo.shape) for _ in range(k)], [0.0] * (k + 1)
+    t0 = time.time()
+    for _ in range(steps):
+        uh = [u.copy()] + uh[:-1]
+        tt = [tt[0]] + tt[:-1]
+        tt[0] += dt
+        _, bb = O.bdfExtK(tt, k)
+        f = sp * (8 * np.pi ** 2 * np.cos(2 * np.pi * tt[0]) - 2 * np.pi * np.sin(2 * np.pi * tt[0]))
+        rhs = O.diffusion_makeRHS(mo, 1.0, f, np.zeros(mo.shape), uh, bb, M)
+        u = O.pcg(rhs, lambda v, bb=bb: O.diffusion_opLHS(v, mo, 1.0, bb[0], M), mult=mo.mult, tol=1e-8)
+    el = time.time() - t0
+    return {"steps_per_s": steps / el, "steps": steps, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{steps} BDF3 steps of the reference-faithful NumPy restatement"}
 
 
 def run_reference(args):

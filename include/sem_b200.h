@@ -290,6 +290,59 @@ int sem_jacobi_diag(sem_mesh_t* mesh, const double* nu_field, double nu, double 
 int sem_adjoint_grad(sem_mesh_t* mesh, const double* lam, const double* u,
                      double* grad, unsigned flags, sem_stream_t stream);
 
+/* ---- time stepping (src/time.jl:31-112, src/diffusion.jl:36-137).
+ * sem_bdf_coeffs: bdfExtK(t; k) on the host.  t[0..k] = [t(i+1), t(i), ...,
+ * t(i-k+1)]; repeated times are dropped (the reference's unique).  Writes the
+ * extrapolation weights a[0..k-1] and the derivative weights b[0..k]; a[0] = 1
+ * when every time is equal (the steady branch). */
+#define SEM_BDF_MAX_ORDER 6
+int sem_bdf_coeffs(int k, const double* t, double* a, double* b);
+
+/* makeRHS! (src/diffusion.jl:51-65):
+ * rhs = QQ'(mask(B f - nu lapl(ub) - sum_{i<order} bdfB[1+i] B uh[i])).
+ * bdfB is a host array of order+1 entries.  f and ub may be NULL (zero
+ * fields).  uh is a host array of `order` device fields.  One gather kernel
+ * does it, plus one fused operator launch when ub is given. */
+int sem_bdf_rhs(sem_mesh_t* mesh, double nu, int order, const double* bdfB, const double* f,
+                const double* ub, const double* const* uh, double* rhs, sem_stream_t stream);
+
+/* sem_bdf_run: nsteps of evolve! (src/diffusion.jl:81-106) on the device.
+ * Each step:
+ *  - shifts the histories (uh[i] <- uh[i-1], uh[0] <- u);
+ *  - advances the host time history time[0..order] (in/out) by dt and
+ *    recomputes bdfExtK;
+ *  - sets ub and f at the new time from modes: f = sum_j fcoef[s*nf+j] F[j]
+ *    and ub = sum_j bcoef[s*nb+j] UB[j], for step s of this call (at most 8
+ *    modes each);
+ *  - builds the right-hand side as sem_bdf_rhs does;
+ *  - solves opLHS u = rhs with pcg from u = 0 and k = bdfB[1];
+ *  - adds ub to u.
+ * The solve options come from `solve`: precond, precision, tol, maxiter,
+ * path, mult_ones.  nu and k are set per step; nu_field must be NULL.
+ * The reference's Diffusion passes mult = msh.mult (mult_ones = 0) and the
+ * identity preconditioner.
+ * Where the single-launch small-mesh solver serves the mesh, steps are queued
+ * without waiting for the host, and results are read back once per 128 steps.
+ * Otherwise each solve reads its convergence flag as sem_pcg does.
+ * info (NULL or nsteps entries) receives each step's solve.  A step that
+ * reaches maxiter does not stop the run (the reference warns and goes on);
+ * the call then returns SEM_ERR_NOT_CONVERGED at the end.  A NaN stops it. */
+typedef struct {
+  int order;                /* k of BDFk, 1..SEM_BDF_MAX_ORDER (the reference defaults to 3) */
+  double nu;                /* scalar viscosity                                */
+  double dt;                /* time step                                       */
+  int nsteps;               /* steps of this call                              */
+  sem_pcg_opts solve;       /* per-step solve options (nu, nu_field, k unused) */
+  int nf;                   /* forcing modes                                   */
+  const double* const* F;   /* host array of nf device fields                  */
+  const double* fcoef;      /* host, nsteps x nf (row per step)                */
+  int nb;                   /* boundary-data modes                             */
+  const double* const* UB;  /* host array of nb device fields                  */
+  const double* bcoef;      /* host, nsteps x nb                               */
+} sem_bdf_desc;
+int sem_bdf_run(sem_mesh_t* mesh, const sem_bdf_desc* desc, double* time, double* u,
+                double* const* uh, sem_solve_info* info, sem_stream_t stream);
+
 /* ---- instrumentation (no counterpart in the reference, which only prints
  * @time): CUDA-event timing of every launch of the fused element-operator
  * kernel while enabled; read returns the summed kernel time and the number of

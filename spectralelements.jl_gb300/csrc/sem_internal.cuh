@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include <string>
@@ -257,6 +258,22 @@ struct SmallProb {
 };
 
 int launch_small_pcg(SmallProb* dev, const OperatorSet& ops, int n, cudaStream_t s);  // sem_small.cu
+
+// results at the tail of a SmallProb, in the same order
+struct SmallOut {
+  int iters, outer, converged, nan;
+  double res_inf, res0_inf;
+};
+static_assert(sizeof(SmallProb) - offsetof(SmallProb, iters) == sizeof(SmallOut),
+              "SmallOut mirrors the result fields of SmallProb");
+
+// sem_pcg.cu, for callers that queue several small-mesh solves without
+// waiting on each: whether sem_pcg would take the single-launch path for o on
+// m, and the record of one such solve (the Jacobi diagonal it reads is
+// enqueued on s into the mesh's workspace)
+bool small_path_taken(const sem_mesh* m, const sem_pcg_opts* o);
+int small_prepare(sem_mesh* m, const sem_pcg_opts* o, const double* b, double* x, SmallProb* rec,
+                  cudaStream_t s);
 
 constexpr int kVariants = SEM_VARIANTS;
 

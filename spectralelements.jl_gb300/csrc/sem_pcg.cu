@@ -700,6 +700,72 @@ int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r
   return SEM_OK;
 }
 
+// inverse Jacobi diagonal of the solve's operator into w.dinv (and w.dinv32
+// for the mixed precisions)
+int jacobi_build(const OpCtx& cx, const WS& w, const sem_pcg_opts* o, cudaStream_t s) {
+  const unsigned nb = nblocks(cx.g.NX * cx.g.NY);
+  SEM_CHECK(diag_build(cx, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
+  k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, cx.g);
+  if (o->precision == SEM_MIXED || o->precision == SEM_MIXED_RR)
+    k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, cx.g);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+// whether the single-launch small-mesh solver serves this problem
+bool small_eligible(const sem_mesh* m, const Grid& g, const sem_pcg_opts* o) {
+  const int prec = o->precision;
+  return m && g.NX * g.NY <= SEM_SMALL_MAX_LOCAL && g.n <= 11 && !o->nu_field &&
+         (prec == SEM_F64_DF || prec == SEM_MIXED || prec == SEM_MIXED_RR);
+}
+
+// the record of one small-mesh solve (the geometry copies it reads are made
+// on first use)
+int small_record(const OpCtx& cx, const WS& w, sem_mesh* m, const sem_pcg_opts* o, const double* b,
+                 double* x, int maxiter, SmallProb& sp, cudaStream_t s) {
+  const int prec = o->precision;
+  SEM_CHECK(ensure_df_geometry(m, s));
+  if (prec != SEM_F64_DF) SEM_CHECK(ensure_f32_geometry(m, s));
+  std::memset(&sp, 0, sizeof(sp));
+  sp.n = cx.g.n;
+  sp.Ex = cx.g.Ex;
+  sp.Ey = cx.g.Ey;
+  sp.NX = cx.g.NX;
+  sp.NY = cx.g.NY;
+  sp.rinfo = cx.g.rinfo;
+  sp.cinfo = cx.g.cinfo;
+  sp.has_bc = cx.has_bc;
+  sp.jacobi = o->precond == SEM_PRECOND_JACOBI ? 1 : 0;
+  sp.mult_ones = o->mult_ones ? 1 : 0;
+  sp.nu = o->nu;
+  sp.k = o->k;
+  sp.tol = o->tol;
+  sp.maxiter = maxiter;
+  sp.precision = prec;
+  const bool rr = prec == SEM_MIXED_RR;
+  sp.inner_tol = o->inner_tol > 0 ? o->inner_tol : (rr ? 0.3 : 1e-4);
+  sp.max_outer = o->max_outer > 0 ? o->max_outer : (rr ? 100 : 6);
+  sp.b = b;
+  sp.x = x;
+  sp.r = w.r;
+  sp.p = w.p;
+  sp.raw = w.x64tmp;
+  sp.dinv = w.dinv;
+  sp.r32 = w.r32;
+  sp.p32 = w.p32;
+  sp.raw32 = w.Ap32;
+  sp.x32 = w.x32;
+  sp.dinv32 = w.dinv32;
+  sp.Gdf = m->Gdf;
+  sp.Gf = m->G11_f;
+  return SEM_OK;
+}
+
+int default_maxiter(const Grid& g, const sem_pcg_opts* o) {
+  const long long L = g.NX * g.NY;
+  return o->maxiter > 0 ? o->maxiter : (int)(L > 2147483647LL ? 2147483647LL : L);
+}
+
 // argument checks shared by the solver entry points
 int pcg_check(const sem_pcg_opts* o, const double* b, double* x) {
   if (!o || !b || !x) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
@@ -719,66 +785,26 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
   const int prec = o->precision;
   OpCtx cx = cx0;
   const long long L = cx.g.NX * cx.g.NY;
-  const int maxiter = o->maxiter > 0 ? o->maxiter : (int)(L > 2147483647LL ? 2147483647LL : L);
+  const int maxiter = default_maxiter(cx.g, o);
   int check_every = o->check_every > 0 ? o->check_every : (L < 200000 ? 64 : 16);
   const unsigned nb = nblocks(L);
   const bool jac = o->precond == SEM_PRECOND_JACOBI;
   Grid gv = cx.g;
   if (o->mult_ones) gv.topo |= M_MULT1;
-  if (jac) {
-    SEM_CHECK(diag_build(cx, o->nu_field, o->nu, o->k, w.x64tmp, w.d, s));
-    k_diag_inv<double><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv, cx.g);
-    if (prec == SEM_MIXED || prec == SEM_MIXED_RR)
-      k_diag_inv<float><<<nb * 4, kRT, 0, s>>>(w.x64tmp, w.dinv32, cx.g);
-    SEM_CUDA(cudaGetLastError());
-  }
+  if (jac) SEM_CHECK(jacobi_build(cx, w, o, s));
   Scalars res;
   std::memset(&res, 0, sizeof(res));
   int outer = 0;
   double res0 = 0.0;
-  const bool small_ok = m && w.small && L <= SEM_SMALL_MAX_LOCAL && cx.g.n <= 11 && !o->nu_field &&
-                        (prec == SEM_F64_DF || prec == SEM_MIXED || prec == SEM_MIXED_RR);
+  const bool small_ok = w.small && small_eligible(m, cx.g, o);
   if (o->path == SEM_PATH_SMALL && !small_ok)
     return set_error(SEM_ERR_UNSUPPORTED,
                      "the small-mesh path serves meshes of at most %d local DOF, n <= 11, scalar nu, "
                      "SEM_F64_DF, SEM_MIXED or SEM_MIXED_RR", SEM_SMALL_MAX_LOCAL);
   if (small_ok && o->path != SEM_PATH_CHUNKED) {
     // the whole solve in one cluster launch
-    SEM_CHECK(ensure_df_geometry(m, s));
-    if (prec != SEM_F64_DF) SEM_CHECK(ensure_f32_geometry(m, s));
     SmallProb sp;
-    std::memset(&sp, 0, sizeof(sp));
-    sp.n = cx.g.n;
-    sp.Ex = cx.g.Ex;
-    sp.Ey = cx.g.Ey;
-    sp.NX = cx.g.NX;
-    sp.NY = cx.g.NY;
-    sp.rinfo = cx.g.rinfo;
-    sp.cinfo = cx.g.cinfo;
-    sp.has_bc = cx.has_bc;
-    sp.jacobi = jac ? 1 : 0;
-    sp.mult_ones = o->mult_ones ? 1 : 0;
-    sp.nu = o->nu;
-    sp.k = o->k;
-    sp.tol = o->tol;
-    sp.maxiter = maxiter;
-    sp.precision = prec;
-    const bool rr = prec == SEM_MIXED_RR;
-    sp.inner_tol = o->inner_tol > 0 ? o->inner_tol : (rr ? 0.3 : 1e-4);
-    sp.max_outer = o->max_outer > 0 ? o->max_outer : (rr ? 100 : 6);
-    sp.b = b;
-    sp.x = x;
-    sp.r = w.r;
-    sp.p = w.p;
-    sp.raw = w.x64tmp;
-    sp.dinv = w.dinv;
-    sp.r32 = w.r32;
-    sp.p32 = w.p32;
-    sp.raw32 = w.Ap32;
-    sp.x32 = w.x32;
-    sp.dinv32 = w.dinv32;
-    sp.Gdf = m->Gdf;
-    sp.Gf = m->G11_f;
+    SEM_CHECK(small_record(cx, w, m, o, b, x, maxiter, sp, s));
     SEM_CUDA(cudaMemcpyAsync(w.small, &sp, sizeof(sp), cudaMemcpyHostToDevice, s));
     SEM_CHECK(launch_small_pcg(w.small, *cx.ops, cx.g.n, s));
     SEM_CUDA(cudaMemcpyAsync(&sp, w.small, sizeof(sp), cudaMemcpyDeviceToHost, s));
@@ -924,6 +950,21 @@ int batch_diag(sem_mesh* m, double nu, double k, double* dinv, double* tmp, cuda
   k_diag_inv<double><<<nblocks(m->g.NX * m->g.NY) * 4, kRT, 0, s>>>(dinv, dinv, m->g);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
+}
+
+bool small_path_taken(const sem_mesh* m, const sem_pcg_opts* o) {
+  return o->path != SEM_PATH_CHUNKED && small_eligible(m, m->g, o);
+}
+
+int small_prepare(sem_mesh* m, const sem_pcg_opts* o, const double* b, double* x, SmallProb* rec,
+                  cudaStream_t s) {
+  SEM_CHECK(pcg_check(o, b, x));
+  if (!small_path_taken(m, o)) return set_error(SEM_ERR_BAD_ARG, "problem is not served by the small path");
+  WS w;
+  SEM_CHECK(get_ws(m, o->precision == SEM_MIXED || o->precision == SEM_MIXED_RR, w));
+  const OpCtx cx = ctx_of(m);
+  if (o->precond == SEM_PRECOND_JACOBI) SEM_CHECK(jacobi_build(cx, w, o, s));
+  return small_record(cx, w, m, o, b, x, default_maxiter(cx.g, o), *rec, s);
 }
 
 }  // namespace sem

@@ -46,7 +46,9 @@ struct PcgOpts
     inner_tol::Cdouble; max_outer::Cint; check_every::Cint; mult_ones::Cint; path::Cint
 end
 
-mutable struct SolveInfo
+# immutable (isbits), so that a Vector{SolveInfo} is a C array of records;
+# single results are read through Ref{SolveInfo}
+struct SolveInfo
     iters::Cint; outer::Cint; res_inf::Cdouble; res0_inf::Cdouble; converged::Cint
 end
 SolveInfo() = SolveInfo(0, 0, 0.0, 0.0, 0)
@@ -231,7 +233,7 @@ function solve(bs::BatchSolver, rhs::Vector{<:CuArray{Float64,2}}, tol::Vector{F
     xs = [similar(r) for r in rhs]
     bp = CuPtr{Cdouble}[pointer(r) for r in rhs]
     xp = CuPtr{Cdouble}[pointer(x) for x in xs]
-    info = [SolveInfo() for _ in rhs]
+    info = fill(SolveInfo(), length(rhs))
     st = ccall((:sem_batch_pcg, libsem), Cint,
                (Ptr{Cvoid}, Ptr{CuPtr{Cdouble}}, Ptr{CuPtr{Cdouble}}, Ptr{Cdouble}, Ptr{Cint}, Cint,
                 Cdouble, Cint, Ptr{SolveInfo}, Ptr{Cvoid}),
@@ -239,6 +241,52 @@ function solve(bs::BatchSolver, rhs::Vector{<:CuArray{Float64,2}}, tol::Vector{F
     st == SEM_ERR_NOT_CONVERGED && println("warning: some batched solves reached maxiter")
     st == SEM_ERR_NOT_CONVERGED || check(st)
     return xs, info
+end
+
+# ---- device time loop: nsteps of evolve! (src/diffusion.jl:81-106) in one
+# sem_bdf_run call.  u and the histories uh are CuArrays of the mesh; time is
+# the TimeStepper's time vector (updated in place); forcing and boundary are
+# vectors of (field, t -> coefficient) pairs, the separable forms of the
+# reference's setForcing!/setBC! closures.  The solve is the reference's
+# Diffusion solve: identity preconditioner, mult = msh.mult, tol absolute.
+struct BdfDesc
+    order::Cint; nu::Cdouble; dt::Cdouble; nsteps::Cint
+    solve::PcgOpts
+    nf::Cint; F::Ptr{CuPtr{Cdouble}}; fcoef::Ptr{Cdouble}
+    nb::Cint; UB::Ptr{CuPtr{Cdouble}}; bcoef::Ptr{Cdouble}
+end
+function bdf_run!(u::CuArray{Float64,2}, uh::Vector{<:CuArray{Float64,2}}, time::Vector{Float64},
+                  msh::Mesh, bc::Vector{Char}, ν::Float64, dt::Float64, nsteps::Int;
+                  forcing=Tuple{CuArray{Float64,2},Function}[],
+                  boundary=Tuple{CuArray{Float64,2},Function}[],
+                  tol=1e-8, precision=SEM_F64_DF, jacobi::Bool=false)
+    set_bc!(msh, bc)
+    k = length(uh)
+    ts = Float64[]
+    t = time[1]
+    for _ in 1:nsteps
+        t += dt
+        push!(ts, t)
+    end
+    fc = Float64[fn(tt) for tt in ts for (_, fn) in forcing]
+    bcf = Float64[fn(tt) for tt in ts for (_, fn) in boundary]
+    F = CuPtr{Cdouble}[pointer(f) for (f, _) in forcing]
+    UB = CuPtr{Cdouble}[pointer(g) for (g, _) in boundary]
+    uhp = CuPtr{Cdouble}[pointer(v) for v in uh]
+    info = fill(SolveInfo(), nsteps)
+    GC.@preserve fc bcf F UB begin
+        d = Ref(BdfDesc(k, ν, dt, nsteps,
+                        PcgOpts(ν, CU_NULL, 0.0, jacobi ? 1 : 0, precision, tol, 0, 0.0, 0, 0, 0, 0),
+                        length(forcing), pointer(F), pointer(fc),
+                        length(boundary), pointer(UB), pointer(bcf)))
+        st = ccall((:sem_bdf_run, libsem), Cint,
+                   (Ptr{Cvoid}, Ref{BdfDesc}, Ptr{Cdouble}, CuPtr{Cdouble}, Ptr{CuPtr{Cdouble}},
+                    Ptr{SolveInfo}, Ptr{Cvoid}),
+                   handle(msh), d, time, pointer(u), uhp, info, stream())
+    end
+    st == SEM_ERR_NOT_CONVERGED && println("warning: some steps reached maxiter")
+    st == SEM_ERR_NOT_CONVERGED || check(st)
+    return info
 end
 
 # ---- differentiable solve of -div(ν grad u) = f with ν folded into G

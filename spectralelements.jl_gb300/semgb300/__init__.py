@@ -7,8 +7,7 @@ Names and argument meanings follow the reference: ``Mesh``, ``generateMask``,
 reference's column-major local layout.
 """
 from ._lib import (SEM_F32, SEM_F64, SEM_F64_DF, SEM_GS, SEM_MASK, SEM_MIXED, SEM_MIXED_RR,  # noqa: F401
-                   SEM_PATH_AUTO,
-                   SEM_PATH_CHUNKED, SEM_PATH_SMALL, NotConverged, SemError, build, load)
+                   SEM_BDF_MAX_ORDER, SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL, NotConverged, SemError, build, load)
 from .host import bdfExtK, derivMat, fixU, gausslobatto, interpMat, ndgrid, semmesh, semq_index  # noqa: F401
 from .mesh import Mesh, QQt, as_local, generateMask, local_empty  # noqa: F401
 from .ops import ABu, gatherScatter, grad, gradT, hlmz, lapl, mask, mass  # noqa: F401
@@ -21,4 +20,5 @@ __all__ = ["Mesh", "QQt", "generateMask", "ABu", "lapl", "mass", "hlmz", "gather
            "linsolve_varcoef", "gausslobatto", "derivMat", "interpMat", "semmesh", "ndgrid",
            "semq_index", "bdfExtK", "fixU", "as_local", "local_empty", "build", "load",
            "SemError", "NotConverged", "SEM_F64", "SEM_F64_DF", "SEM_F32", "SEM_MIXED",
-           "SEM_GS", "SEM_MASK", "SEM_MIXED_RR", "SEM_PATH_AUTO", "SEM_PATH_CHUNKED", "SEM_PATH_SMALL"]
+           "SEM_GS", "SEM_MASK", "SEM_MIXED_RR", "SEM_PATH_AUTO", "SEM_PATH_CHUNKED", "SEM_PATH_SMALL",
+           "SEM_BDF_MAX_ORDER"]

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu", "sem_time.cu"]
 
 
 class SemError(RuntimeError):
@@ -50,6 +50,7 @@ SEM_PRECOND_NONE, SEM_PRECOND_JACOBI = 0, 1
 SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL = 0, 1, 2
 SEM_SMALL_MAX_LOCAL = 100000  # include/sem_b200.h
 SEM_VARIANTS = 6  # fused element-operator kernel variants (include/sem_b200.h)
+SEM_BDF_MAX_ORDER = 6  # include/sem_b200.h
 FIELDS = {"x": 0, "y": 1, "Jac": 2, "Jaci": 3, "rx": 4, "ry": 5, "sx": 6, "sy": 7, "B": 8,
           "Bi": 9, "G11": 10, "G12": 11, "G22": 12, "mult": 13, "mask": 14}
 
@@ -111,6 +112,14 @@ class SolveInfo(ctypes.Structure):
                 ("res0_inf", ctypes.c_double), ("converged", ctypes.c_int)]
 
 
+class BdfDesc(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("nu", ctypes.c_double), ("dt", ctypes.c_double),
+                ("nsteps", ctypes.c_int), ("solve", PcgOpts), ("nf", ctypes.c_int),
+                ("F", ctypes.POINTER(ctypes.c_void_p)), ("fcoef", ctypes.POINTER(ctypes.c_double)),
+                ("nb", ctypes.c_int), ("UB", ctypes.POINTER(ctypes.c_void_p)),
+                ("bcoef", ctypes.POINTER(ctypes.c_double))]
+
+
 class MeshDesc(ctypes.Structure):
     _fields_ = [("nr", ctypes.c_int), ("ns", ctypes.c_int), ("Ex", ctypes.c_int),
                 ("Ey", ctypes.c_int), ("periodic_x", ctypes.c_int), ("periodic_y", ctypes.c_int),
@@ -159,6 +168,10 @@ SIGNATURES = {
                            ctypes.POINTER(SolveInfo), _P]),
     "sem_jacobi_diag": (_I, [_P, _P, _D, _D, _P, _P]),
     "sem_adjoint_grad": (_I, [_P, _P, _P, _P, _U, _P]),
+    "sem_bdf_coeffs": (_I, [_I, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "sem_bdf_rhs": (_I, [_P, _D, _I, ctypes.POINTER(_D), _P, _P, ctypes.POINTER(ctypes.c_void_p), _P, _P]),
+    "sem_bdf_run": (_I, [_P, ctypes.POINTER(BdfDesc), ctypes.POINTER(_D), _P,
+                         ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(SolveInfo), _P]),
     "sem_timing_enable": (_I, [_I]),
     "sem_timing_read": (_I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
 }

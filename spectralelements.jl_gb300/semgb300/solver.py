@@ -353,10 +353,17 @@ class TimeStepper:
 class Diffusion:
     """``Diffusion(bc, msh; Ti, Tf, dt, k)`` (src/diffusion.jl:7-34) with
     device fields u, uh (histories), ub, nu, f.  ``checkpoint_every`` keeps
-    copies of u every that many steps (for adjoint recomputation)."""
+    copies of u every that many steps (for adjoint recomputation).
+
+    The solve is the reference's: pcg on opLHS with mult = msh.mult and the
+    identity preconditioner (src/diffusion.jl:67-77); ``jacobi=True`` uses
+    the Jacobi preconditioner instead.  ``path`` picks the solver path
+    (SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL)."""
 
     def __init__(self, bc, msh: Mesh, Ti=0.0, Tf=0.0, dt=0.0, k=3, nu=1.0,
-                 precision=None, checkpoint_every=0):
+                 precision=None, checkpoint_every=0, jacobi=False, path=0):
+        if not 1 <= k <= _lib.SEM_BDF_MAX_ORDER:
+            raise ValueError(f"order k must be in 1..{_lib.SEM_BDF_MAX_ORDER}")
         self.msh = msh
         self.bc = "".join(bc)
         msh.set_bc(self.bc)
@@ -367,6 +374,8 @@ class Diffusion:
         self.nu = float(nu)
         self.tstep = TimeStepper(Ti, Tf, dt, k)
         self.precision = precision
+        self.jacobi = bool(jacobi)
+        self.path = int(path)
         self.checkpoint_every = checkpoint_every
         self.checkpoints = {}
         self.last_info = {}
@@ -375,24 +384,98 @@ class Diffusion:
         return HelmholtzOp(self.msh, self.nu, self.tstep.bdfB[0], precision=self.precision)
 
     def makeRHS(self):
-        """src/diffusion.jl:51-65."""
-        from .ops import gatherScatter, lapl, mass, mask
-        msh, bdfB = self.msh, self.tstep.bdfB
-        rhs = mass(self.f, msh)
-        if torch.count_nonzero(self.ub):
-            rhs = rhs - self.nu * lapl(self.ub, msh)
-        for i, uh in enumerate(self.uh):
-            if bdfB[1 + i] != 0.0:
-                rhs = rhs - bdfB[1 + i] * mass(uh, msh)
-        rhs = mask(rhs, self.M)
-        return gatherScatter(rhs, msh)
+        """src/diffusion.jl:51-65 as one gather kernel plus one fused lapl
+        launch for the boundary data (``sem_bdf_rhs``)."""
+        lib = _lib.load()
+        msh, k = self.msh, len(self.uh)
+        rhs = msh.empty()
+        bdfB = (ctypes.c_double * (k + 1))(*[float(v) for v in self.tstep.bdfB])
+        uh = (ctypes.c_void_p * k)(*[as_local(u).data_ptr() for u in self.uh])
+        _lib.check(lib.sem_bdf_rhs(msh.handle, self.nu, k, bdfB, as_local(self.f).data_ptr(),
+                                   as_local(self.ub).data_ptr(), uh, rhs.data_ptr(), stream_ptr()))
+        return rhs
+
+    def _opts(self, tol, maxiter=None):
+        o = _lib.PcgOpts()
+        o.nu = self.nu
+        o.precond = _lib.SEM_PRECOND_JACOBI if self.jacobi else _lib.SEM_PRECOND_NONE
+        o.precision = int(self.precision if self.precision is not None else self.msh.precision)
+        o.tol = float(tol)
+        o.maxiter = 0 if maxiter is None else int(maxiter)
+        o.path = self.path
+        o.mult_ones = 0
+        return o
 
     def solve(self, tol=1e-8):
         op = self.opLHS()
         info = {}
-        self.u = pcg(self.makeRHS(), op, opM=Jacobi(op), mult=self.msh.mult, tol=tol, info=info)
+        opM = Jacobi(op) if self.jacobi else None
+        self.u = pcg(self.makeRHS(), op, opM=opM, mult=self.msh.mult, tol=tol, info=info,
+                     path=self.path)
         self.last_info = info
         self.u = self.u + self.ub
+
+    def run(self, nsteps, forcing=(), boundary=(), tol=1e-8, maxiter=None):
+        """``nsteps`` calls of evolve! in one ``sem_bdf_run`` call: the
+        histories, the right-hand side and the solves stay on the device, and
+        where the single-launch small-mesh solver serves the mesh no step
+        waits for the host.
+
+        ``forcing`` and ``boundary`` are lists of ``(field, fn)`` pairs: at the
+        time t of a step, f = sum fn(t) * field and ub = sum fn(t) * field (the
+        reference's setForcing!/setBC! closures, restricted to separable
+        forms; at most 8 each).  Returns the per-step solve records."""
+        lib = _lib.load()
+        msh, ts, k = self.msh, self.tstep, len(self.uh)
+        nsteps = int(nsteps)
+        if nsteps <= 0:
+            return []
+        forcing, boundary = list(forcing), list(boundary)
+        times, t = [], ts.time[0]
+        for _ in range(nsteps):  # the additions the library makes
+            t += ts.dt
+            times.append(t)
+
+        def table(modes):
+            vals = [float(fn(tt)) for tt in times for (_, fn) in modes]
+            return (ctypes.c_double * max(1, len(vals)))(*vals)
+
+        keep = []  # the device fields the call reads
+
+        def fields(modes):
+            keep.extend(as_local(f) for f, _ in modes)
+            return (ctypes.c_void_p * max(1, len(modes)))(*[t.data_ptr() for t in keep[-len(modes):]]
+                                                            if modes else [])
+
+        d = _lib.BdfDesc()
+        d.order, d.nu, d.dt, d.nsteps = k, self.nu, ts.dt, nsteps
+        d.solve = self._opts(tol, maxiter)
+        F, fc, UB, bc = fields(forcing), table(forcing), fields(boundary), table(boundary)
+        d.nf, d.F, d.fcoef = len(forcing), F, fc
+        d.nb, d.UB, d.bcoef = len(boundary), UB, bc
+        time_arr = (ctypes.c_double * (k + 1))(*ts.time)
+        uh = (ctypes.c_void_p * k)(*[as_local(u).data_ptr() for u in self.uh])
+        infos = (_lib.SolveInfo * nsteps)()
+        self.u = as_local(self.u)
+        st = lib.sem_bdf_run(msh.handle, ctypes.byref(d), time_arr, self.u.data_ptr(), uh, infos,
+                             stream_ptr())
+        if st not in (_lib.SEM_OK, _lib.SEM_ERR_NOT_CONVERGED):
+            _lib.check(st)
+        ts.time = [float(v) for v in time_arr]
+        ts.istep += nsteps
+        ts.bdfA, ts.bdfB = bdfExtK(ts.time, k)
+        last = times[-1]
+        if forcing:
+            self.f = sum(float(fn(last)) * as_local(f) for f, fn in forcing)
+        if boundary:
+            self.ub = sum(float(fn(last)) * as_local(f) for f, fn in boundary)
+        out = [dict(iters=i.iters, outer=i.outer, res_inf=i.res_inf, res0_inf=i.res0_inf,
+                    converged=bool(i.converged)) for i in infos]
+        for i in out:
+            if not i["converged"]:
+                print("warning: res:", i["res_inf"])
+        self.last_info = out[-1]
+        return out
 
     def evolve(self, setBC=None, setForcing=None, tol=1e-8):
         """src/diffusion.jl:81-106."""
@@ -410,11 +493,27 @@ class Diffusion:
             self.checkpoints[self.tstep.istep] = self.u.clone(memory_format=torch.preserve_format)
 
     def simulate(self, callback=None, setIC=None, setBC=None, setForcing=None, tol=1e-8):
-        """src/diffusion.jl:110-137."""
+        """src/diffusion.jl:110-137.  Without a callback or setBC/setForcing
+        closures (f and ub then stay as they are) the whole loop runs as one
+        ``run`` on the device."""
         if setIC is not None:
             setIC(self.u, self.msh.x, self.msh.y, self.tstep.time[0])
         if callback is not None:
             callback(self)
+        if callback is None and setBC is None and setForcing is None and not self.checkpoint_every:
+            ts = self.tstep
+            n, t = 0, ts.time[0]
+            while t <= ts.Tf:
+                if ts.dt == 0.0 and t >= 1e-12:
+                    raise ValueError("dt = 0 with Ti > 0 never leaves the loop of src/diffusion.jl:130")
+                t += ts.dt
+                n += 1
+                if t < 1e-12:
+                    break
+            forcing = [(self.f.clone(), lambda _t: 1.0)] if torch.count_nonzero(self.f) else []
+            boundary = [(self.ub.clone(), lambda _t: 1.0)] if torch.count_nonzero(self.ub) else []
+            self.run(n, forcing, boundary, tol=tol)
+            return
         while self.tstep.time[0] <= self.tstep.Tf:
             self.evolve(setBC, setForcing, tol)
             if callback is not None:

@@ -143,7 +143,7 @@ def test_diffusion_driver_matches_oracle(gpu):
                 - np.sin(kx * np.pi * x) * np.sin(ky * np.pi * y) * np.sin(kt * np.pi * t) * (kt * np.pi))
 
     dt, steps, k = 1e-3, 10, 1
-    dfn = S.Diffusion("DDDD", md, Ti=0.0, Tf=steps * dt, dt=dt, k=k, nu=nu)
+    dfn = S.Diffusion("DDDD", md, Ti=0.0, Tf=steps * dt, dt=dt, k=k, nu=nu, jacobi=True)
     x, y = host(md.x), host(md.y)
     dfn.u.copy_(S.as_local(ut(x, y, 0.0)))
     M = O.generateMask(["D"] * 4, mo)

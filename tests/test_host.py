@@ -70,6 +70,7 @@ def test_header_constants_match_binding():
     src = open(os.path.join(ROOT, "include", "sem_b200.h")).read()
     defines = dict(re.findall(r"#define\s+(SEM_[A-Z_]+)\s+(\d+)", src))
     assert int(defines["SEM_VARIANTS"]) == _lib.SEM_VARIANTS
+    assert int(defines["SEM_BDF_MAX_ORDER"]) == _lib.SEM_BDF_MAX_ORDER
     assert int(defines["SEM_NOALLOC_MAX_LOCAL"]) > 0
 
 
@@ -86,6 +87,36 @@ def test_argument_validation_needs_no_gpu(built):
     assert lib.sem_mask(None, None, None, -1, None) == _lib.SEM_ERR_BAD_ARG
     a = np.zeros(4)
     assert lib.sem_abu(None, 0, 0, None, 0, 0, a.ctypes.data, 2, 2, a.ctypes.data, None) == _lib.SEM_ERR_BAD_ARG
+
+
+def test_bdf_coeffs_in_library_match_oracle(built):
+    """sem_bdf_coeffs (host code of the library) against the oracle's
+    bdfExtK (src/time.jl:31-53), including the steady branch and the
+    zero-padded first steps of BDF3."""
+    lib = built
+    dt = 1e-3
+    cases = [([0.0] * 4, 3), ([dt, 0.0, 0.0, 0.0], 3), ([2 * dt, dt, 0.0, 0.0], 3),
+             ([3 * dt, 2 * dt, dt, 0.0], 3), ([0.1, 0.0], 1), ([0.5, 0.4, 0.25], 2),
+             ([0.7, 0.6, 0.45, 0.3, 0.2, 0.1, 0.0], 6)]
+    t = 0.0
+    hist = [0.0] * 4
+    for _ in range(5):  # the additions of TimeStepper.advance
+        hist = [hist[0]] + hist[:-1]
+        t += dt
+        hist[0] = t
+        cases.append((list(hist), 3))
+    for tt, k in cases:
+        a = (ctypes.c_double * k)()
+        b = (ctypes.c_double * (k + 1))()
+        assert lib.sem_bdf_coeffs(k, (ctypes.c_double * (k + 1))(*tt), a, b) == _lib.SEM_OK
+        ao, bo = O.bdfExtK(tt, k)
+        np.testing.assert_allclose(np.array(a[:]), ao, rtol=1e-15, atol=0)
+        np.testing.assert_allclose(np.array(b[:]), bo, rtol=1e-15, atol=0)
+    z = (ctypes.c_double * 8)()
+    assert lib.sem_bdf_coeffs(0, z, z, z) == _lib.SEM_ERR_BAD_ARG
+    assert lib.sem_bdf_coeffs(_lib.SEM_BDF_MAX_ORDER + 1, z, z, z) == _lib.SEM_ERR_BAD_ARG
+    d = _lib.BdfDesc()
+    assert lib.sem_bdf_run(None, ctypes.byref(d), z, None, None, None, None) == _lib.SEM_ERR_BAD_ARG
 
 
 def test_product_has_no_oracle_imports():
