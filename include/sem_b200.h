@@ -195,6 +195,18 @@ int sem_grad(sem_mesh_t* mesh, const double* u, double* ux, double* uy, sem_stre
  * passes them to ABu */
 int sem_grad_t(sem_mesh_t* mesh, const double* u, double* ux, double* uy, sem_stream_t stream);
 
+/* ---- advection (src/advect.jl:27-64), unassembled (no QQ', no mask, as the
+ * reference returns it).  sem_advect: B .* (ux Tx + uy Ty) with
+ * (Tx, Ty) = grad(T).  sem_advect_dealiased: grad T and the velocity
+ * interpolated to the dealiasing grid with ABu(Js,Jr,.) (Jr mr x n, Js ms x n,
+ * host, column-major), multiplied there by the dealiasing mesh's mass Bd
+ * (device, (mr Ex) x (ms Ey)), and brought back with ABu(Js',Jr',.). */
+int sem_advect(sem_mesh_t* mesh, const double* T, const double* ux, const double* uy, double* out,
+               sem_stream_t stream);
+int sem_advect_dealiased(sem_mesh_t* mesh, int mr, int ms, const double* Jr, const double* Js,
+                         const double* Bd, const double* T, const double* ux, const double* uy,
+                         double* out, sem_stream_t stream);
+
 /* ---- solver: pcg(b,opA;opM,mult,ifv,tol,maxiter) (src/pcg.jl:16-60) with
  * opA = mask(QQ'(hlmz(.,nu,k))) (src/diffusion.jl:36-45) */
 enum sem_precond { SEM_PRECOND_NONE = 0, SEM_PRECOND_JACOBI = 1 };
@@ -342,6 +354,32 @@ typedef struct {
 } sem_bdf_desc;
 int sem_bdf_run(sem_mesh_t* mesh, const sem_bdf_desc* desc, double* time, double* u,
                 double* const* uh, sem_solve_info* info, sem_stream_t stream);
+
+/* ---- single-domain spectral operator algebra (src/Spectral/Operators.jl,
+ * src/Spectral/OperatorBasics.jl) on batches of fields.  Fields are DEVICE
+ * column-major arrays, `batch` of them back to back; operator matrices are
+ * DEVICE column-major; a NULL matrix is the identity (the sparse I of
+ * gradOp, src/Spectral/LagrangePolynomialSpace.jl:112-138).  FP64.
+ * sem_mode_product: V[a,i,b] = sum_k M[i,k] U[a,k,b] for U of shape
+ *   (inner, n, outer) and M m x n: the building block of the others.
+ * sem_tp2d: TensorProductOp2D mul! (Operators.jl:150-198): V = A U B' per
+ *   field, U na x nb, V ma x mb.
+ * sem_tp3d: (C (x) B (x) A) U per field, U na x nb x nc (the 3D
+ *   tensor_product!, Operators.jl:133-145, with the B mode applied).
+ * sem_axpby: out = alpha x + beta y (AffineOp, OperatorBasics.jl:130-210;
+ *   x or y NULL drops its term).
+ * sem_diag_apply: v = d .* u, or u ./ d when invert (DiagonalOp mul!/ldiv!,
+ *   Operators.jl:37-75). */
+int sem_mode_product(const double* M, int m, int n, const double* U, double* V, int64_t inner,
+                     int64_t outer, sem_stream_t stream);
+int sem_tp2d(const double* A, int ma, int na, const double* B, int mb, int nb, const double* U, double* V,
+             int batch, sem_stream_t stream);
+int sem_tp3d(const double* A, int ma, int na, const double* B, int mb, int nb, const double* C, int mc,
+             int nc, const double* U, double* V, int batch, sem_stream_t stream);
+int sem_axpby(double alpha, const double* x, double beta, const double* y, double* out, int64_t len,
+              sem_stream_t stream);
+int sem_diag_apply(const double* d, const double* u, double* v, int64_t len, int invert,
+                   sem_stream_t stream);
 
 /* ---- instrumentation (no counterpart in the reference, which only prints
  * @time): CUDA-event timing of every launch of the fused element-operator

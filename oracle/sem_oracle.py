@@ -485,6 +485,38 @@ def pcg(b, opA, opM=None, mult=None, ifv=False, tol=1e-8, maxiter=None, info=Non
 
 
 # --------------------------------------------------------------------------
+# gradient and advection
+# --------------------------------------------------------------------------
+
+
+def grad(u, msh: Mesh):
+    """``src/grad.jl:16-34``: ux = rx ur + sx us, uy = ry ur + sy us with
+    ur = ABu([],Dr,u), us = ABu(Ds,[],u); no continuity across elements."""
+    ur = ABu(None, msh.Dr, u)
+    us = ABu(msh.Ds, None, u)
+    return msh.rx * ur + msh.sx * us, msh.ry * ur + msh.sy * us
+
+
+def advect(T, ux, uy, msh: Mesh):
+    """``src/advect.jl:27-43``: B .* (ux Tx + uy Ty), unassembled."""
+    Tx, Ty = grad(T, msh)
+    return (ux * Tx + uy * Ty) * msh.B
+
+
+def advect_dealiased(T, ux, uy, mshV: Mesh, Bd, Jr, Js):
+    """``src/advect.jl:45-64``: the velocity and grad T interpolated to the
+    dealiasing grid (ABu(Js,Jr,.)), multiplied there by its mass Bd, and
+    brought back with ABu(Js',Jr',.)."""
+    Tx, Ty = grad(T, mshV)
+    JTx = ABu(Js, Jr, Tx)
+    JTy = ABu(Js, Jr, Ty)
+    Jux = ABu(Js, Jr, ux)
+    Juy = ABu(Js, Jr, uy)
+    JCu = (Jux * JTx + Juy * JTy) * Bd
+    return ABu(Js.T, Jr.T, JCu)
+
+
+# --------------------------------------------------------------------------
 # time stepping and the Diffusion driver
 # --------------------------------------------------------------------------
 

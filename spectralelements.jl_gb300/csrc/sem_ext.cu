@@ -3,7 +3,8 @@
 //   * the dealiased (over-integrated) Laplacian, laplace(u,Jr,Js,Dr,Ds,G11,G12,G22)
 //     (src/lapl.jl:83-103), with the metric terms on the fine quadrature grid;
 //   * the functional mass with interpolation, J'(B .* (J u)) (src/mass.jl:32-50);
-//   * grad and grad' (src/grad.jl:16-63).
+//   * grad and grad' (src/grad.jl:16-63);
+//   * advection B .* (u.grad T), plain and dealiased (src/advect.jl:27-64).
 // Each follows the reference's sequence of ABu calls and broadcasts; the
 // broadcasts are separate multiplies and adds (no fused multiply-add), as
 // Julia's @. evaluates them.  Temporaries are stream-ordered allocations.
@@ -50,6 +51,15 @@ __global__ void k_add(const double* __restrict__ x, const double* __restrict__ y
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
        i += (long long)gridDim.x * blockDim.x)
     o[i] = __dadd_rn(x[i], y[i]);
+}
+
+// o = (ux .* Tx + uy .* Ty) .* B
+__global__ void k_advect_mix(const double* __restrict__ ux, const double* __restrict__ Tx,
+                             const double* __restrict__ uy, const double* __restrict__ Ty,
+                             const double* __restrict__ B, double* __restrict__ o, long long len) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (long long)gridDim.x * blockDim.x)
+    o[i] = __dmul_rn(__dadd_rn(__dmul_rn(ux[i], Tx[i]), __dmul_rn(uy[i], Ty[i])), B[i]);
 }
 
 // transpose of a column-major r x c host matrix
@@ -220,6 +230,56 @@ int sem_grad_t(sem_mesh_t* m, const double* u, double* ux, double* uy, sem_strea
     k_add<<<grid_of(L), kThreadsX, 0, s>>>(a, g, outs[q], L);
     SEM_CUDA(cudaGetLastError());
   }
+  return SEM_OK;
+}
+
+int sem_advect(sem_mesh_t* m, const double* T, const double* ux, const double* uy, double* out,
+               sem_stream_t stream) {
+  if (!m || !T || !ux || !uy || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long L = m->g.NX * m->g.NY;
+  Scratch t(s);
+  double *Tx, *Ty;
+  SEM_CHECK(t.get(L, &Tx));
+  SEM_CHECK(t.get(L, &Ty));
+  SEM_CHECK(sem_grad(m, T, Tx, Ty, stream));
+  k_advect_mix<<<grid_of(L), kThreadsX, 0, s>>>(ux, Tx, uy, Ty, m->B, out, L);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int sem_advect_dealiased(sem_mesh_t* m, int mr, int ms, const double* Jr, const double* Js,
+                         const double* Bd, const double* T, const double* ux, const double* uy,
+                         double* out, sem_stream_t stream) {
+  if (!m || !Bd || !T || !ux || !uy || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  const int n = m->g.n;
+  SEM_CHECK(check_block(Jr, mr, n, "Jr"));
+  SEM_CHECK(check_block(Js, ms, n, "Js"));
+  cudaStream_t s = (cudaStream_t)stream;
+  const int NX = (int)m->g.NX, NY = (int)m->g.NY, MX = mr * m->g.Ex, MY = ms * m->g.Ey;
+  const long long L = (long long)NX * NY, Lf = (long long)MX * MY;
+  double Jrt[kMaxBlock * kMaxBlock], Jst[kMaxBlock * kMaxBlock];
+  transpose(Jr, mr, n, Jrt);
+  transpose(Js, ms, n, Jst);
+  Scratch t(s);
+  double *Tx, *Ty, *JTx, *JTy, *Jux, *Juy, *JCu;
+  SEM_CHECK(t.get(L, &Tx));
+  SEM_CHECK(t.get(L, &Ty));
+  SEM_CHECK(t.get(Lf, &JTx));
+  SEM_CHECK(t.get(Lf, &JTy));
+  SEM_CHECK(t.get(Lf, &Jux));
+  SEM_CHECK(t.get(Lf, &Juy));
+  SEM_CHECK(t.get(Lf, &JCu));
+  SEM_CHECK(sem_grad(m, T, Tx, Ty, stream));
+  // JTx = ABu(Js,Jr,Tx), JTy, Jux, Juy likewise
+  SEM_CHECK(launch_abu(Js, ms, n, Jr, mr, n, Tx, NX, NY, JTx, s));
+  SEM_CHECK(launch_abu(Js, ms, n, Jr, mr, n, Ty, NX, NY, JTy, s));
+  SEM_CHECK(launch_abu(Js, ms, n, Jr, mr, n, ux, NX, NY, Jux, s));
+  SEM_CHECK(launch_abu(Js, ms, n, Jr, mr, n, uy, NX, NY, Juy, s));
+  // JCu = (Jux JTx + Juy JTy) .* Bd; Cu = ABu(Js',Jr',JCu)
+  k_advect_mix<<<grid_of(Lf), kThreadsX, 0, s>>>(Jux, JTx, Juy, JTy, Bd, JCu, Lf);
+  SEM_CUDA(cudaGetLastError());
+  SEM_CHECK(launch_abu(Jst, n, ms, Jrt, n, mr, JCu, MX, MY, out, s));
   return SEM_OK;
 }
 

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu", "sem_time.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu"]
 
 
 class SemError(RuntimeError):
@@ -157,6 +157,8 @@ SIGNATURES = {
     "sem_mass_dealiased": (_I, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
     "sem_grad": (_I, [_P, _P, _P, _P, _P]),
     "sem_grad_t": (_I, [_P, _P, _P, _P, _P]),
+    "sem_advect": (_I, [_P, _P, _P, _P, _P, _P]),
+    "sem_advect_dealiased": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sem_pcg": (_I, [_P, ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
     "sem_pcg_noalloc": (_I, [_I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P,
                              ctypes.POINTER(PcgOpts), _P, _P, ctypes.POINTER(SolveInfo), _P]),
@@ -172,6 +174,11 @@ SIGNATURES = {
     "sem_bdf_rhs": (_I, [_P, _D, _I, ctypes.POINTER(_D), _P, _P, ctypes.POINTER(ctypes.c_void_p), _P, _P]),
     "sem_bdf_run": (_I, [_P, ctypes.POINTER(BdfDesc), ctypes.POINTER(_D), _P,
                          ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(SolveInfo), _P]),
+    "sem_mode_product": (_I, [_P, _I, _I, _P, _P, _L, _L, _P]),
+    "sem_tp2d": (_I, [_P, _I, _I, _P, _I, _I, _P, _P, _I, _P]),
+    "sem_tp3d": (_I, [_P, _I, _I, _P, _I, _I, _P, _I, _I, _P, _P, _I, _P]),
+    "sem_axpby": (_I, [_D, _P, _D, _P, _P, _L, _P]),
+    "sem_diag_apply": (_I, [_P, _P, _P, _L, _I, _P]),
     "sem_timing_enable": (_I, [_I]),
     "sem_timing_read": (_I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
 }

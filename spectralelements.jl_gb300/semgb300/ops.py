@@ -291,3 +291,29 @@ def gradT(u, msh):
     ux, uy = msh.empty(), msh.empty()
     _lib.check(lib.sem_grad_t(msh.handle, u.data_ptr(), ux.data_ptr(), uy.data_ptr(), stream_ptr()))
     return ux, uy
+
+
+def advect(T, ux, uy, mshV, mshD=None, Jr=None, Js=None):
+    """advect (src/advect.jl:27-78): B .* (ux Tx + uy Ty) with (Tx, Ty) =
+    grad(T), unassembled.  With a dealiasing mesh mshD the velocity and grad T
+    are interpolated to its grid (Jr = interpMat(mshD.zr, mshV.zr) and Js
+    likewise, unless given), multiplied there by mshD.B and brought back with
+    ABu(Js',Jr',.)."""
+    from .host import interpMat
+    lib = _lib.load()
+    T, ux, uy = (_field(v, mshV) for v in (T, ux, uy))
+    out = mshV.empty()
+    if mshD is None:
+        _lib.check(lib.sem_advect(mshV.handle, T.data_ptr(), ux.data_ptr(), uy.data_ptr(),
+                                  out.data_ptr(), stream_ptr()))
+        return out
+    if mshD.Ex != mshV.Ex or mshD.Ey != mshV.Ey:
+        raise ValueError("the dealiasing mesh must have the same elements")
+    Jr = interpMat(mshD.zr, mshV.zr) if Jr is None else np.asarray(Jr, dtype=np.float64)
+    Js = interpMat(mshD.zs, mshV.zs) if Js is None else np.asarray(Js, dtype=np.float64)
+    Jrb, Jsb = np.asfortranarray(Jr), np.asfortranarray(Js)
+    Bd = as_local(mshD.B)
+    _lib.check(lib.sem_advect_dealiased(mshV.handle, Jrb.shape[0], Jsb.shape[0], Jrb.ctypes.data,
+                                        Jsb.ctypes.data, Bd.data_ptr(), T.data_ptr(), ux.data_ptr(),
+                                        uy.data_ptr(), out.data_ptr(), stream_ptr()))
+    return out
