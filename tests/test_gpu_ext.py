@@ -104,9 +104,10 @@ def test_advect_plain_and_dealiased(gpu, n, m, Ex, Ey, per, amp):
     got = host(S.advect(S.as_local(T), S.as_local(ux), S.as_local(uy), md, mfd))
     ref = O.advect_dealiased(T, ux, uy, mo, mfo.B, J, J)
     assert rel_l2(got, ref) < TOL
-    # explicit Jr, Js give the same result
+    # explicit Jr, Js (the oracle's interpMat, which may differ from the
+    # package's in the last bit) give the same result
     got2 = host(S.advect(S.as_local(T), S.as_local(ux), S.as_local(uy), md, mfd, J, J))
-    assert np.array_equal(got, got2)
+    assert rel_l2(got2, got) < 1e-14
 
 
 def test_advect_dealiased_integrates_exactly(gpu):
