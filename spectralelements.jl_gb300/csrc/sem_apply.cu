@@ -124,6 +124,8 @@ int num_sms() {
 int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
                      int TY, cudaStream_t s) {
   if (!(mode & M_GS)) return SEM_OK;
+  if (g.NX >= (1LL << 31) || g.NY >= (1LL << 31))
+    return set_error(SEM_ERR_UNSUPPORTED, "local dimensions must be below 2^31");
   FixArgs f;
   f.n = g.n;
   f.Ex = g.Ex;
@@ -143,12 +145,23 @@ int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, con
   long long along = std::max(std::max(f.NX, f.NY), f.nxi * f.nyi);
   long long bx = (along + threads - 1) / threads;
   if (bx > 64) bx = 64;
-  const dim3 grid((unsigned)bx, (unsigned)std::min(nI, 65535LL));
+  // a programmatic dependent of the operator kernel before it on the stream:
+  // its CTAs are scheduled once every operator CTA has started, and wait
+  // (griddepcontrol.wait) for the operator grid's completion
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)bx, (unsigned)std::min(nI, 65535LL));
+  cfg.blockDim = dim3(threads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
   if (precision == SEM_F32)
-    k_dss_fixup<float><<<grid, threads, 0, s>>>(static_cast<float*>(out), f);
+    SEM_CUDA(cudaLaunchKernelEx(&cfg, k_dss_fixup<float>, static_cast<float*>(out), f));
   else
-    k_dss_fixup<double><<<grid, threads, 0, s>>>(static_cast<double*>(out), f);
-  SEM_CUDA(cudaGetLastError());
+    SEM_CUDA(cudaLaunchKernelEx(&cfg, k_dss_fixup<double>, static_cast<double*>(out), f));
   return SEM_OK;
 }
 

@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   V* S1 = S0 + TE;                         // in-place work buffer
   GT* R = reinterpret_cast<GT*>(S1 + TE);  // staged G11, G12, G22 (variant 3)
 
+  pdl_trigger();  // the cross-tile fixup may be scheduled now; it waits for this grid
   if (a.skip && *a.skip) return;
   const int t = threadIdx.x;
   const int elem = t / N;

@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   V* S2 = S1 + TE;
   IO* R = reinterpret_cast<IO*>(S2 + TE);  // staged raw inputs (STAGE): slot * TE + ...
 
+  pdl_trigger();  // the cross-tile fixup may be scheduled now; it waits for this grid
   if (a.skip && *a.skip) return;
   const int t = threadIdx.x;
   const int elem = t / N;
@@ -395,7 +396,7 @@ __device__ __forceinline__ void fix_xline(IO* out, const FixArgs& f, long long a
     done(r, c, v);
   };
   for (long long c = c_begin; c < c_end; c += stride) {
-    const int ey = (int)((unsigned long long)c / n);
+    const int ey = (int)((unsigned)c / n);  // NX, NY < 2^31 (checked at launch)
     const int j = (int)(c - (long long)ey * f.n);
     if (xcross_row(ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner of two cross-tile interfaces
     if (j == 0 && ey > 0) continue;                            // in-tile y pair, done from column c-1
@@ -427,7 +428,7 @@ __device__ __forceinline__ void fix_yline(IO* out, const FixArgs& f, long long b
   const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
   const long long cr = b * f.n;
   for (long long r = r_begin; r < r_end; r += stride) {
-    const int ex = (int)((unsigned long long)r / n);
+    const int ex = (int)((unsigned)r / n);
     const int i = (int)(r - (long long)ex * f.n);
     if (xcross_row(ex, i, f.n, f.Ex, f.TX, perx)) continue;
     const IO s = io_add(fix_ld(out + r + cl * f.NX), fix_ld(out + r + cr * f.NX));
@@ -485,6 +486,7 @@ __device__ __forceinline__ void fix_interface(IO* __restrict__ out, const FixArg
 
 template <class IO>
 __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
+  pdl_wait();  // launched as a programmatic dependent of the operator kernel
   if (f.skip && *f.skip) return;
   const long long nI = fix_rows(f);
   const long long stride = (long long)gridDim.x * blockDim.x;

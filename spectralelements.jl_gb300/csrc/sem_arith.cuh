@@ -132,6 +132,15 @@ __device__ __forceinline__ float masked_zero(float v) {
 }
 
 // correctly rounded sums of stored values (never contracted into an FMA)
+// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later): a
+// kernel calls pdl_trigger() to let the next kernel of its stream, when that
+// one is launched with programmatic stream serialization, be scheduled before
+// it has finished; that next kernel calls pdl_wait() before it reads anything
+// the first one writes (it returns once the first grid has completed and its
+// memory operations are visible).  Both are no-ops without such a launch.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ double io_add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float io_add(float a, float b) { return __fadd_rn(a, b); }
 
