@@ -186,7 +186,8 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   V* S1 = S0 + TE;                         // in-place work buffer
   GT* R = reinterpret_cast<GT*>(S1 + TE);  // staged G11, G12, G22 (variant 3)
 
-  pdl_trigger();  // the cross-tile fixup may be scheduled now; it waits for this grid
+  pdl_trigger();  // the next kernel (the cross-tile fixup) may be scheduled now
+  pdl_wait();     // a no-op unless this launch is a programmatic dependent
   if (a.skip && *a.skip) return;
   const int t = threadIdx.x;
   const int elem = t / N;

@@ -54,7 +54,8 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
   GT* RG = reinterpret_cast<GT*>(S1 + TE);  // stage: G11, G12, G22, B  [slot][j][thread]
   IO* RU = reinterpret_cast<IO*>(RG + 4 * N * T);  // stage: u [j][thread]
 
-  pdl_trigger();  // the cross-tile fixup may be scheduled now; it waits for this grid
+  pdl_trigger();  // the next kernel (the cross-tile fixup) may be scheduled now
+  pdl_wait();     // a no-op unless this launch is a programmatic dependent
   if (a.skip && *a.skip) return;
   const int t = threadIdx.x;
   const int elem = t / N;

@@ -211,7 +211,8 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   V* S2 = S1 + TE;
   IO* R = reinterpret_cast<IO*>(S2 + TE);  // staged raw inputs (STAGE): slot * TE + ...
 
-  pdl_trigger();  // the cross-tile fixup may be scheduled now; it waits for this grid
+  pdl_trigger();  // the next kernel (the cross-tile fixup) may be scheduled now
+  pdl_wait();     // a no-op unless this launch is a programmatic dependent
   if (a.skip && *a.skip) return;
   const int t = threadIdx.x;
   const int elem = t / N;

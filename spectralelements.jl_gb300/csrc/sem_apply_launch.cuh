@@ -43,6 +43,26 @@ static void fill_eo(EOCoef<N, typename P::v>& c, const double* src) {
   }
 }
 
+// kern<<<grid, block, smem, s>>>(args...), as a programmatic dependent of
+// the previous kernel on s when pdl is set
+template <class... KArgs, class... Args>
+static int launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                         Args... args) {
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  SEM_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+  return SEM_OK;
+}
+
 template <class P, int N, bool STAGE>
 static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
                           cudaStream_t s) {
@@ -85,8 +105,7 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
   auto* ev = timing_slot();
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
-  kern<<<grid, TS::THREADS, smem, s>>>(a);
-  SEM_CUDA(cudaGetLastError());
+  SEM_CHECK(launch_kernel(kern, grid, TS::THREADS, smem, s, c.pdl != 0, a));
   if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
   return SEM_OK;
 }
@@ -152,8 +171,7 @@ static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCal
   dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
   auto* ev = timing_slot();
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
-  kern<<<grid, TS::THREADS, smem, s>>>(a);
-  SEM_CUDA(cudaGetLastError());
+  SEM_CHECK(launch_kernel(kern, grid, TS::THREADS, smem, s, c.pdl != 0, a));
   if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
   return SEM_OK;
 }
@@ -184,8 +202,7 @@ static int launch_apply_v3(const Grid& g, const OperatorSet* ops, const ApplyCal
   const long long grid = (tiles + rounds - 1) / rounds;
   auto* ev = timing_slot();
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
-  kern<<<(unsigned)grid, TS::THREADS, smem, s>>>(a, tiles_x, (int)tiles);
-  SEM_CUDA(cudaGetLastError());
+  SEM_CHECK(launch_kernel(kern, dim3((unsigned)grid), TS::THREADS, smem, s, c.pdl != 0, a, tiles_x, (int)tiles));
   if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
   return SEM_OK;
 }

@@ -5,6 +5,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <cstring>
 #include <string>
 
 #include "../../include/sem_b200.h"
@@ -226,7 +227,27 @@ struct ApplyCall {
   void* cg_p;
   const double* cg_beta;
   void* cg_dpart;
+  int pdl;         // launch as a programmatic dependent of the previous kernel on the stream
 };
+
+// launch kern<<<grid, block, 0, s>>>(args...) as a programmatic dependent of
+// the previous kernel on s (the kernel must call griddepcontrol.wait before it
+// touches memory)
+template <class... KArgs, class... Args>
+int launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SEM_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+  return SEM_OK;
+}
 
 // number of CTAs (element tiles) of a CG-fused operator launch on grid g
 long long cg_apply_parts(const Grid& g);

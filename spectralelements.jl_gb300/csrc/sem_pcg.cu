@@ -214,6 +214,8 @@ __global__ void k_scal_replace(const double* part, int np, Scalars* sc, double t
 template <class T>
 __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ p,
                        const Scalars* sc, long long L) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   const T beta = (T)sc->beta;
   const bool jac = dinv != nullptr;
@@ -225,6 +227,8 @@ __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* _
 template <class T>
 __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, double* part,
                           const Scalars* sc, Grid g) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   Acc<T> acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
@@ -238,6 +242,8 @@ __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, dou
 // alpha = t / (p . A p) from the per-CTA double-float parts of a CG-fused
 // operator launch, summed in a fixed order (one block)
 __global__ void k_scal_alpha_df(const df* part, long long np, Scalars* sc) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   df x = {0.0f, 0.0f};
   for (long long i = threadIdx.x; i < np; i += blockDim.x) x = df_add(x, part[i]);
@@ -251,6 +257,8 @@ __global__ void k_scal_alpha_df(const df* part, long long np, Scalars* sc) {
 }
 
 __global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   double res[1];
   const bool mx[1] = {false};
@@ -266,6 +274,8 @@ template <class T>
 __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                          const T* __restrict__ Ap, const T* __restrict__ dinv, double* part,
                          const Scalars* sc, Grid g) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   const T alpha = (T)sc->alpha;
   Acc<T> acc;
@@ -285,6 +295,8 @@ __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restri
 }
 
 __global__ void k_scal_beta(const double* part, int np, Scalars* sc) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   double res[2];
   const bool mx[2] = {false, true};
@@ -532,18 +544,26 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
   const long long L = cx.g.NX * cx.g.NY;
   const unsigned nb = nblocks(L);
   const bool fused = c.cg_p != nullptr;  // direction and p.Ap inside the operator launch
+  // every launch of a chunk is a programmatic dependent of the one before it:
+  // it is scheduled while its predecessor finishes and waits for it
+  // (griddepcontrol.wait) before it touches memory
+  ApplyCall cp = c;
+  cp.pdl = 1;
+  const long long np = cg_apply_parts(cx.g);
   for (int it = 0; it < check_every; ++it) {
     if (fused) {
-      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
-      k_scal_alpha_df<<<1, kRT, 0, s>>>(w.dpart, cg_apply_parts(cx.g), w.sc);
+      SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
+      SEM_CHECK(launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc));
     } else {
-      k_pdir<T><<<nb, kRT, 0, s>>>(r, dinv, p, w.sc, L);
-      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
-      k_dot_pap<T><<<nb, kRT, 0, s>>>(p, Ap, w.part, w.sc, gv);
-      k_scal_alpha<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+      SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
+      SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
+      SEM_CHECK(launch_pdl(k_dot_pap<T>, nb, kRT, s, (const T*)p, (const T*)Ap, w.part,
+                           (const Scalars*)w.sc, gv));
+      SEM_CHECK(launch_pdl(k_scal_alpha, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
     }
-    k_update<T><<<nb, kRT, 0, s>>>(x, r, p, Ap, dinv, w.part, w.sc, gv);
-    k_scal_beta<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc);
+    SEM_CHECK(launch_pdl(k_update<T>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
+                         (const Scalars*)w.sc, gv));
+    SEM_CHECK(launch_pdl(k_scal_beta, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
   }
   SEM_CUDA(cudaGetLastError());
   SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
