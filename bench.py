@@ -231,15 +231,12 @@ def run_ours(args, rank, world, local_rank):
     x_pin = torch.from_numpy(np.asfortranarray(u_h)).pin_memory()
     x_pin = x_pin if x_pin.stride() == (1, nx) else x_pin.t().contiguous().t().pin_memory()
     y_pin = torch.empty_strided((nx, ny), (1, nx), dtype=torch.float64, pin_memory=True)
-    x_dev = msh.empty()
     op = S.HelmholtzOp(msh, NU, LAM)
     e2e_ms = []
     for i in range(args.warmup + args.steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        x_dev.copy_(x_pin, non_blocking=True)
-        y = op(x_dev)
-        y_pin.copy_(y, non_blocking=True)
+        op.apply_host(x_pin, y_pin)  # sem_hlmz_host: host in, host out, copies overlapped in slabs
         b.record(stream)
         b.synchronize()
         if i >= args.warmup:
@@ -247,9 +244,11 @@ def run_ours(args, rank, world, local_rank):
     e2e_step, e2e_per_s = replica_throughput(sum(e2e_ms) / len(e2e_ms), G, world, dev)
     e2e = {"value": e2e_per_s / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L, "ms_per_step": e2e_step,
-           "api": "semgb300.HelmholtzOp (sem_hlmz through ctypes), pinned host buffers"}
+           "api": "semgb300.HelmholtzOp.apply_host (sem_hlmz_host through ctypes): pinned host "
+                  "buffers in and out, the copies overlapped with the kernels in 8 slabs of tile rows"}
     # parity of this very output against the F64 arithmetic
     y_dev = op(u)
+    e2e["matches_device_call"] = bool(torch.equal(y_pin, y_dev.cpu()))
     msh.set_precision(S.SEM_F64)
     y64 = op(u)
     t64 = time_apply(lambda: op(u), stream, 5)

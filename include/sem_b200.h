@@ -148,6 +148,17 @@ int sem_lapl_nu(sem_mesh_t* mesh, const double* nu, const double* u, double* out
  * nu_field (device) overrides the scalar nu when not NULL */
 int sem_hlmz(sem_mesh_t* mesh, const double* nu_field, double nu, double k,
              const double* u, double* out, unsigned flags, sem_stream_t stream);
+/* hlmz with mask(QQ') on HOST buffers (the end-to-end call): u_host and
+ * out_host are column-major host arrays of the local layout.  The field moves
+ * in and out in `slabs` slabs of element-tile rows (0: 8), so the copies
+ * overlap the kernels; pinned host memory (cudaHostAlloc / cudaHostRegister)
+ * is needed for that overlap, pageable memory works with serialised copies.
+ * The result is bit-identical to sem_hlmz on device buffers.  nu_field, when
+ * given, is a DEVICE field.  Asynchronous on `stream`: out_host is complete
+ * when the stream is.  The handle keeps two device buffers of the field's
+ * size and two streams for the copies. */
+int sem_hlmz_host(sem_mesh_t* mesh, const double* nu_field, double nu, double k, const double* u_host,
+                  double* out_host, unsigned flags, int slabs, sem_stream_t stream);
 /* variable-coefficient operator D'(nu G)D u + k B u with nu (device field)
  * folded into G11/G12/G22 at every node, as examples/semPS.jl:163-165 and
  * examples/p2d_explicit.jl:105-107 build G from visc */

@@ -171,6 +171,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (m->Gdf) cudaFree(m->Gdf);
   if (m->fix_ctr) cudaFree(m->fix_ctr);
   free_graph_cache(m);
+  free_host_pipe(m);
   if (m->ws) cudaFree(m->ws);
   if (m->info) cudaFree(m->info);
   if (m->ops) free_operator_set(m->ops);

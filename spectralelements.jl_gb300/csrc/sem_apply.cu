@@ -122,7 +122,7 @@ int num_sms() {
 }
 
 int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
-                     int TY, cudaStream_t s) {
+                     int TY, cudaStream_t s, long long key_lo, long long key_hi) {
   if (!(mode & M_GS)) return SEM_OK;
   if (g.NX >= (1LL << 31) || g.NY >= (1LL << 31))
     return set_error(SEM_ERR_UNSUPPORTED, "local dimensions must be below 2^31");
@@ -136,6 +136,8 @@ int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, con
   f.NY = g.NY;
   f.mode = mode;
   f.skip = skip;
+  f.key_lo = key_lo;
+  f.key_hi = key_hi;
   const bool perx = (mode & M_PERX) != 0, pery = (mode & M_PERY) != 0;
   f.nxi = (g.Ex - 1) / f.TX + (perx ? 1 : 0);
   f.nyi = (g.Ey - 1) / f.TY + (pery ? 1 : 0);
@@ -181,6 +183,24 @@ int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cuda
   if (tile[0] == 0) return SEM_OK;  // completed inside the kernel
   return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s);
 }
+
+int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c, long long key_lo,
+                        long long key_hi, cudaStream_t s) {
+  if (c.tyn <= 0) return set_error(SEM_ERR_BAD_ARG, "empty tile-row window");
+  int st;
+  int tile[2] = {0, 0};
+  const bool hi = g.n >= 10;
+  if (c.precision == SEM_F64)
+    st = hi ? launch_apply_f64_hi(g, ops, c, s, tile) : launch_apply_f64_lo(g, ops, c, s, tile);
+  else if (c.precision == SEM_F64_DF)
+    st = hi ? launch_apply_df_hi(g, ops, c, s, tile) : launch_apply_df_lo(g, ops, c, s, tile);
+  else
+    return set_error(SEM_ERR_BAD_ARG, "tile-row windows serve SEM_F64 and SEM_F64_DF");
+  if (st != SEM_OK) return st;
+  return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s, key_lo, key_hi);
+}
+
+void tile_shape_of(int n, int* tx, int* ty) { tile_shape(n, tx, ty); }
 
 long long cg_apply_parts(const Grid& g) {
   int tx = 1, ty = 1;

@@ -55,6 +55,7 @@ struct Apply2Args {
   const int* skip;
   unsigned* ctr;          // interface arrival counters (in-kernel completion), or NULL
   int tiles_x, tiles_y;   // element tiles of the launch (in-kernel completion)
+  int ty0;                // first element-tile row of the launch (a window of the grid)
   // CG-fused launch: u = p = dinv .* r + beta p_old is formed here (p read and
   // written in place) and every CTA stores its share of p . A p in dpart
   const io* r;
@@ -138,6 +139,8 @@ __device__ __forceinline__ void finish_tile_interfaces(IO* out, int n, int Ex, i
   f.NY = (long long)Ey * n;
   f.mode = mode;
   f.skip = nullptr;
+  f.key_lo = 0;
+  f.key_hi = 1LL << 62;
   f.nxi = f.nyi = 0;
   auto none = [](long long, long long, IO) {};
   for (int k = 0; k < 8; ++k) {
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   const int exl = elem % TX;
   const int eyl = elem / TX;
   const int ex = blockIdx.x * TX + exl;
-  const int ey = blockIdx.y * TY + eyl;
+  const int ey = (blockIdx.y + a.ty0) * TY + eyl;
   const bool valid = ex < a.Ex && ey < a.Ey;
   const long long NX = a.NX;
   const long long base = (long long)ex * N + lane + (long long)ey * N * NX;

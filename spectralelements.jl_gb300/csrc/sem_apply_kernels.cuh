@@ -46,6 +46,7 @@ struct ApplyArgs {
   unsigned mode;
   const int* skip;
   int slot_g, slot_b, slot_nu;  // staged-variant shared-memory slots (-1: not staged)
+  int ty0;                      // first element-tile row of the launch (a window of the grid)
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
 
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   const int exl = elem % TX;
   const int eyl = elem / TX;
   const int ex = blockIdx.x * TX + exl;
-  const int ey = blockIdx.y * TY + eyl;
+  const int ey = (blockIdx.y + a.ty0) * TY + eyl;
   const bool valid = ex < a.Ex && ey < a.Ey;
   const long long NX = a.NX;
   const long long base = (long long)ex * N + lane + (long long)ey * N * NX;
@@ -354,7 +355,14 @@ struct FixArgs {
   unsigned mode;
   long long nxi, nyi;  // number of cross-tile interfaces in x and y
   const int* skip;
+  // only the interface points whose highest copy column lies in [key_lo, key_hi)
+  // (a pipeline finishes the columns of one slab of tile rows at a time)
+  long long key_lo, key_hi;
 };
+
+__device__ __forceinline__ bool fix_key_in(long long key, long long lo, long long hi) {
+  return key >= lo && key < hi;
+}
 
 __host__ __device__ inline long long fix_iface(long long q, int T, bool per) {
   return per ? q * T : (q + 1) * T;  // interface index a: between elements a-1 and a
@@ -401,7 +409,9 @@ __device__ __forceinline__ void fix_xline(IO* out, const FixArgs& f, long long a
     const int j = (int)(c - (long long)ey * f.n);
     if (xcross_row(ey, j, f.n, f.Ey, f.TY, pery)) continue;  // corner of two cross-tile interfaces
     if (j == 0 && ey > 0) continue;                            // in-tile y pair, done from column c-1
-    if (j == f.n - 1 && ey + 1 < f.Ey) {
+    const bool quad = j == f.n - 1 && ey + 1 < f.Ey;
+    if (!fix_key_in(quad ? c + 1 : c, f.key_lo, f.key_hi)) continue;
+    if (quad) {
       const long long c2 = c + 1;
       const IO s = io_add(io_add(fix_ld(out + rl + c * f.NX), fix_ld(out + rr + c * f.NX)),
                           io_add(fix_ld(out + rl + c2 * f.NX), fix_ld(out + rr + c2 * f.NX)));
@@ -428,6 +438,7 @@ __device__ __forceinline__ void fix_yline(IO* out, const FixArgs& f, long long b
   const unsigned n = (unsigned)f.n;
   const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
   const long long cr = b * f.n;
+  if (!fix_key_in(cl > cr ? cl : cr, f.key_lo, f.key_hi)) return;
   for (long long r = r_begin; r < r_end; r += stride) {
     const int ex = (int)((unsigned)r / n);
     const int i = (int)(r - (long long)ex * f.n);
@@ -451,6 +462,7 @@ __device__ __forceinline__ void fix_corner(IO* out, const FixArgs& f, long long 
   const long long rr = a * f.n;
   const long long cl = b == 0 ? f.NY - 1 : b * f.n - 1;
   const long long cr = b * f.n;
+  if (!fix_key_in(cl > cr ? cl : cr, f.key_lo, f.key_hi)) return;
   const IO s = io_add(io_add(fix_ld(out + rl + cl * f.NX), fix_ld(out + rr + cl * f.NX)),
                       io_add(fix_ld(out + rl + cr * f.NX), fix_ld(out + rr + cr * f.NX)));
   const long long rs[2] = {rl, rr};

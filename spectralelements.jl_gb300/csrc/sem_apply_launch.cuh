@@ -102,7 +102,8 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   const size_t smem = 2 * te * sizeof(typename P::v) + nslot * te * sizeof(io);
   auto kern = k_apply<P, N, TS::TX, TS::TY, STAGE>;
   if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
+  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, c.tyn > 0 ? c.tyn : (g.Ey + TS::TY - 1) / TS::TY);
+  a.ty0 = c.ty0;
   auto* ev = timing_slot();
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
   SEM_CHECK(launch_kernel(kern, grid, TS::THREADS, smem, s, c.pdl != 0, a));
@@ -168,7 +169,8 @@ static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCal
   const size_t smem = 2 * te * sizeof(typename P::v) + (STAGE ? 3 * te * sizeof(gt) : 0);
   auto kern = k_apply2<P, N, TS::TX, TS::TY, STAGE, FUSE, CG>;
   if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, (g.Ey + TS::TY - 1) / TS::TY);
+  dim3 grid((g.Ex + TS::TX - 1) / TS::TX, c.tyn > 0 ? c.tyn : (g.Ey + TS::TY - 1) / TS::TY);
+  a.ty0 = c.ty0;
   auto* ev = timing_slot();
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
   SEM_CHECK(launch_kernel(kern, grid, TS::THREADS, smem, s, c.pdl != 0, a));
@@ -221,6 +223,14 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
                           cudaStream_t s, int* tile) {
   const bool geo_ok = P::kPrecision != SEM_F64_DF || c.Gdf;
   const bool cg = c.cg_p != nullptr;
+  if (c.tyn > 0) {  // a window of tile rows: the non-persistent kernels with the fixup outside
+    if (cg) return set_error(SEM_ERR_UNSUPPORTED, "a tile-row window takes no CG fusion");
+    if (c.variant == 4 || c.variant == 5) {
+      ApplyCall c2 = c;
+      c2.variant = 2;
+      return launch_apply_n<P, N>(g, ops, c2, s, tile);
+    }
+  }
   if (cg && !(geo_ok && (c.variant == 2 || c.variant == 5) && (c.mode & M_STIFF)))
     return set_error(SEM_ERR_UNSUPPORTED, "CG-fused operator launch needs kernel variant 2 or 5");
   if (c.variant == 5 && geo_ok && c.ctr && (c.mode & M_GS)) {

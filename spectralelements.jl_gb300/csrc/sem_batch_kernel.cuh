@@ -373,6 +373,8 @@ __device__ __noinline__ void bfixup(const BProb& pr, int n, IO* __restrict__ Ap,
   f.NY = pr.NY;
   f.mode = pr.topo | M_GS;
   f.skip = nullptr;
+  f.key_lo = 0;
+  f.key_hi = 1LL << 62;
   const bool perx = (pr.topo & M_PERX) != 0, pery = (pr.topo & M_PERY) != 0;
   f.nxi = (pr.Ex - 1) / TX + (perx ? 1 : 0);
   f.nyi = (pr.Ey - 1) / TY + (pery ? 1 : 0);

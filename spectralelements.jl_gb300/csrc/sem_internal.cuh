@@ -189,6 +189,7 @@ struct sem_mesh {
   int variant[4];          // autotuned kernel variant per precision (SEM_F64, SEM_F64_DF, SEM_F32)
   void* graphs;            // CUDA graphs of the CG iteration chunks (sem_pcg.cu), or NULL
   unsigned* fix_ctr;       // interface arrival counters of kernel variant 5 (3 per tile), or NULL
+  void* host_pipe;         // streams, events and buffers of sem_hlmz_host (sem_host.cu), or NULL
 };
 
 namespace sem {
@@ -228,6 +229,9 @@ struct ApplyCall {
   const double* cg_beta;
   void* cg_dpart;
   int pdl;         // launch as a programmatic dependent of the previous kernel on the stream
+  // a window of element-tile rows [ty0, ty0 + tyn) instead of the whole grid
+  // (tyn = 0: all); variants 0-3 only, no CG fusion, the fixup left to the caller
+  int ty0, tyn;
 };
 
 // launch kern<<<grid, block, 0, s>>>(args...) as a programmatic dependent of
@@ -301,8 +305,14 @@ constexpr int kVariants = SEM_VARIANTS;
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
 bool timing_enabled();                 // sem_timing_enable state (sem_apply.cu)
 void free_graph_cache(sem_mesh* m);    // sem_pcg.cu
+void free_host_pipe(sem_mesh* m);      // sem_host.cu
+void tile_shape_of(int n, int* tx, int* ty);  // element tile of the fused kernels (sem_apply.cu)
 int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
-                     int TY, cudaStream_t s);
+                     int TY, cudaStream_t s, long long key_lo = 0, long long key_hi = 1LL << 62);
+// the operator kernel on a window of tile rows (ApplyCall::ty0, tyn) and the
+// fixup of the interface points whose highest copy column is in [key_lo, key_hi)
+int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c, long long key_lo,
+                        long long key_hi, cudaStream_t s);
 
 // elementwise / structured kernels (sem_vec.cu)
 int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode, cudaStream_t s);

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu", "sem_host.cu"]
 
 
 class SemError(RuntimeError):
@@ -147,6 +147,7 @@ SIGNATURES = {
     "sem_lapl_nu": (_I, [_P, _P, _P, _P, _U, _P]),
     "sem_hlmz": (_I, [_P, _P, _D, _D, _P, _P, _U, _P]),
     "sem_varcoef": (_I, [_P, _P, _D, _P, _P, _U, _P]),
+    "sem_hlmz_host": (_I, [_P, _P, _D, _D, _P, _P, _U, _I, _P]),
     "sem_mass": (_I, [_P, _P, _P, _U, _P]),
     "sem_gather_scatter": (_I, [_P, _P, _P, _P]),
     "sem_mask": (_I, [_P, _P, _P, _L, _P]),

@@ -48,6 +48,29 @@ class HelmholtzOp:
                                 flags, stream_ptr()))
         return out
 
+    def apply_host(self, u_host, out=None, slabs=0):
+        """opA on HOST buffers (``sem_hlmz_host``): u_host is a CPU float64
+        tensor in the column-major local layout (pinned memory lets the copies
+        overlap the kernels); the result goes to ``out`` (a CPU tensor of the
+        same layout, pinned if None) and is complete once the current stream
+        has synchronised.  Scalar nu only."""
+        if self.nu_field is not None:
+            raise NotImplementedError("apply_host takes a scalar nu")
+        lib = _lib.load()
+        msh = self.msh
+        nx, ny = msh.shape
+        if (u_host.device.type != "cpu" or u_host.dtype != torch.float64 or tuple(u_host.shape) != (nx, ny)
+                or u_host.stride() != (1, nx)):
+            raise ValueError("u_host must be a CPU float64 tensor of the local shape, column-major")
+        if out is None:
+            out = torch.empty_strided((nx, ny), (1, nx), dtype=torch.float64, pin_memory=True)
+        elif out.device.type != "cpu" or out.dtype != torch.float64 or out.stride() != (1, nx):
+            raise ValueError("out must be a CPU float64 tensor of the local shape, column-major")
+        flags = _lib.SEM_GS | (_lib.SEM_MASK if msh.bc else 0)
+        _lib.check(lib.sem_hlmz_host(msh.handle, None, self.nu, self.k, u_host.data_ptr(), out.data_ptr(),
+                                     flags, int(slabs), stream_ptr()))
+        return out
+
 
 class Jacobi:
     """opM(r) = r ./ diag(opA) (not in the reference; derived from
