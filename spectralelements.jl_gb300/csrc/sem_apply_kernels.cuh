@@ -485,7 +485,11 @@ __device__ __forceinline__ void fix_interface(IO* __restrict__ out, const FixArg
   const bool perx = (f.mode & M_PERX) != 0;
   const bool pery = (f.mode & M_PERY) != 0;
   if (q < f.nxi) {
-    fix_xline(out, f, fix_iface(q, f.TX, perx), first, f.NY, stride, done);
+    // the columns whose unit key can lie in [key_lo, key_hi): a unit spans
+    // columns c or c, c + 1 and its key is the higher one
+    const long long c_lo = f.key_lo > 0 ? f.key_lo - 1 : 0;
+    const long long c_hi = f.key_hi < f.NY ? f.key_hi : f.NY;
+    fix_xline(out, f, fix_iface(q, f.TX, perx), c_lo + first, c_hi, stride, done);
   } else if (q < f.nxi + f.nyi) {
     fix_yline(out, f, fix_iface(q - f.nxi, f.TY, pery), first, f.NX, stride, done);
   } else {
