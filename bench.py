@@ -567,9 +567,9 @@ def bench_adjoint(S, fd_directions):
     B = msh.B
     out = {"mesh": "128x128 elements, N=8", "tol_rel": 1e-12}
 
-    def gradient():
+    def gradient(**kw):
         nu_t = nu.clone().requires_grad_(True)
-        u = S.linsolve_varcoef(nu_t, b, msh, tol=tol)
+        u = S.linsolve_varcoef(nu_t, b, msh, tol=tol, **kw)
         J = 0.5 * torch.sum(B * (u - ut) ** 2)
         J.backward()
         return J.item(), nu_t.grad
@@ -581,6 +581,15 @@ def bench_adjoint(S, fd_directions):
     torch.cuda.synchronize()
     out["gradient_s"] = time.time() - t
     out["J"] = J0
+    # the same gradient with both solves in mixed precision (FP32 CG on nu .* G
+    # with FP64 residual replacement, same FP64 tolerance)
+    gradient(precision=S.SEM_MIXED_RR)
+    torch.cuda.synchronize()
+    t = time.time()
+    J_rr, g_rr = gradient(precision=S.SEM_MIXED_RR)
+    torch.cuda.synchronize()
+    out["gradient_mixed_rr_s"] = time.time() - t
+    out["gradient_mixed_rr_rel_l2_vs_fp64"] = (torch.linalg.norm(g_rr - g) / torch.linalg.norm(g)).item()
     # central finite differences along continuous directions
     msh.set_precision(S.SEM_F64)
 

@@ -720,6 +720,36 @@ int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r
   return SEM_OK;
 }
 
+// nu .* G11, nu .* G12, nu .* G22 rounded to FP32 (three blocks of L): the
+// metric of the G-folded variable-coefficient operator for an FP32 inner solve
+__global__ void k_nu_geom_f32(const double* __restrict__ nu, const double* __restrict__ G11,
+                              const double* __restrict__ G12, const double* __restrict__ G22,
+                              float* __restrict__ o, long long L) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = nu[i];
+    o[i] = (float)(v * G11[i]);
+    o[L + i] = (float)(v * G12[i]);
+    o[2 * L + i] = (float)(v * G22[i]);
+  }
+}
+
+// scratch of the FP32 metric nu .* G, freed in stream order
+struct NuGeomF32 {
+  cudaStream_t s;
+  float* g = nullptr;
+  explicit NuGeomF32(cudaStream_t st) : s(st) {}
+  int build(const double* nu, const OpCtx& cx, long long L) {
+    SEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&g), sizeof(float) * 3 * (size_t)L, s));
+    k_nu_geom_f32<<<nblocks(L) * 4, kRT, 0, s>>>(nu, cx.G11, cx.G12, cx.G22, g, L);
+    SEM_CUDA(cudaGetLastError());
+    return SEM_OK;
+  }
+  ~NuGeomF32() {
+    if (g) cudaFreeAsync(g, s);
+  }
+};
+
 // inverse Jacobi diagonal of the solve's operator into w.dinv (and w.dinv32
 // for the mixed precisions)
 int jacobi_build(const OpCtx& cx, const WS& w, const sem_pcg_opts* o, cudaStream_t s) {
@@ -847,10 +877,20 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       SEM_CHECK(run_cg<double>(m, cx, gv, w, x, w.r, w.p, w.Ap, jac ? w.dinv : nullptr, prec, o->nu_field,
                                o->nu, o->k, check_every, &res, s));
   } else {
-    if (o->nu_field) return set_error(SEM_ERR_UNSUPPORTED, "mixed precision does not take a nu field");
     if (!m) return set_error(SEM_ERR_UNSUPPORTED, "mixed precision needs a mesh handle");
     SEM_CHECK(ensure_f32_geometry(m, s));
     cx = ctx_of(m);
+    // the FP32 inner operator; with a nu field its metric is nu .* G in FP32
+    // (the G-folded operator with the coefficient already applied)
+    OpCtx cxf = cx;
+    NuGeomF32 nug(s);
+    if (o->nu_field) {
+      SEM_CHECK(nug.build(o->nu_field, cx, L));
+      cxf.G11f = nug.g;
+      cxf.G12f = nug.g + L;
+      cxf.G22f = nug.g + 2 * L;
+    }
+    const double nu_in = o->nu_field ? 1.0 : o->nu;
     const bool rr = prec == SEM_MIXED_RR;
     // SEM_MIXED_RR replaces the FP32 residual after every 0.3-fold drop: rarer
     // replacements let the FP32 recurrence drift (cfg2: 0.3 -> 7,504 iterations,
@@ -874,9 +914,13 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     c.G12 = cx.G12;
     c.G22 = cx.G22;
     c.B = cx.B;
-    c.nu_s = o->nu;
+    c.nu_s = o->nu_field ? 1.0 : o->nu;
     c.k_s = o->k;
     c.mode = cx.g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (cx.has_bc ? M_MASK : 0u);
+    if (o->nu_field) {
+      c.nu = o->nu_field;
+      c.mode |= M_NUG;
+    }
     c.precision = m->precision;
     c.variant = cx.variant[m->precision];
     c.Gdf = cx.Gdf;
@@ -890,8 +934,8 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       SEM_CUDA(cudaGetLastError());
       for (;;) {
         Scalars ir;
-        SEM_CHECK(run_cg<float>(m, cx, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
-                                nullptr, o->nu, o->k, check_every, &ir, s));
+        SEM_CHECK(run_cg<float>(m, cxf, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
+                                nullptr, nu_in, o->k, check_every, &ir, s));
         total_it = ir.k;
         k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
         SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
@@ -917,8 +961,8 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
       SEM_CUDA(cudaGetLastError());
       Scalars ir;
-      SEM_CHECK(run_cg<float>(m, cx, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
-                              nullptr, o->nu, o->k, check_every, &ir, s));
+      SEM_CHECK(run_cg<float>(m, cxf, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
+                              nullptr, nu_in, o->k, check_every, &ir, s));
       total_it += ir.k;
       k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
       SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));

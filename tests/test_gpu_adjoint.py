@@ -84,6 +84,33 @@ def test_steady_adjoint_matches_oracle_and_fd(gpu):
     assert rel_l2(g_ps, g_o) > 1e-3
 
 
+@pytest.mark.parametrize("prec_name", ["SEM_MIXED_RR", "SEM_MIXED"])
+@pytest.mark.parametrize("k", [0.0, 50.0])
+def test_varcoef_mixed_precision_solves(gpu, prec_name, k):
+    """The G-folded variable-coefficient solve in mixed precision: the FP32
+    inner CG runs on nu .* G rounded to FP32, the FP64 residual on the
+    double-float G-folded operator; both stop on the same FP64 tolerance as
+    the FP64 solve, against the oracle."""
+    import semgb300 as S
+    mo, md = meshes(9, 12, 10, (False, False), "DDDD", 0.05)
+    M = O.generateMask(["D"] * 4, mo)
+    nu = np.exp(gaussian_field(mo, 7))
+    b = O.gatherScatter(O.mask(O.mass(np.ones(mo.shape) + mo.x, mo), M), mo)
+    tol = 1e-12 * np.abs(b).max()
+    op = S.HelmholtzOp(md, 1.0, k, nu_field=S.as_local(nu))
+    info, info64 = {}, {}
+    x = S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol,
+              precision=getattr(S, prec_name), info=info)
+    x64 = S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=S.SEM_F64_DF,
+                info=info64)
+    assert info["converged"] and info["res_inf"] <= tol
+    u_o = oracle_varcoef_solve(mo, M, nu, b, k=k, tol=tol)
+    assert rel_l2(host(x), u_o) < 1e-9, rel_l2(host(x), u_o)
+    assert rel_l2(host(x), host(x64)) < 1e-9
+    if prec_name == "SEM_MIXED_RR":  # the search direction survives replacements
+        assert info["iters"] <= 1.5 * info64["iters"] + 10, (info, info64)
+
+
 def test_transient_adjoint_with_checkpoints(gpu):
     import torch
 
