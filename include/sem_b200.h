@@ -224,14 +224,18 @@ enum sem_precond { SEM_PRECOND_NONE = 0, SEM_PRECOND_JACOBI = 1 };
 
 typedef struct {
   double nu;             /* scalar viscosity (ignored when nu_field set)    */
-  const double* nu_field;/* device nu folded into G (variable coefficient)   */
+  const double* nu_field;/* device nu folded into G (variable coefficient); the
+                            mixed precisions run their FP32 CG on nu .* G in FP32 */
   double k;              /* mass coefficient (bdfB[1] / lambda)             */
   int precond;           /* enum sem_precond                                 */
   int precision;         /* SEM_F64, SEM_F64_DF or SEM_MIXED                 */
   double tol;            /* absolute Inf-norm tolerance on the residual      */
   int maxiter;           /* <= 0: length(b), as the reference               */
   double inner_tol;      /* SEM_MIXED: relative inner tolerance (1e-4); SEM_MIXED_RR: residual drop between replacements (0.3) */
-  int max_outer;         /* SEM_MIXED: defect-correction sweeps (6); SEM_MIXED_RR: replacements (100) */
+  int max_outer;         /* SEM_MIXED: defect-correction sweeps (6); SEM_MIXED_RR: replacements (100).
+                            When the sweeps or replacements run out, or an FP32 segment stalls
+                            (runs 4 times longer than the longest before it, at least 500
+                            iterations), the FP64 CG finishes the solve from the current x */
   int check_every;       /* iterations between convergence reads (0 = auto) */
   int mult_ones;         /* 1: unweighted dots, pcg's default mult=ones(size(b)) */
   int path;              /* enum sem_pcg_path                                */

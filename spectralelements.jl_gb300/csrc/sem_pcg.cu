@@ -195,8 +195,9 @@ __global__ void k_scal_init(const double* part, int np, Scalars* sc, double tol,
 }
 
 // after a residual replacement: t from the replaced residual, beta with the
-// previous t (the recurrence continues), a new tolerance; k and maxiter stay
-__global__ void k_scal_replace(const double* part, int np, Scalars* sc, double tol) {
+// previous t (the recurrence continues), a new tolerance and iteration limit;
+// k stays
+__global__ void k_scal_replace(const double* part, int np, Scalars* sc, double tol, int maxiter) {
   double res[2];
   const bool mx[2] = {false, true};
   final_reduce<2>(part, np, mx, res);
@@ -205,6 +206,7 @@ __global__ void k_scal_replace(const double* part, int np, Scalars* sc, double t
     sc->beta = sc->k > 0 ? res[0] / sc->t_prev : 0.0;
     sc->rmax = res[1];
     sc->tol = tol;
+    sc->maxiter = maxiter;
     sc->nan = res[1] != res[1];
     sc->converged = !(res[1] > tol) && !sc->nan;
     sc->done = !(res[1] > tol) || sc->k >= sc->maxiter || sc->nan;
@@ -391,6 +393,12 @@ __global__ void k_axpy_f2d(double* __restrict__ x, const float* __restrict__ d, 
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
        i += (long long)gridDim.x * blockDim.x)
     x[i] += (double)d[i];
+}
+
+__global__ void k_add_d(double* __restrict__ x, const double* __restrict__ d, long long L) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = x[i] + d[i];
 }
 
 __global__ void k_zero(double* __restrict__ x, long long L) {
@@ -932,11 +940,19 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, w.p32, jac ? w.dinv32 : nullptr, w.part, gv);
       k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, maxiter);
       SEM_CUDA(cudaGetLastError());
+      // a segment (the FP32 iterations between replacements) that runs 4 times
+      // longer than the longest before it (at least 500 iterations) has hit
+      // the FP32 floor: the FP64 CG finishes the solve
+      int seg_start = 0, longest = 0, seg_limit = maxiter;
+      bool stalled = false;
       for (;;) {
         Scalars ir;
         SEM_CHECK(run_cg<float>(m, cxf, gv, w, w.x32, w.r32, w.p32, w.Ap32, jac ? w.dinv32 : nullptr, SEM_F32,
                                 nullptr, nu_in, o->k, check_every, &ir, s));
         total_it = ir.k;
+        stalled = !ir.converged && !ir.nan && ir.k >= seg_limit && seg_limit < maxiter;
+        if (ir.k - seg_start > longest) longest = ir.k - seg_start;
+        seg_start = ir.k;
         k_axpy_f2d<<<nb, kRT, 0, s>>>(x, w.x32, L);
         SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
         k_residual<<<nb, kRT, 0, s>>>(b, w.Ap, w.r, w.part, L);
@@ -947,10 +963,12 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
         rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
         nan = rmax != rmax || ir.nan;
         ++outer;
-        if (rmax <= o->tol || nan || ir.k >= maxiter || outer >= max_outer) break;
+        if (rmax <= o->tol || nan || ir.k >= maxiter || outer >= max_outer || stalled) break;
         // replace: r32 = r (FP64 residual), x32 = 0, p32 kept
+        const long long lim = (long long)ir.k + (longest > 125 ? 4LL * longest : 500LL);
+        seg_limit = lim < maxiter ? (int)lim : maxiter;
         k_init<float, double><<<nb, kRT, 0, s>>>(w.r, w.x32, w.r32, nullptr, jac ? w.dinv32 : nullptr, w.part, gv);
-        k_scal_replace<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax);
+        k_scal_replace<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, inner_tol * rmax, seg_limit);
         SEM_CUDA(cudaGetLastError());
       }
     }
@@ -974,10 +992,34 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
       nan = rmax != rmax;
     }
+    bool fin_conv = rmax <= o->tol;
+    if (!fin_conv && !nan && total_it < maxiter) {
+      // the FP32 solves stopped gaining on the FP64 residual (stalled
+      // segment, or the sweep / replacement budget ran out): the FP64 CG
+      // solves A d = r from d = 0 to the same tolerance, then x += d
+      double* d = w.x64tmp;
+      double* rd = w.d;
+      k_init<double, double><<<nb, kRT, 0, s>>>(w.r, d, rd, w.p, jac ? w.dinv : nullptr, w.part, gv);
+      k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter - total_it);
+      SEM_CUDA(cudaGetLastError());
+      SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+      SEM_CUDA(cudaStreamSynchronize(s));
+      Scalars fr = *w.sc_h;
+      if (!fr.done)
+        SEM_CHECK(run_cg<double>(m, cx, gv, w, d, rd, w.p, w.Ap, jac ? w.dinv : nullptr, m->precision,
+                                 o->nu_field, o->nu, o->k, check_every, &fr, s));
+      k_add_d<<<nb, kRT, 0, s>>>(x, d, L);
+      SEM_CUDA(cudaGetLastError());
+      total_it += fr.k;
+      rmax = fr.rmax;
+      nan = nan || fr.nan;
+      fin_conv = fr.converged != 0;
+      ++outer;
+    }
     res.k = total_it;
     res.rmax = rmax;
     res.nan = nan;
-    res.converged = rmax <= o->tol;
+    res.converged = fin_conv;
   }
   if (info) {
     info->iters = res.k;
