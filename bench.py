@@ -581,15 +581,7 @@ def bench_adjoint(S, fd_directions):
     torch.cuda.synchronize()
     out["gradient_s"] = time.time() - t
     out["J"] = J0
-    # the same gradient with both solves in mixed precision (FP32 CG on nu .* G
-    # with FP64 residual replacement, same FP64 tolerance)
-    gradient(precision=S.SEM_MIXED_RR)
-    torch.cuda.synchronize()
-    t = time.time()
-    J_rr, g_rr = gradient(precision=S.SEM_MIXED_RR)
-    torch.cuda.synchronize()
-    out["gradient_mixed_rr_s"] = time.time() - t
-    out["gradient_mixed_rr_rel_l2_vs_fp64"] = (torch.linalg.norm(g_rr - g) / torch.linalg.norm(g)).item()
+
     # central finite differences along continuous directions
     msh.set_precision(S.SEM_F64)
 
