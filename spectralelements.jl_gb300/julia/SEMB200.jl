@@ -176,6 +176,19 @@ function (op::HelmholtzOp)(u::CuArray{Float64,2})
     return out
 end
 
+# opLHS on HOST arrays (the reference's own Array fields): the field streams to
+# the GPU and back in slabs with the copies overlapped (sem_hlmz_host). Pin the
+# arrays once (CUDA.Mem.pin) for the overlap; unpinned arrays work, with
+# serialised copies.
+function (op::HelmholtzOp)(out::Array{Float64,2}, u::Array{Float64,2}; slabs::Integer=0)
+    set_bc!(op.msh, op.bc)
+    check(ccall((:sem_hlmz_host, libsem), Cint,
+                (Ptr{Cvoid}, CuPtr{Cdouble}, Cdouble, Cdouble, Ptr{Cdouble}, Ptr{Cdouble}, Cuint, Cint, Ptr{Cvoid}),
+                handle(op.msh), CU_NULL, op.ν, op.k, u, out, SEM_GS | SEM_MASK, slabs, stream()))
+    CUDA.synchronize()
+    return out
+end
+
 struct Jacobi <: Function
     op::HelmholtzOp
 end
