@@ -270,7 +270,7 @@ int sem_pcg(sem_mesh_t* mesh, const sem_pcg_opts* opts, const double* b, double*
  * arguments instead of a handle: nr = ns, host Dr/Ds, and DEVICE G11, G12,
  * G22, B in the local layout.  All scratch vectors live in one fixed
  * file-scope device array sized for SEM_NOALLOC_MAX_LOCAL local DOF, about
- * 12.9 MB, which every GPU that loads the library holds until the process
+ * 13.4 MB, which every GPU that loads the library holds until the process
  * exits.  The call allocates nothing: no cudaMalloc, cudaFree, pinned host
  * memory or library allocator.  Larger meshes are rejected with
  * SEM_ERR_BAD_ARG.

@@ -66,13 +66,6 @@ struct Apply2Args {
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
 
-// one term of the CG denominator p . A p, formed in double-float
-__device__ __forceinline__ df dot_term(df a, df b) { return df_mul_u(a, b); }
-__device__ __forceinline__ df dot_term(double a, double b) { return df_mul_u(d2df(a), d2df(b)); }
-__device__ __forceinline__ df dot_term(float a, float b) {
-  const float p = __fmul_rn(a, b);
-  return {p, __fmaf_rn(a, b, -p)};
-}
 
 // In-kernel completion of the cross-tile QQ' (kernel variant 5).  Every tile
 // edge and every tile corner on a cross-tile interface has an arrival counter
@@ -160,12 +153,14 @@ __device__ __forceinline__ void finish_tile_interfaces(IO* out, int n, int Ex, i
 }
 
 // resident blocks per SM asked of the register allocator: without the
-// register copy of u the double-float kernel fits four blocks (72 registers,
-// no spills) up to n = 9
+// register copy of u the double-float kernel fits five blocks up to n = 9
+// (56 registers at n = 9, with a few words spilled to L1; 3 % faster than
+// four blocks at 72 registers without spills on the 256^2 n = 9 apply); at
+// n = 8 the 256-thread tile would spill more, so it keeps four
 template <class P, int N, bool STAGE>
 struct MinBlocks2 {
   static constexpr int value =
-      (!STAGE && P::kPrecision == SEM_F64_DF && N <= 9) ? 4 : MinBlocks<P, N, STAGE>::value;
+      (!STAGE && P::kPrecision == SEM_F64_DF && N <= 9) ? (N == 8 ? 4 : 5) : MinBlocks<P, N, STAGE>::value;
 };
 
 // CG: the launch is one CG iteration's operator application (src/pcg.jl:40-47):

@@ -47,6 +47,7 @@ struct ApplyArgs {
   const int* skip;
   int slot_g, slot_b, slot_nu;  // staged-variant shared-memory slots (-1: not staged)
   int ty0;                      // first element-tile row of the launch (a window of the grid)
+  df* dpart;                    // DOT launches: each CTA's part of u . (A u), unassembled
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
 
@@ -199,7 +200,11 @@ __device__ __forceinline__ void tile_dss_store(const typename P::v (&res)[N], ty
   }
 }
 
-template <class P, int N, int TX, int TY, bool STAGE>
+// DOT: the launch is a CG iteration's operator application on the direction
+// u = p and every CTA also writes its part of p . A p, summed over the
+// unassembled local products (equal to the mult-weighted dot of the assembled
+// A p for a continuous, masked p; the same sum as the CG-fused k_apply2)
+template <class P, int N, int TX, int TY, bool STAGE, bool DOT = false>
 __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     k_apply(const __grid_constant__ ApplyArgs<P, N> a) {
   typedef typename P::v V;
@@ -334,6 +339,13 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
       V kb = P::mul(a.k_s, b);
       res[j] = P::fin(P::fma(kb, u[j], res[j]));
     }
+  }
+  if constexpr (DOT) {
+    df acc = {0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc = df_add_u(acc, dot_term(u[j], res[j]));
+    const df tot = block_sum_df(df_norm(acc));
+    if (threadIdx.x == 0) a.dpart[blockIdx.y * gridDim.x + blockIdx.x] = tot;
   }
 
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");

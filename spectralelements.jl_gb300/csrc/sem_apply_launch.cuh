@@ -63,7 +63,7 @@ static int launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t s
   return SEM_OK;
 }
 
-template <class P, int N, bool STAGE>
+template <class P, int N, bool STAGE, bool DOT = false>
 static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall& c,
                           cudaStream_t s) {
   typedef TileShape<N> TS;
@@ -100,7 +100,8 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   fill_eo<P, N>(a.Dst, ops->eo[3]);
   const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
   const size_t smem = 2 * te * sizeof(typename P::v) + nslot * te * sizeof(io);
-  auto kern = k_apply<P, N, TS::TX, TS::TY, STAGE>;
+  a.dpart = static_cast<df*>(c.cg_dpart);
+  auto kern = k_apply<P, N, TS::TX, TS::TY, STAGE, DOT>;
   if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((g.Ex + TS::TX - 1) / TS::TX, c.tyn > 0 ? c.tyn : (g.Ey + TS::TY - 1) / TS::TY);
   a.ty0 = c.ty0;
@@ -223,6 +224,11 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
                           cudaStream_t s, int* tile) {
   const bool geo_ok = P::kPrecision != SEM_F64_DF || c.Gdf;
   const bool cg = c.cg_p != nullptr;
+  // DOT launches (p . A p parts without the direction update) are served by
+  // the k_apply variants 0 and 1
+  const bool dot = !cg && c.cg_dpart != nullptr;
+  if (dot && !(c.variant <= 1 || (P::kPrecision == SEM_F64_DF && !geo_ok)))
+    return set_error(SEM_ERR_UNSUPPORTED, "a p.Ap launch needs kernel variant 0 or 1");
   if (c.tyn > 0) {  // a window of tile rows: the non-persistent kernels with the fixup outside
     if (cg) return set_error(SEM_ERR_UNSUPPORTED, "a tile-row window takes no CG fusion");
     if (c.variant == 4 || c.variant == 5) {
@@ -266,9 +272,10 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
     const int nslot = ((c.mode & M_STIFF) ? 3 : 0) + ((c.mode & M_MASS) ? 1 : 0) +
                       ((c.mode & (M_NU | M_NUG)) ? 1 : 0);
     const size_t smem = 2 * te * sizeof(typename P::v) + nslot * te * sizeof(typename P::io);
-    if (smem <= max_smem_optin()) return launch_apply_v<P, N, true>(g, ops, c, s);
+    if (smem <= max_smem_optin())
+      return dot ? launch_apply_v<P, N, true, true>(g, ops, c, s) : launch_apply_v<P, N, true>(g, ops, c, s);
   }
-  return launch_apply_v<P, N, false>(g, ops, c, s);
+  return dot ? launch_apply_v<P, N, false, true>(g, ops, c, s) : launch_apply_v<P, N, false>(g, ops, c, s);
 }
 
 // element tile (TX, TY) of the non-persistent kernels for n points (host)

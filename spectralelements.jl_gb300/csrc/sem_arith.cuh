@@ -158,6 +158,14 @@ __device__ __forceinline__ float cg_direction(float r, float d, float beta, floa
 
 // block-wide double-float sum in a fixed order (warp trees, then the warps in
 // order); the result is valid in thread 0.  Every thread of the block calls it.
+// one term of the CG denominator p . A p, formed in double-float
+__device__ __forceinline__ df dot_term(df a, df b) { return df_mul_u(a, b); }
+__device__ __forceinline__ df dot_term(double a, double b) { return df_mul_u(d2df(a), d2df(b)); }
+__device__ __forceinline__ df dot_term(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+
 __device__ __forceinline__ df block_sum_df(df x) {
   __shared__ df warp_sums[32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

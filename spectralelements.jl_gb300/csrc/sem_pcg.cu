@@ -562,6 +562,10 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
     if (fused) {
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
       SEM_CHECK(launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc));
+    } else if (cp.cg_dpart) {  // direction pass, then the operator with the p.Ap parts
+      SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
+      SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
+      SEM_CHECK(launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc));
     } else {
       SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
@@ -705,12 +709,16 @@ int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r
   // and 5; double-float arithmetic also needs the pre-split geometry).  Their
   // unassembled p.Ap equals the mult-weighted dot only: unweighted dots
   // (mult = ones) keep the separate passes.
-  if ((c.variant == 2 || c.variant == 5) && (op_precision != SEM_F64_DF || c.Gdf) && w.dpart &&
-      cg_apply_parts(cx.g) <= w.dpart_n && !(gv.topo & M_MULT1)) {
+  const bool geo_ok = op_precision != SEM_F64_DF || c.Gdf;
+  const bool parts_ok = w.dpart && cg_apply_parts(cx.g) <= w.dpart_n && !(gv.topo & M_MULT1);
+  if ((c.variant == 2 || c.variant == 5) && geo_ok && parts_ok) {
     c.cg_r = r;
     c.cg_dinv = dinv;
     c.cg_p = p;
     c.cg_beta = &w.sc->beta;
+    c.cg_dpart = w.dpart;
+  } else if ((c.variant <= 1 || (c.variant != 4 && !geo_ok)) && parts_ok) {
+    // the k_apply variants write the parts of p.Ap (no separate dot pass)
     c.cg_dpart = w.dpart;
   }
   cudaGraphExec_t exec = nullptr;
@@ -1145,7 +1153,10 @@ constexpr long long kNoAllocMaxLocal = SEM_NOALLOC_MAX_LOCAL;
 constexpr size_t kNoAllocVec = (size_t)kNoAllocMaxLocal * sizeof(double);     // 256-multiple
 constexpr size_t kNoAllocInfo = (((size_t)kNoAllocMaxLocal + 1) + 255) & ~(size_t)255;
 constexpr size_t kNoAllocPart = ((sizeof(double) * kRB * 4) + 255) & ~(size_t)255;
-constexpr size_t kNoAllocBytes = 6 * kNoAllocVec + kNoAllocInfo + kNoAllocPart + 256 + 256;
+// per-tile parts of p.Ap: at most one tile per element, n >= 2 points a side
+constexpr long long kNoAllocTiles = kNoAllocMaxLocal / 4;
+constexpr size_t kNoAllocDpart = (((size_t)kNoAllocTiles * sizeof(df)) + 255) & ~(size_t)255;
+constexpr size_t kNoAllocBytes = 6 * kNoAllocVec + kNoAllocInfo + kNoAllocPart + kNoAllocDpart + 256 + 256;
 
 }  // namespace
 }  // namespace sem
@@ -1229,6 +1240,8 @@ extern "C" int sem_pcg_noalloc(int nr, int Ex, int Ey, int periodic_x, int perio
   w.x64tmp = (double*)p; p += kNoAllocVec;
   unsigned char* info_tab = (unsigned char*)p; p += kNoAllocInfo;
   w.part = (double*)p; p += kNoAllocPart;
+  w.dpart = (df*)p; p += kNoAllocDpart;
+  w.dpart_n = kNoAllocTiles;
   w.sc = (Scalars*)p; p += 256;
   w.dmax = (double*)p;
   Scalars host_sc[2];

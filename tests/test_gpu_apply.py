@@ -113,9 +113,11 @@ def test_kernel_variants_bit_identical(gpu, case):
         unfused = host(S.mask(S.gatherScatter(S.hlmz(ud, 1e-2, 1.0, md), md), Md))
         np.testing.assert_array_equal(outs[0][3], unfused)
     # FP32 inner operator: identical mixed-precision solves for every variant
-    # of one CG form.  Variants 2 and 5 run the CG-fused operator launch, whose
-    # p.Ap is summed over the unassembled products: their solves agree with
-    # each other bit for bit and with the other variants' to the tolerance.
+    # of one CG form.  Variants 2 and 5 run the CG-fused operator launch and
+    # variants 0 and 1 the operator launch with the p.Ap parts; both sum p.Ap
+    # over the unassembled products.  Variants 3 and 4 take a separate dot
+    # pass over the assembled A p.  Each form's solves agree bit for bit, and
+    # the forms agree to the tolerance.
     md.set_precision(S.SEM_F64_DF)
     md.set_variant(0)
     M = O.generateMask(list(bc), mo)
@@ -128,15 +130,17 @@ def test_kernel_variants_bit_identical(gpu, case):
         info = {}
         xs.append((host(S.pcg(b, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info,
                               precision=S.SEM_MIXED)), info["iters"]))
-    fused = (2, 5)
-    for v, (x, it) in enumerate(xs):
-        ref_x, ref_it = xs[fused[0]] if v in fused else xs[0]
-        assert it == ref_it, (v, it, ref_it)
-        np.testing.assert_array_equal(x, ref_x)
+    for form in ((0, 1), (2, 5), (3, 4)):
+        ref_x, ref_it = xs[form[0]]
+        for v in form[1:]:
+            x, it = xs[v]
+            assert it == ref_it, (v, it, ref_it)
+            np.testing.assert_array_equal(x, ref_x)
     # FP32 inner iterations react to the dot's summation order (13 % apart on a
     # periodic case); the solutions agree to the outer tolerance
-    assert abs(xs[2][1] - xs[0][1]) <= max(4, xs[0][1] // 4)
-    assert rel_l2(xs[2][0], xs[0][0]) < 1e-6
+    for v in (0, 2):
+        assert abs(xs[v][1] - xs[3][1]) <= max(4, xs[3][1] // 4)
+        assert rel_l2(xs[v][0], xs[3][0]) < 1e-6
 
 
 def test_autotune_reports_every_variant(gpu):
