@@ -170,6 +170,12 @@ def run_ours(args, rank, world, local_rank):
     msh = S.Mesh(N_ORDER + 1, N_ORDER + 1, E_X, E_Y, (False, False), sin_deform(AMP), bc="DDDD")
     tune = {name: msh.autotune(prec) for name, prec in
             (("f64_df", S.SEM_F64_DF), ("f64", S.SEM_F64), ("f32", S.SEM_F32))}
+    if args.variant is not None:
+        # a pinned double-float kernel variant (profiling runs, where the
+        # autotuner's timings are distorted by the profiler)
+        msh.set_variant(args.variant, S.SEM_F64_DF)
+        tune["f64_df"]["chosen"] = args.variant
+        tune["f64_df"]["pinned"] = True
     nx, ny = msh.shape
     L = nx * ny
     G = unique_dof(N_ORDER + 1, E_X, E_Y)
@@ -770,6 +776,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG and order-sweep extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="pin the double-float operator kernel variant instead of the autotuned one")
     ap.add_argument("--extras", default="",
                     help="comma-separated subset of pcg,sweep,batch,adjoint (default: all)")
     ap.add_argument("--fd-directions", type=int, default=8,
