@@ -61,13 +61,18 @@ struct TileShape {
 };
 
 // resident blocks per SM requested from the register allocator: the
-// double-float kernels are latency bound, so up to n = 9 they trade a few
-// spilled registers for a third resident block
+// double-float kernels are latency bound, so they trade a few spilled
+// registers for more resident warps.  Up to n = 9: a third block.  At n = 13
+// three blocks of 208 threads (80 registers, about 50 bytes spilled per
+// thread) run the 167^2 apply in 0.159 ms against 0.214 ms with two blocks and
+// 0.288 ms with one (255 registers); at n = 17 two blocks (96 registers) take
+// 0.241 ms against 0.319 ms with one.  Four blocks at n = 13 and three at
+// n = 17 would spill 200 and 900 bytes.
 template <class P, int N, bool STAGE>
 struct MinBlocks {
   static constexpr int value =
       STAGE ? (N <= 9 ? 2 : 1)
-            : ((P::kPrecision == SEM_F64_DF) ? (N <= 9 ? 3 : (N <= 12 ? 2 : 1))
+            : ((P::kPrecision == SEM_F64_DF) ? (N <= 9 ? 3 : (N <= 12 ? 2 : (N == 13 ? 3 : 2)))
                                               : (N <= 10 ? 3 : (N <= 12 ? 2 : 1)));
 };
 
