@@ -373,6 +373,21 @@ class TimeStepper:
         self.bdfA, self.bdfB = bdfExtK(self.time, self.k)
 
 
+def simulate_steps(t0, dt, Tf):
+    """The number of evolve! calls of the loop of src/diffusion.jl:130-137
+    (``while time <= Tf``, leaving after a step that ends below 1e-12), with
+    the time advanced by the same floating-point additions."""
+    n, t = 0, float(t0)
+    while t <= Tf:
+        if dt == 0.0 and t >= 1e-12:
+            raise ValueError("dt = 0 with Ti > 0 never leaves the loop of src/diffusion.jl:130")
+        t += dt
+        n += 1
+        if t < 1e-12:
+            break
+    return n
+
+
 class Diffusion:
     """``Diffusion(bc, msh; Ti, Tf, dt, k)`` (src/diffusion.jl:7-34) with
     device fields u, uh (histories), ub, nu, f.  ``checkpoint_every`` keeps
@@ -524,15 +539,7 @@ class Diffusion:
         if callback is not None:
             callback(self)
         if callback is None and setBC is None and setForcing is None and not self.checkpoint_every:
-            ts = self.tstep
-            n, t = 0, ts.time[0]
-            while t <= ts.Tf:
-                if ts.dt == 0.0 and t >= 1e-12:
-                    raise ValueError("dt = 0 with Ti > 0 never leaves the loop of src/diffusion.jl:130")
-                t += ts.dt
-                n += 1
-                if t < 1e-12:
-                    break
+            n = simulate_steps(self.tstep.time[0], self.tstep.dt, self.tstep.Tf)
             forcing = [(self.f.clone(), lambda _t: 1.0)] if torch.count_nonzero(self.f) else []
             boundary = [(self.ub.clone(), lambda _t: 1.0)] if torch.count_nonzero(self.ub) else []
             self.run(n, forcing, boundary, tol=tol)

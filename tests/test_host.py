@@ -126,3 +126,25 @@ def test_product_has_no_oracle_imports():
             if f.endswith((".py", ".cu", ".cuh", ".jl")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "sem_oracle" not in txt and "oracle/" not in txt, f
+
+
+def test_simulate_step_count_follows_the_reference_loop():
+    """Diffusion.simulate() without closures runs the number of steps the
+    reference's while loop would (src/diffusion.jl:130-137), computed with the
+    same additions as TimeStepper.advance."""
+    from semgb300.solver import simulate_steps
+
+    def loop(t0, dt, Tf):
+        t, n = t0, 0
+        while t <= Tf:
+            t += dt
+            n += 1
+            if t < 1e-12:
+                break
+        return n
+    for t0, dt, Tf in ((0.0, 1e-3, 0.2), (0.0, 2e-3, 2e-2), (0.0, 0.1, 0.3), (0.5, 0.25, 1.0), (0.0, 0.0, 0.0),
+                       (0.0, 1e-3, 0.0), (1.0, 0.1, 0.5)):
+        assert simulate_steps(t0, dt, Tf) == loop(t0, dt, Tf)
+    assert simulate_steps(0.0, 0.0, 1.0) == 1  # steady: one step, then time < 1e-12 ends the loop
+    with pytest.raises(ValueError):
+        simulate_steps(0.5, 0.0, 1.0)  # the reference would never leave its loop

@@ -143,3 +143,33 @@ def test_c_oracle_matches_numpy():
         got = C.apply(g, msh.Dr, msh.Ds, msh.G11, msh.G12, msh.G22, msh.B, u, nu=0.7, k=1.5)
         assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-14
         np.testing.assert_allclose(C.gather_scatter(g, u), O.gatherScatter(u, msh), rtol=1e-15)
+
+
+def test_grad_and_advect_known_answers():
+    """grad (src/grad.jl:16-34) is exact on polynomials of the element order,
+    and advect (src/advect.jl:27-64) integrates u.grad T over [-1, 1]^2, in
+    the plain and the dealiased form (through a finer GLL grid)."""
+    mo = O.Mesh(7, 7, 3, 2, (False, False), O.identity_deform)
+    gx, gy = O.grad(mo.x ** 3 * mo.y, mo)
+    np.testing.assert_allclose(gx, 3 * mo.x ** 2 * mo.y, atol=1e-11)
+    np.testing.assert_allclose(gy, mo.x ** 3, atol=1e-11)
+    # [-1, 1]^2: T = x^2 y, u = (1, x): integrand 2xy + x^3 is odd -> 0;
+    # T = x^2, u = (x, 0): 2x^2 -> 8/3
+    ones, zeros = np.ones(mo.shape), np.zeros(mo.shape)
+    assert abs(np.sum(O.advect(mo.x ** 2 * mo.y, ones, mo.x, mo))) < 1e-13
+    assert abs(np.sum(O.advect(mo.x ** 2, mo.x, zeros, mo)) - 8.0 / 3.0) < 1e-13
+    mf = O.Mesh(11, 11, 3, 2, (False, False), O.identity_deform)
+    J = O.interpMat(mf.zr, mo.zr)
+    # T = x^4, u = (x^3, 0): 4 x^6 -> 2 * 4/7 * 2; on straight elements the
+    # product of the interpolants stays within the 2n - 3 degrees GLL
+    # integrates, so both forms are exact
+    exact = 16.0 / 7.0
+    dealiased = np.sum(O.advect_dealiased(mo.x ** 4, mo.x ** 3, zeros, mo, mf.B, J, J))
+    plain = np.sum(O.advect(mo.x ** 4, mo.x ** 3, zeros, mo))
+    assert abs(dealiased - exact) < 1e-12 and abs(plain - exact) < 1e-12
+    # on the deformed map the Jacobian is not polynomial: the two forms differ
+    md = O.Mesh(7, 7, 3, 2, (False, False), O.sin_deform(0.1))
+    mdf = O.Mesh(11, 11, 3, 2, (False, False), O.sin_deform(0.1))
+    a = np.sum(O.advect_dealiased(md.x ** 4, md.x ** 3, zeros, md, mdf.B, J, J))
+    b = np.sum(O.advect(md.x ** 4, md.x ** 3, zeros, md))
+    assert 1e-12 < abs(a - b) < 1e-3 * abs(a)
