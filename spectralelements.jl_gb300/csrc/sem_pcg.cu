@@ -844,6 +844,55 @@ int pcg_check(const sem_pcg_opts* o, const double* b, double* x) {
   return SEM_OK;
 }
 
+// the FP64 operator of the solve (the mesh's FP64 arithmetic) applied to x
+// into w.Ap, for residuals r = b - A x
+ApplyCall residual_call(const OpCtx& cx, const sem_mesh* m, const sem_pcg_opts* o, const double* x,
+                        const WS& w) {
+  ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
+  c.u = x;
+  c.out = w.Ap;
+  c.G11 = cx.G11;
+  c.G12 = cx.G12;
+  c.G22 = cx.G22;
+  c.B = cx.B;
+  c.nu_s = o->nu_field ? 1.0 : o->nu;
+  c.k_s = o->k;
+  c.mode = cx.g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (cx.has_bc ? M_MASK : 0u);
+  if (o->nu_field) {
+    c.nu = o->nu_field;
+    c.mode |= M_NUG;
+  }
+  c.precision = m->precision;
+  c.variant = cx.variant[m->precision];
+  c.Gdf = cx.Gdf;
+  c.ctr = cx.ctr;
+  return c;
+}
+
+// Finishes a mixed-precision solve whose FP32 recurrences stopped gaining on
+// the FP64 residual: the FP64 CG solves A d = r (r = b - A x in w.r) from
+// d = 0 to the solve's tolerance, then x += d.  At most `budget` iterations.
+int fp64_finish(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, const sem_pcg_opts* o, double* x,
+                int budget, bool jac, int check_every, Scalars* fr, cudaStream_t s) {
+  const long long L = cx.g.NX * cx.g.NY;
+  const unsigned nb = nblocks(L);
+  double* d = w.x64tmp;
+  double* rd = w.d;
+  k_init<double, double><<<nb, kRT, 0, s>>>(w.r, d, rd, w.p, jac ? w.dinv : nullptr, w.part, gv);
+  k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, budget);
+  SEM_CUDA(cudaGetLastError());
+  SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  SEM_CUDA(cudaStreamSynchronize(s));
+  *fr = *w.sc_h;
+  if (!fr->done)
+    SEM_CHECK(run_cg<double>(m, cx, gv, w, d, rd, w.p, w.Ap, jac ? w.dinv : nullptr, m->precision,
+                             o->nu_field, o->nu, o->k, check_every, fr, s));
+  k_add_d<<<nb, kRT, 0, s>>>(x, d, L);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
 // pcg (src/pcg.jl:16-60) on an operator context with workspace w; the mixed
 // path needs the mesh handle m (FP32 geometry copies)
 int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, const double* b,
@@ -881,6 +930,21 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     res.converged = sp.converged;
     outer = sp.outer;
     res0 = sp.res0_inf;
+    if ((prec == SEM_MIXED || prec == SEM_MIXED_RR) && !res.converged && !res.nan && res.k < maxiter) {
+      // the single-launch mixed solve ran out of sweeps or replacements: the
+      // FP64 CG finishes from the current x, on the whole GPU
+      const ApplyCall c = residual_call(cx, m, o, x, w);
+      SEM_CHECK(launch_apply(cx.g, cx.ops, c, s));
+      k_residual<<<nb, kRT, 0, s>>>(b, w.Ap, w.r, w.part, L);
+      SEM_CUDA(cudaGetLastError());
+      Scalars fr;
+      SEM_CHECK(fp64_finish(m, cx, gv, w, o, x, maxiter - res.k, jac, check_every, &fr, s));
+      res.k += fr.k;
+      res.rmax = fr.rmax;
+      res.nan = fr.nan;
+      res.converged = fr.converged;
+      ++outer;
+    }
   } else if (prec != SEM_MIXED && prec != SEM_MIXED_RR) {
     k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
     k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
@@ -922,25 +986,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     double rmax = *reinterpret_cast<double*>(&w.sc_h[1]);
     res0 = rmax;
     int total_it = 0;
-    ApplyCall c;
-    std::memset(&c, 0, sizeof(c));
-    c.u = x;
-    c.out = w.Ap;
-    c.G11 = cx.G11;
-    c.G12 = cx.G12;
-    c.G22 = cx.G22;
-    c.B = cx.B;
-    c.nu_s = o->nu_field ? 1.0 : o->nu;
-    c.k_s = o->k;
-    c.mode = cx.g.topo | M_STIFF | M_GS | (o->k != 0.0 ? M_MASS : 0u) | (cx.has_bc ? M_MASK : 0u);
-    if (o->nu_field) {
-      c.nu = o->nu_field;
-      c.mode |= M_NUG;
-    }
-    c.precision = m->precision;
-    c.variant = cx.variant[m->precision];
-    c.Gdf = cx.Gdf;
-    c.ctr = cx.ctr;
+    const ApplyCall c = residual_call(cx, m, o, x, w);
     bool nan = rmax != rmax;
     if (rr && !(rmax <= o->tol) && !nan) {
       // one FP32 CG; its residual is replaced by the FP64 b - A x whenever it
@@ -1003,21 +1049,9 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     bool fin_conv = rmax <= o->tol;
     if (!fin_conv && !nan && total_it < maxiter) {
       // the FP32 solves stopped gaining on the FP64 residual (stalled
-      // segment, or the sweep / replacement budget ran out): the FP64 CG
-      // solves A d = r from d = 0 to the same tolerance, then x += d
-      double* d = w.x64tmp;
-      double* rd = w.d;
-      k_init<double, double><<<nb, kRT, 0, s>>>(w.r, d, rd, w.p, jac ? w.dinv : nullptr, w.part, gv);
-      k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter - total_it);
-      SEM_CUDA(cudaGetLastError());
-      SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-      SEM_CUDA(cudaStreamSynchronize(s));
-      Scalars fr = *w.sc_h;
-      if (!fr.done)
-        SEM_CHECK(run_cg<double>(m, cx, gv, w, d, rd, w.p, w.Ap, jac ? w.dinv : nullptr, m->precision,
-                                 o->nu_field, o->nu, o->k, check_every, &fr, s));
-      k_add_d<<<nb, kRT, 0, s>>>(x, d, L);
-      SEM_CUDA(cudaGetLastError());
+      // segment, or the sweep / replacement budget ran out)
+      Scalars fr;
+      SEM_CHECK(fp64_finish(m, cx, gv, w, o, x, maxiter - total_it, jac, check_every, &fr, s));
       total_it += fr.k;
       rmax = fr.rmax;
       nan = nan || fr.nan;

@@ -253,3 +253,24 @@ def test_small_path_options_and_limits(gpu):
     with pytest.raises(S.SemError):
         opb = S.HelmholtzOp(big, 1.0, 0.0)
         S.pcg(S.as_local(np.zeros(big.shape)), opb, mult=big.mult, path=S.SEM_PATH_SMALL)
+
+
+@pytest.mark.parametrize("path", [0, 1])
+@pytest.mark.parametrize("prec_name", ["SEM_MIXED", "SEM_MIXED_RR"])
+def test_mixed_budget_exhausted_finishes_in_fp64(gpu, path, prec_name):
+    """With one sweep / one replacement allowed, the mixed solve cannot reach
+    the tolerance in FP32; the FP64 CG finishes it from the current x, on the
+    single-launch small-mesh path and on the chunked path alike."""
+    import semgb300 as S
+    mo, md = meshes(9, 8, 8, (False, False), "DDDD", 0.1)
+    M = O.generateMask(["D"] * 4, mo)
+    b = O.gatherScatter(O.mask(O.mass(2 * np.pi ** 2 * np.sin(np.pi * mo.x) * np.sin(np.pi * mo.y), mo), M), mo)
+    tol = 1e-11 * np.abs(b).max()
+    op = S.HelmholtzOp(md, 1.0, 0.0)
+    info, info64 = {}, {}
+    x = S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, precision=getattr(S, prec_name),
+              max_outer=1, path=path, info=info)
+    x64 = S.pcg(S.as_local(b), op, opM=S.Jacobi(op), mult=md.mult, tol=tol, path=path, info=info64)
+    assert info["converged"] and info["res_inf"] <= tol, info
+    assert info["outer"] >= 2, info  # the budgeted sweep/segment plus the FP64 finish
+    assert rel_l2(host(x), host(x64)) < 1e-9
