@@ -154,10 +154,15 @@ struct DevScratch {
   }
 };
 
+// pinned host records of queued small-mesh solves; freed only after the
+// stream has consumed them (an error return may leave copies queued)
 struct PinnedRecords {
   SmallProb* h = nullptr;
+  cudaStream_t s = nullptr;
   ~PinnedRecords() {
-    if (h) cudaFreeHost(h);
+    if (!h) return;
+    cudaStreamSynchronize(s);
+    cudaFreeHost(h);
   }
 };
 
@@ -299,6 +304,7 @@ int sem_bdf_run(sem_mesh_t* m, const sem_bdf_desc* d, double* time, double* u, d
   const bool small = small_path_taken(m, &o);
   SmallProb* rec_dev = nullptr;
   PinnedRecords rec_h;
+  rec_h.s = s;
   if (small) {
     SEM_CHECK(sc.get(kBlockSteps, &rec_dev));
     SEM_CUDA(cudaMallocHost(&rec_h.h, sizeof(SmallProb) * kBlockSteps));
