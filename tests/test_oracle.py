@@ -205,3 +205,18 @@ def test_oracle_bdf_time_order(k, order):
     e2 = _oracle_bdf_error(k, 0.01)
     rate = np.log2(e1 / e2)
     assert abs(rate - order) < 0.25, (e1, e2, rate)
+
+
+def test_stiffness_integrals_plain_and_dealiased():
+    """v' A u summed over local copies is the integral of grad v . grad u
+    (src/lapl.jl:70-81, and the over-integrated form of :83-103 with the
+    fine grid's metric): on [-1, 1]^2, u = v = x gives 4, u = v = x^2 gives
+    16/3, and u = x^2, v = 1 gives 0 (the constant is in the kernel)."""
+    mo = O.Mesh(6, 6, 3, 2, (False, False), O.identity_deform)
+    mf = O.Mesh(10, 10, 3, 2, (False, False), O.identity_deform)
+    J = O.interpMat(mf.zr, mo.zr)
+    cases = ((mo.x, mo.x, 4.0), (mo.x ** 2, mo.x ** 2, 16.0 / 3.0), (mo.x ** 2, np.ones(mo.shape), 0.0))
+    for u, v, exact in cases:
+        plain = np.sum(v * O.laplace(u, mo.Dr, mo.Ds, mo.G11, mo.G12, mo.G22))
+        deal = np.sum(v * O.laplace_dealias(u, J, J, mo.Dr, mo.Ds, mf.G11, mf.G12, mf.G22))
+        assert abs(plain - exact) < 1e-12 and abs(deal - exact) < 1e-12, (plain, deal, exact)
