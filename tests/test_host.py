@@ -148,3 +148,37 @@ def test_simulate_step_count_follows_the_reference_loop():
     assert simulate_steps(0.0, 0.0, 1.0) == 1  # steady: one step, then time < 1e-12 ends the loop
     with pytest.raises(ValueError):
         simulate_steps(0.5, 0.0, 1.0)  # the reference would never leave its loop
+
+
+def test_julia_binding_matches_the_header():
+    """SEMB200.jl (not executable here) against include/sem_b200.h: every
+    ccall names a declared entry point, and the Julia mirrors of the C
+    structs have the C field names, in order."""
+    jl = open(os.path.join(ROOT, "spectralelements.jl_gb300", "julia", "SEMB200.jl")).read()
+    hdr = open(os.path.join(ROOT, "include", "sem_b200.h")).read()
+    declared = set(_header_functions())
+    called = set(re.findall(r"ccall\(\(:(sem_[a-z0-9_]+),", jl))
+    assert called and called <= declared, called - declared
+    hdr_nc = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+
+    def c_fields(tag):
+        end = re.search(r"\}\s*" + tag + r"\s*;", hdr_nc).start()
+        start = hdr_nc.rfind("typedef struct {", 0, end) + len("typedef struct {")
+        names = []
+        for decl in hdr_nc[start:end].split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            # "const double* const* F" -> F; "int nr, ns, Ex, Ey" -> nr, ns, Ex, Ey
+            head, _, rest = decl.partition(",")
+            names.append(re.findall(r"\w+", head)[-1])
+            names += [re.findall(r"\w+", n)[-1] for n in rest.split(",") if rest]
+        return names
+
+    def jl_fields(name):
+        body = re.search(r"\nstruct " + name + r"\n(.*?)\nend", jl, flags=re.S).group(1)
+        return re.findall(r"(\w+)::", body)
+    assert jl_fields("PcgOpts") == c_fields("sem_pcg_opts")
+    assert jl_fields("SolveInfo") == c_fields("sem_solve_info")
+    assert jl_fields("BdfDesc") == c_fields("sem_bdf_desc")
+    assert jl_fields("MeshDesc") == c_fields("sem_mesh_desc")
