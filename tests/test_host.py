@@ -152,8 +152,8 @@ def test_simulate_step_count_follows_the_reference_loop():
 
 def test_julia_binding_matches_the_header():
     """SEMB200.jl (not executable here) against include/sem_b200.h: every
-    ccall names a declared entry point, and the Julia mirrors of the C
-    structs have the C field names, in order."""
+    ccall names a declared entry point, and the Julia and ctypes mirrors of
+    the C structs have the C field names, in order."""
     jl = open(os.path.join(ROOT, "spectralelements.jl_gb300", "julia", "SEMB200.jl")).read()
     hdr = open(os.path.join(ROOT, "include", "sem_b200.h")).read()
     declared = set(_header_functions())
@@ -178,7 +178,9 @@ def test_julia_binding_matches_the_header():
     def jl_fields(name):
         body = re.search(r"\nstruct " + name + r"\n(.*?)\nend", jl, flags=re.S).group(1)
         return re.findall(r"(\w+)::", body)
-    assert jl_fields("PcgOpts") == c_fields("sem_pcg_opts")
-    assert jl_fields("SolveInfo") == c_fields("sem_solve_info")
-    assert jl_fields("BdfDesc") == c_fields("sem_bdf_desc")
-    assert jl_fields("MeshDesc") == c_fields("sem_mesh_desc")
+    for jl_name, c_name, py in (("PcgOpts", "sem_pcg_opts", _lib.PcgOpts),
+                                ("SolveInfo", "sem_solve_info", _lib.SolveInfo),
+                                ("BdfDesc", "sem_bdf_desc", _lib.BdfDesc),
+                                ("MeshDesc", "sem_mesh_desc", _lib.MeshDesc)):
+        assert jl_fields(jl_name) == c_fields(c_name), jl_name
+        assert [f[0] for f in py._fields_] == c_fields(c_name), c_name  # the ctypes mirror too
