@@ -295,7 +295,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clocks,
         "f64_native_apply": {"ms": t64, "GDOF/s": G / (t64 * 1e-3) / 1e9},
     }
-    if not args.no_extras:
+    if not args.no_extras and world == 1:  # the N-replica runs measure the headline only
         extras = args.extras.split(",") if args.extras else ["pcg", "sweep", "batch", "adjoint", "time"]
         if "pcg" in extras:
             result["pcg"] = bench_pcg(S, msh, stream)
