@@ -170,6 +170,12 @@ int sem_mass(sem_mesh_t* mesh, const double* u, double* out, unsigned flags,
 /* gatherScatter(u,msh) = QQ' u (src/gatherScatter.jl:8-21) */
 int sem_gather_scatter(sem_mesh_t* mesh, const double* u, double* out,
                        sem_stream_t stream);
+/* functional gatherScatter(u,QQtx,QQty) (src/gatherScatter.jl:8-16) without a
+ * handle: QQtx/QQty are those of semq(Ex,nr,periodic_x) and semq(Ey,ns,
+ * periodic_y) (src/semq.jl:6-25); nr may differ from ns.  Bit-identical to
+ * sem_gather_scatter on a handle of the same grid. */
+int sem_gather_scatter_grid(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y,
+                            const double* u, double* out, sem_stream_t stream);
 /* mask(u,M) = M .* u (src/mask.jl:10-18); M a device array or NULL (copy) */
 int sem_mask(const double* M, const double* u, double* out, int64_t len,
              sem_stream_t stream);
@@ -265,18 +271,22 @@ int sem_pcg(sem_mesh_t* mesh, const sem_pcg_opts* opts, const double* b, double*
  * For callers that may not allocate device memory while they run, such as an
  * application's allocation-free real-time loop, a memory manager that owns
  * every device byte, or a plug-in that may not grow the process's device
- * footprint.  It is the same solve as sem_pcg (opA = mask(QQ'(hlmz)), SEM_F64
- * or SEM_F64_DF, Jacobi or no preconditioner). The mesh is described by
- * arguments instead of a handle: nr = ns, host Dr/Ds, and DEVICE G11, G12,
- * G22, B in the local layout.  All scratch vectors live in one fixed
- * file-scope device array sized for SEM_NOALLOC_MAX_LOCAL local DOF, about
- * 13.4 MB, which every GPU that loads the library holds until the process
- * exits.  The call allocates nothing: no cudaMalloc, cudaFree, pinned host
- * memory or library allocator.  Larger meshes are rejected with
- * SEM_ERR_BAD_ARG.
- *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) once for that device.  Make that first call
- *    before any stream capture.
+ * footprint.  It is the solve of sem_pcg (opA = mask(QQ'(hlmz)), SEM_F64 or
+ * SEM_F64_DF, Jacobi or no preconditioner) with the direct operator kernel
+ * (variant 0: no pre-split geometry), so it runs slower than a tuned sem_pcg
+ * on a mesh handle. The mesh is described by arguments instead of a handle:
+ * nr = ns, host Dr/Ds, and DEVICE G11, G12, G22, B in the local layout.  All
+ * scratch vectors live in one fixed file-scope device array sized for
+ * SEM_NOALLOC_MAX_LOCAL local DOF, about 13.4 MB.  The call allocates
+ * nothing: no cudaMalloc, cudaFree, pinned host memory or library allocator.
+ * Larger meshes are rejected with SEM_ERR_BAD_ARG.
+ *  - Every call looks up the array's device address on the current device
+ *    (cudaGetSymbolAddress).  With CUDA's default lazy module loading the
+ *    first call on a device loads the array and the kernels there, which
+ *    grows that device's memory use once; the array then stays until the
+ *    process exits.  Make a warm-up call of the same order and precision on
+ *    each device before the allocation-free region, and before any stream
+ *    capture.
  *  - Every call reuses the same array and overwrites the part it needs, so
  *    calls whose GPU work overlaps (two streams, two host threads) race and
  *    corrupt each other's results; serialise them.

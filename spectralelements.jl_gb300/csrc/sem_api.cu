@@ -403,6 +403,17 @@ int sem_gather_scatter(sem_mesh_t* m, const double* u, double* out, sem_stream_t
   return launch_gather_scatter(m->g, u, out, m->g.topo, (cudaStream_t)stream);
 }
 
+int sem_gather_scatter_grid(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y, const double* u,
+                            double* out, sem_stream_t stream) {
+  if (nr < 1 || ns < 1 || Ex < 1 || Ey < 1) return set_error(SEM_ERR_BAD_ARG, "bad sizes");
+  if ((long long)nr * Ex >= (1LL << 31) || (long long)ns * Ey >= (1LL << 31))
+    return set_error(SEM_ERR_UNSUPPORTED, "local dimensions must be below 2^31");
+  if (!u || !out) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (u == out) return set_error(SEM_ERR_BAD_ARG, "gatherScatter output must not alias its input");
+  return launch_gather_scatter_grid(nr, ns, Ex, Ey, periodic_x != 0, periodic_y != 0, u, out,
+                                    (cudaStream_t)stream);
+}
+
 int sem_mask(const double* M, const double* u, double* out, int64_t len, sem_stream_t stream) {
   if (len < 0) return set_error(SEM_ERR_BAD_ARG, "negative length");
   if (len > 0 && (!u || !out)) return set_error(SEM_ERR_BAD_ARG, "NULL field");

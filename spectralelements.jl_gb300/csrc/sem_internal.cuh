@@ -316,6 +316,8 @@ int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& 
 
 // elementwise / structured kernels (sem_vec.cu)
 int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode, cudaStream_t s);
+int launch_gather_scatter_grid(int nr, int ns, int Ex, int Ey, bool perx, bool pery, const double* u,
+                               double* out, cudaStream_t s);
 int launch_mask_bc(const Grid& g, const double* u, double* out, unsigned topo, cudaStream_t s);
 int launch_mask_array(const double* M, const double* u, double* out, int64_t len, cudaStream_t s);
 int launch_mass(const Grid& g, const double* B, const double* u, double* out, cudaStream_t s);

@@ -1177,8 +1177,13 @@ int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
 // manager that owns every device byte, a plug-in that may not grow the
 // process's device footprint).  sem_pcg_noalloc serves them: the caller
 // passes the geometry, b and x, and every scratch vector of the solve lives in
-// the file-scope device array below.  Its size is fixed at build time, so
-// every GPU that loads this library holds it until the process exits.
+// the file-scope device array below.  Its size is fixed at build time.  With
+// CUDA's default lazy module loading the array and the kernels are loaded on
+// a device by the first call there, and stay until the process exits, so the
+// first call (a warm-up of the same order and precision) belongs before any
+// allocation-free region and before any stream capture.  The solve runs the
+// direct operator kernel (variant 0, no pre-split geometry, which would need
+// more scratch), so it is slower than a tuned sem_pcg on a mesh handle.
 // ---------------------------------------------------------------------------
 namespace sem {
 namespace {
@@ -1200,23 +1205,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sem::kNoAllocBy
 namespace sem {
 namespace {
 
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64] = {nullptr};
-
-// device address of the scratch array for the current device, looked up once
-// per device (the array's host-side name is not a device address)
+// device address of the scratch array for the current device.  The array's
+// host-side name is not a device address; the lookup runs on every call, so a
+// device whose context was reset and recreated gets the address of its new
+// module image, never a stale one.
 int noalloc_scratch(void** out) {
-  int dev = 0;
-  SEM_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return set_error(SEM_ERR_UNSUPPORTED, "device index %d out of range", dev);
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  *out = p;
   return SEM_OK;
 }
 

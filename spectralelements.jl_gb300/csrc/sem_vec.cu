@@ -46,6 +46,40 @@ __global__ void k_gather_scatter(const double* __restrict__ u, double* __restric
   });
 }
 
+// QQ' u on a grid described by its sizes alone (no mesh handle): the
+// functional gatherScatter(u,QQtx,QQty) (src/gatherScatter.jl:8-16), which
+// may have nr != ns.  Same sums in the same order as k_gather_scatter.
+struct GsGrid {
+  long long NX, NY;
+  int nr, ns, Ex, Ey;
+  bool perx, pery;
+};
+
+__global__ void k_gather_scatter_grid(const double* __restrict__ u, double* __restrict__ out, GsGrid q) {
+  const long long NX = q.NX, total = q.NX * q.NY;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long c = idx / NX, r = idx - c * NX;
+    const long long pr = line_partner(r, line_info(r, q.nr, q.Ex, q.perx, false, false), q.NX);
+    const long long pc = line_partner(c, line_info(c, q.ns, q.Ey, q.pery, false, false), q.NY);
+    const long long r0 = (pr >= 0 && pr < r) ? pr : r;
+    const long long r1 = (pr >= 0 && pr < r) ? r : pr;
+    auto xsum = [&](long long cc) {
+      double s = u[r0 + cc * NX];
+      if (r1 >= 0) s += u[r1 + cc * NX];
+      return s;
+    };
+    double v;
+    if (pc < 0) {
+      v = xsum(c);
+    } else {
+      const long long c0 = pc < c ? pc : c, c1 = pc < c ? c : pc;
+      v = xsum(c0) + xsum(c1);
+    }
+    out[idx] = v;
+  }
+}
+
 __global__ void k_mask_bc(const double* __restrict__ u, double* __restrict__ out, Grid g) {
   for_each_point(g, [&](unsigned r, unsigned c, long long idx) {
     const double v = u[idx];
@@ -168,6 +202,22 @@ int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned 
                           cudaStream_t s) {
   if (!g.rinfo) return set_error(SEM_ERR_BAD_ARG, "gather-scatter needs a mesh handle");
   k_gather_scatter<<<grid_for(g.NX * g.NY), kThreads, 0, s>>>(u, out, g, mode);
+  SEM_CUDA(cudaGetLastError());
+  return SEM_OK;
+}
+
+int launch_gather_scatter_grid(int nr, int ns, int Ex, int Ey, bool perx, bool pery, const double* u,
+                               double* out, cudaStream_t s) {
+  GsGrid q;
+  q.NX = (long long)nr * Ex;
+  q.NY = (long long)ns * Ey;
+  q.nr = nr;
+  q.ns = ns;
+  q.Ex = Ex;
+  q.Ey = Ey;
+  q.perx = perx;
+  q.pery = pery;
+  k_gather_scatter_grid<<<grid_for(q.NX * q.NY), kThreads, 0, s>>>(u, out, q);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
 }

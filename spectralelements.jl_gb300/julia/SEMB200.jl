@@ -15,7 +15,9 @@ module SEMB200
 
 using CUDA
 import ChainRulesCore
-import SpectralElements: ABu, lapl, mass, hlmz, gatherScatter, mask, pcg, pcg!, Mesh, generateMask
+import SpectralElements: ABu, lapl, mass, hlmz, gatherScatter, mask, pcg, pcg!, Mesh, generateMask,
+                         linsolve
+using LinearAlgebra: I
 
 const libsem = get(ENV, "SEM_B200_LIB", joinpath(@__DIR__, "..", "lib", "libsem_b200.so"))
 
@@ -150,6 +152,134 @@ function gatherScatter(u::CuArray{Float64,2}, msh::Mesh)
     check(ccall((:sem_gather_scatter, libsem), Cint, (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ptr{Cvoid}),
                 handle(msh), pointer(u), pointer(out), stream()))
     return out
+end
+
+# ---- functional forms on explicit operands (no Mesh): the calls of
+# examples/p2d_explicit.jl:183-190 and examples/semPS.jl:157-175.
+# QQtx/QQty are the reference's host gather-scatter matrices (Q Q' of semq);
+# their numbering (points per element, elements, periodicity) is read from
+# their couplings, and the sums run on the device without the matrices.
+# An empty QQtx/QQty ([]) leaves the field unassembled, an empty M unmasked,
+# empty Jr/Js select the plain (not dealiased) quadrature, as in the reference.
+function qq_structure(QQ::AbstractMatrix)
+    NL = size(QQ, 1)
+    size(QQ, 2) == NL || throw(ArgumentError("QQ must be square"))
+    periodic = NL > 1 && QQ[1, NL] != 0
+    n = NL
+    for i in 2:NL-1                      # n >= 2: first interface between lines n and n+1
+        if QQ[i, i+1] != 0
+            n = i
+            break
+        end
+    end
+    NL % n == 0 || throw(ArgumentError("QQ is not the gather-scatter matrix of a semq numbering"))
+    return n, div(NL, n), periodic
+end
+
+devarray(A::CuArray{Float64}) = A
+devarray(A::AbstractArray) = CuArray{Float64}(Float64.(A))
+
+# gatherScatter(u,QQtx,QQty) (src/gatherScatter.jl:8-16) -> sem_gather_scatter_grid
+function gatherScatter(u::CuArray{Float64,2}, QQtx::AbstractMatrix, QQty::AbstractMatrix)
+    nr, Ex, px = qq_structure(QQtx)
+    ns, Ey, py = qq_structure(QQty)
+    size(u) == (nr * Ex, ns * Ey) || throw(DimensionMismatch("u does not match QQtx/QQty"))
+    out = similar(u)
+    check(ccall((:sem_gather_scatter_grid, libsem), Cint,
+                (Cint, Cint, Cint, Cint, Cint, Cint, CuPtr{Cdouble}, CuPtr{Cdouble}, Ptr{Cvoid}),
+                nr, ns, Ex, Ey, px, py, pointer(u), pointer(out), stream()))
+    return out
+end
+
+function assemble_mask(v::CuArray{Float64,2}, M, QQtx, QQty)
+    w = (length(QQtx) == 0 && length(QQty) == 0) ? v : gatherScatter(v, QQtx, QQty)
+    return length(M) == 0 ? w : mask(w, devarray(M))
+end
+
+# functional lapl(u,M,Jr,Js,QQtx,QQty,Dr,Ds,G11,G12,G22,mult) (src/lapl.jl:54-68):
+# plain quadrature -> sem_lapl_geom (the fused element operator), dealiased ->
+# sem_laplace_dealiased; then QQ' (sem_gather_scatter_grid) and the mask
+function lapl(u::CuArray{Float64,2}, M, Jr, Js, QQtx, QQty, Dr::AbstractMatrix, Ds::AbstractMatrix,
+              G11::CuArray{Float64,2}, G12::CuArray{Float64,2}, G22::CuArray{Float64,2}, mult;
+              precision=SEM_F64_DF)
+    nr, ns = size(Dr, 1), size(Ds, 1)
+    Ex, Ey = div(size(u, 1), nr), div(size(u, 2), ns)
+    Drm, Dsm = Matrix{Float64}(Dr), Matrix{Float64}(Ds)
+    out = similar(u)
+    if length(Jr) == 0 && length(Js) == 0
+        px = length(QQtx) > 0 && qq_structure(QQtx)[3]
+        py = length(QQty) > 0 && qq_structure(QQty)[3]
+        flags = length(QQtx) > 0 ? SEM_GS : Cuint(0)
+        GC.@preserve Drm Dsm check(ccall((:sem_lapl_geom, libsem), Cint,
+            (Cint, Cint, Cint, Cint, Cint, Cint, Cstring, Ptr{Cdouble}, Ptr{Cdouble}, CuPtr{Cdouble},
+             CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Cint, Ptr{Cvoid}),
+            nr, ns, Ex, Ey, px, py, C_NULL, Drm, Dsm, pointer(G11), pointer(G12), pointer(G22),
+            pointer(u), pointer(out), flags, precision, stream()))
+        return length(M) == 0 ? out : mask(out, devarray(M))
+    end
+    Jrm = length(Jr) == 0 ? Matrix{Float64}(I, nr, nr) : Matrix{Float64}(Jr)
+    Jsm = length(Js) == 0 ? Matrix{Float64}(I, ns, ns) : Matrix{Float64}(Js)
+    GC.@preserve Drm Dsm Jrm Jsm check(ccall((:sem_laplace_dealiased, libsem), Cint,
+        (Cint, Cint, Cint, Cint, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+         CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ptr{Cvoid}),
+        nr, size(Jrm, 1), size(Jsm, 1), Ex, Ey, Jrm, Jsm, Drm, Dsm, pointer(G11), pointer(G12),
+        pointer(G22), pointer(u), pointer(out), stream()))
+    return assemble_mask(out, M, QQtx, QQty)
+end
+
+# functional mass(u,M,B,Jr,Js,QQtx,QQty,mult) (src/mass.jl:32-50):
+# J'(B .* (J u)) (sem_mass_dealiased, or B .* u through sem_mask), QQ', mask
+function mass(u::CuArray{Float64,2}, M, B, Jr, Js, QQtx, QQty, mult)
+    out = similar(u)
+    if length(Jr) == 0 && length(Js) == 0
+        length(B) == 0 ? copyto!(out, u) : (out = mask(u, devarray(B)))
+        return assemble_mask(out, M, QQtx, QQty)
+    end
+    n = length(Jr) == 0 ? size(Js, 2) : size(Jr, 2)
+    Ex, Ey = div(size(u, 1), n), div(size(u, 2), n)
+    Jrm = length(Jr) == 0 ? Matrix{Float64}(I, n, n) : Matrix{Float64}(Jr)
+    Jsm = length(Js) == 0 ? Matrix{Float64}(I, n, n) : Matrix{Float64}(Js)
+    Bd = length(B) == 0 ? nothing : devarray(B)
+    GC.@preserve Jrm Jsm check(ccall((:sem_mass_dealiased, libsem), Cint,
+        (Cint, Cint, Cint, Cint, Cint, Ptr{Cdouble}, Ptr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble},
+         CuPtr{Cdouble}, Ptr{Cvoid}),
+        n, size(Jrm, 1), size(Jsm, 1), Ex, Ey, Jrm, Jsm, Bd === nothing ? CU_NULL : pointer(Bd),
+        pointer(u), pointer(out), stream()))
+    return assemble_mask(out, M, QQtx, QQty)
+end
+
+# Pullbacks of the functional forms in u, with the reference's convention:
+# the cotangent reaching the unassembled operator output is scaled by mult
+# (the Zygote.hook(d -> d .* mult, .) of src/lapl.jl:62 and src/mass.jl:45),
+# and laplace / J'BJ are symmetric, so the same device calls apply the
+# transpose.  Cotangents of the geometry and operator matrices are not
+# implemented here (the reference's own AD serves them on host arrays).
+function ChainRulesCore.rrule(::typeof(lapl), u::CuArray{Float64,2}, M, Jr, Js, QQtx, QQty, Dr, Ds,
+                              G11, G12, G22, mult; kw...)
+    y = lapl(u, M, Jr, Js, QQtx, QQty, Dr, Ds, G11, G12, G22, mult; kw...)
+    function lapl_pullback(ȳ)
+        d = assemble_mask(CuArray{Float64,2}(ChainRulesCore.unthunk(ȳ)), M, QQtx, QQty)
+        d = mask(d, devarray(mult))
+        ū = lapl(d, [], Jr, Js, [], [], Dr, Ds, G11, G12, G22, mult; kw...)
+        nt = ChainRulesCore.@not_implemented("geometry and operator cotangents of the device lapl")
+        return (ChainRulesCore.NoTangent(), ū, ChainRulesCore.NoTangent(), nt, nt,
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), nt, nt, nt, nt, nt,
+                ChainRulesCore.NoTangent())
+    end
+    return y, lapl_pullback
+end
+
+function ChainRulesCore.rrule(::typeof(mass), u::CuArray{Float64,2}, M, B, Jr, Js, QQtx, QQty, mult)
+    y = mass(u, M, B, Jr, Js, QQtx, QQty, mult)
+    function mass_pullback(ȳ)
+        d = assemble_mask(CuArray{Float64,2}(ChainRulesCore.unthunk(ȳ)), M, QQtx, QQty)
+        d = mask(d, devarray(mult))
+        ū = mass(d, [], B, Jr, Js, [], [], mult)
+        nt = ChainRulesCore.@not_implemented("B and interpolation cotangents of the device mass")
+        return (ChainRulesCore.NoTangent(), ū, ChainRulesCore.NoTangent(), nt, nt, nt,
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+    end
+    return y, mass_pullback
 end
 
 function mask(u::CuArray{Float64,2}, M::CuArray{Float64,2})
@@ -302,16 +432,22 @@ function bdf_run!(u::CuArray{Float64,2}, uh::Vector{<:CuArray{Float64,2}}, time:
     return info
 end
 
-# ---- differentiable solve of -div(ν grad u) = f with ν folded into G
+# ---- differentiable solve of -div(ν grad u) + k u = f with ν folded into G
 # (examples/semPS.jl:163-165), the pattern of linsolve + @adjoint in
-# src/adjoint.jl:5-24 as a ChainRulesCore rrule: the pullback solves the
-# adjoint system for λ and returns the per-local-copy gradient
-# -G:(grad λ)(grad u) (sem_adjoint_grad).
+# src/adjoint.jl:5-24 as ChainRulesCore rrules.  The pullbacks solve the
+# adjoint system A λ = mask(QQ'(ū)) and pull back the whole residual
+# rhs - lhs(ν)(u) (src/adjoint.jl:13-16):
+#  - ν: the per-local-copy gradient -G:(grad λ)(grad u) (sem_adjoint_grad);
+#  - the right-hand side: mult .* λ.  Fields are local (a global node is stored
+#    once per element that holds it) and the cotangents of AD sum over local
+#    entries, so an assembled field's cotangent is the global adjoint spread
+#    over its copies: a right-hand side mask(QQ'(B f)) then pulls back to
+#    B .* λ at f, which central differences in f reproduce.
 function varcoef_solve(ν::CuArray{Float64,2}, b::CuArray{Float64,2}, msh::Mesh, bc::Vector{Char};
-                       tol=1e-10)
+                       tol=1e-10, k=0.0, precision=SEM_F64_DF)
     set_bc!(msh, bc)
     x = similar(b)
-    o = Ref(PcgOpts(1.0, pointer(ν), 0.0, 1, SEM_F64_DF, tol, 0, 1e-4, 6, 0, 0, 0))
+    o = Ref(PcgOpts(1.0, pointer(ν), k, 1, precision, tol, 0, 1e-4, 6, 0, 0, 0))
     info = Ref(SolveInfo())
     check(ccall((:sem_pcg, libsem), Cint,
                 (Ptr{Cvoid}, Ref{PcgOpts}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ref{SolveInfo}, Ptr{Cvoid}),
@@ -319,21 +455,96 @@ function varcoef_solve(ν::CuArray{Float64,2}, b::CuArray{Float64,2}, msh::Mesh,
     return x
 end
 
+function adjoint_state(ū, ν, msh::Mesh, bc::Vector{Char}; kw...)
+    rhs = gatherScatter(mask(CuArray{Float64,2}(ChainRulesCore.unthunk(ū)),
+                             CuArray(Float64.(generateMask(bc, msh)))), msh)
+    return varcoef_solve(ν, rhs, msh, bc; kw...)
+end
+
+function adjoint_grad(λ::CuArray{Float64,2}, u::CuArray{Float64,2}, msh::Mesh)
+    g = similar(u)
+    check(ccall((:sem_adjoint_grad, libsem), Cint,
+                (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
+                handle(msh), pointer(λ), pointer(u), pointer(g), 0, stream()))
+    return g
+end
+
+function axpby(α, x::CuArray{Float64,2}, β, y::CuArray{Float64,2})
+    out = similar(x)
+    check(ccall((:sem_axpby, libsem), Cint,
+                (Cdouble, CuPtr{Cdouble}, Cdouble, CuPtr{Cdouble}, CuPtr{Cdouble}, Int64, Ptr{Cvoid}),
+                α, pointer(x), β, pointer(y), pointer(out), length(x), stream()))
+    return out
+end
+
 function ChainRulesCore.rrule(::typeof(varcoef_solve), ν::CuArray{Float64,2}, b::CuArray{Float64,2},
-                              msh::Mesh, bc::Vector{Char}; tol=1e-10)
-    u = varcoef_solve(ν, b, msh, bc; tol=tol)
+                              msh::Mesh, bc::Vector{Char}; kw...)
+    u = varcoef_solve(ν, b, msh, bc; kw...)
     function varcoef_solve_pullback(ū)
-        rhs = gatherScatter(mask(CuArray{Float64,2}(ChainRulesCore.unthunk(ū)),
-                                 CuArray(Float64.(generateMask(bc, msh)))), msh)
-        λ = varcoef_solve(ν, rhs, msh, bc; tol=tol)
-        g = similar(u)
-        check(ccall((:sem_adjoint_grad, libsem), Cint,
-                    (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cuint, Ptr{Cvoid}),
-                    handle(msh), pointer(λ), pointer(u), pointer(g), 0, stream()))
-        return ChainRulesCore.NoTangent(), g, ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(),
+        λ = adjoint_state(ū, ν, msh, bc; kw...)
+        b̄ = mask(λ, CuArray(msh.mult))
+        return ChainRulesCore.NoTangent(), adjoint_grad(λ, u, msh), b̄, ChainRulesCore.NoTangent(),
                ChainRulesCore.NoTangent()
     end
     return u, varcoef_solve_pullback
+end
+
+# ---- linsolve(a,problem,solver) (src/adjoint.jl:5-24) on CuArrays.
+# problem(a) returns (lhs, rhs): lhs the G-folded operator mask(QQ'(D'(a G)D + k B))
+# of `msh` under `bc`, rhs = problem.rhs(a) (any differentiable function of a
+# returning a local CuArray) or a fixed field; solver(lhs, rhs, adjoint) is
+# Jacobi PCG on the device (the operator is symmetric, so the adjoint solve is
+# the same solve).  Other problem or solver types have no device path.
+struct VarCoefProblem
+    msh::Mesh
+    bc::Vector{Char}
+    rhs::Any
+    k::Float64
+end
+VarCoefProblem(msh::Mesh, bc::Vector{Char}, rhs; k=0.0) = VarCoefProblem(msh, bc, rhs, Float64(k))
+
+struct VarCoefLHS
+    msh::Mesh
+    bc::Vector{Char}
+    a::CuArray{Float64,2}
+    k::Float64
+end
+(p::VarCoefProblem)(a::CuArray{Float64,2}) =
+    (VarCoefLHS(p.msh, p.bc, a, p.k), p.rhs isa Function ? p.rhs(a) : p.rhs)
+
+struct PcgSolver
+    tol::Float64
+    precision::Cint
+end
+PcgSolver(; tol=1e-10, precision=SEM_F64_DF) = PcgSolver(tol, precision)
+(s::PcgSolver)(lhs::VarCoefLHS, rhs::CuArray{Float64,2}, adjoint::Bool) =
+    varcoef_solve(lhs.a, rhs, lhs.msh, lhs.bc; tol=s.tol, k=lhs.k, precision=s.precision)
+
+function linsolve(a::CuArray{Float64,2}, problem::VarCoefProblem, solver::PcgSolver)
+    lhs, rhs = problem(a)
+    return solver(lhs, rhs, false)
+end
+linsolve(a::CuArray, problem, solver) =
+    throw(ArgumentError("linsolve on CuArrays takes a SEMB200.VarCoefProblem and a SEMB200.PcgSolver"))
+
+function ChainRulesCore.rrule(config::ChainRulesCore.RuleConfig{>:ChainRulesCore.HasReverseMode},
+                              ::typeof(linsolve), a::CuArray{Float64,2}, problem::VarCoefProblem,
+                              solver::PcgSolver)
+    lhs = VarCoefLHS(problem.msh, problem.bc, a, problem.k)
+    rhs, rhs_back = problem.rhs isa Function ?
+        ChainRulesCore.rrule_via_ad(config, problem.rhs, a) : (problem.rhs, nothing)
+    u = solver(lhs, rhs, false)
+    kw = (tol=solver.tol, k=problem.k, precision=solver.precision)
+    function linsolve_pullback(ū)
+        λ = adjoint_state(ū, a, problem.msh, problem.bc; kw...)
+        ā = adjoint_grad(λ, u, problem.msh)                    # -λ' d(lhs(a) u)/da
+        if rhs_back !== nothing
+            r̄ = ChainRulesCore.unthunk(rhs_back(mask(λ, CuArray(problem.msh.mult)))[2])
+            ā = axpby(1.0, ā, 1.0, CuArray{Float64,2}(r̄))     # + λ' d rhs(a)/da
+        end
+        return ChainRulesCore.NoTangent(), ā, ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent()
+    end
+    return u, linsolve_pullback
 end
 
 end # module

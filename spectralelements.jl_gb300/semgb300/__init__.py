@@ -13,12 +13,13 @@ from .mesh import Mesh, QQt, as_local, generateMask, local_empty  # noqa: F401
 from .ops import ABu, advect, gatherScatter, grad, gradT, hlmz, lapl, mask, mass  # noqa: F401
 from . import spectral  # noqa: F401
 from .solver import (BatchSolver, Diffusion, HelmholtzOp, Jacobi, TimeStepper, identity,  # noqa: F401
-                     linsolve_varcoef, pcg, pcg_, transient_varcoef)
+                     linsolve, linsolve_varcoef, pcg, pcg_, transient_varcoef,
+                     PcgSolver, VarCoefProblem)
 
 __all__ = ["Mesh", "QQt", "generateMask", "ABu", "lapl", "mass", "hlmz", "gatherScatter", "mask",
            "grad", "gradT", "advect",
            "pcg", "pcg_", "HelmholtzOp", "Jacobi", "identity", "Diffusion", "TimeStepper",
-           "linsolve_varcoef", "gausslobatto", "derivMat", "interpMat", "semmesh", "ndgrid",
+           "linsolve_varcoef", "linsolve", "VarCoefProblem", "PcgSolver", "gausslobatto", "derivMat", "interpMat", "semmesh", "ndgrid",
            "semq_index", "bdfExtK", "fixU", "as_local", "local_empty", "build", "load",
            "SemError", "NotConverged", "SEM_F64", "SEM_F64_DF", "SEM_F32", "SEM_MIXED",
            "SEM_GS", "SEM_MASK", "SEM_MIXED_RR", "SEM_PATH_AUTO", "SEM_PATH_CHUNKED", "SEM_PATH_SMALL",

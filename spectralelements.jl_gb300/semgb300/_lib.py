@@ -150,6 +150,7 @@ SIGNATURES = {
     "sem_hlmz_host": (_I, [_P, _P, _D, _D, _P, _P, _U, _I, _P]),
     "sem_mass": (_I, [_P, _P, _P, _U, _P]),
     "sem_gather_scatter": (_I, [_P, _P, _P, _P]),
+    "sem_gather_scatter_grid": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _P]),
     "sem_mask": (_I, [_P, _P, _P, _L, _P]),
     "sem_mask_bc": (_I, [_P, _P, _P, _P]),
     "sem_lapl_geom": (_I, [_I, _I, _I, _I, _I, _I, ctypes.c_char_p, _P, _P, _P, _P, _P, _P, _P,

@@ -135,3 +135,29 @@ def bdfExtK(t, k: int = 3):
 def fixU(x, y):
     """Identity deformation (src/mesh.jl:6-8)."""
     return x, y
+
+
+def qq_structure(QQ):
+    """(n, E, periodic) of a one-direction gather-scatter matrix QQ = Q Q' with
+    Q = semq(E, n, periodic) (src/semq.jl:6-25), read from its couplings: the
+    first element interface couples local lines n-1 and n (0-based) and a
+    periodic direction couples the first and the last line.  Raises
+    ValueError for a matrix without that structure."""
+    Q = np.asarray(QQ)
+    if Q.ndim != 2 or Q.shape[0] != Q.shape[1] or Q.shape[0] < 1:
+        raise ValueError("QQ must be a square matrix")
+    NL = Q.shape[0]
+    periodic = NL > 1 and Q[0, NL - 1] != 0
+    n = NL
+    for i in range(1, NL - 1):  # n >= 2: the first interface is at line n - 1 >= 1
+        if Q[i, i + 1] != 0:
+            n = i + 1
+            break
+    if n < 1 or NL % n:
+        raise ValueError("QQ is not the gather-scatter matrix of a semq numbering")
+    E = NL // n
+    # the couplings of every interface, and nothing else off the diagonal band
+    for e in range(1, E):
+        if Q[e * n - 1, e * n] == 0:
+            raise ValueError("QQ is not the gather-scatter matrix of a semq numbering")
+    return n, E, bool(periodic)

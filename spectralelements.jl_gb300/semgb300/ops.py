@@ -249,12 +249,30 @@ def gatherScatter(u, *args):
         msh = args[0]._mesh() if args[0]._mesh is not None else None
         if msh is None:
             raise ValueError("QQt is not attached to a live mesh")
+    elif len(args) == 2:
+        # dense (or array-like) QQtx, QQty: the numbering is read from them
+        from .host import qq_structure
+        nr, Ex, px = qq_structure(_host_matrix(args[0]))
+        ns, Ey, py = qq_structure(_host_matrix(args[1]))
+        u = as_local(u)
+        if tuple(u.shape) != (nr * Ex, ns * Ey):
+            raise ValueError("field shape does not match QQtx/QQty")
+        out = local_empty(*u.shape)
+        _lib.check(lib.sem_gather_scatter_grid(nr, ns, Ex, Ey, int(px), int(py), u.data_ptr(),
+                                               out.data_ptr(), stream_ptr()))
+        return out
     else:
         raise TypeError("gatherScatter(u, msh) or gatherScatter(u, msh.QQtx, msh.QQty)")
     u = _field(u, msh)
     out = msh.empty()
     _lib.check(lib.sem_gather_scatter(msh.handle, u.data_ptr(), out.data_ptr(), stream_ptr()))
     return out
+
+
+def _host_matrix(A):
+    if isinstance(A, torch.Tensor):
+        return A.detach().cpu().numpy()
+    return np.asarray(A)
 
 
 def mask(u, M):

@@ -233,16 +233,25 @@ def pcg_(x, b, opA, **kw):
 # adjoint: linsolve with a custom backward (src/adjoint.jl:5-24)
 # ---------------------------------------------------------------------------
 class _VarCoefSolve(torch.autograd.Function):
-    """u = A(nu)^{-1} b with A(nu) = mask(QQ'(D'(nu G)D)); backward returns the
-    per-local-copy gradient  -G:(grad lam)(grad u)  at lam = A^{-1} mask(QQ'(u_bar)),
-    i.e. the pullback of resi(u, nu) = rhs - lhs(nu)(u) (src/adjoint.jl:13-16)."""
+    """u = A(nu)^{-1} b with A(nu) = mask(QQ'(D'(nu G)D + k B)); the pullback of
+    resi(u, nu, b) = b - A(nu) u (src/adjoint.jl:13-16) at the adjoint state
+    lam = A^{-1} mask(QQ'(u_bar)):
+
+    * nu: the per-local-copy gradient -G:(grad lam)(grad u) (``sem_adjoint_grad``);
+    * b: mult .* lam.  Fields are local (every global node stored once per
+      element that holds it) and autograd sums cotangents over the local
+      entries, so the cotangent of an assembled field is the global adjoint
+      spread over the copies: for a continuous, masked b = Q b_g the change of
+      the loss is lam_g' db_g = sum(mult .* lam .* db).  A right-hand side
+      built as mask(QQ'(B f)) then pulls back to B .* lam at f, the gradient
+      that finite differences in f give."""
 
     @staticmethod
-    def forward(ctx, nu, b, msh, kw):
-        op = HelmholtzOp(msh, 1.0, 0.0, nu_field=nu.detach())
-        u = pcg(b, op, opM=Jacobi(op), mult=msh.mult, **kw)
+    def forward(ctx, nu, b, msh, k, kw):
+        op = HelmholtzOp(msh, 1.0, k, nu_field=nu.detach())
+        u = pcg(b.detach(), op, opM=Jacobi(op), mult=msh.mult, **kw)
         ctx.save_for_backward(nu.detach(), u)
-        ctx.msh, ctx.kw = msh, kw
+        ctx.msh, ctx.k, ctx.kw = msh, k, kw
         return u
 
     @staticmethod
@@ -251,18 +260,63 @@ class _VarCoefSolve(torch.autograd.Function):
         msh = ctx.msh
         from .ops import gatherScatter, mask
         rhs = gatherScatter(mask(as_local(ubar), generateMask(msh.bc, msh)), msh)
-        op = HelmholtzOp(msh, 1.0, 0.0, nu_field=nu)
+        op = HelmholtzOp(msh, 1.0, ctx.k, nu_field=nu)
         lam = pcg(rhs, op, opM=Jacobi(op), mult=msh.mult, **ctx.kw)
-        g = msh.empty()
-        _lib.check(_lib.load().sem_adjoint_grad(msh.handle, lam.data_ptr(), u.data_ptr(),
-                                                g.data_ptr(), 0, stream_ptr()))
-        return g, None, None, None
+        g_nu = None
+        if ctx.needs_input_grad[0]:
+            g_nu = msh.empty()
+            _lib.check(_lib.load().sem_adjoint_grad(msh.handle, lam.data_ptr(), u.data_ptr(),
+                                                    g_nu.data_ptr(), 0, stream_ptr()))
+        g_b = msh.mult * lam if ctx.needs_input_grad[1] else None
+        return g_nu, g_b, None, None, None
 
 
-def linsolve_varcoef(nu, b, msh: Mesh, **kw):
-    """Differentiable solve of -div(nu grad u) = f (b = mask(QQ'(B f))) w.r.t.
-    the nodal nu, the pattern of ``linsolve`` + ``@adjoint`` (src/adjoint.jl)."""
-    return _VarCoefSolve.apply(nu, b, msh, kw)
+def linsolve_varcoef(nu, b, msh: Mesh, k=0.0, **kw):
+    """Differentiable solve of -div(nu grad u) + k u = f (b = mask(QQ'(B f)))
+    in both the nodal nu and the right-hand side b, the pattern of
+    ``linsolve`` + ``@adjoint`` (src/adjoint.jl:5-24)."""
+    return _VarCoefSolve.apply(nu, b, msh, float(k), kw)
+
+
+class VarCoefProblem:
+    """``problem`` of ``linsolve(a, problem, solver)`` (src/adjoint.jl:5-8) for
+    the G-folded diffusion problem: ``problem(a)`` returns
+    (lhs, rhs) with lhs = mask(QQ'(D'(a G)D + k B)) (a ``HelmholtzOp``) and
+    rhs = ``rhs_fn(a)``, a local field built by differentiable torch
+    operations of a (or a fixed field when ``rhs_fn`` is a tensor)."""
+
+    def __init__(self, msh: Mesh, rhs_fn, k=0.0):
+        self.msh, self.rhs_fn, self.k = msh, rhs_fn, float(k)
+
+    def __call__(self, a):
+        rhs = self.rhs_fn(a) if callable(self.rhs_fn) else self.rhs_fn
+        return HelmholtzOp(self.msh, 1.0, self.k, nu_field=a.detach()), rhs
+
+
+class PcgSolver:
+    """``solver(lhs, rhs, adjoint)`` of src/adjoint.jl:5-16: Jacobi PCG on
+    the device with the SEM multiplicity dots; ``kw`` are ``pcg`` keywords
+    (tol, maxiter, precision, ...).  The operator is symmetric, so the
+    adjoint solve is the same solve."""
+
+    def __init__(self, **kw):
+        self.kw = kw
+
+    def __call__(self, lhs, rhs, adjoint=False):
+        return pcg(as_local(rhs), lhs, opM=Jacobi(lhs), mult=lhs.msh.mult, **self.kw)
+
+
+def linsolve(a, problem, solver):
+    """linsolve(a, problem, solver) (src/adjoint.jl:5-24) on the device:
+    u = solver(lhs, rhs) with (lhs, rhs) = problem(a), differentiable in a
+    through the whole residual rhs(a) - lhs(a)(u) (the nu gradient of the
+    operator plus the pullback of rhs(a) at mult .* lam).  Serves the
+    G-folded diffusion problem (``VarCoefProblem``) with ``PcgSolver``;
+    anything else raises TypeError rather than running a host loop."""
+    if not isinstance(problem, VarCoefProblem) or not isinstance(solver, PcgSolver):
+        raise TypeError("linsolve on the device takes a VarCoefProblem and a PcgSolver")
+    _, rhs = problem(a)
+    return _VarCoefSolve.apply(a, as_local(rhs), problem.msh, problem.k, solver.kw)
 
 
 def _mass_gs_mask(msh, v, scale):
@@ -286,7 +340,10 @@ class _TransientVarCoef(torch.autograd.Function):
     ``checkpoint_every`` steps; backward recomputes each segment from its
     checkpoint and runs the discrete adjoint backwards in time:
     (K + B/dt) lam_T = mask(QQ'(u_bar)), (K + B/dt) lam_n = mask(QQ'(B lam_{n+1}/dt)),
-    dJ/dnu = sum_n -G:(grad lam_n)(grad u_n) per local copy."""
+    dJ/dnu = sum_n -G:(grad lam_n)(grad u_n) per local copy.  The initial
+    state and the forcing enter every step's right-hand side through
+    mask(QQ'(B .)), so their cotangents (summed over local entries, see
+    ``_VarCoefSolve``) are B .* lam_1 / dt for u0 and B .* sum_n lam_n for f."""
 
     @staticmethod
     def forward(ctx, nu, u0, f, msh, dt, nsteps, every, kw):
@@ -313,6 +370,7 @@ class _TransientVarCoef(torch.autograd.Function):
         from .ops import gatherScatter, mask
         M = generateMask(msh.bc, msh) if msh.bc else []
         grad = torch.zeros_like(nu)
+        lam_sum = torch.zeros_like(nu) if ctx.needs_input_grad[2] else None
         starts = sorted(ctx.ckpt)
         lam = None
         n = T
@@ -335,13 +393,18 @@ class _TransientVarCoef(torch.autograd.Function):
                 else:
                     rhs = _mass_gs_mask(msh, lam, 1.0 / dt)
                 lam = _step_solve(msh, nu, dt, rhs, kw)
+                if lam_sum is not None:
+                    lam_sum += lam
                 g = msh.empty()
                 _lib.check(lib.sem_adjoint_grad(msh.handle, lam.data_ptr(), seg[m].data_ptr(),
                                                 g.data_ptr(), 0, stream_ptr()))
                 grad += g
                 n = m
         assert n == 1
-        return grad, None, None, None, None, None, None, None
+        B = msh.B
+        g_u0 = B * lam / dt if ctx.needs_input_grad[1] else None
+        g_f = B * lam_sum if lam_sum is not None else None
+        return grad, g_u0, g_f, None, None, None, None, None
 
 
 def transient_varcoef(nu, u0, f, msh: Mesh, dt, nsteps, checkpoint_every=20, **kw):

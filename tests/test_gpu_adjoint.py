@@ -84,6 +84,72 @@ def test_steady_adjoint_matches_oracle_and_fd(gpu):
     assert rel_l2(g_ps, g_o) > 1e-3
 
 
+def test_rhs_cotangent_and_linsolve_match_fd(gpu):
+    """The whole residual rhs(a) - lhs(a)(u) is pulled back (src/adjoint.jl:13-16):
+    (1) the cotangent of b, mult .* lam, gives the gradient of J with respect
+    to f for b = mask(QQ'(B f)) that central differences in f give; (2)
+    linsolve(a, problem, solver) with a right-hand side that depends on a
+    (built by differentiable torch operations, QQ' as the reference's dense
+    QQtx/QQty) matches central differences in a."""
+    import torch
+
+    import semgb300 as S
+    mo, md = meshes(7, 6, 5, (False, False), "DDDD", 0.05)
+    M = O.generateMask(["D"] * 4, mo)
+    nu = np.exp(gaussian_field(mo, 11))
+    ut = 0.05 * gaussian_field(mo, 12)
+    f0 = 1.0 + 0.3 * gaussian_field(mo, 13)
+    Bd, utd = md.B, S.as_local(ut)
+    md.set_precision(S.SEM_F64)
+
+    def J_of_u(u):
+        return 0.5 * torch.sum(Bd * (u - utd) ** 2)
+
+    # (1) gradient in f through b
+    def b_of(f):
+        return O.gatherScatter(O.mask(mo.B * f, M), mo)
+
+    tol = 1e-12 * np.abs(b_of(f0)).max()
+    b_t = S.as_local(b_of(f0)).requires_grad_(True)
+    u = S.linsolve_varcoef(S.as_local(nu), b_t, md, tol=tol)
+    J_of_u(u).backward()
+    bbar = host(b_t.grad)
+    fbar = mo.B * O.mask(O.gatherScatter(bbar, mo), M)  # pullback of mask(QQ'(B f))
+    rng = np.random.default_rng(21)
+    for _ in range(3):
+        df_ = rng.standard_normal(mo.shape)
+        h = 1e-6
+        Jp = J_of_u(S.linsolve_varcoef(S.as_local(nu), S.as_local(b_of(f0 + h * df_)), md, tol=tol)).item()
+        Jm = J_of_u(S.linsolve_varcoef(S.as_local(nu), S.as_local(b_of(f0 - h * df_)), md, tol=tol)).item()
+        fd = (Jp - Jm) / (2 * h)
+        ad = float(np.sum(fbar * df_))
+        assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-14, (fd, ad)
+
+    # (2) linsolve with rhs(a) = mask(QQ'(B (1 + a/2))) as torch operations
+    QX = torch.tensor(mo.QQtx, device="cuda")
+    QY = torch.tensor(mo.QQty, device="cuda")
+    Mt = S.as_local(M.astype(np.float64))
+
+    def rhs_fn(a):
+        return QX @ (Mt * Bd * (1.0 + 0.5 * a)) @ QY.T
+
+    problem = S.VarCoefProblem(md, rhs_fn)
+    solver = S.PcgSolver(tol=tol)
+    a_t = S.as_local(nu).requires_grad_(True)
+    J_of_u(S.linsolve(a_t, problem, solver)).backward()
+    g = host(a_t.grad)
+    for _ in range(3):
+        delta = mo.mult * O.gatherScatter(rng.standard_normal(mo.shape), mo)
+        h = 1e-6
+        Jp = J_of_u(S.linsolve(S.as_local(nu + h * delta), problem, solver)).item()
+        Jm = J_of_u(S.linsolve(S.as_local(nu - h * delta), problem, solver)).item()
+        fd = (Jp - Jm) / (2 * h)
+        ad = float(np.sum(g * delta))
+        assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-14, (fd, ad)
+    with pytest.raises(TypeError):
+        S.linsolve(a_t, lambda a: None, solver)
+
+
 @pytest.mark.parametrize("prec_name", ["SEM_MIXED_RR", "SEM_MIXED"])
 @pytest.mark.parametrize("k", [0.0, 50.0])
 def test_varcoef_mixed_precision_solves(gpu, prec_name, k):
@@ -153,6 +219,27 @@ def test_transient_adjoint_with_checkpoints(gpu):
         fd = (J_dev(nu + h * delta) - J_dev(nu - h * delta)) / (2 * h)
         ad = float(np.sum(g * delta))
         assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-16, (fd, ad)
+
+    # cotangents of the initial state and of the forcing
+    u0_t = S.as_local(u0).requires_grad_(True)
+    f_t = S.as_local(f).requires_grad_(True)
+    uT = S.transient_varcoef(S.as_local(nu), u0_t, f_t, md, dt, T, every, tol=tol)
+    (0.5 * torch.sum(md.B * (uT - S.as_local(ut)) ** 2)).backward()
+    gu0, gf = host(u0_t.grad), host(f_t.grad)
+
+    def J_uf(u0_np, f_np):
+        u = S.transient_varcoef(S.as_local(nu), S.as_local(u0_np), S.as_local(f_np), md, dt, T, every, tol=tol)
+        return 0.5 * torch.sum(md.B * (u - S.as_local(ut)) ** 2).item()
+
+    h = 1e-6
+    du = O.mask(mo.mult * O.gatherScatter(rng.standard_normal(mo.shape), mo), M)
+    fd = (J_uf(u0 + h * du, f) - J_uf(u0 - h * du, f)) / (2 * h)
+    ad = float(np.sum(gu0 * du))
+    assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-16, (fd, ad)
+    dfv = rng.standard_normal(mo.shape)
+    fd = (J_uf(u0, f + h * dfv) - J_uf(u0, f - h * dfv)) / (2 * h)
+    ad = float(np.sum(gf * dfv))
+    assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-16, (fd, ad)
 
 
 def test_diffusion_driver_matches_oracle(gpu):

@@ -164,6 +164,8 @@ def test_structured_kernels_bit_exact(gpu, case):
     np.testing.assert_array_equal(host(S.gatherScatter(ud, md)),
                                   O.gatherScatter_index(u, mo.l2gx, mo.nxg, mo.l2gy, mo.nyg))
     np.testing.assert_array_equal(host(S.gatherScatter(ud, md.QQtx, md.QQty)), O.gatherScatter(u, mo))
+    # the functional form on the reference's dense QQtx/QQty (no handle)
+    np.testing.assert_array_equal(host(S.gatherScatter(ud, mo.QQtx, mo.QQty)), host(S.gatherScatter(ud, md)))
     Md = S.generateMask(list(bc), md)
     np.testing.assert_array_equal(host(Md), M)
     np.testing.assert_array_equal(host(S.mask(ud, Md)), O.mask(u, M))
@@ -176,6 +178,20 @@ def test_structured_kernels_bit_exact(gpu, case):
     got = host(S.mass(ud, Md, S.as_local(mo.B), [], [], md.QQtx, md.QQty, md.mult))
     ref = O.mask(O.gatherScatter(mo.B * u, mo), M)
     np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("nr,ns,Ex,Ey,per", [(4, 7, 5, 3, (True, False)), (9, 3, 2, 6, (False, True)),
+                                              (2, 5, 1, 4, (True, True)), (6, 6, 1, 1, (False, False))])
+def test_gather_scatter_grid_nr_ne_ns(gpu, nr, ns, Ex, Ey, per):
+    """gatherScatter(u, QQtx, QQty) without a handle, nr != ns allowed: the
+    reference's dense QQtx u QQty' (src/gatherScatter.jl:8-16), bit for bit."""
+    import semgb300 as S
+    Qx = O.semq(Ex, nr, per[0])
+    Qy = O.semq(Ey, ns, per[1])
+    QQx, QQy = Qx @ Qx.T, Qy @ Qy.T
+    u = np.random.default_rng(9).uniform(-1, 1, (nr * Ex, ns * Ey))
+    got = host(S.gatherScatter(S.as_local(u), QQx, QQy))
+    np.testing.assert_array_equal(got, O.gatherScatter(u, QQx, QQy))
 
 
 @pytest.mark.parametrize("n,Ex,Ey,per", [(9, 8, 8, (False, False)), (5, 7, 3, (True, False)),

@@ -184,3 +184,44 @@ def test_julia_binding_matches_the_header():
                                 ("MeshDesc", "sem_mesh_desc", _lib.MeshDesc)):
         assert jl_fields(jl_name) == c_fields(c_name), jl_name
         assert [f[0] for f in py._fields_] == c_fields(c_name), c_name  # the ctypes mirror too
+
+    # every ccall passes as many argument types as the C declaration has parameters
+    decl_arity = {}
+    for name, params in re.findall(r"\b(sem_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", hdr_nc):
+        params = params.strip()
+        decl_arity[name] = 0 if params in ("", "void") else params.count(",") + 1
+
+    def top_level_items(text):
+        depth, items, cur = 0, 0, ""
+        for ch in text:
+            if ch in "({[":
+                depth += 1
+            elif ch in ")}]":
+                depth -= 1
+            if ch == "," and depth == 0:
+                items += 1
+                cur = ""
+            else:
+                cur += ch
+        return items + (1 if cur.strip() else 0)
+
+    for m in re.finditer(r"ccall\(\(:(sem_[a-z0-9_]+), libsem\),\s*\w+,\s*\(", jl):
+        i, depth = m.end(), 1
+        while depth:
+            depth += {"(": 1, ")": -1}.get(jl[i], 0)
+            i += 1
+        types = jl[m.end():i - 1]
+        assert top_level_items(types) == decl_arity[m.group(1)], (m.group(1), types)
+
+    # the Julia methods the drop-in boundary names (functional forms, linsolve + rrule)
+    for pattern in (r"function lapl\(u::CuArray\{Float64,2\}, M, Jr, Js, QQtx, QQty, Dr::AbstractMatrix, "
+                    r"Ds::AbstractMatrix,\s*G11::CuArray\{Float64,2\}, G12::CuArray\{Float64,2\}, "
+                    r"G22::CuArray\{Float64,2\}, mult",
+                    r"function mass\(u::CuArray\{Float64,2\}, M, B, Jr, Js, QQtx, QQty, mult\)",
+                    r"function gatherScatter\(u::CuArray\{Float64,2\}, QQtx::AbstractMatrix, QQty::AbstractMatrix\)",
+                    r"function linsolve\(a::CuArray\{Float64,2\}, problem::VarCoefProblem, solver::PcgSolver\)",
+                    r"ChainRulesCore\.rrule\(config::ChainRulesCore\.RuleConfig\{>:ChainRulesCore\.HasReverseMode\},"
+                    r"\s*::typeof\(linsolve\)",
+                    r"ChainRulesCore\.rrule\(::typeof\(lapl\)", r"ChainRulesCore\.rrule\(::typeof\(mass\)",
+                    r"ChainRulesCore\.rrule\(::typeof\(varcoef_solve\)"):
+        assert re.search(pattern, jl), pattern

@@ -32,6 +32,8 @@ def _opts(S, tol, precond, precision):
 
 @pytest.mark.parametrize("precision", ["DF", "F64"])
 def test_noalloc_solve_matches_pcg_on_two_calls(gpu, precision):
+    import torch
+
     import semgb300 as S
     lib = S.load()
     prec = S.SEM_F64_DF if precision == "DF" else S.SEM_F64
@@ -57,11 +59,16 @@ def test_noalloc_solve_matches_pcg_on_two_calls(gpu, precision):
         x = md.empty()
         x.fill_(float("nan"))  # the solve must overwrite every entry
         info = S._lib.SolveInfo()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]  # driver-level free bytes of the device
         st = lib.sem_pcg_noalloc(9, 8, 8, 0, 0, b"DDDD", Dr.ctypes.data, Ds.ctypes.data,
                                  G11.data_ptr(), G12.data_ptr(), G22.data_ptr(), B.data_ptr(),
                                  ctypes.byref(o), b.data_ptr(), x.data_ptr(), ctypes.byref(info),
                                  stream)
         assert st == 0, lib.sem_last_error()
+        torch.cuda.synchronize()
+        if call == 1:  # after the warm-up call the solve grows the device's memory use by nothing
+            assert torch.cuda.mem_get_info()[0] == free0
         assert info.converged and info.res_inf <= tol, call
         assert info.iters == ref_info["iters"], (call, info.iters, ref_info["iters"])
         assert rel_l2(host(x), x_ref) < 1e-12, call
