@@ -1,13 +1,15 @@
 #!/usr/bin/env python
 """Benchmark of the SEM operator-apply / PCG hot path on one GB300.
 
-Headline (`value`): GDOF/s of the FP64 Helmholtz operator with direct-stiffness
-summation and Dirichlet mask, mask(QQ'(nu lapl u + lambda B u)), on the
-256x256-element, N=8 deformed mesh (4,198,401 unique DOF), inputs resident in
-HBM, L2 flushed between steps.  `e2e` is the same metric through the public
-API with the input copied from pinned host memory and the result copied back
-every step.  Extra keys: PCG solves/s (FP64 vs mixed precision), the order
-sweep N=4/8/12/16, roofline, CPU baseline.
+Headline (`value`): GDOF/s of the Helmholtz operator with direct-stiffness
+summation and Dirichlet mask, mask(QQ'(nu lapl u + lambda B u)), in native FP64
+arithmetic, on the 256x256-element, N=8 deformed mesh (4,198,401 unique DOF),
+inputs resident in HBM, L2 flushed between steps.  `e2e` is the same metric
+through the public API on pinned host buffers (input in, result out every
+step).  `df64` is the same apply in the double-float arithmetic (the library's
+default operator precision, labelled as such), with its own roofline and e2e.
+Extra keys: PCG solves/s (FP64 vs mixed precision), the order sweep
+N=4/8/12/16, batched and adjoint solves, the time loop, CPU baselines.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -152,47 +154,43 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def run_ours(args, rank, world, local_rank):
-    import numpy as np
+FP64_OPS_PEAK = 0.625e12  # FP64 pipe instructions/s: DFMA probe, 1.25 TFLOP/s on this machine's GB300
+DFMA_PROBE = "DFMA chains, 8 per thread, 1216 CTAs of 256 threads: 1.25 TFLOP/s (0.625 T instr/s)"
+
+
+def eo_ops(n):
+    """FP64 (or double-float) operations of one n-point even-odd line apply."""
+    m = n // 2
+    return 2 * m + 2 * m * m + (2 * m if n % 2 else 0) + 2 * m
+
+
+def fp64_ops_per_point(n):
+    """Operations per local point of the fused hlmz+QQ'+mask apply in native
+    FP64: four line contractions and the metric products (4), or + os (1) and
+    the mass term (1; nu is folded into the transposed derivative and k into
+    B); the QQ' sums of interface copies are excluded."""
+    return 4 * eo_ops(n) / n + 6
+
+
+def measure_apply(S, lib, msh, prec, u, flush, stream, args, world, dev, G, L, x_pin, y_pin):
+    """Time mask(QQ'(hlmz(u))) in one arithmetic: K flushed steps through
+    sem_hlmz (device buffers), the operator kernel alone (library CUDA events
+    on the launching stream, a second pass), and the end-to-end call on pinned
+    host buffers in both modes of sem_hlmz_host."""
+    import ctypes
+
     import torch
-    import torch.distributed as dist
-
-    import semgb300 as S
-
-    torch.cuda.set_device(local_rank)
-    S.load()
-    lib = S.load()
-    dev = torch.device("cuda", local_rank)
-    uuid = str(torch.cuda.get_device_properties(dev).uuid)
-    sampler = ClockSampler(uuid if uuid.startswith("GPU-") else "GPU-" + uuid)
-    sampler.start()
-
-    msh = S.Mesh(N_ORDER + 1, N_ORDER + 1, E_X, E_Y, (False, False), sin_deform(AMP), bc="DDDD")
-    tune = {name: msh.autotune(prec) for name, prec in
-            (("f64_df", S.SEM_F64_DF), ("f64", S.SEM_F64), ("f32", S.SEM_F32))}
-    if args.variant is not None:
-        # a pinned double-float kernel variant (profiling runs, where the
-        # autotuner's timings are distorted by the profiler)
-        msh.set_variant(args.variant, S.SEM_F64_DF)
-        tune["f64_df"]["chosen"] = args.variant
-        tune["f64_df"]["pinned"] = True
-    nx, ny = msh.shape
-    L = nx * ny
-    G = unique_dof(N_ORDER + 1, E_X, E_Y)
-    rng = np.random.default_rng(3)
-    u_h = rng.uniform(-1.0, 1.0, (nx, ny))
-    u = S.as_local(u_h)
-    out = msh.empty()
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    stream = torch.cuda.current_stream()
+    msh.set_precision(prec)
     sp = stream.cuda_stream
     flags = S.SEM_GS | S.SEM_MASK
+    out = msh.empty()
 
     def apply():
         S._lib.check(lib.sem_hlmz(msh.handle, None, NU, LAM, u.data_ptr(), out.data_ptr(), flags, sp))
 
     def barrier():
         if world > 1:
+            import torch.distributed as dist
             dist.barrier()
 
     for _ in range(args.warmup):
@@ -213,11 +211,6 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     torch.cuda.synchronize()
     t1 = time.time()
-    # the operator kernel alone: the same K steps again with the library's
-    # CUDA events around each operator launch (on the launching stream); kept
-    # out of the pass above, where an event between the operator kernel and
-    # its fixup would stop the fixup from being scheduled early
-    import ctypes
     lib.sem_timing_read(None, None)
     lib.sem_timing_enable(1)
     for i in range(args.steps):
@@ -229,74 +222,135 @@ def run_ours(args, rank, world, local_rank):
     lib.sem_timing_read(ctypes.byref(kms), ctypes.byref(kn))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms, per_s = replica_throughput(sum(step_ms) / len(step_ms), G, world, dev)
-    value = per_s / 1e9
     kernel_ms = kms.value / max(1, kn.value)
-    clocks = sampler.summary(t0, t1)
-
-    # ---- e2e through the public API: pinned host input -> device -> host
-    x_pin = torch.from_numpy(np.asfortranarray(u_h)).pin_memory()
-    x_pin = x_pin if x_pin.stride() == (1, nx) else x_pin.t().contiguous().t().pin_memory()
-    y_pin = torch.empty_strided((nx, ny), (1, nx), dtype=torch.float64, pin_memory=True)
+    # end to end: pinned host buffers in and out every step, in the two modes
+    # of the host-buffer call (copy-engine slabs; kernels reading and writing
+    # the host buffers in place); the faster is reported
     op = S.HelmholtzOp(msh, NU, LAM)
-    e2e_ms = []
-    for i in range(args.warmup + args.steps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        op.apply_host(x_pin, y_pin)  # sem_hlmz_host: host in, host out, copies overlapped in slabs
-        b.record(stream)
-        b.synchronize()
-        if i >= args.warmup:
-            e2e_ms.append(a.elapsed_time(b))
-    e2e_step, e2e_per_s = replica_throughput(sum(e2e_ms) / len(e2e_ms), G, world, dev)
-    e2e = {"value": e2e_per_s / 1e9, "unit": UNIT,
-           "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L, "ms_per_step": e2e_step,
-           "api": "semgb300.HelmholtzOp.apply_host (sem_hlmz_host through ctypes): pinned host "
-                  "buffers in and out, the copies overlapped with the kernels in 8 slabs of tile rows"}
-    # parity of this very output against the F64 arithmetic
+    modes = {}
+    for mode_name, slabs in (("8 copy-engine slabs overlapped with the kernels", 8),
+                             ("kernels read and write the host buffers in place", S._lib.SEM_HOST_DIRECT)):
+        e2e_ms = []
+        for i in range(args.warmup + args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            op.apply_host(x_pin, y_pin, slabs=slabs)
+            b.record(stream)
+            b.synchronize()
+            if i >= args.warmup:
+                e2e_ms.append(a.elapsed_time(b))
+        modes[mode_name] = (sum(e2e_ms) / len(e2e_ms), slabs)
+    best = min(modes, key=lambda k: modes[k][0])
+    e2e_step, e2e_per_s = replica_throughput(modes[best][0], G, world, dev)
+    op.apply_host(x_pin, y_pin, slabs=modes[best][1])
+    torch.cuda.synchronize()
     y_dev = op(u)
-    e2e["matches_device_call"] = bool(torch.equal(y_pin, y_dev.cpu()))
-    msh.set_precision(S.SEM_F64)
-    y64 = op(u)
-    t64 = time_apply(lambda: op(u), stream, 5)
-    msh.set_precision(S.SEM_F64_DF)
-    rel = (torch.linalg.norm(y_dev - y64) / torch.linalg.norm(y64)).item()
+    e2e = {"value": e2e_per_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
+           "ms_per_step": e2e_step,
+           "api": "semgb300.HelmholtzOp.apply_host (sem_hlmz_host through ctypes), pinned host buffers: " + best,
+           "ms_per_mode": {k: v[0] for k, v in modes.items()},
+           "matches_device_call": bool(torch.equal(y_pin, y_dev.cpu()))}
+    return {"value": per_s / 1e9, "ms": ms, "kernel_ms": kernel_ms, "kernel_launches": kn.value,
+            "e2e": e2e, "t0": t0, "t1": t1, "y": y_dev}
 
-    peak, peak_kind = load_peaks()
-    variant = tune["f64_df"]["chosen"]
+
+def kernel_name(prec_tag, variant):
     kname = ("k_apply", "k_apply", "k_apply2", "k_apply2", "k_apply3", "k_apply2")[variant]
-    ktempl = {0: "<PDF,9,8,3,false>", 1: "<PDF,9,8,3,true>", 2: "<PDF,9,8,3,false,false,false>",
-              3: "<PDF,9,8,3,true,false,false>", 4: "<PDF,9,8,3>",
-              5: "<PDF,9,8,3,false,true,false>"}[variant]
-    bytes_launch = BYTES_PER_LOCAL * L
-    achieved = bytes_launch / (kernel_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": profiled_traffic(f"{kname}_hlmz_df_256x256_n8.md"),
-                "kernel": f"{kname}{ktempl} (fused element operator, double-float, autotuned variant {variant})",
-                "kernel_ms": kernel_ms, "kernel_launches_timed": kn.value,
-                "kernel_timing": "CUDA events around each operator launch on its stream, in a second "
-                                 "pass of the same K flushed steps right after the timed region",
-                "algorithmic_bytes_per_launch": bytes_launch,
-                "flops_per_launch": (8 * 9 ** 3 + 7 * 9 ** 2) * E_X * E_Y,
-                "note": "FP64 runs at 1/64 of FP32 on GB300; the kernel computes in double-float on the FP32 pipe"}
+    targs = {0: "false", 1: "true", 2: "false,false,false", 3: "true,false,false", 4: None,
+             5: "false,true,false"}[variant]
+    return f"{kname}<{prec_tag},9,8,3{',' + targs if targs else ''}>"
 
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import semgb300 as S
+
+    torch.cuda.set_device(local_rank)
+    lib = S.load()
+    dev = torch.device("cuda", local_rank)
+    uuid = str(torch.cuda.get_device_properties(dev).uuid)
+    sampler = ClockSampler(uuid if uuid.startswith("GPU-") else "GPU-" + uuid)
+    sampler.start()
+
+    msh = S.Mesh(N_ORDER + 1, N_ORDER + 1, E_X, E_Y, (False, False), sin_deform(AMP), bc="DDDD")
+    tune = {name: msh.autotune(prec) for name, prec in
+            (("f64", S.SEM_F64), ("df64", S.SEM_F64_DF), ("f32", S.SEM_F32))}
+    if args.variant is not None:
+        # a pinned FP64 kernel variant (profiling runs, where the autotuner's
+        # timings are distorted by the profiler)
+        msh.set_variant(args.variant, S.SEM_F64)
+        tune["f64"]["chosen"] = args.variant
+        tune["f64"]["pinned"] = True
+    nx, ny = msh.shape
+    L = nx * ny
+    G = unique_dof(N_ORDER + 1, E_X, E_Y)
+    rng = np.random.default_rng(3)
+    u_h = rng.uniform(-1.0, 1.0, (nx, ny))
+    u = S.as_local(u_h)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    x_pin = torch.empty_strided((nx, ny), (1, nx), dtype=torch.float64, pin_memory=True)
+    x_pin.copy_(torch.from_numpy(np.asfortranarray(u_h)))
+    y_pin = torch.empty_strided((nx, ny), (1, nx), dtype=torch.float64, pin_memory=True)
+
+    head = measure_apply(S, lib, msh, S.SEM_F64, u, flush, stream, args, world, dev, G, L, x_pin, y_pin)
+    clocks = sampler.summary(head["t0"], head["t1"])
+    df64 = None
+    if world == 1:
+        df64 = measure_apply(S, lib, msh, S.SEM_F64_DF, u, flush, stream, args, world, dev, G, L, x_pin, y_pin)
+    peak, peak_kind = load_peaks()
+    bytes_launch = BYTES_PER_LOCAL * L
+    ops_launch = fp64_ops_per_point(N_ORDER + 1) * L
+
+    def roof(m, tag, variant, prof):
+        achieved = bytes_launch / (m["kernel_ms"] * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": profiled_traffic(prof),
+                "kernel": kernel_name(tag, variant) + f" (fused element operator, autotuned variant {variant})",
+                "kernel_ms": m["kernel_ms"], "kernel_launches_timed": m["kernel_launches"],
+                "kernel_timing": "CUDA events around each operator launch on its stream, in a second pass of the "
+                                 "same K flushed steps right after the timed region",
+                "algorithmic_bytes_per_launch": bytes_launch}
+
+    v64 = tune["f64"]["chosen"]
+    roofline = roof(head, "PF64", v64, "k_apply_hlmz_f64_256x256_n8.md")
+    ops_s = ops_launch / (head["kernel_ms"] * 1e-3)
+    roofline["fp64_pipe"] = {"achieved_instr_per_s": ops_s, "peak_instr_per_s": FP64_OPS_PEAK,
+                             "frac": ops_s / FP64_OPS_PEAK, "peak_source": DFMA_PROBE,
+                             "fp64_instr_per_launch": ops_launch,
+                             "note": "the kernel's bound on GB300: FP64 runs at 1/64 of the FP32 rate, so "
+                                     "native FP64 caps this apply far below the HBM roofline"}
     result = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded U(-1,1) field (seed 3) on the seeded deformed mesh",
         "config": {"workload": WORKLOAD, "elements": [E_X, E_Y], "order": N_ORDER,
                    "unique_dof": G, "local_dof": L,
-                   "arith": "double-float (FP32 pairs) with FP64 storage; rel-L2 vs native FP64 "
-                            f"{rel:.2e}",
+                   "arith": "native FP64 (SEM_F64): every operation an IEEE double instruction",
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "autotune": tune},
-        "roofline": roofline, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clocks,
-        "f64_native_apply": {"ms": t64, "GDOF/s": G / (t64 * 1e-3) / 1e9},
+        "roofline": roofline, "e2e": head["e2e"],
+        "gpu_launches": (1 if v64 == 5 else 2) * args.steps, "clocks": clocks,
     }
+    if df64 is not None:
+        vdf = tune["df64"]["chosen"]
+        rel = (torch.linalg.norm(df64["y"] - head["y"]) / torch.linalg.norm(head["y"])).item()
+        result["df64"] = {
+            "arith": "double-float: each value an unevaluated sum of two FP32 numbers (about 47 significand "
+                     "bits, FP32 exponent range; element tiles whose inputs or intermediates leave the pair "
+                     "format's range are recomputed in native FP64 inside the kernel); FP64 storage",
+            "value": df64["value"], "unit": UNIT, "ms_per_step": df64["ms"], "rel_l2_vs_f64": rel,
+            "roofline": roof(df64, "PDF", vdf, f"{kernel_name('PDF', vdf).split('<')[0]}_hlmz_df_256x256_n8.md"),
+            "e2e": df64["e2e"]}
+        result["f32_inner_operator"] = {"ms": tune["f32"]["ms"][tune["f32"]["chosen"]],
+                                        "note": "FP32 operator of the mixed-precision inner CG (autotune time)"}
     if not args.no_extras and world == 1:  # the N-replica runs measure the headline only
         extras = args.extras.split(",") if args.extras else ["pcg", "sweep", "batch", "adjoint", "time"]
+        msh.set_precision(S.SEM_F64_DF)
         if "pcg" in extras:
             result["pcg"] = bench_pcg(S, msh, stream)
         if "sweep" in extras:
@@ -309,7 +363,9 @@ def run_ours(args, rank, world, local_rank):
             result["time"] = bench_time(S)
     sampler.stop()
     if rank == 0 and world == 1 and not args.no_cpu:
-        result["cpu_baseline"] = cpu_baseline()
+        result["cpu_baseline"] = cpu_baseline(result.get("pcg"), result.get("batch"), result.get("adjoint"))
+    if "batch" in result:
+        result["batch"].pop("_problems", None)
     return result
 
 
@@ -480,12 +536,13 @@ def bench_batch(S):
     import numpy as np
     import torch
     rng = np.random.default_rng(4)
-    meshes, nus, lams, bs, tols = [], [], [], [], []
+    meshes, nus, lams, bs, tols, shapes = [], [], [], [], [], []
     for _ in range(512):
         Ex, Ey = (int(v) for v in rng.integers(4, 65, size=2))
         N = int(rng.choice([4, 6, 8, 10]))
         nus.append(float(10 ** rng.uniform(-3, 0)))
         lams.append(float(rng.uniform(0, 10)))
+        shapes.append((N, Ex, Ey))
         m = S.Mesh(N + 1, N + 1, Ex, Ey, (False, False), sin_deform(0.05), bc="DDDD")
         f = 2 * np.pi ** 2 * torch.sin(np.pi * m.x) * torch.sin(np.pi * m.y)
         M = S.generateMask("DDDD", m)
@@ -508,6 +565,10 @@ def bench_batch(S):
         it = [i["iters"] for i in infos]
         out[name] = {"batch_s": dt, "solves_per_s": 512 / dt, "converged": sum(i["converged"] for i in infos),
                      "iters_max": max(it), "iters_mean": float(np.mean(it))}
+        if name == "fp64":  # per-problem record for the CPU baseline's sample (not printed)
+            out["_problems"] = [{"N": N, "Ex": Ex, "Ey": Ey, "nu": nu, "lam": lam, "iters": i,
+                                 "local": (N + 1) ** 2 * Ex * Ey}
+                                for (N, Ex, Ey), nu, lam, i in zip(shapes, nus, lams, it)]
     for name in ("mixed", "mixed_rr"):
         errs = [(torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() for a, b in zip(xs[name], xs["fp64"])]
         out[name]["rel_l2_vs_fp64_max"] = max(errs)
@@ -587,6 +648,13 @@ def bench_adjoint(S, fd_directions):
     torch.cuda.synchronize()
     out["gradient_s"] = time.time() - t
     out["J"] = J0
+    # iteration counts of the forward and the adjoint solve (for the CPU baseline)
+    opv = S.HelmholtzOp(msh, 1.0, 0.0, nu_field=nu)
+    i_f, i_a = {}, {}
+    u0v = S.pcg(b, opv, opM=S.Jacobi(opv), mult=msh.mult, tol=tol, info=i_f)
+    rhs_a = S.gatherScatter(S.mask(B * (u0v - ut), M), msh)
+    S.pcg(rhs_a, opv, opM=S.Jacobi(opv), mult=msh.mult, tol=tol, info=i_a)
+    out["forward_iters"], out["adjoint_iters"] = i_f["iters"], i_a["iters"]
 
     # central finite differences along continuous directions
     msh.set_precision(S.SEM_F64)
@@ -674,9 +742,10 @@ def reference_apply_timer(threads_note=True):
     return step, mo
 
 
-def cpu_baseline():
-    """Bounded CPU sample on the host cores: the reference-faithful NumPy
-    restatement (kind 'port'), plus the optimised C/OpenMP oracle."""
+def cpu_baseline(pcg=None, batch=None, adjoint=None):
+    """Bounded CPU samples on the host cores: the reference-faithful NumPy
+    restatement (kind 'port') of the apply and of the solves, plus the
+    optimised C/OpenMP oracle."""
     import numpy as np
     step, mo = reference_apply_timer()
     step()
@@ -712,7 +781,130 @@ def cpu_baseline():
     except Exception as e:  # the C oracle is optional for the baseline line
         out["optimised_c_openmp"] = {"error": str(e)}
     out["time_loop_cfg1_mesh_8x8_n8"] = cpu_time_loop()
+    try:
+        out["solves"] = cpu_solve_baselines(pcg, batch, adjoint)
+    except Exception as e:
+        out["solves"] = {"error": str(e)}
     return out
+
+
+def cpu_solve_baselines(pcg=None, batch=None, adjoint=None):
+    """Solves/s of the reference's CPU path (src/pcg.jl:16-60 on
+    src/diffusion.jl:36-45's operator) for each configuration, on bounded
+    samples: the reference-faithful NumPy restatement (dense QQ', the port)
+    and the C/OpenMP oracle (sum-factorised).  Where a full solve would take
+    minutes, the time of a few iterations is multiplied by the iteration
+    count of the GPU solve of the same problem, and the entry says so."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import sem_oracle as O
+    import sem_oracle_c as C
+    res = {"cores": os.cpu_count(), "threads_c": C.threads()}
+
+    def port_solver(mo, nu, k, M, d):
+        return lambda b, tol, maxiter=None, info=None: O.pcg(
+            b, lambda v: O.mask(O.gatherScatter(O.hlmz(v, nu, k, mo), mo), M),
+            opM=lambda r: r / d, mult=mo.mult, tol=tol, maxiter=maxiter, info=info)
+
+    # cfg1: Poisson 8x8, N=8, amp 0.1, Jacobi PCG to 1e-10 relative (full solves)
+    mo = O.Mesh(9, 9, 8, 8, (False, False), O.sin_deform(0.1), dense_qq=True)
+    M = O.generateMask(["D"] * 4, mo)
+    f = 2 * np.pi ** 2 * np.sin(np.pi * mo.x) * np.sin(np.pi * mo.y)
+    b = O.gatherScatter(O.mask(O.mass(f, mo), M), mo)
+    tol = 1e-10 * np.abs(b).max()
+    d = O.jacobi_diag(mo, 1.0, 0.0, M)
+    solve = port_solver(mo, 1.0, 0.0, M, d)
+    info = {}
+    solve(b, tol, info=info)
+    n, t0 = 0, time.time()
+    while time.time() - t0 < 3.0 or n < 2:
+        solve(b, tol)
+        n += 1
+    port1 = n / (time.time() - t0)
+    g1 = C.grid(9, 8, 8, (False, False), "DDDD")
+    C.pcg(g1, mo.Dr, mo.Ds, mo.G11, mo.G12, mo.G22, mo.B, b, nu=1.0, k=0.0, d=d, tol=tol)
+    n, t0 = 0, time.time()
+    while time.time() - t0 < 2.0 or n < 2:
+        _, it1, _ = C.pcg(g1, mo.Dr, mo.Ds, mo.G11, mo.G12, mo.G22, mo.B, b, nu=1.0, k=0.0, d=d, tol=tol)
+        n += 1
+    c1 = n / (time.time() - t0)
+    res["cfg1_poisson_8x8_n8_1e-10"] = {"port_solves_per_s": port1, "port_iters": info.get("iters"),
+                                        "c_openmp_solves_per_s": c1, "c_iters": it1, "sample": "full solves"}
+    res["cfg3"] = {"note": "the reference has no mixed-precision solve; its solve of this problem is cfg1's",
+                   "port_solves_per_s": port1, "c_openmp_solves_per_s": c1}
+
+    # cfg2: Helmholtz 256x256, N=8, 1e-8 relative: per-iteration time x the GPU iteration count
+    if pcg and "cfg2_helmholtz_256x256_n8" in pcg:
+        iters = pcg["cfg2_helmholtz_256x256_n8"]["fp64"]["iters"]
+        mo2 = O.Mesh(9, 9, E_X, E_Y, (False, False), O.sin_deform(AMP), dense_qq=True)
+        M2 = O.generateMask(["D"] * 4, mo2)
+        rng = np.random.default_rng(2)
+        f2 = np.zeros(mo2.shape)
+        for _ in range(16):
+            kx, ky = rng.integers(1, 9, size=2)
+            c = rng.standard_normal() / (kx ** 2 + ky ** 2)
+            f2 += c * np.sin(kx * np.pi * mo2.x) * np.sin(ky * np.pi * mo2.y)
+        b2 = O.gatherScatter(O.mask(O.mass(f2, mo2), M2), mo2)
+        d2 = O.jacobi_diag(mo2, NU, LAM, M2)
+        solve2 = port_solver(mo2, NU, LAM, M2, d2)
+        t0 = time.time()
+        solve2(b2, 0.0, maxiter=3)
+        it_port = (time.time() - t0) / 3
+        g2 = C.grid(9, E_X, E_Y, (False, False), "DDDD")
+        t0 = time.time()
+        C.pcg(g2, mo2.Dr, mo2.Ds, mo2.G11, mo2.G12, mo2.G22, mo2.B, b2, nu=NU, k=LAM, d=d2, tol=0.0, maxiter=20)
+        it_c = (time.time() - t0) / 20
+        res["cfg2_helmholtz_256x256_n8_1e-8"] = {
+            "port_solves_per_s": 1.0 / (it_port * iters), "c_openmp_solves_per_s": 1.0 / (it_c * iters),
+            "port_ms_per_iter": 1e3 * it_port, "c_ms_per_iter": 1e3 * it_c, "iters": iters,
+            "sample": "3 (port) / 20 (C) iterations timed, times the GPU solve's iteration count"}
+
+    # cfg4: a sample of the 512 problems (every 32nd), per-iteration time x that
+    # problem's GPU iteration count, scaled to the whole batch by local DOF-iterations
+    if batch and batch.get("_problems"):
+        probs = batch["_problems"]
+        sample = probs[::32]
+        t_tot = 0.0
+        work_s = 0.0
+        for pb in sample:
+            mo4 = O.Mesh(pb["N"] + 1, pb["N"] + 1, pb["Ex"], pb["Ey"], (False, False), O.sin_deform(0.05))
+            M4 = O.generateMask(["D"] * 4, mo4)
+            f4 = 2 * np.pi ** 2 * np.sin(np.pi * mo4.x) * np.sin(np.pi * mo4.y)
+            b4 = O.gatherScatter(O.mask(O.mass(f4, mo4), M4), mo4)
+            d4 = O.jacobi_diag(mo4, pb["nu"], pb["lam"], M4)
+            g4 = C.grid(pb["N"] + 1, pb["Ex"], pb["Ey"], (False, False), "DDDD")
+            t0 = time.time()
+            C.pcg(g4, mo4.Dr, mo4.Ds, mo4.G11, mo4.G12, mo4.G22, mo4.B, b4, nu=pb["nu"], k=pb["lam"],
+                  d=d4, tol=0.0, maxiter=10)
+            t_it = (time.time() - t0) / 10
+            t_tot += t_it * pb["iters"]
+            work_s += mo4.x.size * pb["iters"]
+        work_all = sum(pb["local"] * pb["iters"] for pb in probs)
+        batch_s = t_tot * work_all / work_s
+        res["cfg4_batch_512"] = {"c_openmp_solves_per_s": len(probs) / batch_s, "c_batch_s_estimate": batch_s,
+                                 "sample": f"{len(sample)} of {len(probs)} problems: 10 iterations each timed, "
+                                           "times the GPU iteration count, scaled by local DOF x iterations"}
+
+    # cfg5: gradient = forward + adjoint solve on 128x128 (per-iteration time x GPU counts)
+    if adjoint and adjoint.get("forward_iters"):
+        mo5 = O.Mesh(9, 9, 128, 128, (False, False), O.sin_deform(0.05))
+        M5 = O.generateMask(["D"] * 4, mo5)
+        nu5 = np.exp(0.5 * np.sin(3 * mo5.x) * np.cos(2 * mo5.y))
+        b5 = O.gatherScatter(O.mask(O.mass(np.ones(mo5.shape), mo5), M5), mo5)
+        G5 = (nu5 * mo5.G11, nu5 * mo5.G12, nu5 * mo5.G22)
+        d5 = O.jacobi_diag(mo5, 1.0, 0.0, M5, G=G5)
+        g5 = C.grid(9, 128, 128, (False, False), "DDDD")
+        t0 = time.time()
+        C.pcg(g5, mo5.Dr, mo5.Ds, mo5.G11, mo5.G12, mo5.G22, mo5.B, b5, nu=1.0, k=0.0, d=d5, nug=nu5,
+              tol=0.0, maxiter=20)
+        t_it = (time.time() - t0) / 20
+        its = adjoint["forward_iters"] + adjoint["adjoint_iters"]
+        res["cfg5_gradient_128x128_n8"] = {"c_openmp_gradient_s": t_it * its, "c_ms_per_iter": 1e3 * t_it,
+                                           "iters": its,
+                                           "sample": "20 iterations of the variable-coefficient CG timed, times "
+                                                     "the GPU forward + adjoint iteration counts"}
+    return res
 
 
 def cpu_time_loop(steps=20):
@@ -777,10 +969,10 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG and order-sweep extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--variant", type=int, default=None,
-                    help="pin the double-float operator kernel variant instead of the autotuned one")
+                    help="pin the FP64 operator kernel variant instead of the autotuned one")
     ap.add_argument("--extras", default="",
                     help="comma-separated subset of pcg,sweep,batch,adjoint (default: all)")
-    ap.add_argument("--fd-directions", type=int, default=8,
+    ap.add_argument("--fd-directions", type=int, default=32,
                     help="finite-difference directions of the adjoint check (the config names 32)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -789,10 +981,6 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        if args.steps > 20:
-            args.steps = 10
-        if args.warmup > 3:
-            args.warmup = 3
         print(json.dumps(run_reference(args)))
         return 0
     if world > 1:

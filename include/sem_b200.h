@@ -49,6 +49,8 @@ enum sem_status {
 /* operator flags: the fused operators compose mask(QQ'(op(u))) on request */
 #define SEM_GS 1u   /* apply direct-stiffness summation QQ' (gatherScatter) */
 #define SEM_MASK 2u /* apply the handle's Dirichlet mask R'R afterwards     */
+#define SEM_NU_IN_G 4u /* sem_hlmz_host: nu_field is folded into G11/G12/G22,
+                          the variable-coefficient operator of sem_varcoef */
 
 /* arithmetic of the fused operators and of the solver */
 enum sem_precision {
@@ -149,14 +151,22 @@ int sem_lapl_nu(sem_mesh_t* mesh, const double* nu, const double* u, double* out
 int sem_hlmz(sem_mesh_t* mesh, const double* nu_field, double nu, double k,
              const double* u, double* out, unsigned flags, sem_stream_t stream);
 /* hlmz with mask(QQ') on HOST buffers (the end-to-end call): u_host and
- * out_host are column-major host arrays of the local layout.  The field moves
- * in and out in `slabs` slabs of element-tile rows (0: 8), so the copies
- * overlap the kernels; pinned host memory (cudaHostAlloc / cudaHostRegister)
- * is needed for that overlap, pageable memory works with serialised copies.
+ * out_host are column-major host arrays of the local layout.
+ *  - slabs >= 1 (0: 8): the field moves in and out in that many slabs of
+ *    element-tile rows by the copy engines, overlapping the kernels; pinned
+ *    host memory is needed for that overlap, pageable memory works with
+ *    serialised copies.
+ *  - slabs = SEM_HOST_DIRECT: the operator kernels read u_host and write
+ *    out_host in place over the CPU-GPU link; the buffers must be addressable
+ *    by the device (cudaHostAlloc / cudaHostRegister memory, or any host
+ *    memory on a system whose device reads pageable memory through the host
+ *    page tables, as Grace-Blackwell does), else SEM_ERR_UNSUPPORTED.
  * The result is bit-identical to sem_hlmz on device buffers.  nu_field, when
- * given, is a DEVICE field.  Asynchronous on `stream`: out_host is complete
- * when the stream is.  The handle keeps two device buffers of the field's
- * size and two streams for the copies. */
+ * given, is a DEVICE field: nu .* lapl(u) as in sem_hlmz, or folded into G as
+ * in sem_varcoef when flags has SEM_NU_IN_G.  Asynchronous on `stream`:
+ * out_host is complete when the stream is.  The slab pipeline keeps two
+ * device buffers of the field's size and two streams in the handle. */
+#define SEM_HOST_DIRECT (-1)
 int sem_hlmz_host(sem_mesh_t* mesh, const double* nu_field, double nu, double k, const double* u_host,
                   double* out_host, unsigned flags, int slabs, sem_stream_t stream);
 /* variable-coefficient operator D'(nu G)D u + k B u with nu (device field)

@@ -170,6 +170,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (m->G11_f) cudaFree(m->G11_f);
   if (m->Gdf) cudaFree(m->Gdf);
   if (m->fix_ctr) cudaFree(m->fix_ctr);
+  if (m->kB) cudaFree(m->kB);
   free_graph_cache(m);
   free_host_pipe(m);
   if (m->ws) cudaFree(m->ws);
@@ -341,6 +342,7 @@ static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, con
   c.variant = m->variant[m->precision];
   c.Gdf = m->Gdf;
   c.ctr = m->fix_ctr;
+  SEM_CHECK(use_kB(m, c, (cudaStream_t)stream));
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 
@@ -386,6 +388,7 @@ int sem_varcoef(sem_mesh_t* m, const double* nu_field, double k, const double* u
   c.variant = m->variant[m->precision];
   c.Gdf = m->Gdf;
   c.ctr = m->fix_ctr;
+  SEM_CHECK(use_kB(m, c, (cudaStream_t)stream));
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 

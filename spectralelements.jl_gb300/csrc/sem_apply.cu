@@ -167,7 +167,17 @@ int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, con
   return SEM_OK;
 }
 
-int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s) {
+// A double-float call whose scalar coefficients lie outside the pair format's
+// window runs in native FP64 (tiles with out-of-window field values are
+// recomputed in FP64 inside the kernels).
+static ApplyCall scalar_window(const ApplyCall& c) {
+  ApplyCall r = c;
+  if (c.precision == SEM_F64_DF && !(df_window_ok(c.nu_s) && df_window_ok(c.k_s))) r.precision = SEM_F64;
+  return r;
+}
+
+int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c0, cudaStream_t s) {
+  const ApplyCall c = scalar_window(c0);
   int st;
   int tile[2] = {0, 0};
   const bool hi = g.n >= 10;
@@ -184,8 +194,9 @@ int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cuda
   return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s);
 }
 
-int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c, long long key_lo,
+int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c0, long long key_lo,
                         long long key_hi, cudaStream_t s) {
+  const ApplyCall c = scalar_window(c0);
   if (c.tyn <= 0) return set_error(SEM_ERR_BAD_ARG, "empty tile-row window");
   int st;
   int tile[2] = {0, 0};
@@ -206,6 +217,31 @@ long long cg_apply_parts(const Grid& g) {
   int tx = 1, ty = 1;
   tile_shape(g.n, &tx, &ty);
   return (long long)((g.Ex + tx - 1) / tx) * ((g.Ey + ty - 1) / ty);
+}
+
+__global__ void k_scale_into(const double* __restrict__ B, double k, double* __restrict__ out, long long L) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x)
+    out[i] = __dmul_rn(k, B[i]);
+}
+
+int use_kB(sem_mesh* m, ApplyCall& c, cudaStream_t s) {
+  if (c.precision != SEM_F64 || !(c.mode & M_MASS) || c.B != m->B || c.k_s == 1.0) return SEM_OK;
+  const long long L = m->g.NX * m->g.NY;
+  if (!m->kB) {
+    SEM_CUDA(cudaMalloc(&m->kB, sizeof(double) * (size_t)L));
+    m->kB_k = std::nan("");  // not yet made
+  }
+  if (!(m->kB_k == c.k_s)) {
+    long long blocks = (L + 255) / 256;
+    if (blocks > 152LL * 16) blocks = 152LL * 16;
+    k_scale_into<<<(unsigned)blocks, 256, 0, s>>>(m->B, c.k_s, m->kB, L);
+    SEM_CUDA(cudaGetLastError());
+    m->kB_k = c.k_s;
+  }
+  c.B = m->kB;
+  c.k_s = 1.0;
+  c.mode |= M_KB;
+  return SEM_OK;
 }
 
 int ensure_fix_counters(sem_mesh* m) {

@@ -49,6 +49,9 @@ struct Apply2Args {
   const io* nu;
   v nu_s;
   v k_s;
+  // FP64 geometry and mass (double-float policy: the FP64 recomputation of a
+  // tile whose double-float results left the pair format's range)
+  const double *G11d, *G12d, *G22d, *Bd;
   int Ex, Ey;
   long long NX;
   unsigned mode;
@@ -306,7 +309,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < N; ++j) res[j] = P::fin(P::mul(a.nu_s, res[j]));
+        for (int j = 0; j < N; ++j) res[j] = P::fin((mode & M_NUFOLD) ? res[j] : P::mul(a.nu_s, res[j]));
       }
     } else {
 #pragma unroll
@@ -317,20 +320,31 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       const V b = valid ? GeoT<P>::ld(a.B + base + (long long)j * NX) : P::zero();
-      res[j] = P::fin(P::fma(P::mul(a.k_s, b), s0[j * SP + lane], res[j]));
+      res[j] = P::fin(P::fma((mode & M_KB) ? b : P::mul(a.k_s, b), s0[j * SP + lane], res[j]));
     }
   }
 
-  if constexpr (CG) {
-    df acc = {0.0f, 0.0f};
+  // a NaN or Inf double-float result: an input or intermediate outside the
+  // pair format's range; the tile is recomputed in native FP64 after its
+  // stores and before its cross-tile completion (sem_tile_f64.cuh)
+  bool bad = false;
+  if constexpr (P::kPrecision == SEM_F64_DF) {
 #pragma unroll
-    for (int j = 0; j < N; ++j) acc = df_add_u(acc, dot_term(s0[j * SP + lane], res[j]));
-    const df tot = block_sum_df(df_norm(acc));
-    if (threadIdx.x == 0) a.dpart[blockIdx.y * gridDim.x + blockIdx.x] = tot;
+    for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
   }
+  if constexpr (CG)
+    store_dot_part<P, N>([&](int j) { return s0[j * SP + lane]; }, [&](int j) { return res[j]; }, a.dpart,
+                         blockIdx.y * gridDim.x + blockIdx.x);
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
   tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
                                ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
+  if constexpr (P::kPrecision == SEM_F64_DF) {
+    if (__syncthreads_or(bad))
+      tile_f64_redo<N, TX, TY>(CG ? a.p : a.u, a.out, NX, a.Ex, a.Ey, blockIdx.x * TX, (blockIdx.y + a.ty0) * TY,
+                               mode, a.G11d, a.G12d, a.G22d, a.Bd, a.nu, df_exact(a.nu_s), df_exact(a.k_s), &a.Dr,
+                               &a.Drt, &a.Ds, &a.Dst, reinterpret_cast<double*>(S0), reinterpret_cast<double*>(S1),
+                               CG ? a.dpart : nullptr, blockIdx.y * gridDim.x + blockIdx.x);
+  }
   if constexpr (FUSE) {
     if (mode & M_GS)
       finish_tile_interfaces<IO, TX, TY>(a.out, N, a.Ex, a.Ey, NX, mode, a.ctr, a.tiles_x, a.tiles_y,

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < N; ++j) res[j] = P::fin(P::mul(a.nu_s, res[j]));
+          for (int j = 0; j < N; ++j) res[j] = P::fin((mode & M_NUFOLD) ? res[j] : P::mul(a.nu_s, res[j]));
         }
       } else {
         cp_async_wait_group<2>();
@@ -209,13 +209,28 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
 #pragma unroll
       for (int j = 0; j < N; ++j) {
         const V b = valid ? GeoT<P>::cvt(RG[(3 * N + j) * T + t]) : P::zero();
-        res[j] = P::fin(P::fma(P::mul(a.k_s, b), s0[j * SP + lane], res[j]));
+        res[j] = P::fin(P::fma((mode & M_KB) ? b : P::mul(a.k_s, b), s0[j * SP + lane], res[j]));
       }
     }
     fetch_b(next);
 
+    bool bad = false;
+    if constexpr (P::kPrecision == SEM_F64_DF) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
+    }
     tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
                                  ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
+    if constexpr (P::kPrecision == SEM_F64_DF) {
+      // a NaN or Inf double-float result: the tile is recomputed in native FP64
+      if (__syncthreads_or(bad)) {
+        const int ty = tile / tiles_x;
+        tile_f64_redo<N, TX, TY>(a.u, a.out, NX, a.Ex, a.Ey, (tile - ty * tiles_x) * TX, ty * TY, mode, a.G11d,
+                                 a.G12d, a.G22d, a.Bd, a.nu, df_exact(a.nu_s), df_exact(a.k_s), &a.Dr, &a.Drt,
+                                 &a.Ds, &a.Dst, reinterpret_cast<double*>(S0), reinterpret_cast<double*>(S1), nullptr,
+                                 0);
+      }
+    }
     __syncthreads();  // the next tile overwrites s0 and s1
   }
   cp_async_wait_all();

@@ -205,6 +205,12 @@ __device__ __forceinline__ void tile_dss_store(const typename P::v (&res)[N], ty
   }
 }
 
+}  // namespace sem
+
+#include "sem_tile_f64.cuh"
+
+namespace sem {
+
 // DOT: the launch is a CG iteration's operator application on the direction
 // u = p and every CTA also writes its part of p . A p, summed over the
 // unassembled local products (equal to the mult-weighted dot of the assembled
@@ -330,7 +336,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
       }
     } else {
 #pragma unroll
-      for (int j = 0; j < N; ++j) res[j] = P::fin(P::mul(a.nu_s, res[j]));
+      for (int j = 0; j < N; ++j) res[j] = P::fin((mode & M_NUFOLD) ? res[j] : P::mul(a.nu_s, res[j]));
     }
   } else {
 #pragma unroll
@@ -341,21 +347,32 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       V b = ldx(a.B, a.slot_b, j);
-      V kb = P::mul(a.k_s, b);
+      V kb = (mode & M_KB) ? b : P::mul(a.k_s, b);
       res[j] = P::fin(P::fma(kb, u[j], res[j]));
     }
   }
-  if constexpr (DOT) {
-    df acc = {0.0f, 0.0f};
+  // a NaN or Inf double-float result: an input or intermediate outside the
+  // pair format's range; the tile is recomputed in native FP64 after its
+  // stores (sem_tile_f64.cuh)
+  bool bad = false;
+  if constexpr (P::kPrecision == SEM_F64_DF) {
 #pragma unroll
-    for (int j = 0; j < N; ++j) acc = df_add_u(acc, dot_term(u[j], res[j]));
-    const df tot = block_sum_df(df_norm(acc));
-    if (threadIdx.x == 0) a.dpart[blockIdx.y * gridDim.x + blockIdx.x] = tot;
+    for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
   }
+  if constexpr (DOT)
+    store_dot_part<P, N>([&](int j) { return u[j]; }, [&](int j) { return res[j]; }, a.dpart,
+                         blockIdx.y * gridDim.x + blockIdx.x);
 
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
   tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S2), elem, lane,
                                ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
+  if constexpr (P::kPrecision == SEM_F64_DF) {
+    if (__syncthreads_or(bad))
+      tile_f64_redo<N, TX, TY>(a.u, a.out, NX, a.Ex, a.Ey, blockIdx.x * TX, (blockIdx.y + a.ty0) * TY, mode, a.G11,
+                               a.G12, a.G22, a.B, a.nu, df_exact(a.nu_s), df_exact(a.k_s), &a.Dr, &a.Drt, &a.Ds,
+                               &a.Dst, reinterpret_cast<double*>(S2), reinterpret_cast<double*>(S1),
+                               DOT ? a.dpart : nullptr, blockIdx.y * gridDim.x + blockIdx.x);
+  }
 }
 
 // Finishes QQ' (and the mask) at the points whose copies sit in different

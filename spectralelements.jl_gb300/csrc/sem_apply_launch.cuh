@@ -26,7 +26,7 @@ int launch_apply_f32_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& 
 int launch_apply_f32_hi(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
 
 template <class P, int N>
-static void fill_eo(EOCoef<N, typename P::v>& c, const double* src) {
+static void fill_eo(EOCoef<N, typename P::v>& c, const double* src, double scale = 1.0) {
   constexpr int M = N / 2;
   const double* A = src;
   const double* C = A + M * M;
@@ -34,14 +34,22 @@ static void fill_eo(EOCoef<N, typename P::v>& c, const double* src) {
   const double* mr = cm + M;
   for (int i = 0; i < M; ++i)
     for (int k = 0; k < M; ++k) {
-      c.A[i][k] = P::from_double(A[i * M + k]);
-      c.Cc[i][k] = P::from_double(C[i * M + k]);
+      c.A[i][k] = P::from_double(scale * A[i * M + k]);
+      c.Cc[i][k] = P::from_double(scale * C[i * M + k]);
     }
   for (int i = 0; i < M; ++i) {
-    c.cm[i] = P::from_double(cm[i]);
-    c.mr[i] = P::from_double(mr[i]);
+    c.cm[i] = P::from_double(scale * cm[i]);
+    c.mr[i] = P::from_double(scale * mr[i]);
   }
 }
+
+// The scalar nu of a call without a nu field multiplies the stiffness part
+// after the last contraction; it is folded into the coefficients of the
+// transposed derivatives instead (D' -> nu D'), which saves one multiply per
+// point (M_NUFOLD).  The scaled coefficients are rounded once, so the results
+// differ from nu .* (D'GD u) by rounding only; every kernel variant folds the
+// same way, so the variants stay bit-identical.
+static inline bool fold_nu(unsigned mode) { return !(mode & M_NU) && (mode & M_STIFF); }
 
 // kern<<<grid, block, smem, s>>>(args...), as a programmatic dependent of
 // the previous kernel on s when pdl is set
@@ -77,12 +85,13 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   a.G22 = static_cast<const io*>(c.G22);
   a.B = static_cast<const io*>(c.B);
   a.nu = static_cast<const io*>(c.nu);
-  a.nu_s = P::from_double(c.nu_s);
+  const bool fold = fold_nu(c.mode);
+  a.nu_s = P::from_double(fold ? 1.0 : c.nu_s);
   a.k_s = P::from_double(c.k_s);
   a.Ex = g.Ex;
   a.Ey = g.Ey;
   a.NX = g.NX;
-  a.mode = c.mode;
+  a.mode = c.mode | (fold ? M_NUFOLD : 0u);
   a.skip = c.skip;
   int nslot = 0;
   a.slot_g = a.slot_b = a.slot_nu = -1;
@@ -95,9 +104,9 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
     if (c.mode & (M_NU | M_NUG)) a.slot_nu = nslot++;
   }
   fill_eo<P, N>(a.Dr, ops->eo[0]);
-  fill_eo<P, N>(a.Drt, ops->eo[1]);
+  fill_eo<P, N>(a.Drt, ops->eo[1], fold ? c.nu_s : 1.0);
   fill_eo<P, N>(a.Ds, ops->eo[2]);
-  fill_eo<P, N>(a.Dst, ops->eo[3]);
+  fill_eo<P, N>(a.Dst, ops->eo[3], fold ? c.nu_s : 1.0);
   const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
   const size_t smem = 2 * te * sizeof(typename P::v) + nslot * te * sizeof(io);
   a.dpart = static_cast<df*>(c.cg_dpart);
@@ -133,17 +142,24 @@ static void fill_args2(Apply2Args<P, N>& a, const Grid& g, const OperatorSet* op
     a.B = static_cast<const gt*>(c.B);
   }
   a.nu = static_cast<const io*>(c.nu);
-  a.nu_s = P::from_double(c.nu_s);
+  const bool fold = fold_nu(c.mode);
+  a.nu_s = P::from_double(fold ? 1.0 : c.nu_s);
   a.k_s = P::from_double(c.k_s);
+  if (P::kPrecision == SEM_F64_DF) {
+    a.G11d = static_cast<const double*>(c.G11);
+    a.G12d = static_cast<const double*>(c.G12);
+    a.G22d = static_cast<const double*>(c.G22);
+    a.Bd = static_cast<const double*>(c.B);
+  }
   a.Ex = g.Ex;
   a.Ey = g.Ey;
   a.NX = g.NX;
-  a.mode = c.mode;
+  a.mode = c.mode | (fold ? M_NUFOLD : 0u);
   a.skip = c.skip;
   fill_eo<P, N>(a.Dr, ops->eo[0]);
-  fill_eo<P, N>(a.Drt, ops->eo[1]);
+  fill_eo<P, N>(a.Drt, ops->eo[1], fold ? c.nu_s : 1.0);
   fill_eo<P, N>(a.Ds, ops->eo[2]);
-  fill_eo<P, N>(a.Dst, ops->eo[3]);
+  fill_eo<P, N>(a.Dst, ops->eo[3], fold ? c.nu_s : 1.0);
 }
 
 template <class P, int N, bool STAGE, bool FUSE = false, bool CG = false>

@@ -99,6 +99,43 @@ __device__ __forceinline__ df d2df(double x) {
   return {h, l};
 }
 
+// Operator inputs of the double-float kernels: d2df inside the window
+// [2^-70, 2^90) of magnitudes, where every product and sum of an operator
+// apply stays in the normal FP32 range with its error terms; a nonzero value
+// outside it (and Inf) becomes NaN.  A NaN in a result of the double-float
+// arithmetic therefore marks an input or an intermediate the pair format
+// cannot carry, and the kernels recompute that element tile in native FP64;
+// zeros pass unchanged.
+constexpr unsigned kDfExpLo = 1023u - 70u;   // biased double exponent of 2^-70
+constexpr unsigned kDfExpHi = 1023u + 90u;   // first biased exponent outside the window
+__device__ __forceinline__ df d2df_op(double x) {
+  const unsigned lo = (unsigned)__double2loint(x);
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned ed = (hi >> 20) & 0x7ffu;
+  const unsigned sg = hi & 0x80000000u;
+  const unsigned hb = (__funnelshift_l(lo, hi, 3) + 0x40000000u) | sg;  // the split of d2df
+  const unsigned pb = (hb & 0xff800000u) - 0x0B800000u;
+  const unsigned fb = pb | ((lo >> 6) & 0x007fffffu);
+  float h = __uint_as_float(hb);
+  float l = __fsub_rn(__uint_as_float(fb), __uint_as_float(pb));
+  if (ed - kDfExpLo >= kDfExpHi - kDfExpLo) {  // rare: zero, or outside the window
+    const bool zero = ed == 0u && ((hi & 0x000fffffu) | lo) == 0u;
+    h = __uint_as_float(zero ? sg : 0x7fc00000u);
+    l = 0.0f;
+  }
+  return {h, l};
+}
+
+// a double-float value whose high part is Inf or NaN
+__device__ __forceinline__ bool df_bad(df a) { return (__float_as_uint(a.h) & 0x7f800000u) == 0x7f800000u; }
+
+// host: whether a nonzero scalar coefficient lies in the double-float window
+inline bool df_window_ok(double v) {
+  if (v == 0.0) return true;
+  const double a = v < 0 ? -v : v;
+  return a >= 0x1p-70 && a < 0x1p90;
+}
+
 // exact float -> double by bit manipulation (subnormal floats flush to zero)
 __device__ __forceinline__ double f2d_bits(float f) {
   const unsigned b = __float_as_uint(f);
@@ -185,6 +222,43 @@ __device__ __forceinline__ df block_sum_df(df x) {
   return x;
 }
 
+// block-wide FP64 sum in a fixed order (warp trees, then the warps in order);
+// valid in thread 0; every thread of the block calls it
+__device__ __forceinline__ double block_sum_d(double x) {
+  __shared__ double warp_sums_d[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) x = __dadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
+  __syncthreads();
+  if (lane == 0) warp_sums_d[w] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    x = warp_sums_d[0];
+    for (int i = 1; i < nw; ++i) x = __dadd_rn(x, warp_sums_d[i]);
+  }
+  return x;
+}
+
+// Each CTA's part of p . A p over its unassembled local products: native FP64
+// for the FP64 policy (stored as a double in the 8-byte part slot), double-float
+// otherwise.  Every thread of the block calls it.
+template <class P, int N, class U, class R>
+__device__ __forceinline__ void store_dot_part(const U& u, const R& res, df* dpart, long long slot) {
+  if constexpr (P::kPrecision == SEM_F64) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc = __fma_rn((double)u(j), (double)res(j), acc);
+    const double tot = block_sum_d(acc);
+    if (threadIdx.x == 0) reinterpret_cast<double*>(dpart)[slot] = tot;
+  } else {
+    df acc = {0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc = df_add_u(acc, dot_term(u(j), res(j)));
+    const df tot = block_sum_df(df_norm(acc));
+    if (threadIdx.x == 0) dpart[slot] = tot;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // policies
 // ---------------------------------------------------------------------------
@@ -228,8 +302,8 @@ struct PDF {
   typedef double io;
   typedef df v;
   static constexpr int kPrecision = SEM_F64_DF;
-  static __device__ __forceinline__ v ld(const io* p) { return d2df(__ldg(p)); }
-  static __device__ __forceinline__ v cvt(io x) { return d2df(x); }
+  static __device__ __forceinline__ v ld(const io* p) { return d2df_op(__ldg(p)); }
+  static __device__ __forceinline__ v cvt(io x) { return d2df_op(x); }
   static __device__ __forceinline__ io st(v a) { return df2d(a); }
   static __device__ __forceinline__ v zero() { return {0.0f, 0.0f}; }
   static __device__ __forceinline__ v add(v a, v b) { return df_add(a, b); }

@@ -46,6 +46,7 @@ struct sem_batch {
   int device = 0;
   int jacobi = 0;
   std::vector<BProb> host;  // per problem, creation order (device pointers inside)
+  std::vector<sem_mesh*> meshes;  // per problem (solves outside the pair format's range)
   std::vector<int> order;   // device slot -> problem index
   std::vector<Group> groups;
   BProb* dev = nullptr;     // device descriptors in slot order
@@ -95,6 +96,7 @@ int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* 
     return cuda_error(e, "batch allocation");
   }
   b->host.resize(count);
+  b->meshes.assign(meshes, meshes + count);
   char* p = static_cast<char*>(b->ws);
   auto take = [&](size_t nbytes) {
     char* q = p;
@@ -206,6 +208,9 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     q[j].tol = tol[i];
     const long long L = q[j].NX * q[j].NY;
     q[j].maxiter = (maxiter && maxiter[i] > 0) ? maxiter[i] : (int)(L > 2147483647LL ? 2147483647LL : L);
+    // a problem whose nu or k lies outside the double-float window is solved
+    // in native FP64 after the launch (none of its iterations run in it)
+    if (!(df_window_ok(q[j].nu) && df_window_ok(q[j].k))) q[j].maxiter = -1;
   }
   SEM_CUDA(cudaMemcpyAsync(b->dev, q.data(), sizeof(BProb) * b->count, cudaMemcpyHostToDevice, s));
   SEM_CUDA(cudaMemsetAsync(b->queues, 0, sizeof(int) * (kBatchMaxN + 1), s));
@@ -232,11 +237,38 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     SEM_CUDA(cudaEventRecord(g.done, g.stream));
     SEM_CUDA(cudaStreamWaitEvent(s, g.done, 0));
   }
+  std::vector<int> wanted(b->count);
+  for (int j = 0; j < b->count; ++j) wanted[j] = q[j].maxiter;
   SEM_CUDA(cudaMemcpyAsync(q.data(), b->dev, sizeof(BProb) * b->count, cudaMemcpyDeviceToHost, s));
   SEM_CUDA(cudaStreamSynchronize(s));
   int bad = 0, nanc = 0;
   for (int j = 0; j < b->count; ++j) {
     const int i = b->order[j];
+    // range guard: a problem outside the double-float window, or one that ended
+    // in NaN/Inf with a finite b, is solved again by the native FP64 sem_pcg
+    const double r0 = q[j].res0_inf;
+    const bool finite_b = r0 == r0 && r0 <= 1.7976931348623157e308;
+    if (wanted[j] < 0 || (q[j].nan && finite_b)) {
+      sem_pcg_opts o;
+      std::memset(&o, 0, sizeof(o));
+      o.nu = q[j].nu;
+      o.k = q[j].k;
+      o.precond = b->jacobi ? SEM_PRECOND_JACOBI : SEM_PRECOND_NONE;
+      o.precision = SEM_F64;
+      o.tol = tol[i];
+      o.maxiter = (maxiter && maxiter[i] > 0) ? maxiter[i] : 0;
+      o.path = SEM_PATH_CHUNKED;
+      sem_solve_info si;
+      std::memset(&si, 0, sizeof(si));
+      const int st = sem_pcg(b->meshes[i], &o, rhs[i], x[i], &si, stream);
+      if (st != SEM_OK && st != SEM_ERR_NOT_CONVERGED && st != SEM_ERR_NAN) return st;
+      q[j].iters = si.iters;
+      q[j].outer = si.outer;
+      q[j].res_inf = si.res_inf;
+      q[j].res0_inf = si.res0_inf;
+      q[j].converged = si.converged;
+      q[j].nan = st == SEM_ERR_NAN;
+    }
     if (info) {
       info[i].iters = q[j].iters;
       info[i].outer = q[j].outer;

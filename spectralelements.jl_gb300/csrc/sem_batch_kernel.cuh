@@ -651,6 +651,17 @@ __device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, 
   typedef BTile<N> T;
   const bool jac = a.jacobi != 0;
   const int maxiter = pr.maxiter;
+  if (maxiter < 0) {  // left to the host's native FP64 solve (scalars outside the pair window)
+    if (rank == 0 && threadIdx.x == 0) {
+      pr.iters = 0;
+      pr.outer = 0;
+      pr.res_inf = 0.0;
+      pr.res0_inf = 0.0;
+      pr.nan = 0;
+      pr.converged = 0;
+    }
+    return;
+  }
   if (a.precision == SEM_MIXED_RR) {
     brr<N>(a, pr, cl, rank, red, rc, buf);
     return;

@@ -92,7 +92,7 @@ __global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, long 
 __global__ void k_d2df(const double* __restrict__ a, df* __restrict__ b, long long len) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
        i += (long long)gridDim.x * blockDim.x)
-    b[i] = d2df(a[i]);
+    b[i] = d2df_op(a[i]);
 }
 
 __global__ void k_maskfield(double* __restrict__ out, Grid g) {

@@ -1,6 +1,13 @@
 // The fused operator on HOST buffers: mask(QQ'(hlmz(u))) for a field that
 // lives in host memory and a result that goes back to it.
 //
+// Direct access (slabs = SEM_HOST_DIRECT): the operator kernel reads u_host
+// and writes out_host in place over the coherent CPU-GPU link (about 200 GB/s
+// each way on GB300), and the cross-tile fixup finishes the interface points
+// there.  Measured on the 256^2, N=8 apply it is slower than the slab pipeline
+// below (0.53 against 0.46 ms in FP64): every CTA waits for its inputs from the
+// link at its start.  It serves buffers the copy engines cannot reach in place
+// (pageable memory read through the host page tables).  Otherwise:
 // The field moves in and out in slabs of element-tile rows (whole columns of
 // the column-major layout, so each slab is one contiguous copy).  The copy
 // in of slab k+1 overlaps the operator kernel of slab k, and the copy out of
@@ -61,6 +68,26 @@ int get_pipe(sem_mesh* m, long long L, HostPipe** out) {
   return SEM_OK;
 }
 
+// Whether the device can read and write p in place: pinned or registered host
+// memory mapped at the same address (unified addressing), or any host memory
+// when `pageable` is set and the device reads pageable memory through the host
+// page tables (Grace-Blackwell's coherent CPU-GPU link).
+bool device_can_address(const void* p, bool pageable) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+  if (a.type == cudaMemoryTypeUnregistered && pageable) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) return false;
+    return v != 0;
+  }
+  return false;
+}
+
 }  // namespace
 
 void free_host_pipe(sem_mesh* m) {
@@ -91,7 +118,8 @@ extern "C" int sem_hlmz_host(sem_mesh_t* m, const double* nu_field, double nu, d
                              sem_stream_t stream) {
   if (!m || !u_host || !out_host) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
   if (u_host == out_host) return set_error(SEM_ERR_BAD_ARG, "output must not alias the input");
-  if (slabs < 0) return set_error(SEM_ERR_BAD_ARG, "slabs must be >= 0");
+  if (slabs < SEM_HOST_DIRECT) return set_error(SEM_ERR_BAD_ARG, "slabs must be >= SEM_HOST_DIRECT (-1)");
+  if ((flags & SEM_NU_IN_G) && !nu_field) return set_error(SEM_ERR_BAD_ARG, "SEM_NU_IN_G needs nu_field");
   int dev = -1;
   SEM_CUDA(cudaGetDevice(&dev));
   if (dev != m->device) return set_error(SEM_ERR_BAD_ARG, "mesh handle lives on device %d", m->device);
@@ -99,8 +127,44 @@ extern "C" int sem_hlmz_host(sem_mesh_t* m, const double* nu_field, double nu, d
   const Grid& g = m->g;
   const long long NX = g.NX, L = g.NX * g.NY;
   if (m->precision == SEM_F64_DF) SEM_CHECK(ensure_df_geometry(m, s));
+
+  unsigned mode = g.topo | M_STIFF | M_MASS;
+  if (flags & SEM_GS) mode |= M_GS;
+  if ((flags & SEM_MASK) && m->has_bc) mode |= M_MASK;
+  if (nu_field) mode |= (flags & SEM_NU_IN_G) ? M_NUG : M_NU;
+  if (k == 0.0) mode &= ~M_MASS;
+  ApplyCall c;
+  std::memset(&c, 0, sizeof(c));
+  c.G11 = m->G11;
+  c.G12 = m->G12;
+  c.G22 = m->G22;
+  c.B = m->B;
+  c.nu = nu_field;
+  c.nu_s = (flags & SEM_NU_IN_G) ? 1.0 : nu;
+  c.k_s = k;
+  c.mode = mode;
+  c.precision = m->precision;
+  c.variant = m->variant[m->precision];
+  c.Gdf = m->Gdf;
+  SEM_CHECK(use_kB(m, c, s));
+
+  // direct access: the operator kernels read u_host and write out_host over
+  // the CPU-GPU link while they compute (no staging buffers, no copy engines)
+  const bool direct =
+      slabs == SEM_HOST_DIRECT && device_can_address(u_host, true) && device_can_address(out_host, true);
+  if (slabs == SEM_HOST_DIRECT && !direct)
+    return set_error(SEM_ERR_UNSUPPORTED, "the device cannot address these host buffers in place");
+  if (direct) {
+    c.u = u_host;
+    c.out = out_host;
+    if (c.variant == 5) c.variant = 2;  // the cross-tile sums run in the fixup launch
+    return launch_apply(g, m->ops, c, s);
+  }
+
   HostPipe* p = nullptr;
   SEM_CHECK(get_pipe(m, L, &p));
+  c.u = p->u;
+  c.out = p->o;
 
   int TX = 1, TY = 1;
   tile_shape_of(g.n, &TX, &TY);
@@ -115,26 +179,6 @@ extern "C" int sem_hlmz_host(sem_mesh_t* m, const double* nu_field, double nu, d
     c0[i] = ey * g.n;
   }
 
-  unsigned mode = g.topo | M_STIFF | M_MASS;
-  if (flags & SEM_GS) mode |= M_GS;
-  if ((flags & SEM_MASK) && m->has_bc) mode |= M_MASK;
-  if (nu_field) mode |= M_NU;
-  if (k == 0.0) mode &= ~M_MASS;
-  ApplyCall c;
-  std::memset(&c, 0, sizeof(c));
-  c.u = p->u;
-  c.out = p->o;
-  c.G11 = m->G11;
-  c.G12 = m->G12;
-  c.G22 = m->G22;
-  c.B = m->B;
-  c.nu = nu_field;
-  c.nu_s = nu;
-  c.k_s = k;
-  c.mode = mode;
-  c.precision = m->precision;
-  c.variant = m->variant[m->precision];
-  c.Gdf = m->Gdf;
 
   // the copies start after everything queued on the caller's stream
   SEM_CUDA(cudaEventRecord(p->start, s));

@@ -51,6 +51,8 @@ enum : unsigned {
   M_STIFF = 1u << 10,  // include the stiffness (lapl) part
   M_NUG = 1u << 11,    // variable coefficient folded into G: D'(nu G)D
   M_MULT1 = 1u << 12,  // solver dots without the SEM multiplicity weights
+  M_NUFOLD = 1u << 13, // the scalar nu is folded into the transposed derivative coefficients
+  M_KB = 1u << 14,     // B already holds k .* B (no k multiply in the mass term)
 };
 
 // per-row / per-column structure bits (device tables of a mesh handle)
@@ -190,6 +192,8 @@ struct sem_mesh {
   void* graphs;            // CUDA graphs of the CG iteration chunks (sem_pcg.cu), or NULL
   unsigned* fix_ctr;       // interface arrival counters of kernel variant 5 (3 per tile), or NULL
   void* host_pipe;         // streams, events and buffers of sem_hlmz_host (sem_host.cu), or NULL
+  double* kB;              // k .* B for the native FP64 operator (lazily created), and its k
+  double kB_k;
 };
 
 namespace sem {
@@ -283,6 +287,11 @@ struct SmallProb {
 };
 
 int launch_small_pcg(SmallProb* dev, const OperatorSet& ops, int n, cudaStream_t s);  // sem_small.cu
+// the SEM_MIXED solve of a small mesh in one thread block with the whole FP32
+// working set in shared memory (sem_tiny.cu); host is the record copied to dev
+int launch_tiny_pcg(SmallProb* dev, const SmallProb& host, const OperatorSet& ops, size_t smem, cudaStream_t s);
+size_t tiny_smem_bytes(long long L, bool mass, bool jac);
+size_t max_smem_optin();  // the device's opt-in shared memory per block (sem_apply.cu)
 
 // results at the tail of a SmallProb, in the same order
 struct SmallOut {
@@ -303,6 +312,9 @@ int small_prepare(sem_mesh* m, const sem_pcg_opts* o, const double* b, double* x
 constexpr int kVariants = SEM_VARIANTS;
 
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
+// native FP64 calls with a mass term read the mesh's k .* B (one multiply fewer
+// per point); made or refreshed on s when k changes
+int use_kB(sem_mesh* m, ApplyCall& c, cudaStream_t s);
 bool timing_enabled();                 // sem_timing_enable state (sem_apply.cu)
 void free_graph_cache(sem_mesh* m);    // sem_pcg.cu
 void free_host_pipe(sem_mesh* m);      // sem_host.cu

@@ -138,6 +138,33 @@ struct Acc<double> {
   __device__ __forceinline__ double max() const { return __longlong_as_double((long long)mx); }
 };
 
+// Native FP64 accumulation for the SEM_F64 solves: the dots span the whole
+// double range (the double-float accumulators above are bound to the FP32
+// exponent range), at the FP64 rate.
+struct AccN {
+  double s = 0.0;
+  unsigned long long mx = 0ull;
+  __device__ __forceinline__ void prod(double a, double b, double m) { s = __fma_rn(__dmul_rn(a, m), b, s); }
+  __device__ __forceinline__ void rhr(double a, double d, double m) {
+    s = __fma_rn(a, __dmul_rn(__dmul_rn(a, d), m), s);
+  }
+  __device__ __forceinline__ void amax(double a) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+    mx = b > mx ? b : mx;
+  }
+  __device__ __forceinline__ double sum() const { return s; }
+  __device__ __forceinline__ double max() const { return __longlong_as_double((long long)mx); }
+};
+
+template <class T, bool NAT>
+struct AccOf {
+  typedef Acc<T> type;
+};
+template <>
+struct AccOf<double, true> {
+  typedef AccN type;
+};
+
 template <>
 struct Acc<float> {
   float s = 0.0f;
@@ -155,10 +182,10 @@ struct Acc<float> {
 // p = h + beta p_old with h = r .* dinv
 // x = 0, r = b (converted), p = 0; partials of t = r.h.mult and max|r|
 // (p == NULL: p is kept, the residual replacement of SEM_MIXED_RR)
-template <class T, class TB>
+template <class T, class TB, bool NAT = false>
 __global__ void k_init(const TB* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
                        T* __restrict__ p, const T* __restrict__ dinv, double* part, Grid g) {
-  Acc<T> acc;
+  typename AccOf<T, NAT>::type acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     const T ri = (T)b[i];
     x[i] = (T)0;
@@ -226,13 +253,13 @@ __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* _
     p[i] = cg_direction(r[i], jac ? dinv[i] : (T)1, beta, p[i], jac);
 }
 
-template <class T>
+template <class T, bool NAT = false>
 __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, double* part,
                           const Scalars* sc, Grid g) {
   pdl_trigger();
   pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
-  Acc<T> acc;
+  typename AccOf<T, NAT>::type acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     acc.prod(p[i], Ap[i], mult_at(rr, cc, g));
   });
@@ -272,7 +299,7 @@ __global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
   }
 }
 
-template <class T>
+template <class T, bool NAT = false>
 __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                          const T* __restrict__ Ap, const T* __restrict__ dinv, double* part,
                          const Scalars* sc, Grid g) {
@@ -280,7 +307,7 @@ __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restri
   pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
   const T alpha = (T)sc->alpha;
-  Acc<T> acc;
+  typename AccOf<T, NAT>::type acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     x[i] = x[i] + alpha * p[i];
     const T ri = r[i] - alpha * Ap[i];
@@ -558,23 +585,39 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
   ApplyCall cp = c;
   cp.pdl = 1;
   const long long np = cg_apply_parts(cx.g);
+  // the native FP64 operator writes FP64 parts of p.Ap and the solve's dots are
+  // native FP64 (the whole double range); the other arithmetics use
+  // double-float parts and dots
+  const bool nat = sizeof(T) == 8 && c.precision == SEM_F64;
+  auto alpha_parts = [&]() -> int {
+    if (nat) return launch_pdl(k_scal_alpha, 1, kRT, s, (const double*)w.dpart, (int)np, w.sc);
+    return launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc);
+  };
   for (int it = 0; it < check_every; ++it) {
     if (fused) {
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
-      SEM_CHECK(launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc));
+      SEM_CHECK(alpha_parts());
     } else if (cp.cg_dpart) {  // direction pass, then the operator with the p.Ap parts
       SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
-      SEM_CHECK(launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc));
+      SEM_CHECK(alpha_parts());
     } else {
       SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
-      SEM_CHECK(launch_pdl(k_dot_pap<T>, nb, kRT, s, (const T*)p, (const T*)Ap, w.part,
-                           (const Scalars*)w.sc, gv));
+      if (nat)
+        SEM_CHECK(launch_pdl(k_dot_pap<T, true>, nb, kRT, s, (const T*)p, (const T*)Ap, w.part,
+                             (const Scalars*)w.sc, gv));
+      else
+        SEM_CHECK(launch_pdl(k_dot_pap<T>, nb, kRT, s, (const T*)p, (const T*)Ap, w.part,
+                             (const Scalars*)w.sc, gv));
       SEM_CHECK(launch_pdl(k_scal_alpha, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
     }
-    SEM_CHECK(launch_pdl(k_update<T>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
-                         (const Scalars*)w.sc, gv));
+    if (nat)
+      SEM_CHECK(launch_pdl(k_update<T, true>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
+                           (const Scalars*)w.sc, gv));
+    else
+      SEM_CHECK(launch_pdl(k_update<T>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
+                           (const Scalars*)w.sc, gv));
     SEM_CHECK(launch_pdl(k_scal_beta, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
   }
   SEM_CUDA(cudaGetLastError());
@@ -705,6 +748,7 @@ int run_cg(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r
   c.Gdf = cx.Gdf;
   c.ctr = cx.ctr;
   c.skip = &w.sc->done;
+  if (m) SEM_CHECK(use_kB(m, c, s));
   // CG-fused operator launches with the kernels that provide them (variants 2
   // and 5; double-float arithmetic also needs the pre-split geometry).  Their
   // unassembled p.Ap equals the mult-weighted dot only: unweighted dots
@@ -782,6 +826,7 @@ int jacobi_build(const OpCtx& cx, const WS& w, const sem_pcg_opts* o, cudaStream
 bool small_eligible(const sem_mesh* m, const Grid& g, const sem_pcg_opts* o) {
   const int prec = o->precision;
   return m && g.NX * g.NY <= SEM_SMALL_MAX_LOCAL && g.n <= 11 && !o->nu_field &&
+         df_window_ok(o->nu) && df_window_ok(o->k) &&
          (prec == SEM_F64_DF || prec == SEM_MIXED || prec == SEM_MIXED_RR);
 }
 
@@ -879,7 +924,10 @@ int fp64_finish(sem_mesh* m, const OpCtx& cx, const Grid& gv, const WS& w, const
   const unsigned nb = nblocks(L);
   double* d = w.x64tmp;
   double* rd = w.d;
-  k_init<double, double><<<nb, kRT, 0, s>>>(w.r, d, rd, w.p, jac ? w.dinv : nullptr, w.part, gv);
+  if (m->precision == SEM_F64)
+    k_init<double, double, true><<<nb, kRT, 0, s>>>(w.r, d, rd, w.p, jac ? w.dinv : nullptr, w.part, gv);
+  else
+    k_init<double, double><<<nb, kRT, 0, s>>>(w.r, d, rd, w.p, jac ? w.dinv : nullptr, w.part, gv);
   k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, budget);
   SEM_CUDA(cudaGetLastError());
   SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
@@ -921,7 +969,14 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     SmallProb sp;
     SEM_CHECK(small_record(cx, w, m, o, b, x, maxiter, sp, s));
     SEM_CUDA(cudaMemcpyAsync(w.small, &sp, sizeof(sp), cudaMemcpyHostToDevice, s));
-    SEM_CHECK(launch_small_pcg(w.small, *cx.ops, cx.g.n, s));
+    // SEM_MIXED in one thread block when its FP32 working set fits the shared
+    // memory of an SM (the restarted form whose FP32 iterations the cluster
+    // kernel cannot make cheaper than FP64 ones)
+    const size_t tiny = tiny_smem_bytes(L, o->k != 0.0, jac);
+    if (prec == SEM_MIXED && tiny <= max_smem_optin())
+      SEM_CHECK(launch_tiny_pcg(w.small, sp, *cx.ops, tiny, s));
+    else
+      SEM_CHECK(launch_small_pcg(w.small, *cx.ops, cx.g.n, s));
     SEM_CUDA(cudaMemcpyAsync(&sp, w.small, sizeof(sp), cudaMemcpyDeviceToHost, s));
     SEM_CUDA(cudaStreamSynchronize(s));
     res.k = sp.iters;
@@ -946,7 +1001,10 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
       ++outer;
     }
   } else if (prec != SEM_MIXED && prec != SEM_MIXED_RR) {
-    k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
+    if (prec == SEM_F64)
+      k_init<double, double, true><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
+    else
+      k_init<double, double><<<nb, kRT, 0, s>>>(b, x, w.r, w.p, jac ? w.dinv : nullptr, w.part, gv);
     k_scal_init<<<1, kRT, 0, s>>>(w.part, (int)nb, w.sc, o->tol, maxiter);
     SEM_CUDA(cudaGetLastError());
     SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
@@ -1077,6 +1135,32 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
 }
 
 
+// pcg_core with the range guard of the pair and FP32 arithmetics: a solve
+// whose scalar coefficients lie outside the double-float window runs in native
+// FP64 from the start, and a double-float or mixed solve that ends in NaN or
+// Inf although b is finite (a value the pair or FP32 format cannot carry) is
+// solved again in native FP64 (operator, vectors and dots), on the chunked
+// path.  A NaN or Inf in b itself is reported as before.
+int pcg_guarded(const OpCtx& cx, const WS& w, sem_mesh* m, const sem_pcg_opts* o, const double* b, double* x,
+                sem_solve_info* info, cudaStream_t s) {
+  sem_pcg_opts o64 = *o;
+  o64.precision = SEM_F64;
+  o64.path = SEM_PATH_CHUNKED;
+  if (o->precision != SEM_F64 && !(df_window_ok(o->nu) && df_window_ok(o->k)))
+    return pcg_core(cx, w, m, &o64, b, x, info, s);
+  sem_solve_info mine;
+  std::memset(&mine, 0, sizeof(mine));
+  const int st = pcg_core(cx, w, m, o, b, x, &mine, s);
+  const double r0 = mine.res0_inf;
+  if (st == SEM_ERR_NAN && o->precision != SEM_F64 && r0 == r0 && r0 <= 1.7976931348623157e308) {
+    const int st64 = pcg_core(cx, w, m, &o64, b, x, info, s);
+    if (info) info->outer += mine.outer;
+    return st64;
+  }
+  if (info) *info = mine;
+  return st;
+}
+
 }  // namespace
 
 void free_graph_cache(sem_mesh* m) {
@@ -1164,7 +1248,7 @@ int sem_pcg(sem_mesh_t* m, const sem_pcg_opts* o, const double* b, double* x,
   SEM_CHECK(pcg_check(o, b, x));
   WS w;
   SEM_CHECK(get_ws(m, o->precision == SEM_MIXED || o->precision == SEM_MIXED_RR, w));
-  return pcg_core(ctx_of(m), w, m, o, b, x, info, (cudaStream_t)stream);
+  return pcg_guarded(ctx_of(m), w, m, o, b, x, info, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -1306,5 +1390,5 @@ extern "C" int sem_pcg_noalloc(int nr, int Ex, int Ey, int periodic_x, int perio
   cx.G22 = G22;
   cx.B = B;
   cx.variant = kDirect;
-  return pcg_core(cx, w, nullptr, o, b, x, info, s);
+  return pcg_guarded(cx, w, nullptr, o, b, x, info, s);
 }

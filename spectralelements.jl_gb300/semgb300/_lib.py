@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu", "sem_host.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_tiny.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu", "sem_host.cu"]
 
 
 class SemError(RuntimeError):
@@ -44,7 +44,8 @@ class NotConverged(SemError):
 
 SEM_OK, SEM_ERR_BAD_ARG, SEM_ERR_NOT_CONVERGED, SEM_ERR_NAN, SEM_ERR_TIMEOUT, SEM_ERR_CUDA, \
     SEM_ERR_UNSUPPORTED, SEM_ERR_NO_MEMORY = range(8)
-SEM_GS, SEM_MASK = 1, 2
+SEM_GS, SEM_MASK, SEM_NU_IN_G = 1, 2, 4
+SEM_HOST_DIRECT = -1  # sem_hlmz_host slabs: kernels read and write the host buffers in place
 SEM_F64, SEM_F64_DF, SEM_F32, SEM_MIXED, SEM_MIXED_RR = 0, 1, 2, 3, 4
 SEM_PRECOND_NONE, SEM_PRECOND_JACOBI = 0, 1
 SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL = 0, 1, 2

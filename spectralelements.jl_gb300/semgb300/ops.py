@@ -269,12 +269,6 @@ def gatherScatter(u, *args):
     return out
 
 
-def _host_matrix(A):
-    if isinstance(A, torch.Tensor):
-        return A.detach().cpu().numpy()
-    return np.asarray(A)
-
-
 def mask(u, M):
     """Mu = M .* u (src/mask.jl:10-18); an empty M returns a copy."""
     lib = _lib.load()

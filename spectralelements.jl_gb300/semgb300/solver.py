@@ -50,12 +50,13 @@ class HelmholtzOp:
 
     def apply_host(self, u_host, out=None, slabs=0):
         """opA on HOST buffers (``sem_hlmz_host``): u_host is a CPU float64
-        tensor in the column-major local layout (pinned memory lets the copies
-        overlap the kernels); the result goes to ``out`` (a CPU tensor of the
-        same layout, pinned if None) and is complete once the current stream
-        has synchronised.  Scalar nu only."""
-        if self.nu_field is not None:
-            raise NotImplementedError("apply_host takes a scalar nu")
+        tensor in the column-major local layout; the result goes to ``out`` (a
+        CPU tensor of the same layout, pinned if None) and is complete once the
+        current stream has synchronised.  ``slabs``: k >= 1 (0: 8) stages the
+        field in k slabs through the copy engines, overlapped with the
+        kernels; ``_lib.SEM_HOST_DIRECT`` has the kernels read and write the
+        host buffers in place over the CPU-GPU link.  A ``nu_field`` (a device
+        field) is folded into G as in ``__call__``."""
         lib = _lib.load()
         msh = self.msh
         nx, ny = msh.shape
@@ -67,7 +68,11 @@ class HelmholtzOp:
         elif out.device.type != "cpu" or out.dtype != torch.float64 or out.stride() != (1, nx):
             raise ValueError("out must be a CPU float64 tensor of the local shape, column-major")
         flags = _lib.SEM_GS | (_lib.SEM_MASK if msh.bc else 0)
-        _lib.check(lib.sem_hlmz_host(msh.handle, None, self.nu, self.k, u_host.data_ptr(), out.data_ptr(),
+        nu_ptr = None
+        if self.nu_field is not None:
+            flags |= _lib.SEM_NU_IN_G
+            nu_ptr = self.nu_field.data_ptr()
+        _lib.check(lib.sem_hlmz_host(msh.handle, nu_ptr, self.nu, self.k, u_host.data_ptr(), out.data_ptr(),
                                      flags, int(slabs), stream_ptr()))
         return out
 
