@@ -171,6 +171,7 @@ int sem_mesh_destroy(sem_mesh_t* m) {
   if (m->Gdf) cudaFree(m->Gdf);
   if (m->fix_ctr) cudaFree(m->fix_ctr);
   if (m->kB) cudaFree(m->kB);
+  if (m->rflag) cudaFree(m->rflag);
   free_graph_cache(m);
   free_host_pipe(m);
   if (m->ws) cudaFree(m->ws);
@@ -343,6 +344,7 @@ static int fused(sem_mesh_t* m, const double* u, double* out, unsigned mode, con
   c.Gdf = m->Gdf;
   c.ctr = m->fix_ctr;
   SEM_CHECK(use_kB(m, c, (cudaStream_t)stream));
+  SEM_CHECK(arm_range_guard(m, c));
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 
@@ -389,6 +391,7 @@ int sem_varcoef(sem_mesh_t* m, const double* nu_field, double k, const double* u
   c.Gdf = m->Gdf;
   c.ctr = m->fix_ctr;
   SEM_CHECK(use_kB(m, c, (cudaStream_t)stream));
+  SEM_CHECK(arm_range_guard(m, c));
   return launch_apply(m->g, m->ops, c, (cudaStream_t)stream);
 }
 
@@ -465,7 +468,8 @@ int sem_lapl_geom(int nr, int ns, int Ex, int Ey, int periodic_x, int periodic_y
   c.nu_s = 1.0;
   c.mode = mode;
   c.precision = precision;
-  const int st = launch_apply(g, ops, c, (cudaStream_t)stream);
+  int st = arm_range_guard(nullptr, c);
+  if (st == SEM_OK) st = launch_apply(g, ops, c, (cudaStream_t)stream);
   free_operator_set(ops);
   return st;
 }

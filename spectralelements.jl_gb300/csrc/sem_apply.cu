@@ -1,5 +1,6 @@
 // Host side of the fused operator kernels: coefficient sets and launches.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -122,7 +123,8 @@ int num_sms() {
 }
 
 int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
-                     int TY, cudaStream_t s, long long key_lo, long long key_hi) {
+                     int TY, cudaStream_t s, long long key_lo, long long key_hi, const unsigned* gate,
+                     unsigned gate_tag) {
   if (!(mode & M_GS)) return SEM_OK;
   if (g.NX >= (1LL << 31) || g.NY >= (1LL << 31))
     return set_error(SEM_ERR_UNSUPPORTED, "local dimensions must be below 2^31");
@@ -138,6 +140,8 @@ int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, con
   f.skip = skip;
   f.key_lo = key_lo;
   f.key_hi = key_hi;
+  f.gate = gate;
+  f.gate_tag = gate_tag;
   const bool perx = (mode & M_PERX) != 0, pery = (mode & M_PERY) != 0;
   f.nxi = (g.Ex - 1) / f.TX + (perx ? 1 : 0);
   f.nyi = (g.Ey - 1) / f.TY + (pery ? 1 : 0);
@@ -176,8 +180,29 @@ static ApplyCall scalar_window(const ApplyCall& c) {
   return r;
 }
 
+// The native FP64 re-run of a guarded double-float call: kernel variant 0 and
+// its fixup, launched after the double-float kernels and gated on the call's
+// flag word (every CTA returns at once unless the word holds the call's tag).
+static int launch_gated_f64(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s,
+                            long long key_lo, long long key_hi) {
+  ApplyCall r = c;
+  r.precision = SEM_F64;
+  r.variant = 0;
+  r.rflag = nullptr;
+  r.gate = c.rflag;
+  r.gate_tag = c.rtag;
+  r.cg_dpart = nullptr;
+  r.cg_p = nullptr;
+  r.pdl = 1;
+  int tile[2] = {0, 0};
+  SEM_CHECK(g.n >= 10 ? launch_apply_f64_hi(g, ops, r, s, tile) : launch_apply_f64_lo(g, ops, r, s, tile));
+  if (tile[0] == 0) return SEM_OK;
+  return launch_dss_fixup(g, r.out, r.mode, SEM_F64, r.skip, tile[0], tile[1], s, key_lo, key_hi, c.rflag, c.rtag);
+}
+
 int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c0, cudaStream_t s) {
-  const ApplyCall c = scalar_window(c0);
+  ApplyCall c = scalar_window(c0);
+  if (c.precision != SEM_F64_DF) c.rflag = nullptr;
   int st;
   int tile[2] = {0, 0};
   const bool hi = g.n >= 10;
@@ -190,13 +215,16 @@ int launch_apply(const Grid& g, const OperatorSet* ops, const ApplyCall& c0, cud
   else
     return set_error(SEM_ERR_BAD_ARG, "unknown precision %d", c.precision);
   if (st != SEM_OK) return st;
-  if (tile[0] == 0) return SEM_OK;  // completed inside the kernel
-  return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s);
+  if (tile[0] != 0)  // otherwise completed inside the kernel
+    SEM_CHECK(launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s));
+  if (c.rflag) SEM_CHECK(launch_gated_f64(g, ops, c, s, 0, 1LL << 62));
+  return SEM_OK;
 }
 
 int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c0, long long key_lo,
                         long long key_hi, cudaStream_t s) {
-  const ApplyCall c = scalar_window(c0);
+  ApplyCall c = scalar_window(c0);
+  if (c.precision != SEM_F64_DF) c.rflag = nullptr;
   if (c.tyn <= 0) return set_error(SEM_ERR_BAD_ARG, "empty tile-row window");
   int st;
   int tile[2] = {0, 0};
@@ -208,7 +236,51 @@ int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& 
   else
     return set_error(SEM_ERR_BAD_ARG, "tile-row windows serve SEM_F64 and SEM_F64_DF");
   if (st != SEM_OK) return st;
-  return launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s, key_lo, key_hi);
+  SEM_CHECK(launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s, key_lo, key_hi));
+  if (c.rflag) SEM_CHECK(launch_gated_f64(g, ops, c, s, key_lo, key_hi));
+  return SEM_OK;
+}
+
+// the device's own guard word, for calls without a mesh handle (one per
+// device, made on first use)
+static unsigned* device_guard_word() {
+  static std::mutex mu;
+  static unsigned* words[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!words[dev]) {
+    unsigned* p = nullptr;
+    if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, sizeof(unsigned)) != cudaSuccess) {
+      cudaFree(p);
+      return nullptr;
+    }
+    words[dev] = p;
+  }
+  return words[dev];
+}
+
+int arm_range_guard(sem_mesh* m, ApplyCall& c) {
+  if (c.precision != SEM_F64_DF) return SEM_OK;
+  static std::atomic<unsigned> dev_tag{0};
+  if (m) {
+    if (!m->rflag) {
+      SEM_CUDA(cudaMalloc(&m->rflag, sizeof(unsigned)));
+      SEM_CUDA(cudaMemset(m->rflag, 0, sizeof(unsigned)));
+    }
+    if (++m->rtag == 0) ++m->rtag;  // tags are never 0 (the word's initial value)
+    c.rflag = m->rflag;
+    c.rtag = m->rtag;
+    return SEM_OK;
+  }
+  unsigned* w = device_guard_word();
+  if (!w) return set_error(SEM_ERR_CUDA, "cannot make the range-guard word");
+  unsigned t = ++dev_tag;
+  if (t == 0) t = ++dev_tag;
+  c.rflag = w;
+  c.rtag = t;
+  return SEM_OK;
 }
 
 void tile_shape_of(int n, int* tx, int* ty) { tile_shape(n, tx, ty); }

@@ -49,9 +49,10 @@ struct Apply2Args {
   const io* nu;
   v nu_s;
   v k_s;
-  // FP64 geometry and mass (double-float policy: the FP64 recomputation of a
-  // tile whose double-float results left the pair format's range)
-  const double *G11d, *G12d, *G22d, *Bd;
+  // range guard (double-float policy): *rflag = rtag when an input row or a
+  // result leaves the pair format's range
+  unsigned* rflag;
+  unsigned rtag;
   int Ex, Ey;
   long long NX;
   unsigned mode;
@@ -138,6 +139,8 @@ __device__ __forceinline__ void finish_tile_interfaces(IO* out, int n, int Ex, i
   f.key_lo = 0;
   f.key_hi = 1LL << 62;
   f.nxi = f.nyi = 0;
+  f.gate = nullptr;
+  f.gate_tag = 0;
   auto none = [](long long, long long, IO) {};
   for (int k = 0; k < 8; ++k) {
     const int kind = s_last[k] - 1;
@@ -205,6 +208,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   V* s0 = S0 + elem * ES;
   V* s1 = S1 + elem * ES;
   const int rofs = elem * ES + lane;
+  RowScale rs;  // range guard of the double-float policy
 
   if (STAGE) {
     if (valid && stiff) {
@@ -236,16 +240,26 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
         IO pn = (IO)0;
         if (valid) {
           const long long gi = base + (long long)j * NX;
-          pn = cg_direction(a.r[gi], jac ? a.dinv[gi] : (IO)1, beta, a.p[gi], jac);
+          if constexpr (P::kPrecision == SEM_F64)  // native FP64 direction (the whole double range)
+            pn = __fma_rn(beta, a.p[gi], jac ? __dmul_rn(a.r[gi], a.dinv[gi]) : a.r[gi]);
+          else
+            pn = cg_direction(a.r[gi], jac ? a.dinv[gi] : (IO)1, beta, a.p[gi], jac);
           a.p[gi] = pn;
         }
+        if constexpr (P::kPrecision == SEM_F64_DF) rs.see(pn);
         u[j] = P::cvt(pn);
         s0[j * SP + lane] = u[j];
       }
     } else {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
+        if constexpr (P::kPrecision == SEM_F64_DF) {
+          const double x = valid ? __ldg(a.u + base + (long long)j * NX) : 0.0;
+          rs.see(x);
+          u[j] = P::cvt(x);
+        } else {
+          u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
+        }
         s0[j * SP + lane] = u[j];
       }
     }
@@ -324,13 +338,12 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
     }
   }
 
-  // a NaN or Inf double-float result: an input or intermediate outside the
-  // pair format's range; the tile is recomputed in native FP64 after its
-  // stores and before its cross-tile completion (sem_tile_f64.cuh)
-  bool bad = false;
   if constexpr (P::kPrecision == SEM_F64_DF) {
+    // range guard: a row of tiny values or a NaN/Inf result flags the call
+    bool bad = rs.tiny();
 #pragma unroll
     for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
+    if (bad && a.rflag) *a.rflag = a.rtag;
   }
   if constexpr (CG)
     store_dot_part<P, N>([&](int j) { return s0[j * SP + lane]; }, [&](int j) { return res[j]; }, a.dpart,
@@ -338,13 +351,6 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
   tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
                                ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
-  if constexpr (P::kPrecision == SEM_F64_DF) {
-    if (__syncthreads_or(bad))
-      tile_f64_redo<N, TX, TY>(CG ? a.p : a.u, a.out, NX, a.Ex, a.Ey, blockIdx.x * TX, (blockIdx.y + a.ty0) * TY,
-                               mode, a.G11d, a.G12d, a.G22d, a.Bd, a.nu, df_exact(a.nu_s), df_exact(a.k_s), &a.Dr,
-                               &a.Drt, &a.Ds, &a.Dst, reinterpret_cast<double*>(S0), reinterpret_cast<double*>(S1),
-                               CG ? a.dpart : nullptr, blockIdx.y * gridDim.x + blockIdx.x);
-  }
   if constexpr (FUSE) {
     if (mode & M_GS)
       finish_tile_interfaces<IO, TX, TY>(a.out, N, a.Ex, a.Ey, NX, mode, a.ctr, a.tiles_x, a.tiles_y,

@@ -125,12 +125,19 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
 
     // ---- A: row `lane` of u; y-direction derivative
     V res[N];
+    RowScale rs;  // range guard of the double-float policy
     cp_async_wait_group<2>();  // u(tile); G(tile), B(tile) may be in flight
     {
       V u[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        u[j] = valid ? P::cvt(RU[j * T + t]) : P::zero();
+        if constexpr (P::kPrecision == SEM_F64_DF) {
+          const double x = valid ? RU[j * T + t] : 0.0;
+          rs.see(x);
+          u[j] = P::cvt(x);
+        } else {
+          u[j] = valid ? P::cvt(RU[j * T + t]) : P::zero();
+        }
         s0[j * SP + lane] = u[j];
       }
       fetch_u(next);
@@ -214,23 +221,15 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
     }
     fetch_b(next);
 
-    bool bad = false;
     if constexpr (P::kPrecision == SEM_F64_DF) {
+      // range guard: a row of tiny values or a NaN/Inf result flags the call
+      bool bad = rs.tiny();
 #pragma unroll
       for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
+      if (bad && a.rflag) *a.rflag = a.rtag;
     }
     tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
                                  ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
-    if constexpr (P::kPrecision == SEM_F64_DF) {
-      // a NaN or Inf double-float result: the tile is recomputed in native FP64
-      if (__syncthreads_or(bad)) {
-        const int ty = tile / tiles_x;
-        tile_f64_redo<N, TX, TY>(a.u, a.out, NX, a.Ex, a.Ey, (tile - ty * tiles_x) * TX, ty * TY, mode, a.G11d,
-                                 a.G12d, a.G22d, a.Bd, a.nu, df_exact(a.nu_s), df_exact(a.k_s), &a.Dr, &a.Drt,
-                                 &a.Ds, &a.Dst, reinterpret_cast<double*>(S0), reinterpret_cast<double*>(S1), nullptr,
-                                 0);
-      }
-    }
     __syncthreads();  // the next tile overwrites s0 and s1
   }
   cp_async_wait_all();

@@ -48,6 +48,13 @@ struct ApplyArgs {
   int slot_g, slot_b, slot_nu;  // staged-variant shared-memory slots (-1: not staged)
   int ty0;                      // first element-tile row of the launch (a window of the grid)
   df* dpart;                    // DOT launches: each CTA's part of u . (A u), unassembled
+  // range guard (double-float policy): *rflag = rtag when an input row or a
+  // result leaves the pair format's range; a gated launch (gate non-NULL)
+  // does nothing unless *gate == gate_tag
+  unsigned* rflag;
+  unsigned rtag;
+  const unsigned* gate;
+  unsigned gate_tag;
   EOCoef<N, v> Dr, Drt, Ds, Dst;
 };
 
@@ -205,12 +212,6 @@ __device__ __forceinline__ void tile_dss_store(const typename P::v (&res)[N], ty
   }
 }
 
-}  // namespace sem
-
-#include "sem_tile_f64.cuh"
-
-namespace sem {
-
 // DOT: the launch is a CG iteration's operator application on the direction
 // u = p and every CTA also writes its part of p . A p, summed over the
 // unassembled local products (equal to the mult-weighted dot of the assembled
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   pdl_trigger();  // the next kernel (the cross-tile fixup) may be scheduled now
   pdl_wait();     // a no-op unless this launch is a programmatic dependent
   if (a.skip && *a.skip) return;
+  if (a.gate && *a.gate != a.gate_tag) return;  // gated re-run not needed
   const int t = threadIdx.x;
   const int elem = t / N;
   const int lane = t - elem * N;
@@ -246,6 +248,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   V* s1 = S1 + elem * ES;
   V* s2 = S2 + elem * ES;
   const int rofs = elem * ES + lane;  // this thread's row inside a staged slot (+ j*SP)
+  RowScale rs;  // range guard of the double-float policy
 
   // ---- staged variant: issue every later global read of this row now
   if (STAGE) {
@@ -273,7 +276,15 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   // ---- A: row `lane` of u; y-direction derivative
   V u[N];
 #pragma unroll
-  for (int j = 0; j < N; ++j) u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
+  for (int j = 0; j < N; ++j) {
+    if constexpr (P::kPrecision == SEM_F64_DF) {
+      const double x = valid ? __ldg(a.u + base + (long long)j * NX) : 0.0;
+      rs.see(x);
+      u[j] = P::cvt(x);
+    } else {
+      u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
+    }
+  }
 
   V res[N];
   if (stiff) {
@@ -351,13 +362,12 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
       res[j] = P::fin(P::fma(kb, u[j], res[j]));
     }
   }
-  // a NaN or Inf double-float result: an input or intermediate outside the
-  // pair format's range; the tile is recomputed in native FP64 after its
-  // stores (sem_tile_f64.cuh)
-  bool bad = false;
   if constexpr (P::kPrecision == SEM_F64_DF) {
+    // range guard: a row of tiny values or a NaN/Inf result flags the call
+    bool bad = rs.tiny();
 #pragma unroll
     for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
+    if (bad && a.rflag) *a.rflag = a.rtag;
   }
   if constexpr (DOT)
     store_dot_part<P, N>([&](int j) { return u[j]; }, [&](int j) { return res[j]; }, a.dpart,
@@ -366,13 +376,6 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
   tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S2), elem, lane,
                                ex, ey, valid, base, a.Ex, a.Ey, NX, mode, a.out);
-  if constexpr (P::kPrecision == SEM_F64_DF) {
-    if (__syncthreads_or(bad))
-      tile_f64_redo<N, TX, TY>(a.u, a.out, NX, a.Ex, a.Ey, blockIdx.x * TX, (blockIdx.y + a.ty0) * TY, mode, a.G11,
-                               a.G12, a.G22, a.B, a.nu, df_exact(a.nu_s), df_exact(a.k_s), &a.Dr, &a.Drt, &a.Ds,
-                               &a.Dst, reinterpret_cast<double*>(S2), reinterpret_cast<double*>(S1),
-                               DOT ? a.dpart : nullptr, blockIdx.y * gridDim.x + blockIdx.x);
-  }
 }
 
 // Finishes QQ' (and the mask) at the points whose copies sit in different
@@ -392,6 +395,8 @@ struct FixArgs {
   // only the interface points whose highest copy column lies in [key_lo, key_hi)
   // (a pipeline finishes the columns of one slab of tile rows at a time)
   long long key_lo, key_hi;
+  const unsigned* gate;  // gated re-run: nothing to do unless *gate == gate_tag
+  unsigned gate_tag;
 };
 
 __device__ __forceinline__ bool fix_key_in(long long key, long long lo, long long hi) {
@@ -539,6 +544,7 @@ template <class IO>
 __global__ void k_dss_fixup(IO* __restrict__ out, const FixArgs f) {
   pdl_wait();  // launched as a programmatic dependent of the operator kernel
   if (f.skip && *f.skip) return;
+  if (f.gate && *f.gate != f.gate_tag) return;
   const long long nI = fix_rows(f);
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;

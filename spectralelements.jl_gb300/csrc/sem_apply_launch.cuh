@@ -93,6 +93,10 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   a.NX = g.NX;
   a.mode = c.mode | (fold ? M_NUFOLD : 0u);
   a.skip = c.skip;
+  a.rflag = c.rflag;
+  a.rtag = c.rtag;
+  a.gate = c.gate;
+  a.gate_tag = c.gate_tag;
   int nslot = 0;
   a.slot_g = a.slot_b = a.slot_nu = -1;
   if (STAGE) {
@@ -145,12 +149,8 @@ static void fill_args2(Apply2Args<P, N>& a, const Grid& g, const OperatorSet* op
   const bool fold = fold_nu(c.mode);
   a.nu_s = P::from_double(fold ? 1.0 : c.nu_s);
   a.k_s = P::from_double(c.k_s);
-  if (P::kPrecision == SEM_F64_DF) {
-    a.G11d = static_cast<const double*>(c.G11);
-    a.G12d = static_cast<const double*>(c.G12);
-    a.G22d = static_cast<const double*>(c.G22);
-    a.Bd = static_cast<const double*>(c.B);
-  }
+  a.rflag = c.rflag;
+  a.rtag = c.rtag;
   a.Ex = g.Ex;
   a.Ey = g.Ey;
   a.NX = g.NX;

@@ -99,32 +99,36 @@ __device__ __forceinline__ df d2df(double x) {
   return {h, l};
 }
 
-// Operator inputs of the double-float kernels: d2df inside the window
-// [2^-70, 2^90) of magnitudes, where every product and sum of an operator
-// apply stays in the normal FP32 range with its error terms; a nonzero value
-// outside it (and Inf) becomes NaN.  A NaN in a result of the double-float
-// arithmetic therefore marks an input or an intermediate the pair format
-// cannot carry, and the kernels recompute that element tile in native FP64;
-// zeros pass unchanged.
-constexpr unsigned kDfExpLo = 1023u - 70u;   // biased double exponent of 2^-70
-constexpr unsigned kDfExpHi = 1023u + 90u;   // first biased exponent outside the window
+// Range guard of the double-float operator.  The pair format holds about 47
+// significand bits in the FP32 exponent range.  Operator inputs are split by
+// d2df_op, which turns a magnitude at or above 2^90 (and Inf) into NaN, so
+// that intermediates never overflow silently; smaller values split as d2df
+// does (magnitudes below 2^-103 keep fewer bits, below 2^-126 flush to zero).
+// A result stays accurate as long as the values of a line are not all tiny:
+// a tiny value next to values of ordinary size changes the result by a
+// negligible amount.  RowScale watches that for the rows a thread loads; a row
+// whose nonzero values all lie below 2^-60, or a NaN/Inf result, flags the
+// call, and the host side re-runs the whole call in native FP64.
+constexpr unsigned kDfExpHi = 1023u + 90u;   // first biased exponent that is poisoned
+constexpr unsigned kDfExpTiny = 1023u - 60u; // a row whose largest exponent is below this is tiny
 __device__ __forceinline__ df d2df_op(double x) {
-  const unsigned lo = (unsigned)__double2loint(x);
-  const unsigned hi = (unsigned)__double2hiint(x);
-  const unsigned ed = (hi >> 20) & 0x7ffu;
-  const unsigned sg = hi & 0x80000000u;
-  const unsigned hb = (__funnelshift_l(lo, hi, 3) + 0x40000000u) | sg;  // the split of d2df
-  const unsigned pb = (hb & 0xff800000u) - 0x0B800000u;
-  const unsigned fb = pb | ((lo >> 6) & 0x007fffffu);
-  float h = __uint_as_float(hb);
-  float l = __fsub_rn(__uint_as_float(fb), __uint_as_float(pb));
-  if (ed - kDfExpLo >= kDfExpHi - kDfExpLo) {  // rare: zero, or outside the window
-    const bool zero = ed == 0u && ((hi & 0x000fffffu) | lo) == 0u;
-    h = __uint_as_float(zero ? sg : 0x7fc00000u);
-    l = 0.0f;
-  }
-  return {h, l};
+  const unsigned ed = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+  df v = d2df(x);
+  if (ed >= kDfExpHi) v = {__uint_as_float(0x7fc00000u), 0.0f};
+  return v;
 }
+
+struct RowScale {
+  unsigned emax = 0u;  // largest biased exponent seen among nonzero values (subnormals count as 1)
+  __device__ __forceinline__ void see(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    unsigned e = (hi >> 20) & 0x7ffu;
+    if (e == 0u && ((hi & 0x000fffffu) | lo)) e = 1u;
+    emax = e > emax ? e : emax;
+  }
+  __device__ __forceinline__ bool tiny() const { return emax != 0u && emax < kDfExpTiny; }
+};
 
 // a double-float value whose high part is Inf or NaN
 __device__ __forceinline__ bool df_bad(df a) { return (__float_as_uint(a.h) & 0x7f800000u) == 0x7f800000u; }

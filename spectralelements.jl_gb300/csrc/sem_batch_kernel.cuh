@@ -375,6 +375,8 @@ __device__ __noinline__ void bfixup(const BProb& pr, int n, IO* __restrict__ Ap,
   f.skip = nullptr;
   f.key_lo = 0;
   f.key_hi = 1LL << 62;
+  f.gate = nullptr;
+  f.gate_tag = 0;
   const bool perx = (pr.topo & M_PERX) != 0, pery = (pr.topo & M_PERY) != 0;
   f.nxi = (pr.Ex - 1) / TX + (perx ? 1 : 0);
   f.nyi = (pr.Ey - 1) / TY + (pery ? 1 : 0);

@@ -147,6 +147,7 @@ extern "C" int sem_hlmz_host(sem_mesh_t* m, const double* nu_field, double nu, d
   c.variant = m->variant[m->precision];
   c.Gdf = m->Gdf;
   SEM_CHECK(use_kB(m, c, s));
+  SEM_CHECK(arm_range_guard(m, c));
 
   // direct access: the operator kernels read u_host and write out_host over
   // the CPU-GPU link while they compute (no staging buffers, no copy engines)

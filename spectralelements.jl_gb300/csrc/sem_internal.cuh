@@ -194,6 +194,8 @@ struct sem_mesh {
   void* host_pipe;         // streams, events and buffers of sem_hlmz_host (sem_host.cu), or NULL
   double* kB;              // k .* B for the native FP64 operator (lazily created), and its k
   double kB_k;
+  unsigned* rflag;         // range-guard word of the double-float calls (lazily created)
+  unsigned rtag;           // tag of the latest guarded call
 };
 
 namespace sem {
@@ -236,7 +238,18 @@ struct ApplyCall {
   // a window of element-tile rows [ty0, ty0 + tyn) instead of the whole grid
   // (tyn = 0: all); variants 0-3 only, no CG fusion, the fixup left to the caller
   int ty0, tyn;
+  // range guard of a double-float call (rflag non-NULL): the kernels set
+  // *rflag = rtag when a value leaves the pair format's range, and
+  // launch_apply follows them with a native FP64 re-run of the whole call,
+  // gated on that word (gate, gate_tag: the gated launch itself)
+  unsigned* rflag;
+  unsigned rtag;
+  const unsigned* gate;
+  unsigned gate_tag;
 };
+// arm the range guard of a double-float call on mesh m (the mesh's flag word)
+// or, without a mesh, on the device's own word
+int arm_range_guard(sem_mesh* m, ApplyCall& c);
 
 // launch kern<<<grid, block, 0, s>>>(args...) as a programmatic dependent of
 // the previous kernel on s (the kernel must call griddepcontrol.wait before it
@@ -320,7 +333,8 @@ void free_graph_cache(sem_mesh* m);    // sem_pcg.cu
 void free_host_pipe(sem_mesh* m);      // sem_host.cu
 void tile_shape_of(int n, int* tx, int* ty);  // element tile of the fused kernels (sem_apply.cu)
 int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
-                     int TY, cudaStream_t s, long long key_lo = 0, long long key_hi = 1LL << 62);
+                     int TY, cudaStream_t s, long long key_lo = 0, long long key_hi = 1LL << 62,
+                     const unsigned* gate = nullptr, unsigned gate_tag = 0);
 // the operator kernel on a window of tile rows (ApplyCall::ty0, tyn) and the
 // fixup of the interface points whose highest copy column is in [key_lo, key_hi)
 int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c, long long key_lo,

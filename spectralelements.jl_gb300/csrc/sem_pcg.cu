@@ -240,7 +240,7 @@ __global__ void k_scal_replace(const double* part, int np, Scalars* sc, double t
   }
 }
 
-template <class T>
+template <class T, bool NAT = false>
 __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ p,
                        const Scalars* sc, long long L) {
   pdl_trigger();
@@ -249,8 +249,12 @@ __global__ void k_pdir(const T* __restrict__ r, const T* __restrict__ dinv, T* _
   const T beta = (T)sc->beta;
   const bool jac = dinv != nullptr;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L;
-       i += (long long)gridDim.x * blockDim.x)
-    p[i] = cg_direction(r[i], jac ? dinv[i] : (T)1, beta, p[i], jac);
+       i += (long long)gridDim.x * blockDim.x) {
+    if constexpr (NAT)  // native FP64 (the whole double range)
+      p[i] = __fma_rn((double)beta, (double)p[i], jac ? __dmul_rn((double)r[i], (double)dinv[i]) : (double)r[i]);
+    else
+      p[i] = cg_direction(r[i], jac ? dinv[i] : (T)1, beta, p[i], jac);
+  }
 }
 
 template <class T, bool NAT = false>
@@ -598,11 +602,17 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
       SEM_CHECK(alpha_parts());
     } else if (cp.cg_dpart) {  // direction pass, then the operator with the p.Ap parts
-      SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
+      if (nat)
+        SEM_CHECK(launch_pdl(k_pdir<T, true>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
+      else
+        SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
       SEM_CHECK(alpha_parts());
     } else {
-      SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
+      if (nat)
+        SEM_CHECK(launch_pdl(k_pdir<T, true>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
+      else
+        SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
       if (nat)
         SEM_CHECK(launch_pdl(k_dot_pap<T, true>, nb, kRT, s, (const T*)p, (const T*)Ap, w.part,

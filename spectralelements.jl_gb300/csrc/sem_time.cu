@@ -119,6 +119,7 @@ int lapl_gs(sem_mesh* m, const double* u, double* out, cudaStream_t s) {
   c.variant = m->variant[m->precision];
   c.Gdf = m->Gdf;
   c.ctr = m->fix_ctr;
+  SEM_CHECK(arm_range_guard(m, c));
   return launch_apply(m->g, m->ops, c, s);
 }
 

@@ -9,7 +9,6 @@
 // inverse diagonal and every FP32 vector of the inner CG in shared memory, and
 // an iteration costs block barriers only:
 //
-//   p   points: p = z + beta p (z = dinv .* r)
 //   P1  lines: row line -> us = Ds u, column line -> ur = Dr u (even-odd form,
 //       one thread per line; the local layout's rows are coalesced across a
 //       warp and its columns are stride-n, both free of bank conflicts)
@@ -18,12 +17,17 @@
 //       block-wide p . A p over the unassembled products (equal to the
 //       mult-weighted dot of the assembled A p for a continuous masked p)
 //   P4  points: A p = QQ'(res) masked (x pairs first, the order of every other
-//       kernel), x += alpha p, r -= alpha A p, r . z . mult and max|r|
+//       kernel), x += alpha p, r -= alpha A p, r . z . mult and max|r|, and p
+//       stored; the direction p = z + beta p_old is formed where P1, P3 and
+//       P4 read it, so it needs no pass of its own
+// Each phase ends at one block barrier (a reduction costs one barrier too), so
+// an iteration holds four.
 //
 // The FP64 defect correction runs in the same launch: x (FP64, global) +=
 // x32, then r = b - A x with the double-float operator (the same phases with
 // double-float line buffers in the shared memory the FP32 vectors free),
-// max|r|, and the next inner solve.  Results go to the SmallProb record as the
+// max|r|, and the next inner solve.  Indices are 32-bit (a 64-bit division per
+// point cost more than the arithmetic).  Results go to the SmallProb record as the
 // cluster solver writes them; the host finishes a solve whose sweeps ran out
 // with the FP64 CG (sem_pcg.cu).
 //
@@ -36,7 +40,7 @@
 
 namespace sem {
 
-constexpr int kTinyMaxThreads = 1024;
+constexpr int kTinyMaxThreads = 512;  // 128 registers a thread; an 8x8-element mesh of order 8 has 512 lines
 
 template <int N>
 struct TinyArgs {
@@ -45,10 +49,22 @@ struct TinyArgs {
   EOCoef<N, df> Dr2, Drt2, Ds2, Dst2;  // double-float FP64 residual
 };
 
+// Block-wide sum and maximum with one barrier: every warp folds its lanes
+// (fixed shuffle tree), lane 0 stores the warp's pair in a slot of `red`, and
+// after the barrier every thread folds the warps' pairs in warp order, so all
+// threads hold the same result.  Consecutive calls alternate between the two
+// slots: a slot is written again only after a later call's barrier, when every
+// thread has read it.
+struct TinyRed {
+  double s[2][32];
+  unsigned long long m[2][32];
+};
+
 // shared-memory layout in 4-byte words: the persistent block (G11, G12, G22,
-// [B], [dinv]) then the work block (x32, r32, p32, line buffers A and B)
+// [B], [dinv]), the work block (x32, r32, p32, line buffers A and B), then
+// the reduction slots
 struct TinyLayout {
-  long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, words;
+  long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, red, words;
 };
 
 __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool jac) {
@@ -65,43 +81,34 @@ __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool j
   t.p32 = o; o += L;
   t.la = o; o += L;
   t.lb = o; o += L;
+  o = (o + 1) & ~1LL;
+  t.red = o; o += (long long)(sizeof(TinyRed) / 4);
   t.words = o;
   return t;
 }
 
-// fixed-order block sums: warp trees, then the warps in order; the result is
-// broadcast to every thread
-__device__ __forceinline__ double tiny_sum(double v, double* red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = red[0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) s += red[i];
-    red[32] = s;
-  }
-  __syncthreads();
-  return red[32];
-}
-
-__device__ __forceinline__ unsigned long long tiny_max(unsigned long long v, unsigned long long* red) {
+__device__ __forceinline__ void tiny_reduce(double& v, unsigned long long& mx, TinyRed& red, int& slot) {
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long y = __shfl_down_sync(0xffffffffu, v, o);
-    v = y > v ? y : v;
+    v += __shfl_down_sync(0xffffffffu, v, o);
+    const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = y > mx ? y : mx;
   }
   const int w = threadIdx.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long m = red[0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) m = red[i] > m ? red[i] : m;
-    red[32] = m;
+  if ((threadIdx.x & 31) == 0) {
+    red.s[slot][w] = v;
+    red.m[slot][w] = mx;
   }
   __syncthreads();
-  return red[32];
+  double s = red.s[slot][0];
+  unsigned long long m = red.m[slot][0];
+  const int nw = (int)(blockDim.x >> 5);
+  for (int i = 1; i < nw; ++i) {
+    s += red.s[slot][i];
+    m = red.m[slot][i] > m ? red.m[slot][i] : m;
+  }
+  v = s;
+  mx = m;
+  slot ^= 1;
 }
 
 // magnitude bits as the bits of the double of the same value (NaN orders above
@@ -114,40 +121,39 @@ __device__ __forceinline__ unsigned long long tiny_abs_bits(double v) {
 }
 
 // The operator, unassembled and unmasked, res = nu (D'G D u) + k B u, on every
-// line of the mesh.  U: the input field (shared or global); A, Bf: two line
-// buffers of L entries (shared); G11..Bm: the metric terms and mass (shared
-// FP32 or global pre-split pairs; Bm NULL without a mass term).  The result
-// is left in A; acc receives this thread's part of u . res.
-template <class P, int N, class GT>
-__device__ __forceinline__ void tiny_apply(const SmallProb& pr, const typename P::io* U, typename P::v* A,
-                                           typename P::v* Bf, const GT* G11, const GT* G12, const GT* G22,
-                                           const GT* Bm, typename P::v nu, typename P::v kk,
-                                           const EOCoef<N, typename P::v>& Dr, const EOCoef<N, typename P::v>& Drt,
-                                           const EOCoef<N, typename P::v>& Ds, const EOCoef<N, typename P::v>& Dst,
-                                           double& acc) {
+// line of the mesh.  ufun(q) gives the input at local point q (shared or
+// global memory, or formed on the fly); A, Bf: two line buffers of L entries
+// (shared); G11..Bm: the metric terms and mass (shared FP32 or global
+// pre-split pairs; Bm NULL without a mass term).  The result is left in A;
+// acc receives this thread's part of u . res.  32-bit indices: a mesh on this
+// path has at most a few thousand points.
+template <class P, int N, class GT, class UF>
+__device__ __forceinline__ void tiny_apply(const SmallProb& pr, UF&& ufun, typename P::v* A, typename P::v* Bf,
+                                           const GT* G11, const GT* G12, const GT* G22, const GT* Bm,
+                                           typename P::v nu, typename P::v kk, const EOCoef<N, typename P::v>& Dr,
+                                           const EOCoef<N, typename P::v>& Drt, const EOCoef<N, typename P::v>& Ds,
+                                           const EOCoef<N, typename P::v>& Dst, double& acc) {
   typedef typename P::v V;
-  const long long NX = pr.NX;
-  const int nl = (int)(NX * pr.Ey);  // lines per direction
+  const int NX = (int)pr.NX;
+  const int nl = NX * pr.Ey;  // lines per direction
   const int Ex = pr.Ex;
   // P1: us on the row lines -> Bf, ur on the column lines -> A
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
     {
-      const long long r = l % NX;
-      const long long c0 = (long long)(l / NX) * N;
+      const int r = l % NX;
+      const int q0 = r + (l / NX) * N * NX;
       V x[N], y[N];
 #pragma unroll
-      for (int j = 0; j < N; ++j) x[j] = P::cvt(U[r + (c0 + j) * NX]);
+      for (int j = 0; j < N; ++j) x[j] = ufun(q0 + j * NX);
       eo_apply<P, N>(Ds, x, y);
 #pragma unroll
-      for (int j = 0; j < N; ++j) Bf[r + (c0 + j) * NX] = y[j];
+      for (int j = 0; j < N; ++j) Bf[q0 + j * NX] = y[j];
     }
     {
-      const long long ex = l % Ex;
-      const long long c = l / Ex;
-      const long long b0 = ex * N + c * NX;
+      const int b0 = (l % Ex) * N + (l / Ex) * NX;
       V x[N], y[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) x[i] = P::cvt(U[b0 + i]);
+      for (int i = 0; i < N; ++i) x[i] = ufun(b0 + i);
       eo_apply<P, N>(Dr, x, y);
 #pragma unroll
       for (int i = 0; i < N; ++i) A[b0 + i] = y[i];
@@ -156,12 +162,11 @@ __device__ __forceinline__ void tiny_apply(const SmallProb& pr, const typename P
   __syncthreads();
   // P2: row lines: wr = G11 ur + G12 us -> A, ws = G12 ur + G22 us, os = Ds' ws -> Bf
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const long long r = l % NX;
-    const long long c0 = (long long)(l / NX) * N;
+    const int q0 = l % NX + (l / NX) * N * NX;
     V ws[N], os[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const long long q = r + (c0 + j) * NX;
+      const int q = q0 + j * NX;
       const V ur = A[q], us = Bf[q];
       const V g11 = GeoT<P>::cvt(G11[q]), g12 = GeoT<P>::cvt(G12[q]), g22 = GeoT<P>::cvt(G22[q]);
       A[q] = P::fma(g11, ur, P::mul(g12, us));
@@ -169,61 +174,77 @@ __device__ __forceinline__ void tiny_apply(const SmallProb& pr, const typename P
     }
     eo_apply<P, N>(Dst, ws, os);
 #pragma unroll
-    for (int j = 0; j < N; ++j) Bf[r + (c0 + j) * NX] = os[j];
+    for (int j = 0; j < N; ++j) Bf[q0 + j * NX] = os[j];
   }
   __syncthreads();
   // P3: column lines: res = nu (Dr' wr + os) + k B u -> A
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const long long ex = l % Ex;
-    const long long c = l / Ex;
-    const long long b0 = ex * N + c * NX;
+    const int b0 = (l % Ex) * N + (l / Ex) * NX;
     V x[N], y[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) x[i] = A[b0 + i];
     eo_apply<P, N>(Drt, x, y);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      const long long q = b0 + i;
+      const int q = b0 + i;
       V res = P::fin(P::mul(nu, P::add(y[i], Bf[q])));
-      if (Bm) res = P::fin(P::fma(P::mul(kk, GeoT<P>::cvt(Bm[q])), P::cvt(U[q]), res));
+      if (Bm || P::kPrecision == SEM_F32) {
+        const V u = ufun(q);
+        if (Bm) res = P::fin(P::fma(P::mul(kk, GeoT<P>::cvt(Bm[q])), u, res));
+        if constexpr (P::kPrecision == SEM_F32) acc += (double)u * (double)res;
+      }
       A[q] = res;
-      if constexpr (P::kPrecision == SEM_F32) acc += (double)U[q] * (double)res;
     }
   }
-  __syncthreads();
+  // no barrier here: the caller's next reduction (or its own barrier) orders
+  // these stores before the gather reads them
 }
 
-__device__ __forceinline__ float tiny_mult(const SmallProb& pr, long long r, long long c) {
-  if (pr.mult_ones) return 1.0f;
-  const int cc = ((pr.rinfo[r] & L_COPY2) ? 2 : 1) * ((pr.cinfo[c] & L_COPY2) ? 2 : 1);
+__device__ __forceinline__ float tiny_mult_bits(unsigned char br, unsigned char bc, bool ones) {
+  if (ones) return 1.0f;
+  const int cc = ((br & L_COPY2) ? 2 : 1) * ((bc & L_COPY2) ? 2 : 1);
   return cc == 1 ? 1.0f : (cc == 2 ? 0.5f : 0.25f);
 }
 
-// QQ' and mask at local point (r, c) of an unassembled field: the sum of its
-// copies, x pairs first (as small_gather); each copy converted by cv first
+// QQ' at local point (r, c) of an unassembled field: the sum of its copies, x
+// pairs first (as small_gather); each copy converted by cv first
 template <class T, class F>
-__device__ __forceinline__ auto tiny_gather(const SmallProb& pr, const T* raw, long long r, long long c, F&& cv,
-                                            bool& zero) {
-  const unsigned char br = pr.rinfo[r], bc = pr.cinfo[c];
-  zero = pr.has_bc && ((br | bc) & L_ZERO);
-  const long long r2 = line_partner(r, br, pr.NX);
-  const long long c2 = line_partner(c, bc, pr.NY);
-  const T* col = raw + c * pr.NX;
+__device__ __forceinline__ auto tiny_gather(const T* raw, int NX, int NY, int r, int c, unsigned char br,
+                                            unsigned char bc, F&& cv) {
+  const int r2 = (int)line_partner(r, br, NX);
+  const int c2 = (int)line_partner(c, bc, NY);
+  const T* col = raw + c * NX;
   if (c2 < 0) return r2 < 0 ? cv(col[r]) : io_add(cv(col[r]), cv(col[r2]));
-  const T* col2 = raw + c2 * pr.NX;
+  const T* col2 = raw + c2 * NX;
   if (r2 < 0) return io_add(cv(col[r]), cv(col2[r]));
   return io_add(io_add(cv(col[r]), cv(col[r2])), io_add(cv(col2[r]), cv(col2[r2])));
+}
+
+// run f(q, r, c, row_bits, col_bits) over the points of the row lines of this
+// thread (the row line's bits are read once)
+template <int N, class F>
+__device__ __forceinline__ void tiny_points(const SmallProb& pr, F&& f) {
+  const int NX = (int)pr.NX;
+  const int nl = NX * pr.Ey;
+  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+    const int r = l % NX;
+    const int c0 = (l / NX) * N;
+    const unsigned char br = pr.rinfo[r];
+#pragma unroll
+    for (int j = 0; j < N; ++j) f(r + (c0 + j) * NX, r, c0 + j, br, pr.cinfo[c0 + j]);
+  }
 }
 
 template <int N>
 __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_constant__ TinyArgs<N> a) {
   SmallProb& pr = *a.pr;
   extern __shared__ __align__(16) float sm[];
-  __shared__ double red_d[33];
-  __shared__ unsigned long long red_m[33];
-  const long long NX = pr.NX, L = pr.NX * pr.NY;
+  int slot = 0;
+  const int NX = (int)pr.NX, NY = (int)pr.NY, L = NX * NY;
   const bool jac = pr.jacobi != 0;
   const bool mass = pr.k != 0.0;
+  const bool ones = pr.mult_ones != 0;
+  const bool has_bc = pr.has_bc;
   const TinyLayout lay = tiny_layout(L, mass, jac);
   float* G11 = sm + lay.g11;
   float* G12 = sm + lay.g12;
@@ -235,10 +256,11 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   float* p32 = sm + lay.p32;
   float* LA = sm + lay.la;
   float* LB = sm + lay.lb;
+  TinyRed& red = *reinterpret_cast<TinyRed*>(sm + lay.red);
   const int T = blockDim.x;
 
   // persistent block: FP32 geometry and Jacobi inverse diagonal
-  for (long long q = threadIdx.x; q < L; q += T) {
+  for (int q = threadIdx.x; q < L; q += T) {
     G11[q] = pr.Gf[q];
     G12[q] = pr.Gf[L + q];
     G22[q] = pr.Gf[2 * L + q];
@@ -247,14 +269,16 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   }
   // x = 0, r = b (FP64, global), max|b|
   unsigned long long m0 = 0ull;
-  for (long long q = threadIdx.x; q < L; q += T) {
+  for (int q = threadIdx.x; q < L; q += T) {
     const double v = pr.b[q];
     pr.x[q] = 0.0;
     pr.r[q] = v;
     const unsigned long long bb = tiny_abs_bits(v);
     m0 = bb > m0 ? bb : m0;
   }
-  double rmax = __longlong_as_double((long long)tiny_max(m0, red_m));
+  double dummy = 0.0;
+  tiny_reduce(dummy, m0, red, slot);
+  double rmax = __longlong_as_double((long long)m0);
   const double res0 = rmax;
   int outer = 0, total = 0;
   bool nan = rmax != rmax;
@@ -264,85 +288,88 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     ++outer;
     // ---- inner FP32 CG on A d = r to inner_tol * |r|_inf: x32 = 0, r32 = r, p32 = 0
     const double thresh = pr.inner_tol * rmax;
-    double tl = 0.0;
+    double t = 0.0;
     unsigned long long ml = 0ull;
-    for (long long q = threadIdx.x; q < L; q += T) {
+    tiny_points<N>(pr, [&](int q, int, int, unsigned char br, unsigned char bc) {
       const float ri = (float)pr.r[q];
       r32[q] = ri;
       x32[q] = 0.0f;
       p32[q] = 0.0f;
-      const long long c = q / NX, r = q - c * NX;
       const float z = jac ? ri * dinv[q] : ri;
-      tl += (double)(ri * z * tiny_mult(pr, r, c));
+      t += (double)(ri * z * tiny_mult_bits(br, bc, ones));
       const unsigned long long bb = tiny_abs_bits(ri);
       ml = bb > ml ? bb : ml;
-    }
-    double t = tiny_sum(tl, red_d);
-    double rin = __longlong_as_double((long long)tiny_max(ml, red_m));
+    });
+    tiny_reduce(t, ml, red, slot);
+    double rin = __longlong_as_double((long long)ml);
     double tprev = 1.0;
     int k = 0;
     bool nin = rin != rin;
     bool done = !(rin > thresh) || nin || total >= pr.maxiter;
     while (!done) {
+      // the new direction p = z + beta p_old is formed where it is read; the
+      // update pass stores it
       const float beta = k == 0 ? 0.0f : (float)(t / tprev);
-      for (long long q = threadIdx.x; q < L; q += T) {
-        const float z = jac ? r32[q] * dinv[q] : r32[q];
-        p32[q] = __fmaf_rn(beta, p32[q], z);
-      }
-      __syncthreads();
-      double pap_l = 0.0;
-      tiny_apply<PF32, N, float>(pr, p32, LA, LB, G11, G12, G22, Bs, nu32, k32, a.Dr, a.Drt, a.Ds, a.Dst,
-                                 pap_l);
-      const double pap = tiny_sum(pap_l, red_d);
+      auto pnew = [&](int q) {
+        const float rr = r32[q];
+        return __fmaf_rn(beta, p32[q], jac ? rr * dinv[q] : rr);
+      };
+      double pap = 0.0;
+      tiny_apply<PF32, N, float>(pr, pnew, LA, LB, G11, G12, G22, Bs, nu32, k32, a.Dr, a.Drt, a.Ds, a.Dst, pap);
+      unsigned long long none = 0ull;
+      tiny_reduce(pap, none, red, slot);
       const double alpha = t / pap;
       const float af = (float)alpha;
       ++k;
       ++total;
       double sl = 0.0;
       unsigned long long mx = 0ull;
-      for (long long q = threadIdx.x; q < L; q += T) {
-        const long long c = q / NX, r = q - c * NX;
-        bool zero;
-        float ap = tiny_gather(pr, LA, r, c, [](float v) { return v; }, zero);
-        if (zero) ap = 0.0f;
-        x32[q] = __fmaf_rn(af, p32[q], x32[q]);
+      tiny_points<N>(pr, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
+        float ap = tiny_gather(LA, NX, NY, r, c, br, bc, [](float v) { return v; });
+        if (has_bc && ((br | bc) & L_ZERO)) ap = 0.0f;
+        const float pk = pnew(q);
+        x32[q] = __fmaf_rn(af, pk, x32[q]);
         const float ri = __fmaf_rn(-af, ap, r32[q]);
         r32[q] = ri;
+        p32[q] = pk;
         const float z = jac ? ri * dinv[q] : ri;
-        sl += (double)(ri * z * tiny_mult(pr, r, c));
+        sl += (double)(ri * z * tiny_mult_bits(br, bc, ones));
         const unsigned long long bb = tiny_abs_bits(ri);
         mx = bb > mx ? bb : mx;
-      }
+      });
+      tiny_reduce(sl, mx, red, slot);
       tprev = t;
-      t = tiny_sum(sl, red_d);
-      rin = __longlong_as_double((long long)tiny_max(mx, red_m));
+      t = sl;
+      rin = __longlong_as_double((long long)mx);
       nin = (rin != rin) || (alpha != alpha);
       done = !(rin > thresh) || nin || total >= pr.maxiter;
     }
     // ---- x += x32 (FP64); r = b - A x with the double-float operator
-    for (long long q = threadIdx.x; q < L; q += T) pr.x[q] += (double)x32[q];
+    for (int q = threadIdx.x; q < L; q += T) pr.x[q] += (double)x32[q];
     __syncthreads();
     df* DA = reinterpret_cast<df*>(sm + lay.x32);  // the work block, free now: 2 L pairs
     df* DB = DA + L;
     double unused = 0.0;
     const df* Gdf = pr.Gdf;
-    tiny_apply<PDF, N, df>(pr, pr.x, DA, DB, Gdf, Gdf + L, Gdf + 2 * L, mass ? Gdf + 3 * L : nullptr, nu2, k2,
-                           a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
+    const double* X = pr.x;
+    tiny_apply<PDF, N, df>(pr, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + L, Gdf + 2 * L,
+                           mass ? Gdf + 3 * L : nullptr, nu2, k2, a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
+    __syncthreads();
     unsigned long long m2 = 0ull;
-    for (long long q = threadIdx.x; q < L; q += T) {
-      const long long c = q / NX, r = q - c * NX;
-      bool zero;
+    tiny_points<N>(pr, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
       // each copy rounded to FP64 first, then summed in FP64 (the order of the
       // chunked path's tile stores and fixup)
-      const double ax = tiny_gather(pr, DA, r, c, [](df v) { return df2d(v); }, zero);
-      const double v = zero ? 0.0 : pr.b[q] - ax;
+      const double ax = tiny_gather(DA, NX, NY, r, c, br, bc, [](df v) { return df2d(v); });
+      const double v = (has_bc && ((br | bc) & L_ZERO)) ? 0.0 : pr.b[q] - ax;
       pr.r[q] = v;
       const unsigned long long bb = tiny_abs_bits(v);
       m2 = bb > m2 ? bb : m2;
-    }
-    rmax = __longlong_as_double((long long)tiny_max(m2, red_m));
+    });
+    double zero = 0.0;
+    tiny_reduce(zero, m2, red, slot);
+    rmax = __longlong_as_double((long long)m2);
     nan = rmax != rmax || nin;
-    __syncthreads();  // the work block is the FP32 vectors again
+    __syncthreads();  // the work block holds the FP32 vectors again
   }
   if (threadIdx.x == 0) {
     pr.iters = total;
