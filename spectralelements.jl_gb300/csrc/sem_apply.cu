@@ -151,12 +151,17 @@ int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, con
   long long along = std::max(std::max(f.NX, f.NY), f.nxi * f.nyi);
   long long bx = (along + threads - 1) / threads;
   if (bx > 64) bx = 64;
+  long long by = std::min(nI, 65535LL);
+  if (gate) {  // a gated re-run: a small grid (it exits at once unless the guard fired)
+    bx = std::min(bx, 4LL);
+    by = std::min(by, std::max(1LL, 2LL * num_sms() / bx));
+  }
   // a programmatic dependent of the operator kernel before it on the stream:
   // its CTAs are scheduled once every operator CTA has started, and wait
   // (griddepcontrol.wait) for the operator grid's completion
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
-  cfg.gridDim = dim3((unsigned)bx, (unsigned)std::min(nI, 65535LL));
+  cfg.gridDim = dim3((unsigned)bx, (unsigned)by);
   cfg.blockDim = dim3(threads);
   cfg.stream = s;
   cudaLaunchAttribute at[1];
@@ -180,14 +185,17 @@ static ApplyCall scalar_window(const ApplyCall& c) {
   return r;
 }
 
-// The native FP64 re-run of a guarded double-float call: kernel variant 0 and
-// its fixup, launched after the double-float kernels and gated on the call's
-// flag word (every CTA returns at once unless the word holds the call's tag).
+// The native FP64 re-run of a guarded double-float call: the persistent
+// kernel (variant 4, one CTA per resident slot) and its fixup on a small grid,
+// launched after the double-float kernels and gated on the call's flag word
+// (every CTA returns at once unless the word holds the call's tag), so that an
+// unflagged call pays two short launches.
 static int launch_gated_f64(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s,
                             long long key_lo, long long key_hi) {
   ApplyCall r = c;
   r.precision = SEM_F64;
-  r.variant = 0;
+  r.variant = 4;
+  r.ctr = nullptr;
   r.rflag = nullptr;
   r.gate = c.rflag;
   r.gate_tag = c.rtag;
@@ -237,8 +245,18 @@ int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& 
     return set_error(SEM_ERR_BAD_ARG, "tile-row windows serve SEM_F64 and SEM_F64_DF");
   if (st != SEM_OK) return st;
   SEM_CHECK(launch_dss_fixup(g, c.out, c.mode, c.precision, c.skip, tile[0], tile[1], s, key_lo, key_hi));
-  if (c.rflag) SEM_CHECK(launch_gated_f64(g, ops, c, s, key_lo, key_hi));
+  // the range guard's re-run covers the whole field once every window is
+  // done (launch_guard_rerun): a window's fixup has already summed the
+  // interface copies of the window before it
   return SEM_OK;
+}
+
+int launch_guard_rerun(const Grid& g, const OperatorSet* ops, const ApplyCall& c0, cudaStream_t s) {
+  ApplyCall c = scalar_window(c0);
+  if (c.precision != SEM_F64_DF || !c.rflag) return SEM_OK;
+  c.ty0 = 0;
+  c.tyn = 0;
+  return launch_gated_f64(g, ops, c, s, 0, 1LL << 62);
 }
 
 // the device's own guard word, for calls without a mesh handle (one per

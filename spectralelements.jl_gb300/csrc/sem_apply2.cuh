@@ -50,9 +50,12 @@ struct Apply2Args {
   v nu_s;
   v k_s;
   // range guard (double-float policy): *rflag = rtag when an input row or a
-  // result leaves the pair format's range
+  // result leaves the pair format's range; a gated launch (gate non-NULL)
+  // does nothing unless *gate == gate_tag
   unsigned* rflag;
   unsigned rtag;
+  const unsigned* gate;
+  unsigned gate_tag;
   int Ex, Ey;
   long long NX;
   unsigned mode;
@@ -193,6 +196,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   pdl_trigger();  // the next kernel (the cross-tile fixup) may be scheduled now
   pdl_wait();     // a no-op unless this launch is a programmatic dependent
   if (a.skip && *a.skip) return;
+  if (a.gate && *a.gate != a.gate_tag) return;  // gated re-run not needed
   const int t = threadIdx.x;
   const int elem = t / N;
   const int lane = t - elem * N;
@@ -330,17 +334,21 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       for (int j = 0; j < N; ++j) res[j] = P::zero();
     }
   }
+  bool kbad = false;  // range guard: a tiny k B product
   if (mode & M_MASS) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       const V b = valid ? GeoT<P>::ld(a.B + base + (long long)j * NX) : P::zero();
-      res[j] = P::fin(P::fma((mode & M_KB) ? b : P::mul(a.k_s, b), s0[j * SP + lane], res[j]));
+      const V kb = (mode & M_KB) ? b : P::mul(a.k_s, b);
+      if constexpr (P::kPrecision == SEM_F64_DF) kbad |= df_tiny_nz(kb, kKbTiny);
+      res[j] = P::fin(P::fma(kb, s0[j * SP + lane], res[j]));
     }
   }
 
   if constexpr (P::kPrecision == SEM_F64_DF) {
-    // range guard: a row of tiny values or a NaN/Inf result flags the call
-    bool bad = rs.tiny();
+    // range guard: a row of tiny values, a tiny k B or a NaN/Inf result
+    // flags the call (degenerate metric terms arrive as NaN pairs)
+    bool bad = rs.tiny() || kbad;
 #pragma unroll
     for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
     if (bad && a.rflag) *a.rflag = a.rtag;

@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
   pdl_trigger();  // the next kernel (the cross-tile fixup) may be scheduled now
   pdl_wait();     // a no-op unless this launch is a programmatic dependent
   if (a.skip && *a.skip) return;
+  if (a.gate && *a.gate != a.gate_tag) return;  // gated re-run not needed
   const int t = threadIdx.x;
   const int elem = t / N;
   const int lane = t - elem * N;
@@ -212,18 +213,22 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
       }
     }
     cp_async_wait_group<2>();  // B(tile); u(next), G(next) may be in flight
+    bool kbad = false;  // range guard: a tiny k B product
     if (mass) {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
         const V b = valid ? GeoT<P>::cvt(RG[(3 * N + j) * T + t]) : P::zero();
-        res[j] = P::fin(P::fma((mode & M_KB) ? b : P::mul(a.k_s, b), s0[j * SP + lane], res[j]));
+        const V kb = (mode & M_KB) ? b : P::mul(a.k_s, b);
+        if constexpr (P::kPrecision == SEM_F64_DF) kbad |= df_tiny_nz(kb, kKbTiny);
+        res[j] = P::fin(P::fma(kb, s0[j * SP + lane], res[j]));
       }
     }
     fetch_b(next);
 
     if constexpr (P::kPrecision == SEM_F64_DF) {
-      // range guard: a row of tiny values or a NaN/Inf result flags the call
-      bool bad = rs.tiny();
+      // range guard: a row of tiny values, a tiny k B or a NaN/Inf result
+      // flags the call (degenerate metric terms arrive as NaN pairs)
+      bool bad = rs.tiny() || kbad;
 #pragma unroll
       for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
       if (bad && a.rflag) *a.rflag = a.rtag;

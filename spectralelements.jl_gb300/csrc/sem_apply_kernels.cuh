@@ -249,6 +249,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   V* s2 = S2 + elem * ES;
   const int rofs = elem * ES + lane;  // this thread's row inside a staged slot (+ j*SP)
   RowScale rs;  // range guard of the double-float policy
+  bool gbad = false;  // range guard: degenerate metric terms or a tiny k B
 
   // ---- staged variant: issue every later global read of this row now
   if (STAGE) {
@@ -313,6 +314,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
         V g11 = ldx(a.G11, a.slot_g, j);
         V g12 = ldx(a.G12, a.slot_g < 0 ? -1 : a.slot_g + 1, j);
         V g22 = ldx(a.G22, a.slot_g < 0 ? -1 : a.slot_g + 2, j);
+        if constexpr (P::kPrecision == SEM_F64_DF) gbad |= geo_tiny(g11, g22);
         V ur = s2[j * SP + lane];
         V wr = P::fma(g11, ur, P::mul(g12, us[j]));
         ws[j] = P::fma(g12, ur, P::mul(g22, us[j]));
@@ -359,12 +361,14 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     for (int j = 0; j < N; ++j) {
       V b = ldx(a.B, a.slot_b, j);
       V kb = (mode & M_KB) ? b : P::mul(a.k_s, b);
+      if constexpr (P::kPrecision == SEM_F64_DF) gbad |= df_tiny_nz(kb, kKbTiny);
       res[j] = P::fin(P::fma(kb, u[j], res[j]));
     }
   }
   if constexpr (P::kPrecision == SEM_F64_DF) {
-    // range guard: a row of tiny values or a NaN/Inf result flags the call
-    bool bad = rs.tiny();
+    // range guard: a row of tiny values, degenerate metric terms, a tiny k B
+    // or a NaN/Inf result flags the call
+    bool bad = rs.tiny() || gbad;
 #pragma unroll
     for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
     if (bad && a.rflag) *a.rflag = a.rtag;

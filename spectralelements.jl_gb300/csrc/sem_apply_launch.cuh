@@ -118,7 +118,7 @@ static int launch_apply_v(const Grid& g, const OperatorSet* ops, const ApplyCall
   if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((g.Ex + TS::TX - 1) / TS::TX, c.tyn > 0 ? c.tyn : (g.Ey + TS::TY - 1) / TS::TY);
   a.ty0 = c.ty0;
-  auto* ev = timing_slot();
+  auto* ev = c.gate ? nullptr : timing_slot();  // gated re-runs are not timed
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
   SEM_CHECK(launch_kernel(kern, grid, TS::THREADS, smem, s, c.pdl != 0, a));
   if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
@@ -151,6 +151,8 @@ static void fill_args2(Apply2Args<P, N>& a, const Grid& g, const OperatorSet* op
   a.k_s = P::from_double(c.k_s);
   a.rflag = c.rflag;
   a.rtag = c.rtag;
+  a.gate = c.gate;
+  a.gate_tag = c.gate_tag;
   a.Ex = g.Ex;
   a.Ey = g.Ey;
   a.NX = g.NX;
@@ -188,7 +190,7 @@ static int launch_apply_v2(const Grid& g, const OperatorSet* ops, const ApplyCal
   if (smem > 48 * 1024) SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((g.Ex + TS::TX - 1) / TS::TX, c.tyn > 0 ? c.tyn : (g.Ey + TS::TY - 1) / TS::TY);
   a.ty0 = c.ty0;
-  auto* ev = timing_slot();
+  auto* ev = c.gate ? nullptr : timing_slot();  // gated re-runs are not timed
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
   SEM_CHECK(launch_kernel(kern, grid, TS::THREADS, smem, s, c.pdl != 0, a));
   if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
@@ -219,7 +221,7 @@ static int launch_apply_v3(const Grid& g, const OperatorSet* ops, const ApplyCal
   const long long slots = (long long)per_sm * num_sms();
   const long long rounds = (tiles + slots - 1) / slots;
   const long long grid = (tiles + rounds - 1) / rounds;
-  auto* ev = timing_slot();
+  auto* ev = c.gate ? nullptr : timing_slot();  // gated re-runs are not timed
   if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
   SEM_CHECK(launch_kernel(kern, dim3((unsigned)grid), TS::THREADS, smem, s, c.pdl != 0, a, tiles_x, (int)tiles));
   if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));

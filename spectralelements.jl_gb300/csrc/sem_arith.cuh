@@ -130,6 +130,27 @@ struct RowScale {
   __device__ __forceinline__ bool tiny() const { return emax != 0u && emax < kDfExpTiny; }
 };
 
+// Geometry and mass-term guard: a point whose metric terms G11 and G22 both
+// lie below 2^-40 in magnitude (a degenerate or absurdly scaled mesh: in 2D
+// the metric terms are scale-free), or a nonzero k B product below 2^-100,
+// would leave the pair format's accurate range inside the contraction.  The
+// pre-split geometry turns such points into NaN pairs; the kernels that split
+// on load test the same conditions.
+constexpr float kGeoTiny = 0x1p-40f;
+constexpr float kKbTiny = 0x1p-100f;
+__host__ __device__ __forceinline__ bool geo_tiny(double g11, double g22) {
+  const double m = fmax(fabs(g11), fabs(g22));
+  return m != 0.0 && m < (double)kGeoTiny;
+}
+__device__ __forceinline__ bool geo_tiny(df g11, df g22) {  // FP32 pipe only
+  const float m = fmaxf(fabsf(g11.h), fabsf(g22.h));
+  return m != 0.0f && m < kGeoTiny;
+}
+__device__ __forceinline__ bool df_tiny_nz(df a, float t) {
+  const float h = fabsf(a.h);
+  return h != 0.0f && h < t;
+}
+
 // a double-float value whose high part is Inf or NaN
 __device__ __forceinline__ bool df_bad(df a) { return (__float_as_uint(a.h) & 0x7f800000u) == 0x7f800000u; }
 

@@ -88,11 +88,23 @@ __global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, long 
     b[i] = (float)a[i];
 }
 
-// the same split the double-float loads perform (d2df), done once
-__global__ void k_d2df(const double* __restrict__ a, df* __restrict__ b, long long len) {
+// the geometry's split, with the range guard's poisoning: a point whose G11
+// and G22 both lie below 2^-40 gets NaN metric pairs, and a nonzero mass entry
+// below 2^-100 a NaN pair, so that every double-float apply on the mesh is
+// flagged and re-run in native FP64
+__global__ void k_geo_d2df(const double* __restrict__ G11, const double* __restrict__ G12,
+                           const double* __restrict__ G22, const double* __restrict__ B, df* __restrict__ out,
+                           long long len) {
+  const df nan = {__uint_as_float(0x7fc00000u), 0.0f};
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
-       i += (long long)gridDim.x * blockDim.x)
-    b[i] = d2df_op(a[i]);
+       i += (long long)gridDim.x * blockDim.x) {
+    const double g11 = G11[i], g22 = G22[i], b = B[i];
+    const bool gt = geo_tiny(g11, g22);
+    out[i] = gt ? nan : d2df_op(g11);
+    out[len + i] = gt ? nan : d2df_op(G12[i]);
+    out[2 * len + i] = gt ? nan : d2df_op(g22);
+    out[3 * len + i] = (b != 0.0 && fabs(b) < (double)kKbTiny) ? nan : d2df_op(b);
+  }
 }
 
 __global__ void k_maskfield(double* __restrict__ out, Grid g) {
@@ -205,10 +217,7 @@ int ensure_df_geometry(sem_mesh* m, cudaStream_t s) {
   df* p = nullptr;
   SEM_CUDA(cudaMalloc(&p, 4 * sizeof(df) * (size_t)len));
   m->Gdf = p;
-  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->G11, p, len);
-  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->G12, p + len, len);
-  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->G22, p + 2 * len, len);
-  k_d2df<<<blocks_for(len), 256, 0, s>>>(m->B, p + 3 * len, len);
+  k_geo_d2df<<<blocks_for(len), 256, 0, s>>>(m->G11, m->G12, m->G22, m->B, p, len);
   SEM_CUDA(cudaGetLastError());
   return SEM_OK;
 }

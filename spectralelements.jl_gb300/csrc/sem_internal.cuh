@@ -339,6 +339,9 @@ int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, con
 // fixup of the interface points whose highest copy column is in [key_lo, key_hi)
 int launch_apply_window(const Grid& g, const OperatorSet* ops, const ApplyCall& c, long long key_lo,
                         long long key_hi, cudaStream_t s);
+// the range guard's native FP64 re-run of a whole double-float call, gated on
+// the call's flag word (for callers that ran the call in windows)
+int launch_guard_rerun(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s);
 
 // elementwise / structured kernels (sem_vec.cu)
 int launch_gather_scatter(const Grid& g, const double* u, double* out, unsigned mode, cudaStream_t s);

@@ -49,14 +49,9 @@ struct TinyArgs {
   EOCoef<N, df> Dr2, Drt2, Ds2, Dst2;  // double-float FP64 residual
 };
 
-// Block-wide sum and maximum with one barrier: every warp folds its lanes
-// (fixed shuffle tree), lane 0 stores the warp's pair in a slot of `red`, and
-// after the barrier every thread folds the warps' pairs in warp order, so all
-// threads hold the same result.  Consecutive calls alternate between the two
-// slots: a slot is written again only after a later call's barrier, when every
-// thread has read it.
+// reduction slots: two of them, each one double-float sum and one maximum per warp
 struct TinyRed {
-  double s[2][32];
+  df s[2][32];
   unsigned long long m[2][32];
 };
 
@@ -87,54 +82,102 @@ __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool j
   return t;
 }
 
-__device__ __forceinline__ void tiny_reduce(double& v, unsigned long long& mx, TinyRed& red, int& slot) {
+// Block-wide sum and maximum with one barrier.  Each thread brings an FP32
+// partial sum (a handful of products) and a magnitude as bits; every warp
+// folds its lanes in double-float (fixed shuffle tree, FP32 pipe only: FP64
+// runs at 1/64 of the FP32 rate), lane 0 stores the warp's pair in a slot of
+// `red`, and after the barrier every thread folds the warps' pairs in warp
+// order, so all threads hold the same result.  Consecutive calls alternate
+// between the two slots: a slot is written again only after a later call's
+// barrier, when every thread has read it.
+__device__ __forceinline__ df tiny_warp_sum(float v) {
+  df s = {v, 0.0f};
   for (int o = 16; o > 0; o >>= 1) {
-    v += __shfl_down_sync(0xffffffffu, v, o);
+    df y;
+    y.h = __shfl_down_sync(0xffffffffu, s.h, o);
+    y.l = __shfl_down_sync(0xffffffffu, s.l, o);
+    s = df_add(s, y);
+  }
+  return s;
+}
+
+__device__ __forceinline__ df tiny_fold(const TinyRed& red, int slot, unsigned long long& mx) {
+  df s = red.s[slot][0];
+  unsigned long long m = red.m[slot][0];
+  const int nw = (int)(blockDim.x >> 5);
+  for (int i = 1; i < nw; ++i) {
+    s = df_add(s, red.s[slot][i]);
+    m = red.m[slot][i] > m ? red.m[slot][i] : m;
+  }
+  mx = m;
+  return s;
+}
+
+// FP32 partial sum and FP32 magnitude bits (the bits of |v|; NaN orders above
+// everything): returns the block sum (rounded to FP32: the inner CG's scalars
+// are FP32), mx the block maximum as an FP32 bit pattern
+__device__ __forceinline__ float tiny_reduce(float v, unsigned& mx, TinyRed& red, int& slot) {
+  const df s = tiny_warp_sum(v);
+  const unsigned m = __reduce_max_sync(0xffffffffu, mx);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red.s[slot][w] = s;
+    red.m[slot][w] = m;
+  }
+  __syncthreads();
+  unsigned long long mm;
+  const df r = tiny_fold(red, slot, mm);
+  mx = (unsigned)mm;
+  slot ^= 1;
+  return r.h + r.l;
+}
+
+// block maximum of FP64 magnitude bits (the FP64 residual, once per sweep)
+__device__ __forceinline__ unsigned long long tiny_reduce_max64(unsigned long long mx, TinyRed& red, int& slot) {
+  for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, o);
     mx = y > mx ? y : mx;
   }
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    red.s[slot][w] = v;
+    red.s[slot][w] = {0.0f, 0.0f};
     red.m[slot][w] = mx;
   }
   __syncthreads();
-  double s = red.s[slot][0];
-  unsigned long long m = red.m[slot][0];
-  const int nw = (int)(blockDim.x >> 5);
-  for (int i = 1; i < nw; ++i) {
-    s += red.s[slot][i];
-    m = red.m[slot][i] > m ? red.m[slot][i] : m;
-  }
-  v = s;
-  mx = m;
+  unsigned long long mm;
+  tiny_fold(red, slot, mm);
   slot ^= 1;
+  return mm;
 }
 
-// magnitude bits as the bits of the double of the same value (NaN orders above
-// everything)
-__device__ __forceinline__ unsigned long long tiny_abs_bits(float v) {
-  return (unsigned long long)__double_as_longlong((double)fabsf(v)) | (v != v ? 0x7ff8000000000000ull : 0ull);
-}
+__device__ __forceinline__ unsigned tiny_abs_bits(float v) { return __float_as_uint(v) & 0x7fffffffu; }
 __device__ __forceinline__ unsigned long long tiny_abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
+
+// the mesh sizes and line bits, held in registers (read once from the
+// problem record, which the stores to shared memory could otherwise alias)
+struct TinyDims {
+  int NX, NY, Ex, Ey;
+  const unsigned char* rinfo;
+  const unsigned char* cinfo;
+};
 
 // The operator, unassembled and unmasked, res = nu (D'G D u) + k B u, on every
 // line of the mesh.  ufun(q) gives the input at local point q (shared or
 // global memory, or formed on the fly); A, Bf: two line buffers of L entries
 // (shared); G11..Bm: the metric terms and mass (shared FP32 or global
 // pre-split pairs; Bm NULL without a mass term).  The result is left in A;
-// acc receives this thread's part of u . res.  32-bit indices: a mesh on this
+// acc receives this thread's part of u . res (FP32 policy).  32-bit indices: a mesh on this
 // path has at most a few thousand points.
 template <class P, int N, class GT, class UF>
-__device__ __forceinline__ void tiny_apply(const SmallProb& pr, UF&& ufun, typename P::v* A, typename P::v* Bf,
+__device__ __forceinline__ void tiny_apply(const TinyDims& pr, UF&& ufun, typename P::v* A, typename P::v* Bf,
                                            const GT* G11, const GT* G12, const GT* G22, const GT* Bm,
                                            typename P::v nu, typename P::v kk, const EOCoef<N, typename P::v>& Dr,
                                            const EOCoef<N, typename P::v>& Drt, const EOCoef<N, typename P::v>& Ds,
-                                           const EOCoef<N, typename P::v>& Dst, double& acc) {
+                                           const EOCoef<N, typename P::v>& Dst, float& acc) {
   typedef typename P::v V;
-  const int NX = (int)pr.NX;
+  const int NX = pr.NX;
   const int nl = NX * pr.Ey;  // lines per direction
   const int Ex = pr.Ex;
   // P1: us on the row lines -> Bf, ur on the column lines -> A
@@ -191,7 +234,7 @@ __device__ __forceinline__ void tiny_apply(const SmallProb& pr, UF&& ufun, typen
       if (Bm || P::kPrecision == SEM_F32) {
         const V u = ufun(q);
         if (Bm) res = P::fin(P::fma(P::mul(kk, GeoT<P>::cvt(Bm[q])), u, res));
-        if constexpr (P::kPrecision == SEM_F32) acc += (double)u * (double)res;
+        if constexpr (P::kPrecision == SEM_F32) acc = __fmaf_rn(u, res, acc);
       }
       A[q] = res;
     }
@@ -223,8 +266,8 @@ __device__ __forceinline__ auto tiny_gather(const T* raw, int NX, int NY, int r,
 // run f(q, r, c, row_bits, col_bits) over the points of the row lines of this
 // thread (the row line's bits are read once)
 template <int N, class F>
-__device__ __forceinline__ void tiny_points(const SmallProb& pr, F&& f) {
-  const int NX = (int)pr.NX;
+__device__ __forceinline__ void tiny_points(const TinyDims& pr, F&& f) {
+  const int NX = pr.NX;
   const int nl = NX * pr.Ey;
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
     const int r = l % NX;
@@ -241,6 +284,8 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   extern __shared__ __align__(16) float sm[];
   int slot = 0;
   const int NX = (int)pr.NX, NY = (int)pr.NY, L = NX * NY;
+  const TinyDims dm = {NX, NY, pr.Ex, pr.Ey, pr.rinfo, pr.cinfo};
+  const int maxiter = pr.maxiter;
   const bool jac = pr.jacobi != 0;
   const bool mass = pr.k != 0.0;
   const bool ones = pr.mult_ones != 0;
@@ -276,55 +321,53 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     const unsigned long long bb = tiny_abs_bits(v);
     m0 = bb > m0 ? bb : m0;
   }
-  double dummy = 0.0;
-  tiny_reduce(dummy, m0, red, slot);
+  m0 = tiny_reduce_max64(m0, red, slot);
   double rmax = __longlong_as_double((long long)m0);
   const double res0 = rmax;
   int outer = 0, total = 0;
   bool nan = rmax != rmax;
   const float nu32 = (float)pr.nu, k32 = (float)pr.k;
   const df nu2 = d2df(pr.nu), k2 = d2df(pr.k);  // both inside the pair window (small_eligible)
-  while (!(rmax <= pr.tol) && !nan && outer < pr.max_outer && total < pr.maxiter) {
+  while (!(rmax <= pr.tol) && !nan && outer < pr.max_outer && total < maxiter) {
     ++outer;
     // ---- inner FP32 CG on A d = r to inner_tol * |r|_inf: x32 = 0, r32 = r, p32 = 0
-    const double thresh = pr.inner_tol * rmax;
-    double t = 0.0;
-    unsigned long long ml = 0ull;
-    tiny_points<N>(pr, [&](int q, int, int, unsigned char br, unsigned char bc) {
+    const float thresh = (float)(pr.inner_tol * rmax);
+    float tl = 0.0f;
+    unsigned ml = 0u;
+    tiny_points<N>(dm, [&](int q, int, int, unsigned char br, unsigned char bc) {
       const float ri = (float)pr.r[q];
       r32[q] = ri;
       x32[q] = 0.0f;
       p32[q] = 0.0f;
       const float z = jac ? ri * dinv[q] : ri;
-      t += (double)(ri * z * tiny_mult_bits(br, bc, ones));
-      const unsigned long long bb = tiny_abs_bits(ri);
+      tl = __fmaf_rn(ri * tiny_mult_bits(br, bc, ones), z, tl);
+      const unsigned bb = tiny_abs_bits(ri);
       ml = bb > ml ? bb : ml;
     });
-    tiny_reduce(t, ml, red, slot);
-    double rin = __longlong_as_double((long long)ml);
-    double tprev = 1.0;
+    float t = tiny_reduce(tl, ml, red, slot);
+    float rin = __uint_as_float(ml);
+    float tprev = 1.0f;
     int k = 0;
     bool nin = rin != rin;
-    bool done = !(rin > thresh) || nin || total >= pr.maxiter;
+    bool done = !(rin > thresh) || nin || total >= maxiter;
     while (!done) {
       // the new direction p = z + beta p_old is formed where it is read; the
       // update pass stores it
-      const float beta = k == 0 ? 0.0f : (float)(t / tprev);
+      const float beta = k == 0 ? 0.0f : t / tprev;
       auto pnew = [&](int q) {
         const float rr = r32[q];
         return __fmaf_rn(beta, p32[q], jac ? rr * dinv[q] : rr);
       };
-      double pap = 0.0;
-      tiny_apply<PF32, N, float>(pr, pnew, LA, LB, G11, G12, G22, Bs, nu32, k32, a.Dr, a.Drt, a.Ds, a.Dst, pap);
-      unsigned long long none = 0ull;
-      tiny_reduce(pap, none, red, slot);
-      const double alpha = t / pap;
-      const float af = (float)alpha;
+      float papl = 0.0f;
+      tiny_apply<PF32, N, float>(dm, pnew, LA, LB, G11, G12, G22, Bs, nu32, k32, a.Dr, a.Drt, a.Ds, a.Dst, papl);
+      unsigned none = 0u;
+      const float pap = tiny_reduce(papl, none, red, slot);
+      const float af = t / pap;
       ++k;
       ++total;
-      double sl = 0.0;
-      unsigned long long mx = 0ull;
-      tiny_points<N>(pr, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
+      float sl = 0.0f;
+      unsigned mx = 0u;
+      tiny_points<N>(dm, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
         float ap = tiny_gather(LA, NX, NY, r, c, br, bc, [](float v) { return v; });
         if (has_bc && ((br | bc) & L_ZERO)) ap = 0.0f;
         const float pk = pnew(q);
@@ -333,30 +376,29 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
         r32[q] = ri;
         p32[q] = pk;
         const float z = jac ? ri * dinv[q] : ri;
-        sl += (double)(ri * z * tiny_mult_bits(br, bc, ones));
-        const unsigned long long bb = tiny_abs_bits(ri);
+        sl = __fmaf_rn(ri * tiny_mult_bits(br, bc, ones), z, sl);
+        const unsigned bb = tiny_abs_bits(ri);
         mx = bb > mx ? bb : mx;
       });
-      tiny_reduce(sl, mx, red, slot);
       tprev = t;
-      t = sl;
-      rin = __longlong_as_double((long long)mx);
-      nin = (rin != rin) || (alpha != alpha);
-      done = !(rin > thresh) || nin || total >= pr.maxiter;
+      t = tiny_reduce(sl, mx, red, slot);
+      rin = __uint_as_float(mx);
+      nin = (rin != rin) || (af != af);
+      done = !(rin > thresh) || nin || total >= maxiter;
     }
     // ---- x += x32 (FP64); r = b - A x with the double-float operator
     for (int q = threadIdx.x; q < L; q += T) pr.x[q] += (double)x32[q];
     __syncthreads();
     df* DA = reinterpret_cast<df*>(sm + lay.x32);  // the work block, free now: 2 L pairs
     df* DB = DA + L;
-    double unused = 0.0;
+    float unused = 0.0f;
     const df* Gdf = pr.Gdf;
     const double* X = pr.x;
-    tiny_apply<PDF, N, df>(pr, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + L, Gdf + 2 * L,
+    tiny_apply<PDF, N, df>(dm, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + L, Gdf + 2 * L,
                            mass ? Gdf + 3 * L : nullptr, nu2, k2, a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
     __syncthreads();
     unsigned long long m2 = 0ull;
-    tiny_points<N>(pr, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
+    tiny_points<N>(dm, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
       // each copy rounded to FP64 first, then summed in FP64 (the order of the
       // chunked path's tile stores and fixup)
       const double ax = tiny_gather(DA, NX, NY, r, c, br, bc, [](df v) { return df2d(v); });
@@ -365,8 +407,7 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
       const unsigned long long bb = tiny_abs_bits(v);
       m2 = bb > m2 ? bb : m2;
     });
-    double zero = 0.0;
-    tiny_reduce(zero, m2, red, slot);
+    m2 = tiny_reduce_max64(m2, red, slot);
     rmax = __longlong_as_double((long long)m2);
     nan = rmax != rmax || nin;
     __syncthreads();  // the work block holds the FP32 vectors again

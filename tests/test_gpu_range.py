@@ -70,21 +70,28 @@ def test_apply_out_of_window_scalars(gpu, nu, k):
     assert np.isfinite(ref).all() and rel_l2(got, ref) < 1e-12
 
 
-def test_apply_out_of_window_geometry(gpu):
-    """Metric terms outside the window (a mesh whose G was uploaded scaled by
-    2^120): their split pairs are NaN, so every tile runs in FP64."""
+@pytest.mark.parametrize("gscale,bscale,nu,k", [(2.0 ** 120, 1.0, 1.0, 0.0), (2.0 ** -120, 1.0, 1.0, 0.0),
+                                                (1.0, 2.0 ** -110, 0.0, 1.0), (1.0, 2.0 ** -60, 0.0, 2.0 ** -60)])
+def test_apply_out_of_window_geometry(gpu, gscale, bscale, nu, k):
+    """Metric terms or a mass term outside the pair format's accurate range (a
+    mesh whose G or B was uploaded scaled): huge metric terms split into NaN
+    pairs, metric terms below 2^-40 and k B products below 2^-100 flag the
+    call, so every variant returns the native FP64 result.  The mass cases
+    take nu = 0, so that the tiny term is the whole result."""
     import semgb300 as S
     mo = O.Mesh(9, 9, 5, 4, (False, False), O.sin_deform(0.05))
-    arrays = {k: getattr(mo, k) for k in ("zr", "wr", "zs", "ws", "Dr", "Ds", "x", "y", "B")}
-    for k in ("G11", "G12", "G22"):
-        arrays[k] = getattr(mo, k) * 2.0 ** 120
+    arrays = {key: getattr(mo, key) for key in ("zr", "wr", "zs", "ws", "Dr", "Ds", "x", "y")}
+    for key in ("G11", "G12", "G22"):
+        arrays[key] = getattr(mo, key) * gscale
+    arrays["B"] = mo.B * bscale
     md = S.Mesh.from_arrays(9, 5, 4, (False, False), arrays, bc="DDDD")
     u = np.random.default_rng(4).uniform(-1, 1, mo.shape)
-    ref = _apply(S, md, S.SEM_F64, u, nu=1.0, k=0.0)
+    ref = _apply(S, md, S.SEM_F64, u, nu=nu, k=k)
+    assert np.isfinite(ref).all() and np.abs(ref).max() > 0
     for v in range(S._lib.SEM_VARIANTS):
         md.set_variant(v, S.SEM_F64_DF)
-        got = _apply(S, md, S.SEM_F64_DF, u, nu=1.0, k=0.0)
-        assert rel_l2(got, ref) < 1e-12, v
+        got = _apply(S, md, S.SEM_F64_DF, u, nu=nu, k=k)
+        assert rel_l2(got, ref) < 1e-12, (v, rel_l2(got, ref))
 
 
 def test_nan_input_stays_nan(gpu):
