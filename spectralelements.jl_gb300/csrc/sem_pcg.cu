@@ -982,7 +982,7 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     // SEM_MIXED in one thread block when its FP32 working set fits the shared
     // memory of an SM (the restarted form whose FP32 iterations the cluster
     // kernel cannot make cheaper than FP64 ones)
-    const size_t tiny = tiny_smem_bytes(L, o->k != 0.0, jac);
+    const size_t tiny = tiny_smem_bytes(L, o->k != 0.0, jac, cx.g.NX + cx.g.NY);
     if (prec == SEM_MIXED && tiny <= max_smem_optin())
       SEM_CHECK(launch_tiny_pcg(w.small, sp, *cx.ops, tiny, s));
     else

@@ -40,7 +40,9 @@
 
 namespace sem {
 
-constexpr int kTinyMaxThreads = 512;  // 128 registers a thread; an 8x8-element mesh of order 8 has 512 lines
+// one thread per line where the mesh allows (an 8x8-element mesh of order 8
+// has 576 lines); 102 registers a thread at most
+constexpr int kTinyMaxThreads = 640;
 
 template <int N>
 struct TinyArgs {
@@ -56,13 +58,13 @@ struct TinyRed {
 };
 
 // shared-memory layout in 4-byte words: the persistent block (G11, G12, G22,
-// [B], [dinv]), the work block (x32, r32, p32, line buffers A and B), then
-// the reduction slots
+// [B], [dinv]), the work block (x32, r32, p32, line buffers A and B), the
+// reduction slots and the line bits
 struct TinyLayout {
-  long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, red, words;
+  long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, red, bits, words;
 };
 
-__host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool jac) {
+__host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool jac, long long nbits) {
   TinyLayout t;
   long long o = 0;
   t.g11 = o; o += L;
@@ -78,6 +80,7 @@ __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool j
   t.lb = o; o += L;
   o = (o + 1) & ~1LL;
   t.red = o; o += (long long)(sizeof(TinyRed) / 4);
+  t.bits = o; o += (nbits + 3) / 4;  // line bits of the rows, then of the columns
   t.words = o;
   return t;
 }
@@ -155,127 +158,205 @@ __device__ __forceinline__ unsigned long long tiny_abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
-// the mesh sizes and line bits, held in registers (read once from the
-// problem record, which the stores to shared memory could otherwise alias)
+// The mesh sizes, line bits and this thread's line walks, held in registers
+// (read once from the problem record, which stores through generic pointers
+// could otherwise alias).  Thread t handles lines t, t + T, t + 2T, ...; a
+// row line l has row r = l mod NX and element row e = l div NX, a column line
+// l has element column x = l mod Ex and column c = l div Ex.  The walks
+// advance (r, e) and (x, c) by T without dividing.
 struct TinyDims {
-  int NX, NY, Ex, Ey;
-  const unsigned char* rinfo;
+  int NX, NY, Ex, Ey, nl, T;
+  int r0, e0, dr, de;  // row-line walk
+  int x0, c0, dx, dc;  // column-line walk
+  const unsigned char* rinfo;  // line bits (shared-memory copies)
   const unsigned char* cinfo;
 };
+
+__device__ __forceinline__ void tiny_step(int& a, int& b, int da, int db, int n) {
+  a += da;
+  b += db;
+  if (a >= n) {
+    a -= n;
+    ++b;
+  }
+}
 
 // The operator, unassembled and unmasked, res = nu (D'G D u) + k B u, on every
 // line of the mesh.  ufun(q) gives the input at local point q (shared or
 // global memory, or formed on the fly); A, Bf: two line buffers of L entries
 // (shared); G11..Bm: the metric terms and mass (shared FP32 or global
 // pre-split pairs; Bm NULL without a mass term).  The result is left in A;
-// acc receives this thread's part of u . res (FP32 policy).  32-bit indices: a mesh on this
-// path has at most a few thousand points.
+// acc receives this thread's part of u . res (FP32 policy).  32-bit indices:
+// a mesh on this path has at most a few thousand points.
 template <class P, int N, class GT, class UF>
-__device__ __forceinline__ void tiny_apply(const TinyDims& pr, UF&& ufun, typename P::v* A, typename P::v* Bf,
+__device__ __forceinline__ void tiny_apply(const TinyDims& d, UF&& ufun, typename P::v* A, typename P::v* Bf,
                                            const GT* G11, const GT* G12, const GT* G22, const GT* Bm,
                                            typename P::v nu, typename P::v kk, const EOCoef<N, typename P::v>& Dr,
                                            const EOCoef<N, typename P::v>& Drt, const EOCoef<N, typename P::v>& Ds,
                                            const EOCoef<N, typename P::v>& Dst, float& acc) {
   typedef typename P::v V;
-  const int NX = pr.NX;
-  const int nl = NX * pr.Ey;  // lines per direction
-  const int Ex = pr.Ex;
+  const int NX = d.NX;
+  const int EN = N * NX;  // points per element row
   // P1: us on the row lines -> Bf, ur on the column lines -> A
-  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    {
-      const int r = l % NX;
-      const int q0 = r + (l / NX) * N * NX;
-      V x[N], y[N];
+  {
+    int r = d.r0, e = d.e0, x = d.x0, c = d.c0;
+    for (int l = threadIdx.x; l < d.nl; l += d.T) {
+      {
+        const int q0 = r + e * EN;
+        V xs[N], ys[N];
 #pragma unroll
-      for (int j = 0; j < N; ++j) x[j] = ufun(q0 + j * NX);
-      eo_apply<P, N>(Ds, x, y);
+        for (int j = 0; j < N; ++j) xs[j] = ufun(q0 + j * NX);
+        eo_apply<P, N>(Ds, xs, ys);
 #pragma unroll
-      for (int j = 0; j < N; ++j) Bf[q0 + j * NX] = y[j];
-    }
-    {
-      const int b0 = (l % Ex) * N + (l / Ex) * NX;
-      V x[N], y[N];
+        for (int j = 0; j < N; ++j) Bf[q0 + j * NX] = ys[j];
+      }
+      {
+        const int b0 = x * N + c * NX;
+        V xs[N], ys[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) x[i] = ufun(b0 + i);
-      eo_apply<P, N>(Dr, x, y);
+        for (int i = 0; i < N; ++i) xs[i] = ufun(b0 + i);
+        eo_apply<P, N>(Dr, xs, ys);
 #pragma unroll
-      for (int i = 0; i < N; ++i) A[b0 + i] = y[i];
+        for (int i = 0; i < N; ++i) A[b0 + i] = ys[i];
+      }
+      tiny_step(r, e, d.dr, d.de, NX);
+      tiny_step(x, c, d.dx, d.dc, d.Ex);
     }
   }
   __syncthreads();
   // P2: row lines: wr = G11 ur + G12 us -> A, ws = G12 ur + G22 us, os = Ds' ws -> Bf
-  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const int q0 = l % NX + (l / NX) * N * NX;
-    V ws[N], os[N];
+  {
+    int r = d.r0, e = d.e0;
+    for (int l = threadIdx.x; l < d.nl; l += d.T) {
+      const int q0 = r + e * EN;
+      V ws[N], os[N];
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const int q = q0 + j * NX;
-      const V ur = A[q], us = Bf[q];
-      const V g11 = GeoT<P>::cvt(G11[q]), g12 = GeoT<P>::cvt(G12[q]), g22 = GeoT<P>::cvt(G22[q]);
-      A[q] = P::fma(g11, ur, P::mul(g12, us));
-      ws[j] = P::fma(g12, ur, P::mul(g22, us));
+      for (int j = 0; j < N; ++j) {
+        const int q = q0 + j * NX;
+        const V ur = A[q], us = Bf[q];
+        const V g11 = GeoT<P>::cvt(G11[q]), g12 = GeoT<P>::cvt(G12[q]), g22 = GeoT<P>::cvt(G22[q]);
+        A[q] = P::fma(g11, ur, P::mul(g12, us));
+        ws[j] = P::fma(g12, ur, P::mul(g22, us));
+      }
+      eo_apply<P, N>(Dst, ws, os);
+#pragma unroll
+      for (int j = 0; j < N; ++j) Bf[q0 + j * NX] = os[j];
+      tiny_step(r, e, d.dr, d.de, NX);
     }
-    eo_apply<P, N>(Dst, ws, os);
-#pragma unroll
-    for (int j = 0; j < N; ++j) Bf[q0 + j * NX] = os[j];
   }
   __syncthreads();
   // P3: column lines: res = nu (Dr' wr + os) + k B u -> A
-  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const int b0 = (l % Ex) * N + (l / Ex) * NX;
-    V x[N], y[N];
+  {
+    int x = d.x0, c = d.c0;
+    for (int l = threadIdx.x; l < d.nl; l += d.T) {
+      const int b0 = x * N + c * NX;
+      V xs[N], ys[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) x[i] = A[b0 + i];
-    eo_apply<P, N>(Drt, x, y);
+      for (int i = 0; i < N; ++i) xs[i] = A[b0 + i];
+      eo_apply<P, N>(Drt, xs, ys);
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      const int q = b0 + i;
-      V res = P::fin(P::mul(nu, P::add(y[i], Bf[q])));
-      if (Bm || P::kPrecision == SEM_F32) {
-        const V u = ufun(q);
-        if (Bm) res = P::fin(P::fma(P::mul(kk, GeoT<P>::cvt(Bm[q])), u, res));
-        if constexpr (P::kPrecision == SEM_F32) acc = __fmaf_rn(u, res, acc);
+      for (int i = 0; i < N; ++i) {
+        const int q = b0 + i;
+        V res = P::fin(P::mul(nu, P::add(ys[i], Bf[q])));
+        if (Bm || P::kPrecision == SEM_F32) {
+          const V u = ufun(q);
+          if (Bm) res = P::fin(P::fma(P::mul(kk, GeoT<P>::cvt(Bm[q])), u, res));
+          if constexpr (P::kPrecision == SEM_F32) acc = __fmaf_rn(u, res, acc);
+        }
+        A[q] = res;
       }
-      A[q] = res;
+      tiny_step(x, c, d.dx, d.dc, d.Ex);
     }
   }
   // no barrier here: the caller's next reduction (or its own barrier) orders
   // these stores before the gather reads them
 }
 
-__device__ __forceinline__ float tiny_mult_bits(unsigned char br, unsigned char bc, bool ones) {
-  if (ones) return 1.0f;
-  const int cc = ((br & L_COPY2) ? 2 : 1) * ((bc & L_COPY2) ? 2 : 1);
-  return cc == 1 ? 1.0f : (cc == 2 ? 0.5f : 0.25f);
-}
+// one local point of a row line, with what QQ', the mask and the weighted
+// dots need: its copies' rows and columns (-1: none), 1/multiplicity, and
+// whether the mask zeroes it
+struct TinyPt {
+  int q, r, c, r2, c2;
+  float mult;
+  bool zero;
+};
 
-// QQ' at local point (r, c) of an unassembled field: the sum of its copies, x
+// QQ' at a local point of an unassembled field: the sum of its copies, x
 // pairs first (as small_gather); each copy converted by cv first
 template <class T, class F>
-__device__ __forceinline__ auto tiny_gather(const T* raw, int NX, int NY, int r, int c, unsigned char br,
-                                            unsigned char bc, F&& cv) {
-  const int r2 = (int)line_partner(r, br, NX);
-  const int c2 = (int)line_partner(c, bc, NY);
-  const T* col = raw + c * NX;
-  if (c2 < 0) return r2 < 0 ? cv(col[r]) : io_add(cv(col[r]), cv(col[r2]));
-  const T* col2 = raw + c2 * NX;
-  if (r2 < 0) return io_add(cv(col[r]), cv(col2[r]));
-  return io_add(io_add(cv(col[r]), cv(col[r2])), io_add(cv(col2[r]), cv(col2[r2])));
+__device__ __forceinline__ auto tiny_gather(const T* raw, int NX, const TinyPt& p, F&& cv) {
+  const T* col = raw + p.c * NX;
+  if (p.c2 < 0) return p.r2 < 0 ? cv(col[p.r]) : io_add(cv(col[p.r]), cv(col[p.r2]));
+  const T* col2 = raw + p.c2 * NX;
+  if (p.r2 < 0) return io_add(cv(col[p.r]), cv(col2[p.r]));
+  return io_add(io_add(cv(col[p.r]), cv(col[p.r2])), io_add(cv(col2[p.r]), cv(col2[p.r2])));
 }
 
-// run f(q, r, c, row_bits, col_bits) over the points of the row lines of this
-// thread (the row line's bits are read once)
+// run f(point) over the points of this thread's row lines; the row's bits
+// are decoded once per line
 template <int N, class F>
-__device__ __forceinline__ void tiny_points(const TinyDims& pr, F&& f) {
-  const int NX = pr.NX;
-  const int nl = NX * pr.Ey;
-  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const int r = l % NX;
-    const int c0 = (l / NX) * N;
-    const unsigned char br = pr.rinfo[r];
+__device__ __forceinline__ void tiny_points(const TinyDims& d, bool ones, bool has_bc, F&& f) {
+  int r = d.r0, e = d.e0;
+  for (int l = threadIdx.x; l < d.nl; l += d.T) {
+    const unsigned char br = d.rinfo[r];
+    const int r2 = (int)line_partner(r, br, d.NX);
+    const float mr = (!ones && (br & L_COPY2)) ? 0.5f : 1.0f;
+    const bool zr = has_bc && (br & L_ZERO);
 #pragma unroll
-    for (int j = 0; j < N; ++j) f(r + (c0 + j) * NX, r, c0 + j, br, pr.cinfo[c0 + j]);
+    for (int j = 0; j < N; ++j) {
+      const int c = e * N + j;
+      const unsigned char bc = d.cinfo[c];
+      TinyPt p;
+      p.q = r + c * d.NX;
+      p.r = r;
+      p.c = c;
+      p.r2 = r2;
+      p.c2 = (int)line_partner(c, bc, d.NY);
+      p.mult = (!ones && (bc & L_COPY2)) ? 0.5f * mr : mr;
+      p.zero = zr || (has_bc && (bc & L_ZERO));
+      f(p);
+    }
+    tiny_step(r, e, d.dr, d.de, d.NX);
   }
+}
+
+// The FP64 defect-correction step of a sweep: x += x32 (FP64, global), then
+// r = b - A x with the double-float operator in the work block (free while no
+// inner solve runs), and the block maximum of |r|.  A separate function, so
+// that the double-float registers do not crowd the FP32 inner loop.  Its
+// arguments are values (no address of a caller's register variable is taken);
+// it uses reduction slot `slot`, so the caller flips its slot after the call.
+template <int N>
+__device__ __noinline__ double tiny_residual(const TinyArgs<N>& a, SmallProb* prp, TinyDims d, float* sm,
+                                             TinyLayout lay, TinyRed* redp, int slot, bool mass, bool has_bc) {
+  SmallProb& pr = *prp;
+  TinyRed& red = *redp;
+  const int L = d.NX * d.NY;
+  const float* x32 = sm + lay.x32;
+  for (int q = threadIdx.x; q < L; q += d.T) pr.x[q] += (double)x32[q];
+  __syncthreads();
+  df* DA = reinterpret_cast<df*>(sm + lay.x32);  // 2 L pairs
+  df* DB = DA + L;
+  float unused = 0.0f;
+  const df* Gdf = pr.Gdf;
+  const double* X = pr.x;
+  const df nu2 = d2df(pr.nu), k2 = d2df(pr.k);  // both inside the pair window (small_eligible)
+  tiny_apply<PDF, N, df>(d, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + L, Gdf + 2 * L,
+                         mass ? Gdf + 3 * L : nullptr, nu2, k2, a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
+  __syncthreads();
+  unsigned long long m2 = 0ull;
+  tiny_points<N>(d, true, has_bc, [&](const TinyPt& p) {
+    // each copy rounded to FP64 first, then summed in FP64 (the order of the
+    // chunked path's tile stores and fixup)
+    const double ax = tiny_gather(DA, d.NX, p, [](df v) { return df2d(v); });
+    const double v = p.zero ? 0.0 : pr.b[p.q] - ax;
+    pr.r[p.q] = v;
+    const unsigned long long bb = tiny_abs_bits(v);
+    m2 = bb > m2 ? bb : m2;
+  });
+  m2 = tiny_reduce_max64(m2, red, slot);
+  __syncthreads();  // the work block holds the FP32 vectors again
+  return __longlong_as_double((long long)m2);
 }
 
 template <int N>
@@ -284,13 +365,12 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   extern __shared__ __align__(16) float sm[];
   int slot = 0;
   const int NX = (int)pr.NX, NY = (int)pr.NY, L = NX * NY;
-  const TinyDims dm = {NX, NY, pr.Ex, pr.Ey, pr.rinfo, pr.cinfo};
   const int maxiter = pr.maxiter;
   const bool jac = pr.jacobi != 0;
   const bool mass = pr.k != 0.0;
   const bool ones = pr.mult_ones != 0;
   const bool has_bc = pr.has_bc;
-  const TinyLayout lay = tiny_layout(L, mass, jac);
+  const TinyLayout lay = tiny_layout(L, mass, jac, NX + NY);
   float* G11 = sm + lay.g11;
   float* G12 = sm + lay.g12;
   float* G22 = sm + lay.g22;
@@ -302,9 +382,27 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   float* LA = sm + lay.la;
   float* LB = sm + lay.lb;
   TinyRed& red = *reinterpret_cast<TinyRed*>(sm + lay.red);
+  unsigned char* bits = reinterpret_cast<unsigned char*>(sm + lay.bits);
   const int T = blockDim.x;
+  TinyDims dm;
+  dm.NX = NX;
+  dm.NY = NY;
+  dm.Ex = pr.Ex;
+  dm.Ey = pr.Ey;
+  dm.nl = NX * pr.Ey;
+  dm.T = T;
+  dm.r0 = (int)threadIdx.x % NX;
+  dm.e0 = (int)threadIdx.x / NX;
+  dm.dr = T % NX;
+  dm.de = T / NX;
+  dm.x0 = (int)threadIdx.x % dm.Ex;
+  dm.c0 = (int)threadIdx.x / dm.Ex;
+  dm.dx = T % dm.Ex;
+  dm.dc = T / dm.Ex;
+  dm.rinfo = bits;
+  dm.cinfo = bits + NX;
 
-  // persistent block: FP32 geometry and Jacobi inverse diagonal
+  // persistent block: FP32 geometry, Jacobi inverse diagonal, line bits
   for (int q = threadIdx.x; q < L; q += T) {
     G11[q] = pr.Gf[q];
     G12[q] = pr.Gf[L + q];
@@ -312,6 +410,7 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     if (mass) Bs[q] = pr.Gf[3 * L + q];
     if (jac) dinv[q] = pr.dinv32[q];
   }
+  for (int i = threadIdx.x; i < NX + NY; i += T) bits[i] = i < NX ? pr.rinfo[i] : pr.cinfo[i - NX];
   // x = 0, r = b (FP64, global), max|b|
   unsigned long long m0 = 0ull;
   for (int q = threadIdx.x; q < L; q += T) {
@@ -321,26 +420,25 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     const unsigned long long bb = tiny_abs_bits(v);
     m0 = bb > m0 ? bb : m0;
   }
-  m0 = tiny_reduce_max64(m0, red, slot);
+  m0 = tiny_reduce_max64(m0, red, slot);  // its barrier also publishes the staged blocks
   double rmax = __longlong_as_double((long long)m0);
   const double res0 = rmax;
   int outer = 0, total = 0;
   bool nan = rmax != rmax;
   const float nu32 = (float)pr.nu, k32 = (float)pr.k;
-  const df nu2 = d2df(pr.nu), k2 = d2df(pr.k);  // both inside the pair window (small_eligible)
   while (!(rmax <= pr.tol) && !nan && outer < pr.max_outer && total < maxiter) {
     ++outer;
     // ---- inner FP32 CG on A d = r to inner_tol * |r|_inf: x32 = 0, r32 = r, p32 = 0
     const float thresh = (float)(pr.inner_tol * rmax);
     float tl = 0.0f;
     unsigned ml = 0u;
-    tiny_points<N>(dm, [&](int q, int, int, unsigned char br, unsigned char bc) {
-      const float ri = (float)pr.r[q];
-      r32[q] = ri;
-      x32[q] = 0.0f;
-      p32[q] = 0.0f;
-      const float z = jac ? ri * dinv[q] : ri;
-      tl = __fmaf_rn(ri * tiny_mult_bits(br, bc, ones), z, tl);
+    tiny_points<N>(dm, ones, has_bc, [&](const TinyPt& p) {
+      const float ri = (float)pr.r[p.q];
+      r32[p.q] = ri;
+      x32[p.q] = 0.0f;
+      p32[p.q] = 0.0f;
+      const float z = jac ? ri * dinv[p.q] : ri;
+      tl = __fmaf_rn(ri * p.mult, z, tl);
       const unsigned bb = tiny_abs_bits(ri);
       ml = bb > ml ? bb : ml;
     });
@@ -367,16 +465,16 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
       ++total;
       float sl = 0.0f;
       unsigned mx = 0u;
-      tiny_points<N>(dm, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
-        float ap = tiny_gather(LA, NX, NY, r, c, br, bc, [](float v) { return v; });
-        if (has_bc && ((br | bc) & L_ZERO)) ap = 0.0f;
-        const float pk = pnew(q);
-        x32[q] = __fmaf_rn(af, pk, x32[q]);
-        const float ri = __fmaf_rn(-af, ap, r32[q]);
-        r32[q] = ri;
-        p32[q] = pk;
-        const float z = jac ? ri * dinv[q] : ri;
-        sl = __fmaf_rn(ri * tiny_mult_bits(br, bc, ones), z, sl);
+      tiny_points<N>(dm, ones, has_bc, [&](const TinyPt& p) {
+        float ap = tiny_gather(LA, NX, p, [](float v) { return v; });
+        if (p.zero) ap = 0.0f;
+        const float pk = pnew(p.q);
+        x32[p.q] = __fmaf_rn(af, pk, x32[p.q]);
+        const float ri = __fmaf_rn(-af, ap, r32[p.q]);
+        r32[p.q] = ri;
+        p32[p.q] = pk;
+        const float z = jac ? ri * dinv[p.q] : ri;
+        sl = __fmaf_rn(ri * p.mult, z, sl);
         const unsigned bb = tiny_abs_bits(ri);
         mx = bb > mx ? bb : mx;
       });
@@ -386,31 +484,9 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
       nin = (rin != rin) || (af != af);
       done = !(rin > thresh) || nin || total >= maxiter;
     }
-    // ---- x += x32 (FP64); r = b - A x with the double-float operator
-    for (int q = threadIdx.x; q < L; q += T) pr.x[q] += (double)x32[q];
-    __syncthreads();
-    df* DA = reinterpret_cast<df*>(sm + lay.x32);  // the work block, free now: 2 L pairs
-    df* DB = DA + L;
-    float unused = 0.0f;
-    const df* Gdf = pr.Gdf;
-    const double* X = pr.x;
-    tiny_apply<PDF, N, df>(dm, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + L, Gdf + 2 * L,
-                           mass ? Gdf + 3 * L : nullptr, nu2, k2, a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
-    __syncthreads();
-    unsigned long long m2 = 0ull;
-    tiny_points<N>(dm, [&](int q, int r, int c, unsigned char br, unsigned char bc) {
-      // each copy rounded to FP64 first, then summed in FP64 (the order of the
-      // chunked path's tile stores and fixup)
-      const double ax = tiny_gather(DA, NX, NY, r, c, br, bc, [](df v) { return df2d(v); });
-      const double v = (has_bc && ((br | bc) & L_ZERO)) ? 0.0 : pr.b[q] - ax;
-      pr.r[q] = v;
-      const unsigned long long bb = tiny_abs_bits(v);
-      m2 = bb > m2 ? bb : m2;
-    });
-    m2 = tiny_reduce_max64(m2, red, slot);
-    rmax = __longlong_as_double((long long)m2);
+    rmax = tiny_residual<N>(a, &pr, dm, sm, lay, &red, slot, mass, has_bc);
+    slot ^= 1;
     nan = rmax != rmax || nin;
-    __syncthreads();  // the work block holds the FP32 vectors again
   }
   if (threadIdx.x == 0) {
     pr.iters = total;
@@ -443,8 +519,8 @@ static void fill_eo_tiny(EOCoef<N, V>& c, const double* src, V (*cvt)(double)) {
 static float to_f32(double d) { return (float)d; }
 static df to_df(double d) { return PDF::from_double(d); }
 
-size_t tiny_smem_bytes(long long L, bool mass, bool jac) {
-  return (size_t)tiny_layout(L, mass, jac).words * 4;
+size_t tiny_smem_bytes(long long L, bool mass, bool jac, long long nbits) {
+  return (size_t)tiny_layout(L, mass, jac, nbits).words * 4;
 }
 
 template <int N>
