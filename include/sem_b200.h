@@ -326,6 +326,53 @@ int sem_batch_pcg(sem_batch_t* batch, const double* const* b, double* const* x, 
                   const int* maxiter, int precision, double inner_tol, int max_outer,
                   sem_solve_info* info, sem_stream_t stream);
 
+/* ---- batch launch configuration and its autotuner (new: no counterpart in
+ * the reference).  Problems are grouped by order n (groups in increasing n);
+ * each group is one persistent launch whose shape is its configuration:
+ * cluster_size CTAs per cluster (2, 4, 8 or 16), ctas_per_sm resident CTAs
+ * per SM asked of the register allocator (1: up to 255 registers a thread,
+ * 2: up to 128), and clusters persistent clusters (0: the group's share of
+ * the SMs in proportion to its estimated work).  The default is 8, 2, 0.
+ * n and problems are filled by sem_batch_get_config and checked by
+ * sem_batch_set_config.  The queue order (sem_batch_get_order /
+ * sem_batch_set_order) lists problem indices slot by slot; a group's slots
+ * hold its own problems, largest estimated work first by default.
+ *
+ * sem_batch_timeline returns the last sem_batch_pcg's per-problem timeline:
+ * device-clock start and end in ns from the first start, and the SM of the
+ * cluster's first CTA (-1 and zeros for problems the host solved in FP64),
+ * plus the solve's device time in ms.
+ *
+ * sem_batch_autotune solves the batch once per launch shape that fits every
+ * group (all groups alike, default cluster counts), builds each group's
+ * makespan model from the measured per-problem durations (list scheduling
+ * onto k clusters, largest first; a cluster costs cluster_size/ctas_per_sm
+ * SMs), picks per group the shape and cluster count of the smallest makespan
+ * whose SM costs fit the device, orders each group's queue by measured
+ * duration, verifies the pick with one more solve and keeps whichever
+ * measured fastest.  With cache_path, the choice is appended to that file
+ * under the batch's signature (device, arithmetic, every problem's shape,
+ * coefficients and tolerance), and a later call with the same signature
+ * loads it without solving.  runs receives the solves it made, best_ms the
+ * fastest device time measured (0 when loaded).  x receives the last solve. */
+typedef struct sem_batch_group_config {
+  int n;            /* GLL points per direction of the group's problems */
+  int problems;     /* problems in the group */
+  int cluster_size; /* CTAs per cluster: 2, 4, 8 or 16 */
+  int ctas_per_sm;  /* 1 or 2 */
+  int clusters;     /* persistent clusters; 0: work-proportional share */
+} sem_batch_group_config;
+int sem_batch_group_count(const sem_batch_t* batch);
+int sem_batch_get_config(const sem_batch_t* batch, sem_batch_group_config* cfg, int count);
+int sem_batch_set_config(sem_batch_t* batch, const sem_batch_group_config* cfg, int count);
+int sem_batch_get_order(const sem_batch_t* batch, int* order, int count);
+int sem_batch_set_order(sem_batch_t* batch, const int* order, int count);
+int sem_batch_timeline(const sem_batch_t* batch, long long* start_ns, long long* end_ns, int* sm, int count,
+                       double* total_ms);
+int sem_batch_autotune(sem_batch_t* batch, const double* const* b, double* const* x, const double* tol,
+                       const int* maxiter, int precision, double inner_tol, int max_outer, const char* cache_path,
+                       int* runs, double* best_ms, sem_stream_t stream);
+
 /* Jacobi diagonal of mask(QQ'(hlmz)) with masked entries set to 1 (new: the
  * reference has no Jacobi preconditioner; derived from src/lapl.jl:70-81) */
 int sem_jacobi_diag(sem_mesh_t* mesh, const double* nu_field, double nu, double k,

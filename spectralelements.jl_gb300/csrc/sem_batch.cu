@@ -1,24 +1,77 @@
 // Host side of the batched solver: per-problem workspace and Jacobi set-up,
 // problems grouped by polynomial order (largest estimated work first inside a
 // group), and one persistent cluster launch per order on its own stream, all
-// joined back into the caller's stream.
+// joined back into the caller's stream.  Each group's launch shape (cluster
+// size, register budget, cluster count) and problem order come from its
+// configuration, which the autotuner below chooses from measured per-problem
+// timelines.
 #include <algorithm>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <functional>
+#include <queue>
+#include <string>
 #include <vector>
 
 #include "sem_batch_kernel.cuh"
 
 namespace sem {
-int launch_batch_group_a(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s);
-int launch_batch_group_b(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s);
-int launch_batch_group_c(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s);
+#define SEM_BATCH_UNIT(u)                                                                  \
+  int launch_batch_##u(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s); \
+  int max_clusters_##u(int n, int csize);
+SEM_BATCH_UNIT(ka)
+SEM_BATCH_UNIT(kb)
+SEM_BATCH_UNIT(kc)
+SEM_BATCH_UNIT(kd)
+SEM_BATCH_UNIT(ke)
+SEM_BATCH_UNIT(kf)
+#undef SEM_BATCH_UNIT
 int batch_diag(sem_mesh* m, double nu, double k, double* dinv, double* tmp, cudaStream_t s);
 
 namespace {
+// the translation unit of order n at register budget c.ctas_per_sm
 int launch_group(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
-  if (n <= 6) return launch_batch_group_a(n, c, ops, s);
-  if (n <= 9) return launch_batch_group_b(n, c, ops, s);
-  return launch_batch_group_c(n, c, ops, s);
+  if (c.ctas_per_sm != 1 && c.ctas_per_sm != 2)
+    return set_error(SEM_ERR_BAD_ARG, "batch CTAs per SM %d (1 or 2)", c.ctas_per_sm);
+  const bool two = c.ctas_per_sm == 2;
+  if (n <= 6) return two ? launch_batch_ka(n, c, ops, s) : launch_batch_kd(n, c, ops, s);
+  if (n <= 9) return two ? launch_batch_kb(n, c, ops, s) : launch_batch_ke(n, c, ops, s);
+  return two ? launch_batch_kc(n, c, ops, s) : launch_batch_kf(n, c, ops, s);
+}
+
+// clusters of the given shape that fit the device at once (0: none)
+int max_clusters(int n, int csize, int mb) {
+  if (mb != 1 && mb != 2) return 0;
+  const bool two = mb == 2;
+  if (n <= 6) return two ? max_clusters_ka(n, csize) : max_clusters_kd(n, csize);
+  if (n <= 9) return two ? max_clusters_kb(n, csize) : max_clusters_ke(n, csize);
+  return two ? max_clusters_kc(n, csize) : max_clusters_kf(n, csize);
+}
+
+// makespan of list-scheduling durations d (queue order) onto k identical
+// clusters: each problem goes to the cluster that frees first
+double list_makespan(const std::vector<double>& d, int k) {
+  if (d.empty()) return 0.0;
+  std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+  for (int i = 0; i < std::max(1, k); ++i) free_at.push(0.0);
+  double end = 0.0;
+  for (double x : d) {
+    const double t = free_at.top() + x;
+    free_at.pop();
+    free_at.push(t);
+    end = std::max(end, t);
+  }
+  return end;
+}
+
+// FNV-1a over the bytes of a value
+void fnv(unsigned long long& h, const void* p, size_t n) {
+  const unsigned char* c = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= c[i];
+    h *= 1099511628211ull;
+  }
 }
 
 __global__ void k_d2f_copy(const double* __restrict__ a, float* __restrict__ b, long long len) {
@@ -41,6 +94,9 @@ struct sem_batch {
     const OperatorSet* ops;
     cudaStream_t stream;
     cudaEvent_t done;
+    // launch configuration: CTAs per cluster, resident CTAs per SM (register
+    // budget), persistent clusters (0: the work-proportional share)
+    int csize, mb, clusters;
   };
   int count = 0;
   int device = 0;
@@ -53,6 +109,11 @@ struct sem_batch {
   int* queues = nullptr;    // one work-queue counter per group
   void* ws = nullptr;       // all per-problem vectors
   cudaEvent_t start = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;  // timing of the last solve
+  // timeline of the last solve, per problem in creation order
+  std::vector<long long> t_start, t_end;
+  std::vector<int> sm;
+  double last_ms = 0.0;
 };
 
 extern "C" {
@@ -91,6 +152,8 @@ int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* 
   if (e == cudaSuccess) e = cudaMalloc(&b->dev, sizeof(BProb) * count);
   if (e == cudaSuccess) e = cudaMalloc(&b->queues, sizeof(int) * (kBatchMaxN + 1));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
   if (e != cudaSuccess) {
     sem_batch_destroy(b);
     return cuda_error(e, "batch allocation");
@@ -164,6 +227,9 @@ int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* 
                      [&](int x, int y) { return work_of(b->host[x]) > work_of(b->host[y]); });
     gr.stream = nullptr;
     gr.done = nullptr;
+    gr.csize = 8;
+    gr.mb = 2;
+    gr.clusters = 0;
     if ((e = cudaStreamCreateWithFlags(&gr.stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&gr.done, cudaEventDisableTiming)) != cudaSuccess) {
       b->groups.push_back(gr);
@@ -183,6 +249,8 @@ int sem_batch_destroy(sem_batch_t* b) {
     if (g.done) cudaEventDestroy(g.done);
   }
   if (b->start) cudaEventDestroy(b->start);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
   if (b->ws) cudaFree(b->ws);
   if (b->dev) cudaFree(b->dev);
   if (b->queues) cudaFree(b->queues);
@@ -215,11 +283,11 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   SEM_CUDA(cudaMemcpyAsync(b->dev, q.data(), sizeof(BProb) * b->count, cudaMemcpyHostToDevice, s));
   SEM_CUDA(cudaMemsetAsync(b->queues, 0, sizeof(int) * (kBatchMaxN + 1), s));
   SEM_CUDA(cudaEventRecord(b->start, s));
+  SEM_CUDA(cudaEventRecord(b->t0, s));
   double wtot = 0.0;
   for (auto& g : b->groups) wtot += g.work;
   int sms = 0;
   SEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-  const int budget = std::max(1, sms * kBatchCtasPerSm / kCluster);  // resident clusters
   for (size_t gi = 0; gi < b->groups.size(); ++gi) {
     auto& g = b->groups[gi];
     BatchCommon c;
@@ -231,16 +299,42 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     const bool rr = precision == SEM_MIXED_RR;
     c.inner_tol = inner_tol > 0 ? inner_tol : (rr ? 0.3 : 1e-4);
     c.max_outer = max_outer > 0 ? max_outer : (rr ? 100 : 6);
-    c.clusters = b->groups.size() == 1 ? 0 : std::max(1, (int)(budget * g.work / wtot + 0.5));
+    c.cluster_size = g.csize;
+    c.ctas_per_sm = g.mb;
+    // default share: the group's fraction of the estimated work, in SMs
+    c.clusters = g.clusters > 0 ? g.clusters
+                 : b->groups.size() == 1 ? 0
+                 : std::max(1, (int)(sms * g.work / wtot * g.mb / g.csize + 0.5));
     SEM_CUDA(cudaStreamWaitEvent(g.stream, b->start, 0));
     SEM_CHECK(launch_group(g.n, c, *g.ops, g.stream));
     SEM_CUDA(cudaEventRecord(g.done, g.stream));
     SEM_CUDA(cudaStreamWaitEvent(s, g.done, 0));
   }
+  SEM_CUDA(cudaEventRecord(b->t1, s));
   std::vector<int> wanted(b->count);
   for (int j = 0; j < b->count; ++j) wanted[j] = q[j].maxiter;
   SEM_CUDA(cudaMemcpyAsync(q.data(), b->dev, sizeof(BProb) * b->count, cudaMemcpyDeviceToHost, s));
   SEM_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  SEM_CUDA(cudaEventElapsedTime(&ms, b->t0, b->t1));
+  b->last_ms = ms;
+  b->t_start.assign(b->count, 0);
+  b->t_end.assign(b->count, 0);
+  b->sm.assign(b->count, -1);
+  long long tmin = 0;
+  bool any = false;
+  for (int j = 0; j < b->count; ++j)
+    if (q[j].maxiter >= 0 && (!any || q[j].t_start < tmin)) {
+      tmin = q[j].t_start;
+      any = true;
+    }
+  for (int j = 0; j < b->count; ++j) {
+    const int i = b->order[j];
+    if (q[j].maxiter < 0) continue;  // left to the host's FP64 solve
+    b->t_start[i] = q[j].t_start - tmin;
+    b->t_end[i] = q[j].t_end - tmin;
+    b->sm[i] = q[j].sm;
+  }
   int bad = 0, nanc = 0;
   for (int j = 0; j < b->count; ++j) {
     const int i = b->order[j];
@@ -281,6 +375,287 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   }
   if (nanc) return set_error(SEM_ERR_NAN, "%d of %d problems hit NaN/Inf", nanc, b->count);
   if (bad) return set_error(SEM_ERR_NOT_CONVERGED, "%d of %d problems reached maxiter", bad, b->count);
+  return SEM_OK;
+}
+
+int sem_batch_group_count(const sem_batch_t* b) { return b ? (int)b->groups.size() : 0; }
+
+int sem_batch_get_config(const sem_batch_t* b, sem_batch_group_config* cfg, int count) {
+  if (!b || !cfg || count < (int)b->groups.size()) return set_error(SEM_ERR_BAD_ARG, "bad batch config arguments");
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    const auto& g = b->groups[gi];
+    cfg[gi].n = g.n;
+    cfg[gi].problems = g.count;
+    cfg[gi].cluster_size = g.csize;
+    cfg[gi].ctas_per_sm = g.mb;
+    cfg[gi].clusters = g.clusters;
+  }
+  return SEM_OK;
+}
+
+int sem_batch_set_config(sem_batch_t* b, const sem_batch_group_config* cfg, int count) {
+  if (!b || !cfg || count != (int)b->groups.size()) return set_error(SEM_ERR_BAD_ARG, "one config per group");
+  for (int gi = 0; gi < count; ++gi) {
+    const auto& c = cfg[gi];
+    if (c.n != b->groups[gi].n) return set_error(SEM_ERR_BAD_ARG, "config %d is for n = %d, the group has n = %d", gi, c.n, b->groups[gi].n);
+    if (c.cluster_size != 2 && c.cluster_size != 4 && c.cluster_size != 8 && c.cluster_size != 16)
+      return set_error(SEM_ERR_BAD_ARG, "cluster size %d (2, 4, 8 or 16)", c.cluster_size);
+    if (c.ctas_per_sm != 1 && c.ctas_per_sm != 2) return set_error(SEM_ERR_BAD_ARG, "CTAs per SM %d (1 or 2)", c.ctas_per_sm);
+    if (c.clusters < 0) return set_error(SEM_ERR_BAD_ARG, "negative cluster count");
+    const int fit = max_clusters(c.n, c.cluster_size, c.ctas_per_sm);
+    if (fit < 1) return set_error(SEM_ERR_UNSUPPORTED, "clusters of %d CTAs (%d per SM) do not fit for n = %d", c.cluster_size, c.ctas_per_sm, c.n);
+  }
+  for (int gi = 0; gi < count; ++gi) {
+    auto& g = b->groups[gi];
+    g.csize = cfg[gi].cluster_size;
+    g.mb = cfg[gi].ctas_per_sm;
+    g.clusters = cfg[gi].clusters;
+  }
+  return SEM_OK;
+}
+
+int sem_batch_get_order(const sem_batch_t* b, int* order, int count) {
+  if (!b || !order || count != b->count) return set_error(SEM_ERR_BAD_ARG, "order takes one entry per problem");
+  std::memcpy(order, b->order.data(), sizeof(int) * b->count);
+  return SEM_OK;
+}
+
+int sem_batch_set_order(sem_batch_t* b, const int* order, int count) {
+  if (!b || !order || count != b->count) return set_error(SEM_ERR_BAD_ARG, "order takes one entry per problem");
+  // a permutation that keeps every group's problems in the group's slots
+  std::vector<char> seen(b->count, 0);
+  for (const auto& g : b->groups)
+    for (int j = g.first; j < g.first + g.count; ++j) {
+      const int i = order[j];
+      if (i < 0 || i >= b->count || seen[i] || b->host[i].n != g.n)
+        return set_error(SEM_ERR_BAD_ARG, "order[%d] = %d is not a problem of order n = %d", j, i, g.n);
+      seen[i] = 1;
+    }
+  b->order.assign(order, order + count);
+  return SEM_OK;
+}
+
+int sem_batch_timeline(const sem_batch_t* b, long long* start_ns, long long* end_ns, int* sm, int count,
+                       double* total_ms) {
+  if (!b || count != b->count) return set_error(SEM_ERR_BAD_ARG, "the timeline has one entry per problem");
+  if (b->t_start.empty()) return set_error(SEM_ERR_BAD_ARG, "no solve has run on this batch");
+  for (int i = 0; i < count; ++i) {
+    if (start_ns) start_ns[i] = b->t_start[i];
+    if (end_ns) end_ns[i] = b->t_end[i];
+    if (sm) sm[i] = b->sm[i];
+  }
+  if (total_ms) *total_ms = b->last_ms;
+  return SEM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// the batch's signature: device, arithmetic and every problem's shape,
+// coefficients and tolerance
+unsigned long long batch_signature(const sem_batch* b, const double* tol, const int* maxiter, int precision,
+                                   double inner_tol, int max_outer) {
+  unsigned long long h = 1469598103934665603ull;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  fnv(h, &sms, sizeof(sms));
+  fnv(h, &precision, sizeof(precision));
+  fnv(h, &inner_tol, sizeof(inner_tol));
+  fnv(h, &max_outer, sizeof(max_outer));
+  fnv(h, &b->jacobi, sizeof(b->jacobi));
+  for (int i = 0; i < b->count; ++i) {
+    const BProb& q = b->host[i];
+    fnv(h, &q.n, sizeof(q.n));
+    fnv(h, &q.Ex, sizeof(q.Ex));
+    fnv(h, &q.Ey, sizeof(q.Ey));
+    fnv(h, &q.topo, sizeof(q.topo));
+    fnv(h, &q.nu, sizeof(q.nu));
+    fnv(h, &q.k, sizeof(q.k));
+    fnv(h, &tol[i], sizeof(double));
+    const int mi = maxiter ? maxiter[i] : 0;
+    fnv(h, &mi, sizeof(mi));
+  }
+  return h;
+}
+
+// cache file: one line per signature,
+//   <hex signature> <groups> {n csize mb clusters}... <count> order...
+bool load_tuned(sem_batch* b, const char* path, unsigned long long sig) {
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  bool found = false;
+  std::vector<sem_batch_group_config> cfg;
+  std::vector<int> order;
+  char hex[32];
+  while (std::fscanf(f, "%31s", hex) == 1) {
+    unsigned long long s = std::strtoull(hex, nullptr, 16);
+    int ng = 0;
+    if (std::fscanf(f, "%d", &ng) != 1 || ng < 0 || ng > 64) break;
+    std::vector<sem_batch_group_config> c(ng);
+    bool ok = true;
+    for (int gi = 0; gi < ng && ok; ++gi) {
+      ok = std::fscanf(f, "%d %d %d %d", &c[gi].n, &c[gi].cluster_size, &c[gi].ctas_per_sm, &c[gi].clusters) == 4;
+      c[gi].problems = 0;
+    }
+    int cnt = 0;
+    ok = ok && std::fscanf(f, "%d", &cnt) == 1 && cnt >= 0 && cnt <= (1 << 24);
+    if (!ok) break;
+    std::vector<int> o(cnt);
+    for (int j = 0; j < cnt && ok; ++j) ok = std::fscanf(f, "%d", &o[j]) == 1;
+    if (!ok) break;
+    if (s == sig && ng == (int)b->groups.size() && cnt == b->count) {
+      found = true;
+      cfg = c;
+      order = o;
+    }
+  }
+  std::fclose(f);
+  if (!found) return false;
+  for (int gi = 0; gi < (int)cfg.size(); ++gi) cfg[gi].problems = b->groups[gi].count;
+  if (sem_batch_set_config(b, cfg.data(), (int)cfg.size()) != SEM_OK) return false;
+  return sem_batch_set_order(b, order.data(), (int)order.size()) == SEM_OK;
+}
+
+void store_tuned(const sem_batch* b, const char* path, unsigned long long sig) {
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%016llx %d", sig, (int)b->groups.size());
+  for (const auto& g : b->groups) std::fprintf(f, " %d %d %d %d", g.n, g.csize, g.mb, g.clusters);
+  std::fprintf(f, " %d", b->count);
+  for (int i : b->order) std::fprintf(f, " %d", i);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* x, const double* tol,
+                       const int* maxiter, int precision, double inner_tol, int max_outer, const char* cache_path,
+                       int* runs_out, double* best_ms, sem_stream_t stream) {
+  if (!b || !rhs || !x || !tol) return set_error(SEM_ERR_BAD_ARG, "NULL argument");
+  if (runs_out) *runs_out = 0;
+  const unsigned long long sig = batch_signature(b, tol, maxiter, precision, inner_tol, max_outer);
+  if (cache_path && load_tuned(b, cache_path, sig)) {
+    if (best_ms) *best_ms = 0.0;
+    return SEM_OK;
+  }
+  int sms = 0;
+  SEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+  const int G = (int)b->groups.size();
+  // ---- measure every launch shape that fits every group, all groups alike,
+  // with the default (work-proportional) cluster counts and the estimated order
+  struct Opt {
+    int csize, mb;
+  };
+  const Opt cand[] = {{8, 2}, {4, 2}, {16, 2}, {2, 2}, {8, 1}, {4, 1}, {16, 1}};
+  const std::vector<int> order0 = b->order;
+  std::vector<Opt> opts;
+  std::vector<double> wall;
+  std::vector<std::vector<double>> dur;  // per option, per problem (creation order), ns
+  int runs = 0;
+  for (const Opt& o : cand) {
+    bool fits = true;
+    for (const auto& g : b->groups) fits = fits && max_clusters(g.n, o.csize, o.mb) > 0;
+    if (!fits) continue;
+    for (auto& g : b->groups) {
+      g.csize = o.csize;
+      g.mb = o.mb;
+      g.clusters = 0;
+    }
+    b->order = order0;
+    const int st = sem_batch_pcg(b, rhs, x, tol, maxiter, precision, inner_tol, max_outer, nullptr, stream);
+    ++runs;
+    if (st != SEM_OK && st != SEM_ERR_NOT_CONVERGED && st != SEM_ERR_NAN) return st;
+    opts.push_back(o);
+    wall.push_back(b->last_ms);
+    std::vector<double> d(b->count);
+    for (int i = 0; i < b->count; ++i) d[i] = (double)(b->t_end[i] - b->t_start[i]);
+    dur.push_back(d);
+  }
+  if (opts.empty()) return set_error(SEM_ERR_UNSUPPORTED, "no batch launch shape fits");
+  // ---- model: per group and shape, the makespan of k clusters under list
+  // scheduling of the measured durations, largest first; the SM cost of a
+  // cluster is csize / mb.  The smallest makespan T whose cheapest per-group
+  // choices fit the SMs wins.
+  struct Choice {
+    double T, cost;
+    int opt, k;
+  };
+  std::vector<std::vector<Choice>> ch(G);
+  std::vector<double> Ts;
+  for (int gi = 0; gi < G; ++gi) {
+    const auto& g = b->groups[gi];
+    for (size_t oi = 0; oi < opts.size(); ++oi) {
+      std::vector<double> d;
+      for (int j = g.first; j < g.first + g.count; ++j) d.push_back(dur[oi][b->order[j]]);
+      std::sort(d.begin(), d.end(), std::greater<double>());
+      const int kmax = std::min(g.count, max_clusters(g.n, opts[oi].csize, opts[oi].mb));
+      for (int k = 1; k <= kmax; ++k) {
+        const double T = list_makespan(d, k);
+        ch[gi].push_back({T, (double)k * opts[oi].csize / opts[oi].mb, (int)oi, k});
+        Ts.push_back(T);
+      }
+    }
+  }
+  std::sort(Ts.begin(), Ts.end());
+  std::vector<Choice> pick(G);
+  bool feasible = false;
+  for (double T : Ts) {
+    double total = 0.0;
+    for (int gi = 0; gi < G; ++gi) {
+      const Choice* best = nullptr;
+      for (const Choice& c : ch[gi])
+        if (c.T <= T && (!best || c.cost < best->cost)) best = &c;
+      if (!best) {
+        total = 1e300;
+        break;
+      }
+      pick[gi] = *best;
+      total += best->cost;
+    }
+    if (total <= (double)sms) {
+      feasible = true;
+      break;
+    }
+  }
+  // ---- verify the model's choice against the best measured shape
+  size_t best_uniform = 0;
+  for (size_t oi = 1; oi < opts.size(); ++oi)
+    if (wall[oi] < wall[best_uniform]) best_uniform = oi;
+  double best = wall[best_uniform];
+  std::vector<sem_batch_group_config> keep(G);
+  std::vector<int> keep_order = order0;
+  for (int gi = 0; gi < G; ++gi) keep[gi] = {b->groups[gi].n, b->groups[gi].count, opts[best_uniform].csize, opts[best_uniform].mb, 0};
+  if (feasible) {
+    std::vector<int> ord = order0;
+    for (int gi = 0; gi < G; ++gi) {
+      const auto& g = b->groups[gi];
+      const auto& d = dur[pick[gi].opt];
+      std::stable_sort(ord.begin() + g.first, ord.begin() + g.first + g.count, [&](int p, int q) { return d[p] > d[q]; });
+      auto& gg = b->groups[gi];
+      gg.csize = opts[pick[gi].opt].csize;
+      gg.mb = opts[pick[gi].opt].mb;
+      gg.clusters = G == 1 ? 0 : pick[gi].k;
+    }
+    b->order = ord;
+    const int st = sem_batch_pcg(b, rhs, x, tol, maxiter, precision, inner_tol, max_outer, nullptr, stream);
+    ++runs;
+    if (st != SEM_OK && st != SEM_ERR_NOT_CONVERGED && st != SEM_ERR_NAN) return st;
+    if (b->last_ms < best) {
+      best = b->last_ms;
+      keep_order = ord;
+      for (int gi = 0; gi < G; ++gi)
+        keep[gi] = {b->groups[gi].n, b->groups[gi].count, b->groups[gi].csize, b->groups[gi].mb, b->groups[gi].clusters};
+    }
+  }
+  SEM_CHECK(sem_batch_set_config(b, keep.data(), G));
+  b->order = keep_order;
+  if (cache_path) store_tuned(b, cache_path, sig);
+  if (runs_out) *runs_out = runs;
+  if (best_ms) *best_ms = best;
   return SEM_OK;
 }
 

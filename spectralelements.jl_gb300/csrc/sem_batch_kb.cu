@@ -1,13 +1,9 @@
-// Persistent batched-PCG kernels for n = 7, 8, 9 (one template instance per order).
+// Persistent batched-PCG kernels for n = 7, 8, 9, two resident CTAs per SM (up to 128 registers a thread).
 #include "sem_batch_kernel.cuh"
 
 namespace sem {
-int launch_batch_group_b(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
-  switch (n) {
-    case 7: return launch_batch_order<7>(c, ops, s);
-    case 8: return launch_batch_order<8>(c, ops, s);
-    case 9: return launch_batch_order<9>(c, ops, s);
-    default: return set_error(SEM_ERR_UNSUPPORTED, "batch order %d not in this group", n);
-  }
+int launch_batch_kb(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
+  return launch_batch_range<7, 9, 2>(n, c, ops, s);
 }
+int max_clusters_kb(int n, int csize) { return max_clusters_range<7, 9, 2>(n, csize); }
 }  // namespace sem

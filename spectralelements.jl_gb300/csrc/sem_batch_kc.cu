@@ -1,12 +1,9 @@
-// Persistent batched-PCG kernels for n = 10, 11 (one template instance per order).
+// Persistent batched-PCG kernels for n = 10, 11, two resident CTAs per SM (up to 128 registers a thread).
 #include "sem_batch_kernel.cuh"
 
 namespace sem {
-int launch_batch_group_c(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
-  switch (n) {
-    case 10: return launch_batch_order<10>(c, ops, s);
-    case 11: return launch_batch_order<11>(c, ops, s);
-    default: return set_error(SEM_ERR_UNSUPPORTED, "batch order %d not in this group", n);
-  }
+int launch_batch_kc(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
+  return launch_batch_range<10, 11, 2>(n, c, ops, s);
 }
+int max_clusters_kc(int n, int csize) { return max_clusters_range<10, 11, 2>(n, csize); }
 }  // namespace sem

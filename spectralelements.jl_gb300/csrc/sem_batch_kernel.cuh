@@ -3,11 +3,11 @@
 // polynomial order (each with the register budget of its order), all running
 // concurrently.
 //
-// Each cluster (kCluster CTAs of kBT threads) takes problems from a device
+// Each cluster (C CTAs of kBT threads; C chosen per launch) takes problems from a device
 // work queue (problems sorted by estimated work, largest first) and runs the
 // whole CG loop of src/pcg.jl:16-60 for one problem before taking the next.
 // Inside a problem the cluster's CTAs share the element tiles (tile t goes to
-// CTA t mod kCluster) and every pointwise vector operation runs on the points
+// CTA t mod C) and every pointwise vector operation runs on the points
 // of the CTA's own tiles, so one iteration needs three cluster barriers:
 //
 //   apply   own tiles: p = dinv.*r + beta p fused into the element operator,
@@ -36,9 +36,26 @@ namespace cg = cooperative_groups;
 namespace sem {
 
 constexpr int kBT = 256;             // threads per CTA
-constexpr int kCluster = 8;          // CTAs per cluster (portable size)
 constexpr int kBatchMaxN = 11;       // GLL points per direction served by the batch kernel
-constexpr int kBatchCtasPerSm = 2;   // resident CTAs per SM asked of the register allocator
+
+// CTAs of this CTA's cluster (the launch's cluster size: 2, 4, 8 or 16)
+__device__ __forceinline__ int bcsize() {
+  unsigned v;
+  asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(v));
+  return (int)v;
+}
+
+__device__ __forceinline__ long long bclock_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return (long long)t;
+}
+
+__device__ __forceinline__ int bsmid() {
+  unsigned v;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(v));
+  return (int)v;
+}
 
 template <int N>
 struct BTile {  // element tile of the batch kernel: TX*TY*N <= kBT
@@ -68,6 +85,10 @@ struct BProb {
   // results
   int iters, outer, converged, nan;
   double res_inf, res0_inf;
+  // timeline: device clock (ns) when the cluster took the problem and when it
+  // finished it, and the SM of the cluster's rank 0
+  long long t_start, t_end;
+  int sm;
 };
 
 // launch description shared by the per-order kernels
@@ -79,7 +100,9 @@ struct BatchCommon {
   int jacobi;
   double inner_tol;
   int max_outer;
-  int clusters;  // <= 0: as many as fit
+  int clusters;      // <= 0: as many as fit
+  int cluster_size;  // CTAs per cluster: 2, 4, 8 or 16
+  int ctas_per_sm;   // register budget of the kernel: 1 or 2 resident CTAs per SM
 };
 
 template <int N>
@@ -219,16 +242,17 @@ __device__ __forceinline__ void cluster_reduce(cg::cluster_group& cl, BRed& sh, 
   // warp 0 combines the ranks' parts in rank order and shares the result
   // through shared memory (identical in every CTA)
   if (threadIdx.x == 0) {
+    const int csz = bcsize();
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
       df x = *cl.map_shared_rank(&sh.slot_s[slot][q], 0);
-      for (int rk = 1; rk < kCluster; ++rk) x = df_add(x, *cl.map_shared_rank(&sh.slot_s[slot][q], rk));
+      for (int rk = 1; rk < csz; ++rk) x = df_add(x, *cl.map_shared_rank(&sh.slot_s[slot][q], rk));
       sh.res_s[q] = x;
     }
 #pragma unroll
     for (int q = 0; q < NM; ++q) {
       unsigned long long x = *cl.map_shared_rank(&sh.slot_m[slot][q], 0);
-      for (int rk = 1; rk < kCluster; ++rk) {
+      for (int rk = 1; rk < csz; ++rk) {
         const unsigned long long y = *cl.map_shared_rank(&sh.slot_m[slot][q], rk);
         x = y > x ? y : x;
       }
@@ -384,7 +408,7 @@ __device__ __noinline__ void bfixup(const BProb& pr, int n, IO* __restrict__ Ap,
   const long long first = (long long)rank * kBT + threadIdx.x;
   const unsigned un = (unsigned)n;
   for (long long q = 0; q < nI; ++q)
-    fix_interface(Ap, f, q, first, (long long)kCluster * kBT, [&](long long r, long long c, IO v) {
+    fix_interface(Ap, f, q, first, (long long)bcsize() * kBT, [&](long long r, long long c, IO v) {
       const int ex = (int)((unsigned)r / un), ey = (int)((unsigned)c / un);
       const int cc = bcopies(ex, (int)r - ex * n, n, pr.Ex, perx) * bcopies(ey, (int)c - ey * n, n, pr.Ey, pery);
       acc.prod(p[r + c * pr.NX], v, bmult(cc));
@@ -400,7 +424,7 @@ __device__ __forceinline__ void own_points(const BProb& pr, int rank, F&& f) {
   const int elem = t / N, lane = t - elem * N;
   const int exl = elem % TX, eyl = elem / TX;
   const bool perx = (pr.topo & M_PERX) != 0, pery = (pr.topo & M_PERY) != 0;
-  for (int tile = rank; tile < ntx * nty; tile += kCluster) {
+  for (int tile = rank, csz = bcsize(); tile < ntx * nty; tile += csz) {
     const int by = tile / ntx, bx = tile - by * ntx;
     const int ex = bx * TX + exl, ey = by * TY + eyl;
     if (ex >= pr.Ex || ey >= pr.Ey) continue;
@@ -476,7 +500,7 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
   while (!done) {
     const double beta = k == 0 ? 0.0 : t / tprev;
     BAcc<IO> dot;
-    for (int tile = rank; tile < ntx * nty; tile += kCluster) {
+    for (int tile = rank, csz = bcsize(); tile < ntx * nty; tile += csz) {
       const int by = tile / ntx, bx = tile - by * ntx;
       btile<P, N, T::TX, T::TY>(pr, D, bx, by, nullptr, r, dinv, (IO)beta, p, true, Ap, Geo, L,
                                 buf.template s0<P>(), buf.template s1<P>(), buf.template x0<P>(), dot);
@@ -522,7 +546,7 @@ __device__ double bresidual(const BatchArgs<N>& a, BProb& pr, cg::cluster_group&
   const long long L = pr.NX * pr.NY;
   const int ntx = (pr.Ex + T::TX - 1) / T::TX, nty = (pr.Ey + T::TY - 1) / T::TY;
   BAcc<double> unused;
-  for (int tile = rank; tile < ntx * nty; tile += kCluster) {
+  for (int tile = rank, csz = bcsize(); tile < ntx * nty; tile += csz) {
     const int by = tile / ntx, bx = tile - by * ntx;
     btile<PDF, N, T::TX, T::TY>(pr, a.cdf, bx, by, pr.x, nullptr, nullptr, 0.0, nullptr, false, pr.Ap,
                                 pr.Gdf, L, buf.S0, buf.S1, buf.X0, unused);
@@ -592,7 +616,7 @@ __device__ void brr(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
   while (!done) {
     const float beta = k == 0 ? 0.0f : (float)(t / tprev);
     BAcc<float> dot;
-    for (int tile = rank; tile < ntx * nty; tile += kCluster) {
+    for (int tile = rank, csz = bcsize(); tile < ntx * nty; tile += csz) {
       const int by = tile / ntx, bx = tile - by * ntx;
       btile<PF32, N, T::TX, T::TY>(pr, a.cf, bx, by, nullptr, pr.r32, dinv32, beta, pr.p32, true, pr.Ap32,
                                    pr.G11f, L, buf.template s0<PF32>(), buf.template s1<PF32>(),
@@ -722,9 +746,12 @@ __device__ void bsolve(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, 
   }
 }
 
-template <int N>
-__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kBT, kBatchCtasPerSm)
-    k_batch_pcg(const __grid_constant__ BatchArgs<N> a) {
+// The persistent kernel: clusters take problems from the group's queue until
+// it runs dry.  MB: resident CTAs per SM asked of the register allocator (1:
+// up to 255 registers a thread, 2: up to 128); the cluster size is the
+// launch's.
+template <int N, int MB>
+__global__ void __launch_bounds__(kBT, MB) k_batch_pcg(const __grid_constant__ BatchArgs<N> a) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   extern __shared__ __align__(16) unsigned char smem[];
@@ -738,15 +765,19 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kBT, kBatchCt
     const int pid = *cl.map_shared_rank(&s_pid, 0);
     cl.sync();  // every CTA has read s_pid before rank 0 may overwrite it
     if (pid >= a.count) return;
-    bsolve<N>(a, a.probs[pid], cl, rank, red, rc, buf);
+    BProb& pr = a.probs[pid];
+    if (rank == 0 && threadIdx.x == 0) {
+      pr.t_start = bclock_ns();
+      pr.sm = bsmid();
+    }
+    bsolve<N>(a, pr, cl, rank, red, rc, buf);
     cl.sync();  // the problem's results are written before the next one starts
+    if (rank == 0 && threadIdx.x == 0) pr.t_end = bclock_ns();
   }
 }
 
-// host: launch the persistent kernel of order N over `count` problems
 template <int N>
-int launch_batch_order(const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
-  BatchArgs<N> a;
+static void fill_batch_args(BatchArgs<N>& a, const BatchCommon& c, const OperatorSet& ops) {
   std::memset(&a, 0, sizeof(a));
   a.probs = c.probs;
   a.count = c.count;
@@ -776,23 +807,94 @@ int launch_batch_order(const BatchCommon& c, const OperatorSet& ops, cudaStream_
       a.cf[b].mr[i] = (float)mr[i];
     }
   }
-  typedef BTile<N> T;
-  const size_t smem = (size_t)T::SLOTS * T::ES * (2 * sizeof(df) + sizeof(double));
-  SEM_CUDA(cudaFuncSetAttribute(k_batch_pcg<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int nclusters = c.clusters;
-  if (nclusters <= 0) {
-    cudaLaunchConfig_t cfg;
-    std::memset(&cfg, 0, sizeof(cfg));
-    cfg.blockDim = dim3(kBT);
-    cfg.gridDim = dim3(kCluster * 64);
-    cfg.dynamicSmemBytes = smem;
-    SEM_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, k_batch_pcg<N>, &cfg));
-  }
-  if (nclusters < 1) nclusters = 1;
-  if (nclusters > c.count) nclusters = c.count;
-  k_batch_pcg<N><<<dim3(kCluster * nclusters), dim3(kBT), smem, s>>>(a);
-  SEM_CUDA(cudaGetLastError());
+}
+
+template <int N>
+constexpr size_t batch_smem_bytes() {
+  return (size_t)BTile<N>::SLOTS * BTile<N>::ES * (2 * sizeof(df) + sizeof(double));
+}
+
+// the launch configuration of one group: cluster size and register budget
+template <int N, int MB>
+static void batch_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* at, int csize, int nclusters,
+                         cudaStream_t s) {
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)(csize * nclusters));
+  cfg.blockDim = dim3(kBT);
+  cfg.dynamicSmemBytes = batch_smem_bytes<N>();
+  cfg.stream = s;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+}
+
+template <int N, int MB>
+static int prepare_batch_kernel() {
+  auto kern = k_batch_pcg<N, MB>;
+  SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem_bytes<N>()));
+  SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   return SEM_OK;
+}
+
+// clusters of the given shape that fit the device at once (0: the shape does not launch)
+template <int N, int MB>
+static int batch_max_clusters_mb(int csize) {
+  if ((prepare_batch_kernel<N, MB>()) != SEM_OK) return 0;
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[1];
+  batch_config<N, MB>(cfg, at, csize, 64, nullptr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_batch_pcg<N, MB>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+// host: launch the persistent kernel of order N over `count` problems
+template <int N, int MB>
+static int launch_batch_mb(const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
+  BatchArgs<N> a;
+  fill_batch_args<N>(a, c, ops);
+  SEM_CHECK((prepare_batch_kernel<N, MB>()));
+  int nclusters = c.clusters;
+  if (nclusters <= 0) nclusters = batch_max_clusters_mb<N, MB>(c.cluster_size);
+  if (nclusters < 1) return set_error(SEM_ERR_UNSUPPORTED, "a cluster of %d CTAs does not fit (n = %d)", c.cluster_size, N);
+  if (nclusters > c.count) nclusters = c.count;
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[1];
+  batch_config<N, MB>(cfg, at, c.cluster_size, nclusters, s);
+  SEM_CUDA(cudaLaunchKernelEx(&cfg, k_batch_pcg<N, MB>, a));
+  return SEM_OK;
+}
+
+// the orders LO..HI at one register budget (one translation unit each)
+template <int LO, int HI, int MB>
+int launch_batch_range(int n, const BatchCommon& c, const OperatorSet& ops, cudaStream_t s) {
+  if constexpr (LO > HI) {
+    return set_error(SEM_ERR_UNSUPPORTED, "batch order %d not in this unit", n);
+  } else {
+    if (n == LO) {
+      const int cs = c.cluster_size;
+      if (cs != 2 && cs != 4 && cs != 8 && cs != 16)
+        return set_error(SEM_ERR_BAD_ARG, "batch cluster size %d (2, 4, 8 or 16)", cs);
+      return launch_batch_mb<LO, MB>(c, ops, s);
+    }
+    return launch_batch_range<LO + 1, HI, MB>(n, c, ops, s);
+  }
+}
+
+template <int LO, int HI, int MB>
+int max_clusters_range(int n, int csize) {
+  if constexpr (LO > HI) {
+    return 0;
+  } else {
+    if (n == LO) return batch_max_clusters_mb<LO, MB>(csize);
+    return max_clusters_range<LO + 1, HI, MB>(n, csize);
+  }
 }
 
 }  // namespace sem

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["sem_api.cu", "sem_apply.cu", "sem_apply_f64.cu", "sem_apply_df.cu", "sem_apply_f32.cu",
            "sem_apply_f64_hi.cu", "sem_apply_df_hi.cu", "sem_apply_f32_hi.cu", "sem_vec.cu", "sem_geom.cu", "sem_pcg.cu", "sem_batch.cu", "sem_batch_ka.cu",
-           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_small.cu", "sem_tiny.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu", "sem_host.cu"]
+           "sem_batch_kb.cu", "sem_batch_kc.cu", "sem_batch_kd.cu", "sem_batch_ke.cu", "sem_batch_kf.cu", "sem_small.cu", "sem_tiny.cu", "sem_ext.cu", "sem_time.cu", "sem_spectral.cu", "sem_host.cu"]
 
 
 class SemError(RuntimeError):
@@ -113,6 +113,11 @@ class SolveInfo(ctypes.Structure):
                 ("res0_inf", ctypes.c_double), ("converged", ctypes.c_int)]
 
 
+class BatchGroupConfig(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("problems", ctypes.c_int), ("cluster_size", ctypes.c_int),
+                ("ctas_per_sm", ctypes.c_int), ("clusters", ctypes.c_int)]
+
+
 class BdfDesc(ctypes.Structure):
     _fields_ = [("order", ctypes.c_int), ("nu", ctypes.c_double), ("dt", ctypes.c_double),
                 ("nsteps", ctypes.c_int), ("solve", PcgOpts), ("nf", ctypes.c_int),
@@ -171,6 +176,16 @@ SIGNATURES = {
     "sem_batch_pcg": (_I, [_P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                            ctypes.POINTER(_D), ctypes.POINTER(_I), _I, _D, _I,
                            ctypes.POINTER(SolveInfo), _P]),
+    "sem_batch_group_count": (_I, [_P]),
+    "sem_batch_get_config": (_I, [_P, ctypes.POINTER(BatchGroupConfig), _I]),
+    "sem_batch_set_config": (_I, [_P, ctypes.POINTER(BatchGroupConfig), _I]),
+    "sem_batch_get_order": (_I, [_P, ctypes.POINTER(_I), _I]),
+    "sem_batch_set_order": (_I, [_P, ctypes.POINTER(_I), _I]),
+    "sem_batch_timeline": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                ctypes.POINTER(_I), _I, ctypes.POINTER(_D)]),
+    "sem_batch_autotune": (_I, [_P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                ctypes.POINTER(_D), ctypes.POINTER(_I), _I, _D, _I, ctypes.c_char_p,
+                                ctypes.POINTER(_I), ctypes.POINTER(_D), _P]),
     "sem_jacobi_diag": (_I, [_P, _P, _D, _D, _P, _P]),
     "sem_adjoint_grad": (_I, [_P, _P, _P, _P, _U, _P]),
     "sem_bdf_coeffs": (_I, [_I, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]),

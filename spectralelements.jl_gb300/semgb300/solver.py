@@ -226,6 +226,69 @@ class BatchSolver:
         _lib.check(st)
         return xs
 
+    def config(self):
+        """The launch configuration of every order group (a list of dicts: n,
+        problems, cluster_size, ctas_per_sm, clusters; clusters 0 is the
+        work-proportional share)."""
+        g = self._lib.sem_batch_group_count(self._h)
+        cfg = (_lib.BatchGroupConfig * g)()
+        _lib.check(self._lib.sem_batch_get_config(self._h, cfg, g))
+        return [dict(n=c.n, problems=c.problems, cluster_size=c.cluster_size, ctas_per_sm=c.ctas_per_sm,
+                     clusters=c.clusters) for c in cfg]
+
+    def set_config(self, groups):
+        """Set every order group's launch configuration (dicts as config())."""
+        g = len(groups)
+        cfg = (_lib.BatchGroupConfig * g)()
+        for c, d in zip(cfg, groups):
+            c.n, c.problems = int(d["n"]), int(d.get("problems", 0))
+            c.cluster_size, c.ctas_per_sm, c.clusters = int(d["cluster_size"]), int(d["ctas_per_sm"]), int(d["clusters"])
+        _lib.check(self._lib.sem_batch_set_config(self._h, cfg, g))
+
+    def order(self):
+        """Queue order: problem indices slot by slot (groups in order of n)."""
+        n = len(self.meshes)
+        o = (ctypes.c_int * n)()
+        _lib.check(self._lib.sem_batch_get_order(self._h, o, n))
+        return list(o)
+
+    def timeline(self):
+        """Per-problem timeline of the last solve: start and end (ns from the
+        first start, device clock), the SM of the cluster's first CTA, and the
+        solve's total device time in ms."""
+        import numpy as np
+        n = len(self.meshes)
+        t0 = (ctypes.c_longlong * n)()
+        t1 = (ctypes.c_longlong * n)()
+        sm = (ctypes.c_int * n)()
+        ms = ctypes.c_double()
+        _lib.check(self._lib.sem_batch_timeline(self._h, t0, t1, sm, n, ctypes.byref(ms)))
+        return dict(start_ns=np.array(t0[:], dtype=np.int64), end_ns=np.array(t1[:], dtype=np.int64),
+                    sm=np.array(sm[:], dtype=np.int32), total_ms=ms.value)
+
+    def autotune(self, bs, tols, precision=_lib.SEM_F64_DF, maxiter=None, xs=None, inner_tol=None,
+                 max_outer=None, cache=None):
+        """Choose every group's launch shape (cluster size, CTAs per SM), its
+        cluster count and the queue order from measured per-problem
+        timelines (``sem_batch_autotune``); the choice is kept on the batch
+        and, with ``cache`` (a file path), stored under the batch's signature
+        and reused by later calls.  Returns dict(runs, best_ms, config)."""
+        n = len(self.meshes)
+        bs = [as_local(b) for b in bs]
+        if xs is None:
+            xs = [m.empty() for m in self.meshes]
+        B = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+        X = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+        T = (ctypes.c_double * n)(*[float(t) for t in tols])
+        M = None if maxiter is None else (ctypes.c_int * n)(*[int(v) for v in maxiter])
+        runs, best = ctypes.c_int(), ctypes.c_double()
+        _lib.check(self._lib.sem_batch_autotune(self._h, B, X, T, M, int(precision),
+                                                0.0 if inner_tol is None else float(inner_tol),
+                                                0 if max_outer is None else int(max_outer),
+                                                None if cache is None else str(cache).encode(),
+                                                ctypes.byref(runs), ctypes.byref(best), stream_ptr()))
+        return dict(runs=runs.value, best_ms=best.value, config=self.config())
+
 
 def pcg_(x, b, opA, **kw):
     """pcg!(x, b, opA; ...) (src/pcg.jl:64-79): x .= pcg(b, opA; ...)."""

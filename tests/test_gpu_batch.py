@@ -93,3 +93,90 @@ def test_batch_rejects_large_orders(gpu):
     _, md = meshes(13, 2, 2)
     with pytest.raises(S.SemError):
         S.BatchSolver([md], [1.0], [1.0])
+
+
+@pytest.mark.parametrize("cluster_size,ctas_per_sm", [(2, 2), (4, 1), (16, 2), (16, 1)])
+def test_batch_launch_shapes_give_the_same_solution(gpu, cluster_size, ctas_per_sm):
+    """Every launch shape solves the batch: the cluster size changes which CTA
+    owns a tile and so the grouping of the dot products' partial sums, so the
+    solutions agree to the solve's accuracy, not bit for bit.  One cluster
+    per group runs the group's problems one after another (the timeline)."""
+    import semgb300 as S
+    probs = _problems(12, 8)
+    ms, bs, tols = [], [], []
+    for (n, Ex, Ey, nu, lam) in probs:
+        mo, md = meshes(n, Ex, Ey, (False, False), "DDDD", 0.05)
+        b = _rhs(mo, O.generateMask(["D"] * 4, mo))
+        ms.append(md)
+        bs.append(S.as_local(b))
+        tols.append(1e-10 * np.abs(b).max())
+    solver = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
+    ref_infos = []
+    ref = [host(x) for x in solver.solve(bs, tols, precision=S.SEM_F64_DF, infos=ref_infos)]
+    cfg = solver.config()
+    assert [c["n"] for c in cfg] == sorted({p[0] for p in probs})
+    assert all(c["cluster_size"] == 8 and c["ctas_per_sm"] == 2 and c["clusters"] == 0 for c in cfg)
+    solver.set_config([dict(c, cluster_size=cluster_size, ctas_per_sm=ctas_per_sm, clusters=1) for c in cfg])
+    infos = []
+    xs = solver.solve(bs, tols, precision=S.SEM_F64_DF, infos=infos)
+    for x, x0, inf, inf0 in zip(xs, ref, infos, ref_infos):
+        assert inf["converged"]
+        assert rel_l2(host(x), x0) < 1e-9, (inf, inf0)
+    tl = solver.timeline()
+    assert (tl["end_ns"] >= tl["start_ns"]).all() and (tl["start_ns"] >= 0).all()
+    assert tl["total_ms"] > 0 and (tl["sm"] >= 0).all()
+    # one cluster per group: a group's problems run one after another
+    for c in solver.config():
+        idx = [i for i, p in enumerate(probs) if p[0] == c["n"]]
+        spans = sorted((tl["start_ns"][i], tl["end_ns"][i]) for i in idx)
+        assert all(a[1] <= b[0] for a, b in zip(spans, spans[1:]))
+
+
+def test_batch_set_config_rejects_bad_shapes(gpu):
+    import semgb300 as S
+    from semgb300._lib import SemError
+    mo, md = meshes(5, 3, 3, (False, False), "DDDD", 0.05)
+    solver = S.BatchSolver([md], [1.0], [1.0])
+    cfg = solver.config()
+    for bad in (dict(cluster_size=3), dict(ctas_per_sm=3), dict(clusters=-1), dict(n=7)):
+        with pytest.raises(SemError):
+            solver.set_config([dict(cfg[0], **bad)])
+    assert solver.config() == cfg
+
+
+def test_batch_autotune_chooses_persists_and_reloads(gpu, tmp_path):
+    import semgb300 as S
+    probs = _problems(13, 16)
+    ms, bs, tols, refs = [], [], [], []
+    for (n, Ex, Ey, nu, lam) in probs:
+        mo, md = meshes(n, Ex, Ey, (False, False), "DDDD", 0.05)
+        M = O.generateMask(["D"] * 4, mo)
+        b = _rhs(mo, M)
+        ms.append(md)
+        bs.append(S.as_local(b))
+        tols.append(1e-10 * np.abs(b).max())
+        refs.append((mo, M, b, nu, lam))
+    cache = tmp_path / "batch_tune.txt"
+    solver = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
+    r = solver.autotune(bs, tols, precision=S.SEM_MIXED, cache=cache)
+    assert r["runs"] >= 2 and r["best_ms"] > 0
+    chosen, order = solver.config(), solver.order()
+    assert sorted(order) == list(range(len(probs)))
+    for c in chosen:
+        assert c["cluster_size"] in (2, 4, 8, 16) and c["ctas_per_sm"] in (1, 2) and c["clusters"] >= 0
+    # the tuned batch solves correctly
+    infos = []
+    xs = solver.solve(bs, tols, precision=S.SEM_MIXED, infos=infos)
+    for x, inf, (mo, M, b, nu, lam) in zip(xs, infos, refs):
+        assert inf["converged"]
+        res = b - O.mask(O.gatherScatter(O.hlmz(host(x), nu, lam, mo), mo), M)
+        assert np.abs(res).max() <= 2 * np.abs(b).max() * 1e-10 + 1e-300
+    # a new batch of the same signature loads the choice without solving
+    again = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
+    r2 = again.autotune(bs, tols, precision=S.SEM_MIXED, cache=cache)
+    assert r2["runs"] == 0
+    assert again.config() == chosen and again.order() == order
+    # another tolerance is another signature
+    other = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
+    r3 = other.autotune(bs, [2 * t for t in tols], precision=S.SEM_MIXED, cache=cache)
+    assert r3["runs"] >= 2
