@@ -395,8 +395,9 @@ def fourier_forcing(msh_x, msh_y, seed, nmodes=16):
 
 
 def bench_pcg(S, msh, stream):
-    """Jacobi PCG to 1e-8 relative residual: FP64 (double-float operator) vs
-    mixed precision (FP32 inner CG to 1e-4, <= 6 FP64 defect-correction sweeps)."""
+    """Jacobi PCG to 1e-8 relative residual: native FP64, double-float (FP64
+    storage, FP32-pair arithmetic) and mixed precision (FP32 inner CG to
+    1e-4, <= 6 FP64 defect-correction sweeps; or residual replacement)."""
     import numpy as np
     import torch
     out = {}
@@ -408,7 +409,9 @@ def bench_pcg(S, msh, stream):
     op = S.HelmholtzOp(msh, NU, LAM)
     jac = S.Jacobi(op)
     res = {}
-    for name, prec in (("fp64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED), ("mixed_rr", S.SEM_MIXED_RR)):
+    msh.autotune(S.SEM_F64)
+    for name, prec in (("fp64", S.SEM_F64), ("df64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED),
+                       ("mixed_rr", S.SEM_MIXED_RR)):
         info = {}
         S.pcg(b, op, opM=jac, mult=msh.mult, tol=tol, precision=prec, info=info)  # warm
         torch.cuda.synchronize()
@@ -418,22 +421,29 @@ def bench_pcg(S, msh, stream):
         dt = time.time() - t
         res[name] = (x, dt, dict(info))
     x64, dt64, i64 = res["fp64"]
+
+    def rel(x):
+        return (torch.linalg.norm(x - x64) / torch.linalg.norm(x64)).item()
+
+    xd, dtd, idf = res["df64"]
     xm, dtm, im = res["mixed"]
     xr, dtr, ir = res["mixed_rr"]
     out["cfg2_helmholtz_256x256_n8"] = {
-        "tol_rel": 1e-8, "fp64": {"solves_per_s": 1 / dt64, "iters": i64["iters"],
-                                   "res_inf": i64["res_inf"], "res0_inf": i64["res0_inf"]},
+        "tol_rel": 1e-8,
+        "fp64": {"solves_per_s": 1 / dt64, "iters": i64["iters"], "res_inf": i64["res_inf"],
+                 "res0_inf": i64["res0_inf"], "arith": "native FP64 operator, vectors and dots"},
+        "df64": {"solves_per_s": 1 / dtd, "iters": idf["iters"], "res_inf": idf["res_inf"],
+                 "rel_l2_vs_fp64": rel(xd),
+                 "arith": "double-float operator (FP32 pairs, about 47 bits), FP64 vectors, double-float dots"},
         "mixed": {"solves_per_s": 1 / dtm, "inner_iters": im["iters"], "outer": im["outer"],
-                  "res_inf": im["res_inf"],
-                  "rel_l2_vs_fp64": (torch.linalg.norm(xm - x64) / torch.linalg.norm(x64)).item(),
+                  "res_inf": im["res_inf"], "rel_l2_vs_fp64": rel(xm),
                   "form": "FP32 inner CG to 1e-4 relative, restarted, inside FP64 defect-correction sweeps"},
-        "mixed_over_fp64": dt64 / dtm,
         "mixed_rr": {"solves_per_s": 1 / dtr, "iters": ir["iters"], "replacements": ir["outer"],
-                     "res_inf": ir["res_inf"],
-                     "rel_l2_vs_fp64": (torch.linalg.norm(xr - x64) / torch.linalg.norm(x64)).item(),
+                     "res_inf": ir["res_inf"], "rel_l2_vs_fp64": rel(xr),
                      "form": "one FP32 CG; its residual replaced by the FP64 b - A x (x in FP64) "
                              "whenever it has fallen by 0.3; search direction kept"},
-        "mixed_rr_over_fp64": dt64 / dtr}
+        "mixed_over_fp64": dt64 / dtm, "mixed_rr_over_fp64": dt64 / dtr,
+        "mixed_over_df64": dtd / dtm, "mixed_rr_over_df64": dtd / dtr}
     # cfg1 / cfg3: Poisson 8x8, N=8, amp 0.1, exact solution sin(pi x) sin(pi y), 1e-10
     m1 = S.Mesh(9, 9, 8, 8, (False, False), sin_deform(0.1), bc="DDDD")
     m1.autotune(S.SEM_F64_DF)
@@ -464,6 +474,7 @@ def bench_pcg(S, msh, stream):
                    "res_inf": info["res_inf"], "tol_rel": tolr,
                    "err_vs_exact_inf": (x - ut).abs().max().item()}
     r["cfg3_mixed_over_cfg1_fp64"] = r["cfg3_mixed"]["solves_per_s"] / r["cfg1_fp64"]["solves_per_s"]
+    r["cfg3_mixed_over_cfg1_df64"] = r["cfg3_mixed"]["solves_per_s"] / r["cfg1_df64"]["solves_per_s"]
     r["note"] = ("cfg1_fp64: native FP64 arithmetic throughout; cfg1_df64: double-float operator and dots; "
                  "cfg3_mixed: FP32 inner CG in one thread block, double-float FP64 residual sweeps")
     out["cfg1_cfg3_poisson_8x8_n8"] = r
@@ -557,27 +568,66 @@ def bench_batch(S):
         tols.append(1e-8 * b.abs().max().item())
     local = sum(m.shape[0] * m.shape[1] for m in meshes)
     solver = S.BatchSolver(meshes, nus, lams, jacobi=True)
-    out = {"problems": 512, "local_dof": local}
-    xs = {}
-    for name, prec in (("fp64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED), ("mixed_rr", S.SEM_MIXED_RR)):
+    out = {"problems": 512, "local_dof": local,
+           "arith": {"df64": "double-float operator and dots (FP32 pairs, about 47 bits), FP64 vectors; "
+                             "the batch kernels have no native-FP64 form",
+                     "mixed": "FP32 inner CG inside FP64 defect-correction sweeps",
+                     "mixed_rr": "FP32 CG with FP64 residual replacement"}}
+    default_cfg, default_order = solver.config(), solver.order()
+    cache = os.path.join(os.environ.get("TMPDIR", "/tmp"), "sem_batch_tune_bench.txt")
+    if os.path.exists(cache):
+        os.remove(cache)  # tune afresh on this device
+
+    def timed(prec):
         infos = []
-        solver.solve(bs, tols, precision=prec, infos=infos)  # warm
         torch.cuda.synchronize()
         t = time.time()
-        xs[name] = solver.solve(bs, tols, precision=prec, infos=infos)
+        x = solver.solve(bs, tols, precision=prec, infos=infos)
         torch.cuda.synchronize()
-        dt = time.time() - t
+        return x, time.time() - t, infos
+
+    def timeline_summary():
+        tl = solver.timeline()
+        busy = {}
+        for s0, s1, sm in zip(tl["start_ns"], tl["end_ns"], tl["sm"]):
+            if sm >= 0:
+                busy.setdefault(int(sm), []).append((int(s0), int(s1)))
+        ends = sorted(max(e for _, e in v) for v in busy.values())
+        per = sorted(sum(e - b for b, e in v) for v in busy.values())
+        span = max(ends) if ends else 0
+        return {"device_ms": tl["total_ms"], "clusters_seen": len(busy), "makespan_ms": span / 1e6,
+                "cluster_busy_ms": {"min": per[0] / 1e6, "median": per[len(per) // 2] / 1e6, "max": per[-1] / 1e6},
+                "first_cluster_done_ms": ends[0] / 1e6,
+                "busy_fraction": sum(per) / (span * len(per)) if span else 0.0}
+
+    xs = {}
+    for name, prec in (("df64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED), ("mixed_rr", S.SEM_MIXED_RR)):
+        solver.set_config(default_cfg)
+        solver.set_order(default_order)
+        solver.solve(bs, tols, precision=prec)  # warm
+        x0, dt0, infos = timed(prec)
+        tl0 = timeline_summary()
+        t = time.time()
+        tune = solver.autotune(bs, tols, precision=prec, cache=cache)
+        tune_s = time.time() - t
+        xs[name], dt, infos = timed(prec)
         it = [i["iters"] for i in infos]
         out[name] = {"batch_s": dt, "solves_per_s": 512 / dt, "converged": sum(i["converged"] for i in infos),
-                     "iters_max": max(it), "iters_mean": float(np.mean(it))}
-        if name == "fp64":  # per-problem record for the CPU baseline's sample (not printed)
+                     "iters_max": max(it), "iters_mean": float(np.mean(it)),
+                     "tuned_config": [{k: c[k] for k in ("n", "problems", "cluster_size", "ctas_per_sm", "clusters")}
+                                      for c in tune["config"]],
+                     "tune": {"solves": tune["runs"], "seconds": tune_s}, "timeline": timeline_summary(),
+                     "default": {"batch_s": dt0, "solves_per_s": 512 / dt0,
+                                 "config": "cluster_size 8, ctas_per_sm 2, work-proportional cluster counts, "
+                                           "estimated-work order", "timeline": tl0}}
+        if name == "df64":  # per-problem record for the CPU baseline's sample (not printed)
             out["_problems"] = [{"N": N, "Ex": Ex, "Ey": Ey, "nu": nu, "lam": lam, "iters": i,
                                  "local": (N + 1) ** 2 * Ex * Ey}
                                 for (N, Ex, Ey), nu, lam, i in zip(shapes, nus, lams, it)]
     for name in ("mixed", "mixed_rr"):
-        errs = [(torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() for a, b in zip(xs[name], xs["fp64"])]
-        out[name]["rel_l2_vs_fp64_max"] = max(errs)
-        out[name + "_over_fp64"] = out["fp64"]["batch_s"] / out[name]["batch_s"]
+        errs = [(torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() for a, b in zip(xs[name], xs["df64"])]
+        out[name]["rel_l2_vs_df64_max"] = max(errs)
+        out[name + "_over_df64"] = out["df64"]["batch_s"] / out[name]["batch_s"]
     del solver, meshes, bs, xs
     # cfg1 / cfg3 through the persistent kernel (one cluster, one problem)
     m1 = S.Mesh(9, 9, 8, 8, (False, False), sin_deform(0.1), bc="DDDD")
@@ -586,7 +636,7 @@ def bench_batch(S):
     b1 = S.gatherScatter(S.mask(S.mass(2 * np.pi ** 2 * ut, m1), M1), m1)
     one = S.BatchSolver([m1], [1.0], [0.0], jacobi=True)
     res = {}
-    for name, prec, tolr in (("cfg1_fp64", S.SEM_F64_DF, 1e-10), ("cfg3_mixed", S.SEM_MIXED, 1e-10)):
+    for name, prec, tolr in (("cfg1_df64", S.SEM_F64_DF, 1e-10), ("cfg3_mixed", S.SEM_MIXED, 1e-10)):
         tol1 = [tolr * b1.abs().max().item()]
         infos = []
         one.solve([b1], tol1, precision=prec, infos=infos)

@@ -252,6 +252,13 @@ class BatchSolver:
         _lib.check(self._lib.sem_batch_get_order(self._h, o, n))
         return list(o)
 
+    def set_order(self, order):
+        """Set the queue order (as order(): every group's slots must hold its
+        own problems)."""
+        n = len(self.meshes)
+        o = (ctypes.c_int * n)(*[int(i) for i in order])
+        _lib.check(self._lib.sem_batch_set_order(self._h, o, n))
+
     def timeline(self):
         """Per-problem timeline of the last solve: start and end (ns from the
         first start, device clock), the SM of the cluster's first CTA, and the
