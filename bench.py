@@ -589,9 +589,9 @@ def bench_batch(S):
     def timeline_summary():
         tl = solver.timeline()
         busy = {}
-        for s0, s1, sm in zip(tl["start_ns"], tl["end_ns"], tl["sm"]):
-            if sm >= 0:
-                busy.setdefault(int(sm), []).append((int(s0), int(s1)))
+        for s0, s1, c in zip(tl["start_ns"], tl["end_ns"], tl["cluster"]):
+            if c >= 0:
+                busy.setdefault(int(c), []).append((int(s0), int(s1)))
         ends = sorted(max(e for _, e in v) for v in busy.values())
         per = sorted(sum(e - b for b, e in v) for v in busy.values())
         span = max(ends) if ends else 0

@@ -339,9 +339,10 @@ int sem_batch_pcg(sem_batch_t* batch, const double* const* b, double* const* x, 
  * hold its own problems, largest estimated work first by default.
  *
  * sem_batch_timeline returns the last sem_batch_pcg's per-problem timeline:
- * device-clock start and end in ns from the first start, and the SM of the
- * cluster's first CTA (-1 and zeros for problems the host solved in FP64),
- * plus the solve's device time in ms.
+ * device-clock start and end in ns from the first start, and the cluster that
+ * solved it (group index * 65536 + the cluster's index in the group's launch;
+ * -1 and zeros for problems the host solved in FP64), plus the solve's
+ * device time in ms.
  *
  * sem_batch_autotune solves the batch once per launch shape that fits every
  * group (all groups alike, default cluster counts), builds each group's
@@ -367,8 +368,8 @@ int sem_batch_get_config(const sem_batch_t* batch, sem_batch_group_config* cfg, 
 int sem_batch_set_config(sem_batch_t* batch, const sem_batch_group_config* cfg, int count);
 int sem_batch_get_order(const sem_batch_t* batch, int* order, int count);
 int sem_batch_set_order(sem_batch_t* batch, const int* order, int count);
-int sem_batch_timeline(const sem_batch_t* batch, long long* start_ns, long long* end_ns, int* sm, int count,
-                       double* total_ms);
+int sem_batch_timeline(const sem_batch_t* batch, long long* start_ns, long long* end_ns, int* cluster,
+                       int count, double* total_ms);
 int sem_batch_autotune(sem_batch_t* batch, const double* const* b, double* const* x, const double* tol,
                        const int* maxiter, int precision, double inner_tol, int max_outer, const char* cache_path,
                        int* runs, double* best_ms, sem_stream_t stream);

@@ -112,7 +112,7 @@ struct sem_batch {
   cudaEvent_t t0 = nullptr, t1 = nullptr;  // timing of the last solve
   // timeline of the last solve, per problem in creation order
   std::vector<long long> t_start, t_end;
-  std::vector<int> sm;
+  std::vector<int> cluster;  // group index * 65536 + the cluster's index in its launch
   double last_ms = 0.0;
 };
 
@@ -320,7 +320,12 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   b->last_ms = ms;
   b->t_start.assign(b->count, 0);
   b->t_end.assign(b->count, 0);
-  b->sm.assign(b->count, -1);
+  b->cluster.assign(b->count, -1);
+  auto gi_of_slot = [&](int j) {
+    int gi = 0;
+    while (gi + 1 < (int)b->groups.size() && j >= b->groups[gi + 1].first) ++gi;
+    return gi;
+  };
   long long tmin = 0;
   bool any = false;
   for (int j = 0; j < b->count; ++j)
@@ -333,7 +338,7 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     if (q[j].maxiter < 0) continue;  // left to the host's FP64 solve
     b->t_start[i] = q[j].t_start - tmin;
     b->t_end[i] = q[j].t_end - tmin;
-    b->sm[i] = q[j].sm;
+    b->cluster[i] = gi_of_slot(j) * 65536 + q[j].cluster;
   }
   int bad = 0, nanc = 0;
   for (int j = 0; j < b->count; ++j) {
@@ -435,14 +440,14 @@ int sem_batch_set_order(sem_batch_t* b, const int* order, int count) {
   return SEM_OK;
 }
 
-int sem_batch_timeline(const sem_batch_t* b, long long* start_ns, long long* end_ns, int* sm, int count,
+int sem_batch_timeline(const sem_batch_t* b, long long* start_ns, long long* end_ns, int* cluster, int count,
                        double* total_ms) {
   if (!b || count != b->count) return set_error(SEM_ERR_BAD_ARG, "the timeline has one entry per problem");
   if (b->t_start.empty()) return set_error(SEM_ERR_BAD_ARG, "no solve has run on this batch");
   for (int i = 0; i < count; ++i) {
     if (start_ns) start_ns[i] = b->t_start[i];
     if (end_ns) end_ns[i] = b->t_end[i];
-    if (sm) sm[i] = b->sm[i];
+    if (cluster) cluster[i] = b->cluster[i];
   }
   if (total_ms) *total_ms = b->last_ms;
   return SEM_OK;

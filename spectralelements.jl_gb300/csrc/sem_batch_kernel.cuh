@@ -51,11 +51,6 @@ __device__ __forceinline__ long long bclock_ns() {
   return (long long)t;
 }
 
-__device__ __forceinline__ int bsmid() {
-  unsigned v;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(v));
-  return (int)v;
-}
 
 template <int N>
 struct BTile {  // element tile of the batch kernel: TX*TY*N <= kBT
@@ -86,9 +81,9 @@ struct BProb {
   int iters, outer, converged, nan;
   double res_inf, res0_inf;
   // timeline: device clock (ns) when the cluster took the problem and when it
-  // finished it, and the SM of the cluster's rank 0
+  // finished it, and the cluster (its index in the launch)
   long long t_start, t_end;
-  int sm;
+  int cluster;
 };
 
 // launch description shared by the per-order kernels
@@ -768,7 +763,7 @@ __global__ void __launch_bounds__(kBT, MB) k_batch_pcg(const __grid_constant__ B
     BProb& pr = a.probs[pid];
     if (rank == 0 && threadIdx.x == 0) {
       pr.t_start = bclock_ns();
-      pr.sm = bsmid();
+      pr.cluster = (int)(blockIdx.x / (unsigned)bcsize());
     }
     bsolve<N>(a, pr, cl, rank, red, rc, buf);
     cl.sync();  // the problem's results are written before the next one starts

@@ -300,10 +300,12 @@ struct SmallProb {
 };
 
 int launch_small_pcg(SmallProb* dev, const OperatorSet& ops, int n, cudaStream_t s);  // sem_small.cu
-// the SEM_MIXED solve of a small mesh in one thread block with the whole FP32
-// working set in shared memory (sem_tiny.cu); host is the record copied to dev
+// the SEM_MIXED solve of a small mesh in one launch of a small cluster whose
+// CTAs hold the FP32 working set of a strip of element rows each in shared
+// memory (sem_tiny.cu); host is the record copied to dev, smem the per-CTA
+// shared memory tiny_smem_bytes gives
 int launch_tiny_pcg(SmallProb* dev, const SmallProb& host, const OperatorSet& ops, size_t smem, cudaStream_t s);
-size_t tiny_smem_bytes(long long L, bool mass, bool jac, long long nbits);
+size_t tiny_smem_bytes(int n, int Ex, int Ey, bool mass, bool jac);
 size_t max_smem_optin();  // the device's opt-in shared memory per block (sem_apply.cu)
 
 // results at the tail of a SmallProb, in the same order

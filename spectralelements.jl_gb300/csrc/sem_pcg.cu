@@ -979,10 +979,11 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
     SmallProb sp;
     SEM_CHECK(small_record(cx, w, m, o, b, x, maxiter, sp, s));
     SEM_CUDA(cudaMemcpyAsync(w.small, &sp, sizeof(sp), cudaMemcpyHostToDevice, s));
-    // SEM_MIXED in one thread block when its FP32 working set fits the shared
-    // memory of an SM (the restarted form whose FP32 iterations the cluster
-    // kernel cannot make cheaper than FP64 ones)
-    const size_t tiny = tiny_smem_bytes(L, o->k != 0.0, jac, cx.g.NX + cx.g.NY);
+    // SEM_MIXED in a small cluster whose CTAs hold the FP32 working set in
+    // shared memory, one strip of element rows each, when it fits (the
+    // restarted form whose FP32 iterations the single-cluster kernel cannot
+    // make cheaper than FP64 ones)
+    const size_t tiny = tiny_smem_bytes(cx.g.n, cx.g.Ex, cx.g.Ey, o->k != 0.0, jac);
     if (prec == SEM_MIXED && tiny <= max_smem_optin())
       SEM_CHECK(launch_tiny_pcg(w.small, sp, *cx.ops, tiny, s));
     else

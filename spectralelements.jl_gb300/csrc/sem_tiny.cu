@@ -1,47 +1,52 @@
-// Mixed-precision PCG of a whole small mesh in ONE thread block (SEM_MIXED on
-// meshes whose FP32 working set fits an SM's shared memory: cfg3, 8x8
-// elements, N=8, 5,184 local DOF, 187 KB).
+// Mixed-precision PCG of a whole small mesh in ONE launch of a small cluster
+// of thread blocks (SEM_MIXED on meshes whose FP32 working set fits the
+// cluster's shared memory: cfg3, 8x8 elements, N=8, 5,184 local DOF).
 //
-// The single-cluster solver of sem_small.cu spends its ~12 us per iteration on
-// cluster barriers and distributed-shared-memory reductions, in either
-// arithmetic, so its FP32 inner iterations are no cheaper than FP64 ones.
-// Here one CTA holds the FP32 geometry (G11, G12, G22, B), the Jacobi
-// inverse diagonal and every FP32 vector of the inner CG in shared memory, and
-// an iteration costs block barriers only:
+// Each CTA of the cluster owns a strip of whole element rows and keeps, in
+// its shared memory, the strip's FP32 geometry (G11, G12, G22, B), Jacobi
+// inverse diagonal and every FP32 vector of the inner CG.  The element
+// operator's lines lie inside one element row, so the line phases of an
+// iteration touch the CTA's own shared memory only:
 //
 //   P1  lines: row line -> us = Ds u, column line -> ur = Dr u (even-odd form,
 //       one thread per line; the local layout's rows are coalesced across a
 //       warp and its columns are stride-n, both free of bank conflicts)
 //   P2  row lines: wr, ws = G (ur, us), os = Ds' ws; wr and os stored in place
 //   P3  column lines: res = nu (Dr' wr + os) + k B u, unassembled, and the
-//       block-wide p . A p over the unassembled products (equal to the
+//       cluster-wide p . A p over the unassembled products (equal to the
 //       mult-weighted dot of the assembled A p for a continuous masked p)
 //   P4  points: A p = QQ'(res) masked (x pairs first, the order of every other
-//       kernel), x += alpha p, r -= alpha A p, r . z . mult and max|r|, and p
-//       stored; the direction p = z + beta p_old is formed where P1, P3 and
-//       P4 read it, so it needs no pass of its own
-// Each phase ends at one block barrier (a reduction costs one barrier too), so
-// an iteration holds four.
+//       kernel; a copy across a strip boundary is read from the neighbouring
+//       CTA's shared memory), x += alpha p, r -= alpha A p, r . z . mult and
+//       max|r|, and p stored; the direction p = z + beta p_old is formed where
+//       P1, P3 and P4 read it, so it needs no pass of its own
+//
+// P1 and P2 end at block barriers; each reduction (after P3 and after P4)
+// costs a block barrier and one cluster barrier, which also orders the
+// neighbours' reads of the unassembled result against its next writes.
 //
 // The FP64 defect correction runs in the same launch: x (FP64, global) +=
 // x32, then r = b - A x with the double-float operator (the same phases with
 // double-float line buffers in the shared memory the FP32 vectors free),
-// max|r|, and the next inner solve.  Indices are 32-bit (a 64-bit division per
-// point cost more than the arithmetic).  Results go to the SmallProb record as the
-// cluster solver writes them; the host finishes a solve whose sweeps ran out
-// with the FP64 CG (sem_pcg.cu).
+// max|r|, and the next inner solve.  Indices are 32-bit.  Results go to the
+// SmallProb record as the single-cluster solver of sem_small.cu writes them;
+// the host finishes a solve whose sweeps ran out with the FP64 CG (sem_pcg.cu).
 //
 // Reference: pcg (src/pcg.jl:16-60), laplace (src/lapl.jl:70-81), hlmz
 // (src/hlmz.jl:12-19), gatherScatter (src/gatherScatter.jl:8-16), mask
 // (src/mask.jl:10-18).
+#include <cooperative_groups.h>
+
+#include <cstdlib>
 #include <cstring>
 
 #include "sem_apply2.cuh"
 
+namespace cg = cooperative_groups;
+
 namespace sem {
 
-// one thread per line where the mesh allows (an 8x8-element mesh of order 8
-// has 576 lines); 102 registers a thread at most
+// one thread per line where the strip allows; 102 registers a thread at most
 constexpr int kTinyMaxThreads = 640;
 
 template <int N>
@@ -51,15 +56,18 @@ struct TinyArgs {
   EOCoef<N, df> Dr2, Drt2, Ds2, Dst2;  // double-float FP64 residual
 };
 
-// reduction slots: two of them, each one double-float sum and one maximum per warp
+// reduction slots: per warp a double-float sum and a maximum, and the CTA's
+// folded pair that the other CTAs of the cluster read; two of each
 struct TinyRed {
   df s[2][32];
   unsigned long long m[2][32];
+  df cs[2];
+  unsigned long long cm[2];
 };
 
-// shared-memory layout in 4-byte words: the persistent block (G11, G12, G22,
-// [B], [dinv]), the work block (x32, r32, p32, line buffers A and B), the
-// reduction slots and the line bits
+// shared-memory layout in 4-byte words for a strip of L local points: the
+// persistent block (G11, G12, G22, [B], [dinv]), the work block (x32, r32,
+// p32, line buffers A and B), the reduction slots and the line bits
 struct TinyLayout {
   long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, red, bits, words;
 };
@@ -85,16 +93,26 @@ __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool j
   return t;
 }
 
-// Block-wide sum and maximum with one barrier.  Each thread brings an FP32
-// partial sum (a handful of products) and a magnitude as bits; every warp
-// folds its lanes in double-float (fixed shuffle tree, FP32 pipe only: FP64
-// runs at 1/64 of the FP32 rate), lane 0 stores the warp's pair in a slot of
-// `red`, and after the barrier every thread folds the warps' pairs in warp
-// order, so all threads hold the same result.  Consecutive calls alternate
-// between the two slots: a slot is written again only after a later call's
-// barrier, when every thread has read it.
-__device__ __forceinline__ df tiny_warp_sum(float v) {
-  df s = {v, 0.0f};
+// first element row of strip k when Ey element rows are split over C CTAs,
+// and the strip that holds element row e
+__host__ __device__ __forceinline__ int tiny_strip_row(int k, int Ey, int C) { return (int)((long long)k * Ey / C); }
+__device__ __forceinline__ int tiny_strip_of(int e, int Ey, int C) { return (int)(((long long)(e + 1) * C - 1) / Ey); }
+
+__device__ __forceinline__ void tiny_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Cluster-wide sum and maximum.  Each thread brings an FP32 partial sum (a
+// handful of products) and a magnitude as bits.  Every warp folds its lanes
+// in double-float (fixed shuffle tree, FP32 pipe only: FP64 runs at 1/64 of
+// the FP32 rate) and lane 0 stores the warp's pair; after a block barrier
+// thread 0 folds the warps in order into the CTA's pair; after a cluster
+// barrier every warp reads the CTAs' pairs (lane j: CTA j) and folds them in
+// rank order with the same tree, so every thread of the cluster holds the
+// same result.  Consecutive calls alternate between two slots: a slot is
+// written again only after the next call's cluster barrier, which every CTA
+// reaches after it has read the slot.
+__device__ __forceinline__ df tiny_warp_sum(df s) {
   for (int o = 16; o > 0; o >>= 1) {
     df y;
     y.h = __shfl_down_sync(0xffffffffu, s.h, o);
@@ -104,23 +122,50 @@ __device__ __forceinline__ df tiny_warp_sum(float v) {
   return s;
 }
 
-__device__ __forceinline__ df tiny_fold(const TinyRed& red, int slot, unsigned long long& mx) {
-  df s = red.s[slot][0];
-  unsigned long long m = red.m[slot][0];
-  const int nw = (int)(blockDim.x >> 5);
-  for (int i = 1; i < nw; ++i) {
-    s = df_add(s, red.s[slot][i]);
-    m = red.m[slot][i] > m ? red.m[slot][i] : m;
+__device__ __forceinline__ unsigned long long tiny_warp_max(unsigned long long m) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_down_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
   }
-  mx = m;
+  return m;
+}
+
+__device__ __forceinline__ df tiny_cluster_fold(TinyRed& red, int slot, unsigned long long& mx) {
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    df s = red.s[slot][0];
+    unsigned long long m = red.m[slot][0];
+    const int nw = (int)(blockDim.x >> 5);
+    for (int i = 1; i < nw; ++i) {
+      s = df_add(s, red.s[slot][i]);
+      m = red.m[slot][i] > m ? red.m[slot][i] : m;
+    }
+    red.cs[slot] = s;
+    red.cm[slot] = m;
+  }
+  tiny_cluster_sync();
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  df s = {0.0f, 0.0f};
+  unsigned long long m = 0ull;
+  if (lane < C) {
+    const TinyRed* rr = cl.map_shared_rank(&red, lane);
+    s = rr->cs[slot];
+    m = rr->cm[slot];
+  }
+  s = tiny_warp_sum(s);
+  m = tiny_warp_max(m);
+  s.h = __shfl_sync(0xffffffffu, s.h, 0);
+  s.l = __shfl_sync(0xffffffffu, s.l, 0);
+  mx = __shfl_sync(0xffffffffu, m, 0);
   return s;
 }
 
 // FP32 partial sum and FP32 magnitude bits (the bits of |v|; NaN orders above
-// everything): returns the block sum (rounded to FP32: the inner CG's scalars
-// are FP32), mx the block maximum as an FP32 bit pattern
+// everything): returns the cluster sum (rounded to FP32: the inner CG's
+// scalars are FP32), mx the cluster maximum as an FP32 bit pattern
 __device__ __forceinline__ float tiny_reduce(float v, unsigned& mx, TinyRed& red, int& slot) {
-  const df s = tiny_warp_sum(v);
+  const df s = tiny_warp_sum(df{v, 0.0f});
   const unsigned m = __reduce_max_sync(0xffffffffu, mx);
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
@@ -129,18 +174,15 @@ __device__ __forceinline__ float tiny_reduce(float v, unsigned& mx, TinyRed& red
   }
   __syncthreads();
   unsigned long long mm;
-  const df r = tiny_fold(red, slot, mm);
+  const df r = tiny_cluster_fold(red, slot, mm);
   mx = (unsigned)mm;
   slot ^= 1;
   return r.h + r.l;
 }
 
-// block maximum of FP64 magnitude bits (the FP64 residual, once per sweep)
+// cluster maximum of FP64 magnitude bits (the FP64 residual, once per sweep)
 __device__ __forceinline__ unsigned long long tiny_reduce_max64(unsigned long long mx, TinyRed& red, int& slot) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, o);
-    mx = y > mx ? y : mx;
-  }
+  mx = tiny_warp_max(mx);
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
     red.s[slot][w] = {0.0f, 0.0f};
@@ -148,7 +190,7 @@ __device__ __forceinline__ unsigned long long tiny_reduce_max64(unsigned long lo
   }
   __syncthreads();
   unsigned long long mm;
-  tiny_fold(red, slot, mm);
+  tiny_cluster_fold(red, slot, mm);
   slot ^= 1;
   return mm;
 }
@@ -158,17 +200,20 @@ __device__ __forceinline__ unsigned long long tiny_abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
-// The mesh sizes, line bits and this thread's line walks, held in registers
-// (read once from the problem record, which stores through generic pointers
-// could otherwise alias).  Thread t handles lines t, t + T, t + 2T, ...; a
-// row line l has row r = l mod NX and element row e = l div NX, a column line
-// l has element column x = l mod Ex and column c = l div Ex.  The walks
-// advance (r, e) and (x, c) by T without dividing.
+// The strip, the mesh sizes, line bits and this thread's line walks, held in
+// registers (read once from the problem record, which stores through generic
+// pointers could otherwise alias).  Local indices are the strip's: point
+// (r, c) of the mesh, c in [c0, c0 + NYs), is q = r + (c - c0) NX, global
+// g = q + c0 NX.  Thread t handles lines t, t + T, ...; a row line l has row
+// r = l mod NX and element row e = l div NX (of the strip), a column line l
+// has element column x = l mod Ex and column c = l div Ex (of the strip).
+// The walks advance (r, e) and (x, c) by T without dividing.
 struct TinyDims {
   int NX, NY, Ex, Ey, nl, T;
-  int r0, e0, dr, de;  // row-line walk
-  int x0, c0, dx, dc;  // column-line walk
-  const unsigned char* rinfo;  // line bits (shared-memory copies)
+  int C, rank, c0, NYs;  // cluster size, this CTA's rank, first column and columns of its strip
+  int r0, e0, dr, de;    // row-line walk
+  int x0, cc0, dx, dc;   // column-line walk
+  const unsigned char* rinfo;  // line bits (shared-memory copies, whole mesh)
   const unsigned char* cinfo;
 };
 
@@ -182,12 +227,12 @@ __device__ __forceinline__ void tiny_step(int& a, int& b, int da, int db, int n)
 }
 
 // The operator, unassembled and unmasked, res = nu (D'G D u) + k B u, on every
-// line of the mesh.  ufun(q) gives the input at local point q (shared or
-// global memory, or formed on the fly); A, Bf: two line buffers of L entries
-// (shared); G11..Bm: the metric terms and mass (shared FP32 or global
-// pre-split pairs; Bm NULL without a mass term).  The result is left in A;
-// acc receives this thread's part of u . res (FP32 policy).  32-bit indices:
-// a mesh on this path has at most a few thousand points.
+// line of the strip.  ufun(q) gives the input at local point q (shared or
+// global memory, or formed on the fly); A, Bf: two line buffers of the
+// strip's size (shared); G11..Bm: the metric terms and mass, strip-indexed
+// (shared FP32 or global pre-split pairs; Bm NULL without a mass term).  The
+// result is left in A; acc receives this thread's part of u . res (FP32
+// policy).
 template <class P, int N, class GT, class UF>
 __device__ __forceinline__ void tiny_apply(const TinyDims& d, UF&& ufun, typename P::v* A, typename P::v* Bf,
                                            const GT* G11, const GT* G12, const GT* G22, const GT* Bm,
@@ -199,7 +244,7 @@ __device__ __forceinline__ void tiny_apply(const TinyDims& d, UF&& ufun, typenam
   const int EN = N * NX;  // points per element row
   // P1: us on the row lines -> Bf, ur on the column lines -> A
   {
-    int r = d.r0, e = d.e0, x = d.x0, c = d.c0;
+    int r = d.r0, e = d.e0, x = d.x0, c = d.cc0;
     for (int l = threadIdx.x; l < d.nl; l += d.T) {
       {
         const int q0 = r + e * EN;
@@ -247,7 +292,7 @@ __device__ __forceinline__ void tiny_apply(const TinyDims& d, UF&& ufun, typenam
   __syncthreads();
   // P3: column lines: res = nu (Dr' wr + os) + k B u -> A
   {
-    int x = d.x0, c = d.c0;
+    int x = d.x0, c = d.cc0;
     for (int l = threadIdx.x; l < d.nl; l += d.T) {
       const int b0 = x * N + c * NX;
       V xs[N], ys[N];
@@ -268,26 +313,35 @@ __device__ __forceinline__ void tiny_apply(const TinyDims& d, UF&& ufun, typenam
       tiny_step(x, c, d.dx, d.dc, d.Ex);
     }
   }
-  // no barrier here: the caller's next reduction (or its own barrier) orders
-  // these stores before the gather reads them
+  // no barrier here: the caller's next reduction orders these stores before
+  // the gather reads them (here and in the neighbouring CTAs)
 }
 
-// one local point of a row line, with what QQ', the mask and the weighted
-// dots need: its copies' rows and columns (-1: none), 1/multiplicity, and
-// whether the mask zeroes it
+// one local point of a row line of the strip, with what QQ', the mask and the
+// weighted dots need: local and global index, its copies' rows and columns
+// (mesh columns; -1: none), 1/multiplicity, and whether the mask zeroes it
 struct TinyPt {
-  int q, r, c, r2, c2;
+  int q, g, r, c, r2, c2;
   float mult;
   bool zero;
 };
 
-// QQ' at a local point of an unassembled field: the sum of its copies, x
-// pairs first (as small_gather); each copy converted by cv first
+// QQ' at a point of an unassembled strip-indexed field `raw` of this CTA: the
+// sum of its copies, x pairs first (as small_gather); a copy in another strip
+// is read from that CTA's `raw` (the same offset in every CTA's shared
+// memory); each copy converted by cv first
 template <class T, class F>
-__device__ __forceinline__ auto tiny_gather(const T* raw, int NX, const TinyPt& p, F&& cv) {
-  const T* col = raw + p.c * NX;
+__device__ __forceinline__ auto tiny_gather(const TinyDims& d, T* raw, const TinyPt& p, F&& cv) {
+  const T* col = raw + (p.c - d.c0) * d.NX;
   if (p.c2 < 0) return p.r2 < 0 ? cv(col[p.r]) : io_add(cv(col[p.r]), cv(col[p.r2]));
-  const T* col2 = raw + p.c2 * NX;
+  const T* col2;
+  if (p.c2 >= d.c0 && p.c2 < d.c0 + d.NYs) {
+    col2 = raw + (p.c2 - d.c0) * d.NX;
+  } else {
+    const int k = tiny_strip_of(p.c2 / (d.NY / d.Ey), d.Ey, d.C);
+    const int c0k = tiny_strip_row(k, d.Ey, d.C) * (d.NY / d.Ey);
+    col2 = cg::this_cluster().map_shared_rank(raw, k) + (p.c2 - c0k) * d.NX;
+  }
   if (p.r2 < 0) return io_add(cv(col[p.r]), cv(col2[p.r]));
   return io_add(io_add(cv(col[p.r]), cv(col[p.r2])), io_add(cv(col2[p.r]), cv(col2[p.r2])));
 }
@@ -304,10 +358,12 @@ __device__ __forceinline__ void tiny_points(const TinyDims& d, bool ones, bool h
     const bool zr = has_bc && (br & L_ZERO);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const int c = e * N + j;
+      const int cl = e * N + j;  // strip column
+      const int c = d.c0 + cl;   // mesh column
       const unsigned char bc = d.cinfo[c];
       TinyPt p;
-      p.q = r + c * d.NX;
+      p.q = r + cl * d.NX;
+      p.g = p.q + d.c0 * d.NX;
       p.r = r;
       p.c = c;
       p.r2 = r2;
@@ -322,7 +378,7 @@ __device__ __forceinline__ void tiny_points(const TinyDims& d, bool ones, bool h
 
 // The FP64 defect-correction step of a sweep: x += x32 (FP64, global), then
 // r = b - A x with the double-float operator in the work block (free while no
-// inner solve runs), and the block maximum of |r|.  A separate function, so
+// inner solve runs), and the cluster maximum of |r|.  A separate function, so
 // that the double-float registers do not crowd the FP32 inner loop.  Its
 // arguments are values (no address of a caller's register variable is taken);
 // it uses reduction slot `slot`, so the caller flips its slot after the call.
@@ -331,31 +387,37 @@ __device__ __noinline__ double tiny_residual(const TinyArgs<N>& a, SmallProb* pr
                                              TinyLayout lay, TinyRed* redp, int slot, bool mass, bool has_bc) {
   SmallProb& pr = *prp;
   TinyRed& red = *redp;
-  const int L = d.NX * d.NY;
+  const int L = d.NX * d.NYs;  // the strip's points
+  const int off = d.c0 * d.NX;
+  const long long LG = (long long)d.NX * d.NY;
   const float* x32 = sm + lay.x32;
-  for (int q = threadIdx.x; q < L; q += d.T) pr.x[q] += (double)x32[q];
+  for (int q = threadIdx.x; q < L; q += d.T) pr.x[off + q] += (double)x32[q];
   __syncthreads();
-  df* DA = reinterpret_cast<df*>(sm + lay.x32);  // 2 L pairs
-  df* DB = DA + L;
+  // two strip-sized pair buffers in the work block (5 strip sizes of words),
+  // at the same offsets in every CTA
+  df* DA = reinterpret_cast<df*>(sm + lay.x32);
+  df* DB = DA + (lay.r32 - lay.x32);
   float unused = 0.0f;
-  const df* Gdf = pr.Gdf;
-  const double* X = pr.x;
+  const df* Gdf = pr.Gdf + off;
+  const double* X = pr.x + off;
   const df nu2 = d2df(pr.nu), k2 = d2df(pr.k);  // both inside the pair window (small_eligible)
-  tiny_apply<PDF, N, df>(d, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + L, Gdf + 2 * L,
-                         mass ? Gdf + 3 * L : nullptr, nu2, k2, a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
-  __syncthreads();
+  tiny_apply<PDF, N, df>(d, [&](int q) { return PDF::cvt(X[q]); }, DA, DB, Gdf, Gdf + LG, Gdf + 2 * LG,
+                         mass ? Gdf + 3 * LG : nullptr, nu2, k2, a.Dr2, a.Drt2, a.Ds2, a.Dst2, unused);
+  // the neighbours' copies are read below: a cluster barrier
+  tiny_cluster_sync();
   unsigned long long m2 = 0ull;
   tiny_points<N>(d, true, has_bc, [&](const TinyPt& p) {
     // each copy rounded to FP64 first, then summed in FP64 (the order of the
     // chunked path's tile stores and fixup)
-    const double ax = tiny_gather(DA, d.NX, p, [](df v) { return df2d(v); });
-    const double v = p.zero ? 0.0 : pr.b[p.q] - ax;
-    pr.r[p.q] = v;
+    const double ax = tiny_gather(d, DA, p, [](df v) { return df2d(v); });
+    const double v = p.zero ? 0.0 : pr.b[p.g] - ax;
+    pr.r[p.g] = v;
     const unsigned long long bb = tiny_abs_bits(v);
     m2 = bb > m2 ? bb : m2;
   });
+  // the reduction's cluster barrier also ends the neighbours' reads of DA
+  // before the work block holds FP32 vectors again
   m2 = tiny_reduce_max64(m2, red, slot);
-  __syncthreads();  // the work block holds the FP32 vectors again
   return __longlong_as_double((long long)m2);
 }
 
@@ -364,13 +426,19 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   SmallProb& pr = *a.pr;
   extern __shared__ __align__(16) float sm[];
   int slot = 0;
-  const int NX = (int)pr.NX, NY = (int)pr.NY, L = NX * NY;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int rank = (int)cl.block_rank();
+  const int NX = (int)pr.NX, NY = (int)pr.NY;
+  const int Ey = pr.Ey;
   const int maxiter = pr.maxiter;
   const bool jac = pr.jacobi != 0;
   const bool mass = pr.k != 0.0;
   const bool ones = pr.mult_ones != 0;
   const bool has_bc = pr.has_bc;
-  const TinyLayout lay = tiny_layout(L, mass, jac, NX + NY);
+  const int e0 = tiny_strip_row(rank, Ey, C), e1 = tiny_strip_row(rank + 1, Ey, C);
+  const int Ls_max = NX * N * (int)((Ey + C - 1) / C);
+  const TinyLayout lay = tiny_layout(Ls_max, mass, jac, NX + NY);  // the same offsets in every CTA
   float* G11 = sm + lay.g11;
   float* G12 = sm + lay.g12;
   float* G22 = sm + lay.g22;
@@ -388,39 +456,47 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   dm.NX = NX;
   dm.NY = NY;
   dm.Ex = pr.Ex;
-  dm.Ey = pr.Ey;
-  dm.nl = NX * pr.Ey;
+  dm.Ey = Ey;
+  dm.C = C;
+  dm.rank = rank;
+  dm.c0 = e0 * N;
+  dm.NYs = (e1 - e0) * N;
+  dm.nl = NX * (e1 - e0);
   dm.T = T;
   dm.r0 = (int)threadIdx.x % NX;
   dm.e0 = (int)threadIdx.x / NX;
   dm.dr = T % NX;
   dm.de = T / NX;
   dm.x0 = (int)threadIdx.x % dm.Ex;
-  dm.c0 = (int)threadIdx.x / dm.Ex;
+  dm.cc0 = (int)threadIdx.x / dm.Ex;
   dm.dx = T % dm.Ex;
   dm.dc = T / dm.Ex;
   dm.rinfo = bits;
   dm.cinfo = bits + NX;
+  const int Ls = NX * dm.NYs;     // this strip's points
+  const int off = dm.c0 * NX;     // its first global index
+  const long long LG = (long long)NX * NY;
 
-  // persistent block: FP32 geometry, Jacobi inverse diagonal, line bits
-  for (int q = threadIdx.x; q < L; q += T) {
-    G11[q] = pr.Gf[q];
-    G12[q] = pr.Gf[L + q];
-    G22[q] = pr.Gf[2 * L + q];
-    if (mass) Bs[q] = pr.Gf[3 * L + q];
-    if (jac) dinv[q] = pr.dinv32[q];
+  // persistent block: the strip's FP32 geometry and Jacobi inverse diagonal,
+  // and the mesh's line bits
+  for (int q = threadIdx.x; q < Ls; q += T) {
+    G11[q] = pr.Gf[off + q];
+    G12[q] = pr.Gf[LG + off + q];
+    G22[q] = pr.Gf[2 * LG + off + q];
+    if (mass) Bs[q] = pr.Gf[3 * LG + off + q];
+    if (jac) dinv[q] = pr.dinv32[off + q];
   }
   for (int i = threadIdx.x; i < NX + NY; i += T) bits[i] = i < NX ? pr.rinfo[i] : pr.cinfo[i - NX];
   // x = 0, r = b (FP64, global), max|b|
   unsigned long long m0 = 0ull;
-  for (int q = threadIdx.x; q < L; q += T) {
-    const double v = pr.b[q];
-    pr.x[q] = 0.0;
-    pr.r[q] = v;
+  for (int q = threadIdx.x; q < Ls; q += T) {
+    const double v = pr.b[off + q];
+    pr.x[off + q] = 0.0;
+    pr.r[off + q] = v;
     const unsigned long long bb = tiny_abs_bits(v);
     m0 = bb > m0 ? bb : m0;
   }
-  m0 = tiny_reduce_max64(m0, red, slot);  // its barrier also publishes the staged blocks
+  m0 = tiny_reduce_max64(m0, red, slot);  // its barriers also publish the staged blocks
   double rmax = __longlong_as_double((long long)m0);
   const double res0 = rmax;
   int outer = 0, total = 0;
@@ -433,7 +509,7 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     float tl = 0.0f;
     unsigned ml = 0u;
     tiny_points<N>(dm, ones, has_bc, [&](const TinyPt& p) {
-      const float ri = (float)pr.r[p.q];
+      const float ri = (float)pr.r[p.g];
       r32[p.q] = ri;
       x32[p.q] = 0.0f;
       p32[p.q] = 0.0f;
@@ -466,7 +542,7 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
       float sl = 0.0f;
       unsigned mx = 0u;
       tiny_points<N>(dm, ones, has_bc, [&](const TinyPt& p) {
-        float ap = tiny_gather(LA, NX, p, [](float v) { return v; });
+        float ap = tiny_gather(dm, LA, p, [](float v) { return v; });
         if (p.zero) ap = 0.0f;
         const float pk = pnew(p.q);
         x32[p.q] = __fmaf_rn(af, pk, x32[p.q]);
@@ -488,7 +564,7 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     slot ^= 1;
     nan = rmax != rmax || nin;
   }
-  if (threadIdx.x == 0) {
+  if (rank == 0 && threadIdx.x == 0) {
     pr.iters = total;
     pr.outer = outer;
     pr.res_inf = rmax;
@@ -496,6 +572,8 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     pr.nan = nan;
     pr.converged = rmax <= pr.tol && !nan;
   }
+  // no CTA leaves while another may still read its shared memory
+  tiny_cluster_sync();
 }
 
 template <class V, int N>
@@ -519,8 +597,23 @@ static void fill_eo_tiny(EOCoef<N, V>& c, const double* src, V (*cvt)(double)) {
 static float to_f32(double d) { return (float)d; }
 static df to_df(double d) { return PDF::from_double(d); }
 
-size_t tiny_smem_bytes(long long L, bool mass, bool jac, long long nbits) {
-  return (size_t)tiny_layout(L, mass, jac, nbits).words * 4;
+// CTAs of the cluster for an Ey-element-row mesh: SEM_TINY_CLUSTER (1, 2, 4
+// or 8) when set, else 4 (at most one strip per element row)
+int tiny_cluster_size(int Ey) {
+  int c = 4;
+  if (const char* e = std::getenv("SEM_TINY_CLUSTER")) {
+    const int v = std::atoi(e);
+    if (v == 1 || v == 2 || v == 4 || v == 8) c = v;
+  }
+  while (c > 1 && c > Ey) c >>= 1;
+  return c;
+}
+
+size_t tiny_smem_bytes(int n, int Ex, int Ey, bool mass, bool jac) {
+  const int C = tiny_cluster_size(Ey);
+  const long long NX = (long long)n * Ex, NY = (long long)n * Ey;
+  const long long Ls_max = NX * n * ((Ey + C - 1) / C);
+  return (size_t)tiny_layout(Ls_max, mass, jac, NX + NY).words * 4;
 }
 
 template <int N>
@@ -536,14 +629,27 @@ static int launch_tiny(SmallProb* dev, const SmallProb& host, const OperatorSet&
   fill_eo_tiny<df, N>(a.Drt2, ops.eo[1], to_df);
   fill_eo_tiny<df, N>(a.Ds2, ops.eo[2], to_df);
   fill_eo_tiny<df, N>(a.Dst2, ops.eo[3], to_df);
-  const long long nl = host.NX * host.Ey;
+  const int C = tiny_cluster_size(host.Ey);
+  const long long nl = host.NX * ((host.Ey + C - 1) / C);  // lines of the largest strip
   int threads = (int)((nl + 31) / 32 * 32);
   if (threads > kTinyMaxThreads) threads = kTinyMaxThreads;
   if (threads < 64) threads = 64;
   auto kern = k_tiny_pcg<N>;
   SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<1, threads, smem, s>>>(a);
-  SEM_CUDA(cudaGetLastError());
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)C);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SEM_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
   return SEM_OK;
 }
 

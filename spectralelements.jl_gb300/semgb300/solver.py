@@ -261,17 +261,18 @@ class BatchSolver:
 
     def timeline(self):
         """Per-problem timeline of the last solve: start and end (ns from the
-        first start, device clock), the SM of the cluster's first CTA, and the
+        first start, device clock), the cluster that solved it (unique over the
+        solve's launches; -1 for problems the host solved in FP64), and the
         solve's total device time in ms."""
         import numpy as np
         n = len(self.meshes)
         t0 = (ctypes.c_longlong * n)()
         t1 = (ctypes.c_longlong * n)()
-        sm = (ctypes.c_int * n)()
+        cl = (ctypes.c_int * n)()
         ms = ctypes.c_double()
-        _lib.check(self._lib.sem_batch_timeline(self._h, t0, t1, sm, n, ctypes.byref(ms)))
+        _lib.check(self._lib.sem_batch_timeline(self._h, t0, t1, cl, n, ctypes.byref(ms)))
         return dict(start_ns=np.array(t0[:], dtype=np.int64), end_ns=np.array(t1[:], dtype=np.int64),
-                    sm=np.array(sm[:], dtype=np.int32), total_ms=ms.value)
+                    cluster=np.array(cl[:], dtype=np.int32), total_ms=ms.value)
 
     def autotune(self, bs, tols, precision=_lib.SEM_F64_DF, maxiter=None, xs=None, inner_tol=None,
                  max_outer=None, cache=None):

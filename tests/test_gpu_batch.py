@@ -124,7 +124,9 @@ def test_batch_launch_shapes_give_the_same_solution(gpu, cluster_size, ctas_per_
         assert rel_l2(host(x), x0) < 1e-9, (inf, inf0)
     tl = solver.timeline()
     assert (tl["end_ns"] >= tl["start_ns"]).all() and (tl["start_ns"] >= 0).all()
-    assert tl["total_ms"] > 0 and (tl["sm"] >= 0).all()
+    assert tl["total_ms"] > 0 and (tl["cluster"] >= 0).all()
+    # one cluster per group: every group's problems carry one cluster id
+    assert len(set(tl["cluster"].tolist())) == len(solver.config())
     # one cluster per group: a group's problems run one after another
     for c in solver.config():
         idx = [i for i, p in enumerate(probs) if p[0] == c["n"]]
