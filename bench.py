@@ -604,6 +604,7 @@ def bench_batch(S):
     for name, prec in (("df64", S.SEM_F64_DF), ("mixed", S.SEM_MIXED), ("mixed_rr", S.SEM_MIXED_RR)):
         solver.set_config(default_cfg)
         solver.set_order(default_order)
+        solver.set_wide([0] * len(meshes))
         solver.solve(bs, tols, precision=prec)  # warm
         x0, dt0, infos = timed(prec)
         tl0 = timeline_summary()
@@ -616,6 +617,7 @@ def bench_batch(S):
                      "iters_max": max(it), "iters_mean": float(np.mean(it)),
                      "tuned_config": [{k: c[k] for k in ("n", "problems", "cluster_size", "ctas_per_sm", "clusters")}
                                       for c in tune["config"]],
+                     "wide_problems": sum(tune["wide"]),
                      "tune": {"solves": tune["runs"], "seconds": tune_s}, "timeline": timeline_summary(),
                      "default": {"batch_s": dt0, "solves_per_s": 512 / dt0,
                                  "config": "cluster_size 8, ctas_per_sm 2, work-proportional cluster counts, "

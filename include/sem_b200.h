@@ -338,20 +338,28 @@ int sem_batch_pcg(sem_batch_t* batch, const double* const* b, double* const* x, 
  * sem_batch_set_order) lists problem indices slot by slot; a group's slots
  * hold its own problems, largest estimated work first by default.
  *
+ * A problem marked wide (sem_batch_set_wide, one flag per problem) is solved
+ * before the persistent launches, alone on the whole GPU, by sem_pcg's
+ * chunked path in the batch's arithmetic; the launches skip it.
+ *
  * sem_batch_timeline returns the last sem_batch_pcg's per-problem timeline:
  * device-clock start and end in ns from the first start, and the cluster that
  * solved it (group index * 65536 + the cluster's index in the group's launch;
- * -1 and zeros for problems the host solved in FP64), plus the solve's
- * device time in ms.
+ * -2 for a wide problem, whose interval is its whole-GPU solve, before the
+ * launches; -1 and zeros for problems the host solved in FP64), plus the
+ * solve's device time in ms.
  *
  * sem_batch_autotune solves the batch once per launch shape that fits every
  * group (all groups alike, default cluster counts), builds each group's
  * makespan model from the measured per-problem durations (list scheduling
  * onto k clusters, largest first; a cluster costs cluster_size/ctas_per_sm
  * SMs), picks per group the shape and cluster count of the smallest makespan
- * whose SM costs fit the device, orders each group's queue by measured
- * duration, verifies the pick with one more solve and keeps whichever
- * measured fastest.  With cache_path, the choice is appended to that file
+ * whose SM costs fit the device and orders each group's queue by measured
+ * duration.  It then solves once with the 32 longest problems wide, which
+ * times each of them on the whole GPU, and picks how many of them (longest
+ * first) to keep wide: the sum of their whole-GPU times plus the modelled
+ * makespan of the rest.  Every pick is verified by a solve, and whichever
+ * configuration measured fastest is kept.  With cache_path, the choice is appended to that file
  * under the batch's signature (device, arithmetic, every problem's shape,
  * coefficients and tolerance), and a later call with the same signature
  * loads it without solving.  runs receives the solves it made, best_ms the
@@ -370,6 +378,8 @@ int sem_batch_get_order(const sem_batch_t* batch, int* order, int count);
 int sem_batch_set_order(sem_batch_t* batch, const int* order, int count);
 int sem_batch_timeline(const sem_batch_t* batch, long long* start_ns, long long* end_ns, int* cluster,
                        int count, double* total_ms);
+int sem_batch_get_wide(const sem_batch_t* batch, int* wide, int count);
+int sem_batch_set_wide(sem_batch_t* batch, const int* wide, int count);
 int sem_batch_autotune(sem_batch_t* batch, const double* const* b, double* const* x, const double* tol,
                        const int* maxiter, int precision, double inner_tol, int max_outer, const char* cache_path,
                        int* runs, double* best_ms, sem_stream_t stream);

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   V* s0 = S0 + elem * ES;
   V* s1 = S1 + elem * ES;
   const int rofs = elem * ES + lane;
-  RowScale rs;  // range guard of the double-float policy
+  bool kbad = false;  // range guard: a tiny stiffness row or a tiny k B product
 
   if (STAGE) {
     if (valid && stiff) {
@@ -250,20 +250,13 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
             pn = cg_direction(a.r[gi], jac ? a.dinv[gi] : (IO)1, beta, a.p[gi], jac);
           a.p[gi] = pn;
         }
-        if constexpr (P::kPrecision == SEM_F64_DF) rs.see(pn);
         u[j] = P::cvt(pn);
         s0[j * SP + lane] = u[j];
       }
     } else {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        if constexpr (P::kPrecision == SEM_F64_DF) {
-          const double x = valid ? __ldg(a.u + base + (long long)j * NX) : 0.0;
-          rs.see(x);
-          u[j] = P::cvt(x);
-        } else {
-          u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
-        }
+        u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
         s0[j * SP + lane] = u[j];
       }
     }
@@ -319,6 +312,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       // ---- E: assemble
 #pragma unroll
       for (int j = 0; j < N; ++j) res[j] = P::add(s1[j * SP + lane], os[j]);
+      if constexpr (P::kPrecision == SEM_F64_DF) kbad |= df_row_tiny(res);  // the stiffness sum, before nu
       if (mode & M_NU) {
 #pragma unroll
         for (int j = 0; j < N; ++j) {
@@ -334,7 +328,6 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       for (int j = 0; j < N; ++j) res[j] = P::zero();
     }
   }
-  bool kbad = false;  // range guard: a tiny k B product
   if (mode & M_MASS) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
@@ -346,9 +339,9 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   }
 
   if constexpr (P::kPrecision == SEM_F64_DF) {
-    // range guard: a row of tiny values, a tiny k B or a NaN/Inf result
-    // flags the call (degenerate metric terms arrive as NaN pairs)
-    bool bad = rs.tiny() || kbad;
+    // range guard: a tiny stiffness or result row, a tiny k B or a NaN/Inf
+    // result flags the call (degenerate metric terms arrive as NaN pairs)
+    bool bad = kbad || df_row_tiny(res);
 #pragma unroll
     for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
     if (bad && a.rflag) *a.rflag = a.rtag;

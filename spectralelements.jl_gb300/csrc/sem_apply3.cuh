@@ -126,19 +126,13 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
 
     // ---- A: row `lane` of u; y-direction derivative
     V res[N];
-    RowScale rs;  // range guard of the double-float policy
+    bool kbad = false;  // range guard: a tiny stiffness row or a tiny k B product
     cp_async_wait_group<2>();  // u(tile); G(tile), B(tile) may be in flight
     {
       V u[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        if constexpr (P::kPrecision == SEM_F64_DF) {
-          const double x = valid ? RU[j * T + t] : 0.0;
-          rs.see(x);
-          u[j] = P::cvt(x);
-        } else {
-          u[j] = valid ? P::cvt(RU[j * T + t]) : P::zero();
-        }
+        u[j] = valid ? P::cvt(RU[j * T + t]) : P::zero();
         s0[j * SP + lane] = u[j];
       }
       fetch_u(next);
@@ -195,6 +189,7 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
         // ---- E: assemble
 #pragma unroll
         for (int j = 0; j < N; ++j) res[j] = P::add(s1[j * SP + lane], os[j]);
+        if constexpr (P::kPrecision == SEM_F64_DF) kbad |= df_row_tiny(res);  // the stiffness sum, before nu
         if (mode & M_NU) {
 #pragma unroll
           for (int j = 0; j < N; ++j) {
@@ -213,7 +208,6 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
       }
     }
     cp_async_wait_group<2>();  // B(tile); u(next), G(next) may be in flight
-    bool kbad = false;  // range guard: a tiny k B product
     if (mass) {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
@@ -226,9 +220,9 @@ __global__ void __launch_bounds__(TX* TY* N, 2) k_apply3(const __grid_constant__
     fetch_b(next);
 
     if constexpr (P::kPrecision == SEM_F64_DF) {
-      // range guard: a row of tiny values, a tiny k B or a NaN/Inf result
-      // flags the call (degenerate metric terms arrive as NaN pairs)
-      bool bad = rs.tiny() || kbad;
+      // range guard: a tiny stiffness or result row, a tiny k B or a NaN/Inf
+      // result flags the call (degenerate metric terms arrive as NaN pairs)
+      bool bad = kbad || df_row_tiny(res);
 #pragma unroll
       for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
       if (bad && a.rflag) *a.rflag = a.rtag;

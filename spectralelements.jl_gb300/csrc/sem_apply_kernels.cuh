@@ -248,8 +248,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   V* s1 = S1 + elem * ES;
   V* s2 = S2 + elem * ES;
   const int rofs = elem * ES + lane;  // this thread's row inside a staged slot (+ j*SP)
-  RowScale rs;  // range guard of the double-float policy
-  bool gbad = false;  // range guard: degenerate metric terms or a tiny k B
+  bool gbad = false;  // range guard: degenerate metric terms, a tiny row or a tiny k B
 
   // ---- staged variant: issue every later global read of this row now
   if (STAGE) {
@@ -278,13 +277,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
   V u[N];
 #pragma unroll
   for (int j = 0; j < N; ++j) {
-    if constexpr (P::kPrecision == SEM_F64_DF) {
-      const double x = valid ? __ldg(a.u + base + (long long)j * NX) : 0.0;
-      rs.see(x);
-      u[j] = P::cvt(x);
-    } else {
-      u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
-    }
+    u[j] = valid ? P::ld(a.u + base + (long long)j * NX) : P::zero();
   }
 
   V res[N];
@@ -341,6 +334,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     // ---- E: assemble
 #pragma unroll
     for (int j = 0; j < N; ++j) res[j] = P::add(s2[j * SP + lane], os[j]);
+    if constexpr (P::kPrecision == SEM_F64_DF) gbad |= df_row_tiny(res);  // the stiffness sum, before nu
     if (mode & M_NU) {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
@@ -366,9 +360,9 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks<P, N, STAGE>::value))
     }
   }
   if constexpr (P::kPrecision == SEM_F64_DF) {
-    // range guard: a row of tiny values, degenerate metric terms, a tiny k B
-    // or a NaN/Inf result flags the call
-    bool bad = rs.tiny() || gbad;
+    // range guard: a tiny stiffness or result row, degenerate metric terms, a
+    // tiny k B or a NaN/Inf result flags the call
+    bool bad = gbad || df_row_tiny(res);
 #pragma unroll
     for (int j = 0; j < N; ++j) bad |= df_bad(res[j]);
     if (bad && a.rflag) *a.rflag = a.rtag;

@@ -99,36 +99,37 @@ __device__ __forceinline__ df d2df(double x) {
   return {h, l};
 }
 
-// Range guard of the double-float operator.  The pair format holds about 47
-// significand bits in the FP32 exponent range.  Operator inputs are split by
-// d2df_op, which turns a magnitude at or above 2^90 (and Inf) into NaN, so
-// that intermediates never overflow silently; smaller values split as d2df
-// does (magnitudes below 2^-103 keep fewer bits, below 2^-126 flush to zero).
-// A result stays accurate as long as the values of a line are not all tiny:
-// a tiny value next to values of ordinary size changes the result by a
-// negligible amount.  RowScale watches that for the rows a thread loads; a row
-// whose nonzero values all lie below 2^-60, or a NaN/Inf result, flags the
-// call, and the host side re-runs the whole call in native FP64.
+// Range guard of the double-float format.  Pairs keep about 47 bits for
+// magnitudes from 2^-101 up to the FP32 range; the FP32 subnormals below give
+// an absolute resolution of 2^-149.  Loads split with d2df_op, which turns a
+// magnitude at or above 2^90 (and Inf) into NaN, so that intermediates never
+// overflow silently, and a nonzero magnitude below 2^-126 (which the split
+// would flush to zero) into NaN as well.  A NaN or Inf result flags the call.
+// A value that is small only next to the others of its field changes the
+// result by a negligible amount; a row whose stiffness sum (before nu) or
+// result is tiny throughout, below 2^-90 and not zero, is small because of
+// its scale and flags the call.  The host side re-runs a flagged call in
+// native FP64.
 constexpr unsigned kDfExpHi = 1023u + 90u;   // first biased exponent that is poisoned
-constexpr unsigned kDfExpTiny = 1023u - 60u; // a row whose largest exponent is below this is tiny
+constexpr unsigned kDfExpLo = 1023u - 126u;  // nonzero values below this biased exponent are poisoned
+constexpr float kRowTiny = 0x1p-90f;
 __device__ __forceinline__ df d2df_op(double x) {
-  const unsigned ed = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned mag = hi & 0x7fffffffu;
   df v = d2df(x);
-  if (ed >= kDfExpHi) v = {__uint_as_float(0x7fc00000u), 0.0f};
+  if (mag >= (kDfExpHi << 20) || (mag < (kDfExpLo << 20) && (mag | (unsigned)__double2loint(x)) != 0u))
+    v = {__uint_as_float(0x7fc00000u), 0.0f};
   return v;
 }
 
-struct RowScale {
-  unsigned emax = 0u;  // largest biased exponent seen among nonzero values (subnormals count as 1)
-  __device__ __forceinline__ void see(double x) {
-    const unsigned hi = (unsigned)__double2hiint(x);
-    const unsigned lo = (unsigned)__double2loint(x);
-    unsigned e = (hi >> 20) & 0x7ffu;
-    if (e == 0u && ((hi & 0x000fffffu) | lo)) e = 1u;
-    emax = e > emax ? e : emax;
-  }
-  __device__ __forceinline__ bool tiny() const { return emax != 0u && emax < kDfExpTiny; }
-};
+// a row of pairs whose largest magnitude lies in (0, 2^-90)
+template <int N>
+__device__ __forceinline__ bool df_row_tiny(const df (&v)[N]) {
+  float m = 0.0f;
+#pragma unroll
+  for (int j = 0; j < N; ++j) m = fmaxf(m, fabsf(v[j].h));
+  return m != 0.0f && m < kRowTiny;
+}
 
 // Geometry and mass-term guard: a point whose metric terms G11 and G22 both
 // lie below 2^-40 in magnitude (a degenerate or absurdly scaled mesh: in 2D

@@ -110,10 +110,15 @@ struct sem_batch {
   void* ws = nullptr;       // all per-problem vectors
   cudaEvent_t start = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;  // timing of the last solve
+  cudaEvent_t w0 = nullptr, w1 = nullptr;  // timing of one wide problem
   // timeline of the last solve, per problem in creation order
   std::vector<long long> t_start, t_end;
   std::vector<int> cluster;  // group index * 65536 + the cluster's index in its launch
   double last_ms = 0.0;
+  // problems solved on the whole GPU (sem_pcg's chunked path) before the
+  // persistent launches, and their last solve times
+  std::vector<char> wide;
+  std::vector<double> wide_ms;
 };
 
 extern "C" {
@@ -154,12 +159,16 @@ int sem_batch_create(sem_mesh_t* const* meshes, const double* nu, const double* 
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->w0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->w1);
   if (e != cudaSuccess) {
     sem_batch_destroy(b);
     return cuda_error(e, "batch allocation");
   }
   b->host.resize(count);
   b->meshes.assign(meshes, meshes + count);
+  b->wide.assign(count, 0);
+  b->wide_ms.assign(count, 0.0);
   char* p = static_cast<char*>(b->ws);
   auto take = [&](size_t nbytes) {
     char* q = p;
@@ -251,6 +260,8 @@ int sem_batch_destroy(sem_batch_t* b) {
   if (b->start) cudaEventDestroy(b->start);
   if (b->t0) cudaEventDestroy(b->t0);
   if (b->t1) cudaEventDestroy(b->t1);
+  if (b->w0) cudaEventDestroy(b->w0);
+  if (b->w1) cudaEventDestroy(b->w1);
   if (b->ws) cudaFree(b->ws);
   if (b->dev) cudaFree(b->dev);
   if (b->queues) cudaFree(b->queues);
@@ -279,11 +290,48 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     // a problem whose nu or k lies outside the double-float window is solved
     // in native FP64 after the launch (none of its iterations run in it)
     if (!(df_window_ok(q[j].nu) && df_window_ok(q[j].k))) q[j].maxiter = -1;
+    // a wide problem is solved on the whole GPU before the launch
+    else if (b->wide[i]) q[j].maxiter = -2;
   }
   SEM_CUDA(cudaMemcpyAsync(b->dev, q.data(), sizeof(BProb) * b->count, cudaMemcpyHostToDevice, s));
   SEM_CUDA(cudaMemsetAsync(b->queues, 0, sizeof(int) * (kBatchMaxN + 1), s));
-  SEM_CUDA(cudaEventRecord(b->start, s));
   SEM_CUDA(cudaEventRecord(b->t0, s));
+  // ---- the wide problems, one after another on the whole GPU (sem_pcg's
+  // chunked path, the batch's arithmetic), each timed on the stream
+  double wide_total_ms = 0.0;
+  for (int j = 0; j < b->count; ++j) {
+    if (q[j].maxiter != -2) continue;
+    const int i = b->order[j];
+    sem_pcg_opts o;
+    std::memset(&o, 0, sizeof(o));
+    o.nu = q[j].nu;
+    o.k = q[j].k;
+    o.precond = b->jacobi ? SEM_PRECOND_JACOBI : SEM_PRECOND_NONE;
+    o.precision = precision;
+    o.tol = tol[i];
+    o.maxiter = (maxiter && maxiter[i] > 0) ? maxiter[i] : 0;
+    o.inner_tol = inner_tol;
+    o.max_outer = max_outer;
+    o.path = SEM_PATH_CHUNKED;
+    sem_solve_info si;
+    std::memset(&si, 0, sizeof(si));
+    SEM_CUDA(cudaEventRecord(b->w0, s));
+    const int st = sem_pcg(b->meshes[i], &o, rhs[i], x[i], &si, stream);
+    if (st != SEM_OK && st != SEM_ERR_NOT_CONVERGED && st != SEM_ERR_NAN) return st;
+    SEM_CUDA(cudaEventRecord(b->w1, s));
+    SEM_CUDA(cudaEventSynchronize(b->w1));
+    float wms = 0.0f;
+    SEM_CUDA(cudaEventElapsedTime(&wms, b->w0, b->w1));
+    b->wide_ms[i] = wms;
+    wide_total_ms += wms;
+    q[j].iters = si.iters;
+    q[j].outer = si.outer;
+    q[j].res_inf = si.res_inf;
+    q[j].res0_inf = si.res0_inf;
+    q[j].converged = si.converged;
+    q[j].nan = st == SEM_ERR_NAN;
+  }
+  SEM_CUDA(cudaEventRecord(b->start, s));
   double wtot = 0.0;
   for (auto& g : b->groups) wtot += g.work;
   int sms = 0;
@@ -313,8 +361,21 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   SEM_CUDA(cudaEventRecord(b->t1, s));
   std::vector<int> wanted(b->count);
   for (int j = 0; j < b->count; ++j) wanted[j] = q[j].maxiter;
+  std::vector<BProb> wide_res;
+  for (int j = 0; j < b->count; ++j)
+    if (wanted[j] == -2) wide_res.push_back(q[j]);
   SEM_CUDA(cudaMemcpyAsync(q.data(), b->dev, sizeof(BProb) * b->count, cudaMemcpyDeviceToHost, s));
   SEM_CUDA(cudaStreamSynchronize(s));
+  for (int j = 0, w = 0; j < b->count; ++j)  // the wide problems' results (the kernel skipped them)
+    if (wanted[j] == -2) {
+      const BProb& r = wide_res[w++];
+      q[j].iters = r.iters;
+      q[j].outer = r.outer;
+      q[j].res_inf = r.res_inf;
+      q[j].res0_inf = r.res0_inf;
+      q[j].converged = r.converged;
+      q[j].nan = r.nan;
+    }
   float ms = 0.0f;
   SEM_CUDA(cudaEventElapsedTime(&ms, b->t0, b->t1));
   b->last_ms = ms;
@@ -329,15 +390,26 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   long long tmin = 0;
   bool any = false;
   for (int j = 0; j < b->count; ++j)
-    if (q[j].maxiter >= 0 && (!any || q[j].t_start < tmin)) {
+    if (wanted[j] >= 0 && (!any || q[j].t_start < tmin)) {
       tmin = q[j].t_start;
       any = true;
     }
+  // the wide phase comes first (cluster -2), then the launches' problems
+  const long long woff = (long long)(wide_total_ms * 1e6);
+  long long wt = 0;
   for (int j = 0; j < b->count; ++j) {
     const int i = b->order[j];
-    if (q[j].maxiter < 0) continue;  // left to the host's FP64 solve
-    b->t_start[i] = q[j].t_start - tmin;
-    b->t_end[i] = q[j].t_end - tmin;
+    if (wanted[j] == -2) {
+      const long long d = (long long)(b->wide_ms[i] * 1e6);
+      b->t_start[i] = wt;
+      b->t_end[i] = wt + d;
+      b->cluster[i] = -2;
+      wt += d;
+      continue;
+    }
+    if (wanted[j] < 0) continue;  // left to the host's FP64 solve
+    b->t_start[i] = q[j].t_start - tmin + woff;
+    b->t_end[i] = q[j].t_end - tmin + woff;
     b->cluster[i] = gi_of_slot(j) * 65536 + q[j].cluster;
   }
   int bad = 0, nanc = 0;
@@ -347,7 +419,7 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     // in NaN/Inf with a finite b, is solved again by the native FP64 sem_pcg
     const double r0 = q[j].res0_inf;
     const bool finite_b = r0 == r0 && r0 <= 1.7976931348623157e308;
-    if (wanted[j] < 0 || (q[j].nan && finite_b)) {
+    if (wanted[j] == -1 || (q[j].nan && finite_b)) {
       sem_pcg_opts o;
       std::memset(&o, 0, sizeof(o));
       o.nu = q[j].nu;
@@ -440,6 +512,18 @@ int sem_batch_set_order(sem_batch_t* b, const int* order, int count) {
   return SEM_OK;
 }
 
+int sem_batch_get_wide(const sem_batch_t* b, int* wide, int count) {
+  if (!b || !wide || count != b->count) return set_error(SEM_ERR_BAD_ARG, "wide takes one entry per problem");
+  for (int i = 0; i < count; ++i) wide[i] = b->wide[i];
+  return SEM_OK;
+}
+
+int sem_batch_set_wide(sem_batch_t* b, const int* wide, int count) {
+  if (!b || !wide || count != b->count) return set_error(SEM_ERR_BAD_ARG, "wide takes one entry per problem");
+  for (int i = 0; i < count; ++i) b->wide[i] = wide[i] != 0;
+  return SEM_OK;
+}
+
 int sem_batch_timeline(const sem_batch_t* b, long long* start_ns, long long* end_ns, int* cluster, int count,
                        double* total_ms) {
   if (!b || count != b->count) return set_error(SEM_ERR_BAD_ARG, "the timeline has one entry per problem");
@@ -485,13 +569,13 @@ unsigned long long batch_signature(const sem_batch* b, const double* tol, const 
 }
 
 // cache file: one line per signature,
-//   <hex signature> <groups> {n csize mb clusters}... <count> order...
+//   <hex signature> <groups> {n csize mb clusters}... <count> order... wide...
 bool load_tuned(sem_batch* b, const char* path, unsigned long long sig) {
   FILE* f = std::fopen(path, "r");
   if (!f) return false;
   bool found = false;
   std::vector<sem_batch_group_config> cfg;
-  std::vector<int> order;
+  std::vector<int> order, wide;
   char hex[32];
   while (std::fscanf(f, "%31s", hex) == 1) {
     unsigned long long s = std::strtoull(hex, nullptr, 16);
@@ -506,19 +590,22 @@ bool load_tuned(sem_batch* b, const char* path, unsigned long long sig) {
     int cnt = 0;
     ok = ok && std::fscanf(f, "%d", &cnt) == 1 && cnt >= 0 && cnt <= (1 << 24);
     if (!ok) break;
-    std::vector<int> o(cnt);
+    std::vector<int> o(cnt), w(cnt);
     for (int j = 0; j < cnt && ok; ++j) ok = std::fscanf(f, "%d", &o[j]) == 1;
+    for (int j = 0; j < cnt && ok; ++j) ok = std::fscanf(f, "%d", &w[j]) == 1;
     if (!ok) break;
     if (s == sig && ng == (int)b->groups.size() && cnt == b->count) {
       found = true;
       cfg = c;
       order = o;
+      wide = w;
     }
   }
   std::fclose(f);
   if (!found) return false;
   for (int gi = 0; gi < (int)cfg.size(); ++gi) cfg[gi].problems = b->groups[gi].count;
   if (sem_batch_set_config(b, cfg.data(), (int)cfg.size()) != SEM_OK) return false;
+  if (sem_batch_set_wide(b, wide.data(), (int)wide.size()) != SEM_OK) return false;
   return sem_batch_set_order(b, order.data(), (int)order.size()) == SEM_OK;
 }
 
@@ -529,6 +616,7 @@ void store_tuned(const sem_batch* b, const char* path, unsigned long long sig) {
   for (const auto& g : b->groups) std::fprintf(f, " %d %d %d %d", g.n, g.csize, g.mb, g.clusters);
   std::fprintf(f, " %d", b->count);
   for (int i : b->order) std::fprintf(f, " %d", i);
+  for (char w : b->wide) std::fprintf(f, " %d", (int)w);
   std::fprintf(f, "\n");
   std::fclose(f);
 }
@@ -557,6 +645,7 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
   };
   const Opt cand[] = {{8, 2}, {4, 2}, {16, 2}, {2, 2}, {8, 1}, {4, 1}, {16, 1}};
   const std::vector<int> order0 = b->order;
+  b->wide.assign(b->count, 0);
   std::vector<Opt> opts;
   std::vector<double> wall;
   std::vector<std::vector<double>> dur;  // per option, per problem (creation order), ns
@@ -626,38 +715,113 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
       break;
     }
   }
-  // ---- verify the model's choice against the best measured shape
+  // ---- the model's shapes, measured against the best uniform shape
   size_t best_uniform = 0;
   for (size_t oi = 1; oi < opts.size(); ++oi)
     if (wall[oi] < wall[best_uniform]) best_uniform = oi;
   double best = wall[best_uniform];
   std::vector<sem_batch_group_config> keep(G);
   std::vector<int> keep_order = order0;
-  for (int gi = 0; gi < G; ++gi) keep[gi] = {b->groups[gi].n, b->groups[gi].count, opts[best_uniform].csize, opts[best_uniform].mb, 0};
-  if (feasible) {
+  std::vector<char> keep_wide(b->count, 0);
+  for (int gi = 0; gi < G; ++gi)
+    keep[gi] = {b->groups[gi].n, b->groups[gi].count, opts[best_uniform].csize, opts[best_uniform].mb, 0};
+  // per group: the shape (option), its cluster count and the durations the model uses
+  std::vector<int> g_opt(G, (int)best_uniform), g_k(G, 0);
+  auto apply_shapes = [&](const std::vector<char>& wide) {
     std::vector<int> ord = order0;
     for (int gi = 0; gi < G; ++gi) {
       const auto& g = b->groups[gi];
-      const auto& d = dur[pick[gi].opt];
-      std::stable_sort(ord.begin() + g.first, ord.begin() + g.first + g.count, [&](int p, int q) { return d[p] > d[q]; });
+      const auto& d = dur[g_opt[gi]];
+      std::stable_sort(ord.begin() + g.first, ord.begin() + g.first + g.count,
+                       [&](int p, int q) { return d[p] > d[q]; });
       auto& gg = b->groups[gi];
-      gg.csize = opts[pick[gi].opt].csize;
-      gg.mb = opts[pick[gi].opt].mb;
-      gg.clusters = G == 1 ? 0 : pick[gi].k;
+      gg.csize = opts[g_opt[gi]].csize;
+      gg.mb = opts[g_opt[gi]].mb;
+      gg.clusters = g_k[gi];
     }
     b->order = ord;
+    b->wide.assign(wide.begin(), wide.end());
+  };
+  auto run_and_keep = [&]() -> int {
     const int st = sem_batch_pcg(b, rhs, x, tol, maxiter, precision, inner_tol, max_outer, nullptr, stream);
     ++runs;
     if (st != SEM_OK && st != SEM_ERR_NOT_CONVERGED && st != SEM_ERR_NAN) return st;
     if (b->last_ms < best) {
       best = b->last_ms;
-      keep_order = ord;
+      keep_order = b->order;
+      keep_wide = b->wide;
       for (int gi = 0; gi < G; ++gi)
         keep[gi] = {b->groups[gi].n, b->groups[gi].count, b->groups[gi].csize, b->groups[gi].mb, b->groups[gi].clusters};
     }
+    return SEM_OK;
+  };
+  if (feasible) {
+    for (int gi = 0; gi < G; ++gi) {
+      g_opt[gi] = pick[gi].opt;
+      g_k[gi] = G == 1 ? 0 : pick[gi].k;
+    }
+    apply_shapes(std::vector<char>(b->count, 0));
+    SEM_CHECK(run_and_keep());
+  }
+  // ---- wide problems: the candidates are the problems whose clusters took
+  // longest; one solve puts them all on the whole GPU and times each, then
+  // the model picks how many of them (largest first) to keep wide:
+  // sum of their whole-GPU times + the makespan of the rest on the clusters
+  std::vector<int> byd(b->count);
+  for (int i = 0; i < b->count; ++i) byd[i] = i;
+  std::vector<double> dmodel(b->count);
+  for (int gi = 0; gi < G; ++gi)
+    for (int j = b->groups[gi].first; j < b->groups[gi].first + b->groups[gi].count; ++j)
+      dmodel[order0[j]] = dur[g_opt[gi]][order0[j]];
+  std::stable_sort(byd.begin(), byd.end(), [&](int p, int q) { return dmodel[p] > dmodel[q]; });
+  const int K = std::min(b->count, 32);
+  std::vector<char> cand_wide(b->count, 0);
+  for (int r = 0; r < K; ++r) cand_wide[byd[r]] = 1;
+  apply_shapes(cand_wide);
+  SEM_CHECK(run_and_keep());
+  std::vector<double> wms(b->wide_ms.begin(), b->wide_ms.end());
+  auto group_of = [&](int i) {
+    for (int gi = 0; gi < G; ++gi)
+      if (b->host[i].n == b->groups[gi].n) return gi;
+    return 0;
+  };
+  double bestT = 1e300;
+  int bestk = 0;
+  for (int k = 0; k <= K; ++k) {
+    double T = 0.0;
+    for (int r = 0; r < k; ++r) T += wms[byd[r]] * 1e6;
+    std::vector<std::vector<double>> rest(G);
+    std::vector<char> isw(b->count, 0);
+    for (int r = 0; r < k; ++r) isw[byd[r]] = 1;
+    for (int i = 0; i < b->count; ++i)
+      if (!isw[i]) rest[group_of(i)].push_back(dmodel[i]);
+    double M = 0.0;
+    for (int gi = 0; gi < G; ++gi) {
+      std::sort(rest[gi].begin(), rest[gi].end(), std::greater<double>());
+      const auto& o = opts[g_opt[gi]];
+      int kc = g_k[gi] > 0 ? g_k[gi] : max_clusters(b->groups[gi].n, o.csize, o.mb);
+      if (g_k[gi] == 0 && G > 1) {  // the work-proportional share the launch would take
+        double wtot = 0.0;
+        for (const auto& g : b->groups) wtot += g.work;
+        kc = std::max(1, (int)(sms * b->groups[gi].work / wtot * o.mb / o.csize + 0.5));
+      }
+      M = std::max(M, list_makespan(rest[gi], std::max(1, kc)));
+    }
+    T += M;
+    if (T < bestT) {
+      bestT = T;
+      bestk = k;
+    }
+  }
+  if (bestk > 0 && bestk < K) {
+    std::vector<char> w(b->count, 0);
+    for (int r = 0; r < bestk; ++r) w[byd[r]] = 1;
+    apply_shapes(w);
+    SEM_CHECK(run_and_keep());
   }
   SEM_CHECK(sem_batch_set_config(b, keep.data(), G));
   b->order = keep_order;
+  b->wide = keep_wide;
   if (cache_path) store_tuned(b, cache_path, sig);
   if (runs_out) *runs_out = runs;
   if (best_ms) *best_ms = best;

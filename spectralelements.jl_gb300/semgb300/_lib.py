@@ -183,6 +183,8 @@ SIGNATURES = {
     "sem_batch_set_order": (_I, [_P, ctypes.POINTER(_I), _I]),
     "sem_batch_timeline": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                 ctypes.POINTER(_I), _I, ctypes.POINTER(_D)]),
+    "sem_batch_get_wide": (_I, [_P, ctypes.POINTER(_I), _I]),
+    "sem_batch_set_wide": (_I, [_P, ctypes.POINTER(_I), _I]),
     "sem_batch_autotune": (_I, [_P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                 ctypes.POINTER(_D), ctypes.POINTER(_I), _I, _D, _I, ctypes.c_char_p,
                                 ctypes.POINTER(_I), ctypes.POINTER(_D), _P]),

@@ -259,6 +259,19 @@ class BatchSolver:
         o = (ctypes.c_int * n)(*[int(i) for i in order])
         _lib.check(self._lib.sem_batch_set_order(self._h, o, n))
 
+    def wide(self):
+        """Per problem: 1 if it is solved alone on the whole GPU before the
+        persistent launches (sem_pcg's chunked path), else 0."""
+        n = len(self.meshes)
+        w = (ctypes.c_int * n)()
+        _lib.check(self._lib.sem_batch_get_wide(self._h, w, n))
+        return list(w)
+
+    def set_wide(self, flags):
+        n = len(self.meshes)
+        w = (ctypes.c_int * n)(*[1 if f else 0 for f in flags])
+        _lib.check(self._lib.sem_batch_set_wide(self._h, w, n))
+
     def timeline(self):
         """Per-problem timeline of the last solve: start and end (ns from the
         first start, device clock), the cluster that solved it (unique over the
@@ -280,7 +293,9 @@ class BatchSolver:
         cluster count and the queue order from measured per-problem
         timelines (``sem_batch_autotune``); the choice is kept on the batch
         and, with ``cache`` (a file path), stored under the batch's signature
-        and reused by later calls.  Returns dict(runs, best_ms, config)."""
+        and reused by later calls; it also decides which of the longest
+        problems to solve alone on the whole GPU (wide()).  Returns
+        dict(runs, best_ms, config, wide)."""
         n = len(self.meshes)
         bs = [as_local(b) for b in bs]
         if xs is None:
@@ -295,7 +310,7 @@ class BatchSolver:
                                                 0 if max_outer is None else int(max_outer),
                                                 None if cache is None else str(cache).encode(),
                                                 ctypes.byref(runs), ctypes.byref(best), stream_ptr()))
-        return dict(runs=runs.value, best_ms=best.value, config=self.config())
+        return dict(runs=runs.value, best_ms=best.value, config=self.config(), wide=self.wide())
 
 
 def pcg_(x, b, opA, **kw):

@@ -161,9 +161,10 @@ def test_batch_autotune_chooses_persists_and_reloads(gpu, tmp_path):
     cache = tmp_path / "batch_tune.txt"
     solver = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
     r = solver.autotune(bs, tols, precision=S.SEM_MIXED, cache=cache)
-    assert r["runs"] >= 2 and r["best_ms"] > 0
-    chosen, order = solver.config(), solver.order()
+    assert r["runs"] >= 3 and r["best_ms"] > 0
+    chosen, order, wide = solver.config(), solver.order(), solver.wide()
     assert sorted(order) == list(range(len(probs)))
+    assert len(wide) == len(probs) and set(wide) <= {0, 1} and r["wide"] == wide
     for c in chosen:
         assert c["cluster_size"] in (2, 4, 8, 16) and c["ctas_per_sm"] in (1, 2) and c["clusters"] >= 0
     # the tuned batch solves correctly
@@ -177,8 +178,45 @@ def test_batch_autotune_chooses_persists_and_reloads(gpu, tmp_path):
     again = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
     r2 = again.autotune(bs, tols, precision=S.SEM_MIXED, cache=cache)
     assert r2["runs"] == 0
-    assert again.config() == chosen and again.order() == order
+    assert again.config() == chosen and again.order() == order and again.wide() == wide
     # another tolerance is another signature
     other = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
     r3 = other.autotune(bs, [2 * t for t in tols], precision=S.SEM_MIXED, cache=cache)
-    assert r3["runs"] >= 2
+    assert r3["runs"] >= 3
+
+
+@pytest.mark.parametrize("precision", ["DF", "MIXED"])
+def test_batch_wide_problems_solve_on_the_whole_gpu(gpu, precision):
+    """Problems marked wide are solved alone on the whole GPU before the
+    persistent launches; the batch's results stay converged and match the
+    all-cluster solve to the tolerance, and the timeline puts them first."""
+    import semgb300 as S
+    probs = _problems(14, 10)
+    ms, bs, tols, refs = [], [], [], []
+    for (n, Ex, Ey, nu, lam) in probs:
+        mo, md = meshes(n, Ex, Ey, (False, False), "DDDD", 0.05)
+        M = O.generateMask(["D"] * 4, mo)
+        b = _rhs(mo, M)
+        ms.append(md)
+        bs.append(S.as_local(b))
+        tols.append(1e-10 * np.abs(b).max())
+        refs.append((mo, M, b, nu, lam))
+    prec = getattr(S, "SEM_" + ("F64_DF" if precision == "DF" else precision))
+    solver = S.BatchSolver(ms, [p[3] for p in probs], [p[4] for p in probs], jacobi=True)
+    x0 = [host(x) for x in solver.solve(bs, tols, precision=prec)]
+    wide = [1 if i in (0, 3, 7) else 0 for i in range(len(probs))]
+    solver.set_wide(wide)
+    assert solver.wide() == wide
+    infos = []
+    xs = solver.solve(bs, tols, precision=prec, infos=infos)
+    for x, xr, inf, (mo, M, b, nu, lam) in zip(xs, x0, infos, refs):
+        assert inf["converged"], inf
+        assert rel_l2(host(x), xr) < 1e-8
+        res = b - O.mask(O.gatherScatter(O.hlmz(host(x), nu, lam, mo), mo), M)
+        assert np.abs(res).max() <= 2 * np.abs(b).max() * 1e-10 + 1e-300
+    tl = solver.timeline()
+    widx = [i for i, w in enumerate(wide) if w]
+    rest = [i for i, w in enumerate(wide) if not w]
+    assert all(tl["cluster"][i] == -2 for i in widx)
+    assert all(tl["cluster"][i] >= 0 for i in rest)
+    assert max(tl["end_ns"][i] for i in widx) <= min(tl["start_ns"][i] for i in rest)
