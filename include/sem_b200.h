@@ -332,7 +332,9 @@ int sem_batch_pcg(sem_batch_t* batch, const double* const* b, double* const* x, 
  * cluster_size CTAs per cluster (2, 4, 8 or 16), ctas_per_sm resident CTAs
  * per SM asked of the register allocator (1: up to 255 registers a thread,
  * 2: up to 128), and clusters persistent clusters (0: the group's share of
- * the SMs in proportion to its estimated work).  The default is 8, 2, 0.
+ * the estimated work times the clusters of its shape the device holds at
+ * once, so that all groups' clusters are resident together; the heaviest
+ * group launches first).  The default is 8, 2, 0.
  * n and problems are filled by sem_batch_get_config and checked by
  * sem_batch_set_config.  The queue order (sem_batch_get_order /
  * sem_batch_set_order) lists problem indices slot by slot; a group's slots
@@ -352,9 +354,10 @@ int sem_batch_pcg(sem_batch_t* batch, const double* const* b, double* const* x, 
  * sem_batch_autotune solves the batch once per launch shape that fits every
  * group (all groups alike, default cluster counts), builds each group's
  * makespan model from the measured per-problem durations (list scheduling
- * onto k clusters, largest first; a cluster costs cluster_size/ctas_per_sm
- * SMs), picks per group the shape and cluster count of the smallest makespan
- * whose SM costs fit the device and orders each group's queue by measured
+ * onto k clusters, largest first; a cluster costs the fraction of the device
+ * one cluster of its shape takes when the device holds as many as fit),
+ * picks per group the shape and cluster count of the smallest makespan whose
+ * costs fit the device together and orders each group's queue by measured
  * duration.  It then solves once with the 32 longest problems wide, which
  * times each of them on the whole GPU, and picks how many of them (longest
  * first) to keep wide: the sum of their whole-GPU times plus the modelled

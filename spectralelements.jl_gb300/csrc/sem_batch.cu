@@ -334,9 +334,16 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   SEM_CUDA(cudaEventRecord(b->start, s));
   double wtot = 0.0;
   for (auto& g : b->groups) wtot += g.work;
-  int sms = 0;
-  SEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+  // the heaviest group launches first; each group's default cluster count is
+  // its share of the estimated work times the clusters of its shape that fit
+  // the device at once, so that every group's clusters are resident together
+  // (clusters are placed within one GPC each, so 38 clusters of 8 do not fit
+  // 152 SMs at two CTAs each)
+  std::vector<int> launch_order(b->groups.size());
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) launch_order[gi] = (int)gi;
+  std::stable_sort(launch_order.begin(), launch_order.end(),
+                   [&](int p, int q) { return b->groups[p].work > b->groups[q].work; });
+  for (int gi : launch_order) {
     auto& g = b->groups[gi];
     BatchCommon c;
     c.probs = b->dev + g.first;
@@ -349,10 +356,8 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
     c.max_outer = max_outer > 0 ? max_outer : (rr ? 100 : 6);
     c.cluster_size = g.csize;
     c.ctas_per_sm = g.mb;
-    // default share: the group's fraction of the estimated work, in SMs
     c.clusters = g.clusters > 0 ? g.clusters
-                 : b->groups.size() == 1 ? 0
-                 : std::max(1, (int)(sms * g.work / wtot * g.mb / g.csize + 0.5));
+                 : std::max(1, (int)(max_clusters(g.n, g.csize, g.mb) * g.work / wtot));
     SEM_CUDA(cudaStreamWaitEvent(g.stream, b->start, 0));
     SEM_CHECK(launch_group(g.n, c, *g.ops, g.stream));
     SEM_CUDA(cudaEventRecord(g.done, g.stream));
@@ -635,8 +640,6 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
     if (best_ms) *best_ms = 0.0;
     return SEM_OK;
   }
-  int sms = 0;
-  SEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
   const int G = (int)b->groups.size();
   // ---- measure every launch shape that fits every group, all groups alike,
   // with the default (work-proportional) cluster counts and the estimated order
@@ -671,9 +674,10 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
   }
   if (opts.empty()) return set_error(SEM_ERR_UNSUPPORTED, "no batch launch shape fits");
   // ---- model: per group and shape, the makespan of k clusters under list
-  // scheduling of the measured durations, largest first; the SM cost of a
-  // cluster is csize / mb.  The smallest makespan T whose cheapest per-group
-  // choices fit the SMs wins.
+  // scheduling of the measured durations, largest first; a cluster costs the
+  // fraction 1/fit of the device, fit being the clusters of that shape that
+  // the device holds at once.  The smallest makespan T whose cheapest
+  // per-group choices fit the device together wins.
   struct Choice {
     double T, cost;
     int opt, k;
@@ -686,10 +690,11 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
       std::vector<double> d;
       for (int j = g.first; j < g.first + g.count; ++j) d.push_back(dur[oi][b->order[j]]);
       std::sort(d.begin(), d.end(), std::greater<double>());
-      const int kmax = std::min(g.count, max_clusters(g.n, opts[oi].csize, opts[oi].mb));
+      const int fit = max_clusters(g.n, opts[oi].csize, opts[oi].mb);
+      const int kmax = std::min(g.count, fit);
       for (int k = 1; k <= kmax; ++k) {
         const double T = list_makespan(d, k);
-        ch[gi].push_back({T, (double)k * opts[oi].csize / opts[oi].mb, (int)oi, k});
+        ch[gi].push_back({T, (double)k / fit, (int)oi, k});
         Ts.push_back(T);
       }
     }
@@ -710,7 +715,7 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
       pick[gi] = *best;
       total += best->cost;
     }
-    if (total <= (double)sms) {
+    if (total <= 1.0) {
       feasible = true;
       break;
     }
@@ -758,7 +763,7 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
   if (feasible) {
     for (int gi = 0; gi < G; ++gi) {
       g_opt[gi] = pick[gi].opt;
-      g_k[gi] = G == 1 ? 0 : pick[gi].k;
+      g_k[gi] = pick[gi].k;
     }
     apply_shapes(std::vector<char>(b->count, 0));
     SEM_CHECK(run_and_keep());
@@ -799,11 +804,11 @@ int sem_batch_autotune(sem_batch_t* b, const double* const* rhs, double* const* 
     for (int gi = 0; gi < G; ++gi) {
       std::sort(rest[gi].begin(), rest[gi].end(), std::greater<double>());
       const auto& o = opts[g_opt[gi]];
-      int kc = g_k[gi] > 0 ? g_k[gi] : max_clusters(b->groups[gi].n, o.csize, o.mb);
-      if (g_k[gi] == 0 && G > 1) {  // the work-proportional share the launch would take
+      int kc = g_k[gi];
+      if (kc == 0) {  // the default share the launch would take
         double wtot = 0.0;
         for (const auto& g : b->groups) wtot += g.work;
-        kc = std::max(1, (int)(sms * b->groups[gi].work / wtot * o.mb / o.csize + 0.5));
+        kc = std::max(1, (int)(max_clusters(b->groups[gi].n, o.csize, o.mb) * b->groups[gi].work / wtot));
       }
       M = std::max(M, list_makespan(rest[gi], std::max(1, kc)));
     }
