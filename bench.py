@@ -574,9 +574,11 @@ def bench_batch(S):
                      "mixed": "FP32 inner CG inside FP64 defect-correction sweeps",
                      "mixed_rr": "FP32 CG with FP64 residual replacement"}}
     default_cfg, default_order = solver.config(), solver.order()
-    cache = os.path.join(os.environ.get("TMPDIR", "/tmp"), "sem_batch_tune_bench.txt")
-    if os.path.exists(cache):
-        os.remove(cache)  # tune afresh on this device
+    # the autotuner's choices persist per batch signature (device, arithmetic,
+    # every problem's shape, coefficients and tolerance) in the package's
+    # cache file; a signature found there is loaded without solving
+    cache = os.path.join(ROOT, "spectralelements.jl_gb300", "semgb300", "tuned", "batch.txt")
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
 
     def timed(prec):
         infos = []
@@ -618,7 +620,9 @@ def bench_batch(S):
                      "tuned_config": [{k: c[k] for k in ("n", "problems", "cluster_size", "ctas_per_sm", "clusters")}
                                       for c in tune["config"]],
                      "wide_problems": sum(tune["wide"]),
-                     "tune": {"solves": tune["runs"], "seconds": tune_s}, "timeline": timeline_summary(),
+                     "tune": {"solves": tune["runs"], "seconds": tune_s,
+                              "source": "loaded from the tuning cache" if tune["runs"] == 0 else "tuned now"},
+                     "timeline": timeline_summary(),
                      "default": {"batch_s": dt0, "solves_per_s": 512 / dt0,
                                  "config": "cluster_size 8, ctas_per_sm 2, work-proportional cluster counts, "
                                            "estimated-work order", "timeline": tl0}}
