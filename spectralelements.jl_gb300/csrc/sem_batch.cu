@@ -420,11 +420,13 @@ int sem_batch_pcg(sem_batch_t* b, const double* const* rhs, double* const* x, co
   int bad = 0, nanc = 0;
   for (int j = 0; j < b->count; ++j) {
     const int i = b->order[j];
-    // range guard: a problem outside the double-float window, or one that ended
-    // in NaN/Inf with a finite b, is solved again by the native FP64 sem_pcg
+    // range guard: a problem outside the double-float window, one that ended
+    // in NaN/Inf with a finite b, or one whose b lies below 2^-60, is solved
+    // again by the native FP64 sem_pcg
     const double r0 = q[j].res0_inf;
     const bool finite_b = r0 == r0 && r0 <= 1.7976931348623157e308;
-    if (wanted[j] == -1 || (q[j].nan && finite_b)) {
+    const bool tiny_b = wanted[j] >= 0 && r0 > 0.0 && r0 < 0x1p-60;  // as pcg_guarded
+    if (wanted[j] == -1 || (q[j].nan && finite_b) || tiny_b) {
       sem_pcg_opts o;
       std::memset(&o, 0, sizeof(o));
       o.nu = q[j].nu;

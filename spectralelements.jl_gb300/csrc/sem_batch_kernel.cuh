@@ -488,6 +488,8 @@ __device__ void bcg(const BatchArgs<N>& a, BProb& pr, cg::cluster_group& cl, int
   unsigned long long m1[1] = {acc.max_bits()};
   cluster_reduce<1, 1>(cl, red, rc, s1, m1);
   double t = df2d(s1[0]), rmax = bits_to_double(m1[0]);
+  // the FP64-vector solve starts from x = 0: its first max|r| is max|b|
+  if (P::kPrecision == SEM_F64_DF && rank == 0 && threadIdx.x == 0) pr.res0_inf = rmax;
   double tprev = 1.0;
   int k = 0;
   bool nan = rmax != rmax;

@@ -1149,9 +1149,10 @@ int pcg_core(const OpCtx& cx0, const WS& w, sem_mesh* m, const sem_pcg_opts* o, 
 // pcg_core with the range guard of the pair and FP32 arithmetics: a solve
 // whose scalar coefficients lie outside the double-float window runs in native
 // FP64 from the start, and a double-float or mixed solve that ends in NaN or
-// Inf although b is finite (a value the pair or FP32 format cannot carry) is
-// solved again in native FP64 (operator, vectors and dots), on the chunked
-// path.  A NaN or Inf in b itself is reported as before.
+// Inf although b is finite (a value the pair or FP32 format cannot carry), or
+// whose b lies below 2^-60 in magnitude, is solved again in native FP64
+// (operator, vectors and dots), on the chunked path.  A NaN or Inf in b
+// itself is reported as before.
 int pcg_guarded(const OpCtx& cx, const WS& w, sem_mesh* m, const sem_pcg_opts* o, const double* b, double* x,
                 sem_solve_info* info, cudaStream_t s) {
   sem_pcg_opts o64 = *o;
@@ -1163,7 +1164,11 @@ int pcg_guarded(const OpCtx& cx, const WS& w, sem_mesh* m, const sem_pcg_opts* o
   std::memset(&mine, 0, sizeof(mine));
   const int st = pcg_core(cx, w, m, o, b, x, &mine, s);
   const double r0 = mine.res0_inf;
-  if (st == SEM_ERR_NAN && o->precision != SEM_F64 && r0 == r0 && r0 <= 1.7976931348623157e308) {
+  // a right-hand side below 2^-60 takes the solve's vectors below the pair
+  // format's accurate range (2^-101) by the usual 1e-12 reduction
+  const bool tiny_b = r0 > 0.0 && r0 < 0x1p-60;
+  if (o->precision != SEM_F64 &&
+      ((st == SEM_ERR_NAN && r0 == r0 && r0 <= 1.7976931348623157e308) || tiny_b)) {
     const int st64 = pcg_core(cx, w, m, &o64, b, x, info, s);
     if (info) info->outer += mine.outer;
     return st64;
