@@ -104,12 +104,12 @@ __device__ __forceinline__ df d2df(double x) {
 // an absolute resolution of 2^-149.  Loads split with d2df_op, which turns a
 // magnitude at or above 2^90 (and Inf) into NaN, so that intermediates never
 // overflow silently, and a nonzero magnitude below 2^-126 (which the split
-// would flush to zero) into the smallest FP32 subnormal of its sign: as
-// negligible as zero next to values of ordinary size, but not zero, so that a
-// row made only of such values gives a tiny nonzero result.  A NaN or Inf
-// result flags the call, and so does a row whose stiffness sum (before nu) or
-// result is tiny throughout, below 2^-90 and not zero: it is small because of
-// its scale.  The host side re-runs a flagged call in native FP64.
+// would flush to zero) into NaN as well: a marker value would not survive the
+// arithmetic (products of the smallest subnormals underflow to zero, and the
+// derivative of a constant row is zero).  A NaN or Inf result flags the
+// call, and so does a row whose stiffness sum (before nu) or result is tiny
+// throughout, below 2^-90 and not zero: it is small because of its scale.
+// The host side re-runs a flagged call in native FP64.
 constexpr unsigned kDfExpHi = 1023u + 90u;   // first biased exponent that is poisoned
 constexpr unsigned kDfExpLo = 1023u - 126u;  // nonzero values below this biased exponent are poisoned
 constexpr float kRowTiny = 0x1p-90f;
@@ -117,9 +117,8 @@ __device__ __forceinline__ df d2df_op(double x) {
   const unsigned hi = (unsigned)__double2hiint(x);
   const unsigned mag = hi & 0x7fffffffu;
   df v = d2df(x);
-  if (mag >= (kDfExpHi << 20)) v = {__uint_as_float(0x7fc00000u), 0.0f};
-  else if (mag < (kDfExpLo << 20) && (mag | (unsigned)__double2loint(x)) != 0u)
-    v = {__uint_as_float((hi & 0x80000000u) | 1u), 0.0f};
+  if (mag >= (kDfExpHi << 20) || (mag < (kDfExpLo << 20) && (mag | (unsigned)__double2loint(x)) != 0u))
+    v = {__uint_as_float(0x7fc00000u), 0.0f};
   return v;
 }
 
