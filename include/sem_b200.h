@@ -152,12 +152,10 @@ int sem_hlmz(sem_mesh_t* mesh, const double* nu_field, double nu, double k,
              const double* u, double* out, unsigned flags, sem_stream_t stream);
 /* hlmz with mask(QQ') on HOST buffers (the end-to-end call): u_host and
  * out_host are column-major host arrays of the local layout.
- *  - slabs >= 1 (0: 8): u moves in by the copy engines in that many slabs
- *    of element-tile rows, overlapping the kernels.  When out_host is
- *    addressable by the device (pinned: cudaHostAlloc / cudaHostRegister),
- *    the kernels write the result into it in place; otherwise it moves out
- *    by the copy engines in slabs as well.  Pinned host memory is needed for
- *    the overlap; pageable memory works with serialised copies.
+ *  - slabs >= 1 (0: 8): the field moves in and out in that many slabs of
+ *    element-tile rows by the copy engines, overlapping the kernels; pinned
+ *    host memory is needed for that overlap, pageable memory works with
+ *    serialised copies.
  *  - slabs = SEM_HOST_DIRECT: the operator kernels read u_host and write
  *    out_host in place over the CPU-GPU link; the buffers must be addressable
  *    by the device (cudaHostAlloc / cudaHostRegister memory, or any host

@@ -165,11 +165,7 @@ extern "C" int sem_hlmz_host(sem_mesh_t* m, const double* nu_field, double nu, d
   HostPipe* p = nullptr;
   SEM_CHECK(get_pipe(m, L, &p));
   c.u = p->u;
-  // results go straight into a host buffer the device can address (the
-  // kernels' stores cross the CPU-GPU link while they compute, no copy-engine
-  // pass back); otherwise through the device buffer and copy-engine slabs
-  const bool out_direct = device_can_address(out_host, false);
-  c.out = out_direct ? out_host : p->o;
+  c.out = p->o;
 
   int TX = 1, TY = 1;
   tile_shape_of(g.n, &TX, &TY);
@@ -202,12 +198,6 @@ extern "C" int sem_hlmz_host(sem_mesh_t* m, const double* nu_field, double nu, d
     const long long key_hi = i + 1 < K ? c0[i + 1] : (1LL << 62);
     SEM_CHECK(launch_apply_window(g, m->ops, c, c0[i], key_hi, s));
     SEM_CUDA(cudaEventRecord(p->ev_fix[i], s));
-  }
-  if (out_direct) {
-    SEM_CUDA(cudaEventRecord(p->done, s));
-    if (!c.rflag) return SEM_OK;
-    c.u = p->u;
-    return launch_guard_rerun(g, m->ops, c, s);  // writes out_host in place, as the windows did
   }
   // slab i is final after the fixup of slab i + 1 (their shared interface);
   // with a periodic y direction slab 0 also waits for the last slab (the wrap)

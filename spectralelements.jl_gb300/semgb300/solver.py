@@ -52,11 +52,10 @@ class HelmholtzOp:
         """opA on HOST buffers (``sem_hlmz_host``): u_host is a CPU float64
         tensor in the column-major local layout; the result goes to ``out`` (a
         CPU tensor of the same layout, pinned if None) and is complete once the
-        current stream has synchronised.  ``slabs``: k >= 1 (0: 8) stages u
-        in k slabs through the copy engines, overlapped with the kernels, and
-        the kernels write a pinned ``out`` in place (a pageable one returns
-        through copy-engine slabs); ``_lib.SEM_HOST_DIRECT`` has the kernels
-        read and write the host buffers in place over the CPU-GPU link.  A ``nu_field`` (a device
+        current stream has synchronised.  ``slabs``: k >= 1 (0: 8) stages the
+        field in k slabs through the copy engines, overlapped with the
+        kernels; ``_lib.SEM_HOST_DIRECT`` has the kernels read and write the
+        host buffers in place over the CPU-GPU link.  A ``nu_field`` (a device
         field) is folded into G as in ``__call__``."""
         lib = _lib.load()
         msh = self.msh
