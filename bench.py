@@ -355,6 +355,8 @@ def run_ours(args, rank, world, local_rank):
         msh.set_precision(S.SEM_F64_DF)
         if "pcg" in extras:
             result["pcg"] = bench_pcg(S, msh, stream)
+        elif "small" in extras:  # cfg1/cfg3 only
+            result["pcg"] = bench_pcg(S, msh, stream, parts=("small",))
         if "sweep" in extras:
             result["sweep"] = bench_sweep(S, stream)
         if "batch" in extras:
@@ -396,13 +398,24 @@ def fourier_forcing(msh_x, msh_y, seed, nmodes=16):
     return f
 
 
-def bench_pcg(S, msh, stream):
+def bench_pcg(S, msh, stream, parts=("cfg2", "small")):
     """Jacobi PCG to 1e-8 relative residual: native FP64, double-float (FP64
     storage, FP32-pair arithmetic) and mixed precision (FP32 inner CG to
-    1e-4, <= 6 FP64 defect-correction sweeps; or residual replacement)."""
+    1e-4, <= 6 FP64 defect-correction sweeps; or residual replacement).
+    ``parts``: "cfg2" (256x256) and "small" (cfg1/cfg3, 8x8)."""
     import numpy as np
     import torch
     out = {}
+    if "cfg2" in parts:
+        bench_pcg_cfg2(S, msh, out)
+    if "small" in parts:
+        bench_pcg_small(S, out)
+    return out
+
+
+def bench_pcg_cfg2(S, msh, out):
+    import numpy as np
+    import torch
     # cfg2: Helmholtz 256x256, N=8, 16 Fourier modes (seed 2)
     f = fourier_forcing(msh.x, msh.y, 2)
     M = S.generateMask("DDDD", msh)
@@ -446,6 +459,11 @@ def bench_pcg(S, msh, stream):
                              "whenever it has fallen by 0.3; search direction kept"},
         "mixed_over_fp64": dt64 / dtm, "mixed_rr_over_fp64": dt64 / dtr,
         "mixed_over_df64": dtd / dtm, "mixed_rr_over_df64": dtd / dtr}
+
+
+def bench_pcg_small(S, out):
+    import numpy as np
+    import torch
     # cfg1 / cfg3: Poisson 8x8, N=8, amp 0.1, exact solution sin(pi x) sin(pi y), 1e-10
     m1 = S.Mesh(9, 9, 8, 8, (False, False), sin_deform(0.1), bc="DDDD")
     m1.autotune(S.SEM_F64_DF)
@@ -480,7 +498,6 @@ def bench_pcg(S, msh, stream):
     r["note"] = ("cfg1_fp64: native FP64 arithmetic throughout; cfg1_df64: double-float operator and dots; "
                  "cfg3_mixed: FP32 inner CG in one thread block, double-float FP64 residual sweeps")
     out["cfg1_cfg3_poisson_8x8_n8"] = r
-    return out
 
 
 def d2d_problem(S, msh):

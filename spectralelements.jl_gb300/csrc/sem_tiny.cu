@@ -67,9 +67,9 @@ struct TinyRed {
 
 // shared-memory layout in 4-byte words for a strip of L local points: the
 // persistent block (G11, G12, G22, [B], [dinv]), the work block (x32, r32,
-// p32, line buffers A and B), the reduction slots and the line bits
+// p32, line buffers A, B, C and D), the reduction slots and the line bits
 struct TinyLayout {
-  long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, red, bits, words;
+  long long g11, g12, g22, b, dinv, x32, r32, p32, la, lb, lc, ld, red, bits, words;
 };
 
 __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool jac, long long nbits) {
@@ -86,6 +86,8 @@ __host__ __device__ inline TinyLayout tiny_layout(long long L, bool mass, bool j
   t.p32 = o; o += L;
   t.la = o; o += L;
   t.lb = o; o += L;
+  t.lc = o; o += L;
+  t.ld = o; o += L;
   o = (o + 1) & ~1LL;
   t.red = o; o += (long long)(sizeof(TinyRed) / 4);
   t.bits = o; o += (nbits + 3) / 4;  // line bits of the rows, then of the columns
@@ -213,9 +215,57 @@ struct TinyDims {
   int C, rank, c0, NYs;  // cluster size, this CTA's rank, first column and columns of its strip
   int r0, e0, dr, de;    // row-line walk
   int x0, cc0, dx, dc;   // column-line walk
+  // the FP32 inner loop runs two threads per line, in two warps: warp pair k
+  // takes lines 32 k + lane, 32 k + lane + T/2, ...; half h = warp & 1 owns
+  // the points j < H or j >= N - H of a line (h = 0) or the others (h = 1),
+  // H = ceil(N/4), and forms the contraction outputs at those points
+  int pl0, pls, half;
+  int pr0, pe0, pdr, pde;  // pair row-line walk
+  int px0, pcc0, pdx, pdc; // pair column-line walk
   const unsigned char* rinfo;  // line bits (shared-memory copies, whole mesh)
   const unsigned char* cinfo;
 };
+
+// the points of a line that half HH owns
+template <int N, int HH>
+__device__ __forceinline__ constexpr bool tiny_owns(int j) {
+  return (j < (N / 2 + 1) / 2 || j >= N - (N / 2 + 1) / 2) == (HH == 0);
+}
+
+// eo_apply for the outputs half h owns: the even-odd sums in full, then the
+// rows i of the half's pairs (i, N-1-i), and the middle output for h = 1
+template <class P, int N, int HH>
+__device__ __forceinline__ void eo_apply_half(const EOCoef<N, typename P::v>& D, const typename P::v (&x)[N],
+                                              typename P::v (&y)[N]) {
+  typedef typename P::v V;
+  constexpr int M = N / 2;
+  constexpr int H = (M + 1) / 2;
+  V e[M], o[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    e[k] = P::add_u(x[k], x[N - 1 - k]);
+    o[k] = P::sub_u(x[k], x[N - 1 - k]);
+  }
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    if ((i < H) != (HH == 0)) continue;
+    V s = P::mul(D.A[i][0], o[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) s = P::fma(D.A[i][k], o[k], s);
+    V t = P::mul(D.Cc[i][0], e[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) t = P::fma(D.Cc[i][k], e[k], t);
+    if (N & 1) t = P::fma(D.cm[i], x[M], t);
+    y[i] = P::add_u(s, t);
+    y[N - 1 - i] = P::sub_u(s, t);
+  }
+  if ((N & 1) && HH == 1) {
+    V s = P::mul(D.mr[0], o[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) s = P::fma(D.mr[k], o[k], s);
+    y[M] = s;
+  }
+}
 
 __device__ __forceinline__ void tiny_step(int& a, int& b, int da, int db, int n) {
   a += da;
@@ -376,6 +426,139 @@ __device__ __forceinline__ void tiny_points(const TinyDims& d, bool ones, bool h
   }
 }
 
+// The FP32 operator of the inner loop with two threads per line (pair walks
+// of TinyDims), in three phases without barriers; the caller separates them
+// with block barriers at the same program point for every warp:
+// res = nu (D'G D u) + k B u, unassembled, left in A.  Each half reads whole
+// lines and writes only the points it owns, so no line buffer is read and
+// written by different threads in one phase: P1 writes ur to A and us to Bf,
+// P2 reads them and writes wr to Cb and os to Db, P3 reads Cb and its own
+// points of Db and writes res to A.  P3 adds this thread's part of u . res
+// over its points to acc.
+template <int N, int HH, class UF>
+__device__ __forceinline__ void tiny_pair_p1(const TinyDims& d, UF&& ufun, float* A, float* Bf,
+                                             const EOCoef<N, float>& Dr, const EOCoef<N, float>& Ds) {
+  const int NX = d.NX;
+  const int EN = N * NX;
+  int r = d.pr0, e = d.pe0, x = d.px0, c = d.pcc0;
+  for (int l = d.pl0; l < d.nl; l += d.pls) {
+    {
+      const int q0 = r + e * EN;
+      float xs[N], ys[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) xs[j] = ufun(q0 + j * NX);
+      eo_apply_half<PF32, N, HH>(Ds, xs, ys);
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        if (tiny_owns<N, HH>(j)) Bf[q0 + j * NX] = ys[j];
+    }
+    {
+      const int b0 = x * N + c * NX;
+      float xs[N], ys[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) xs[i] = ufun(b0 + i);
+      eo_apply_half<PF32, N, HH>(Dr, xs, ys);
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (tiny_owns<N, HH>(i)) A[b0 + i] = ys[i];
+    }
+    tiny_step(r, e, d.pdr, d.pde, NX);
+    tiny_step(x, c, d.pdx, d.pdc, d.Ex);
+  }
+}
+
+template <int N, int HH>
+__device__ __forceinline__ void tiny_pair_p2(const TinyDims& d, const float* A, const float* Bf, float* Cb,
+                                             float* Db, const float* G11, const float* G12, const float* G22,
+                                             const EOCoef<N, float>& Dst) {
+  const int NX = d.NX;
+  const int EN = N * NX;
+  int r = d.pr0, e = d.pe0;
+  for (int l = d.pl0; l < d.nl; l += d.pls) {
+    const int q0 = r + e * EN;
+    float ws[N], os[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const int q = q0 + j * NX;
+      const float ur = A[q], us = Bf[q];
+      const float g12 = G12[q];
+      ws[j] = __fmaf_rn(g12, ur, G22[q] * us);
+      if (tiny_owns<N, HH>(j)) Cb[q] = __fmaf_rn(G11[q], ur, g12 * us);
+    }
+    eo_apply_half<PF32, N, HH>(Dst, ws, os);
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+      if (tiny_owns<N, HH>(j)) Db[q0 + j * NX] = os[j];
+    tiny_step(r, e, d.pdr, d.pde, NX);
+  }
+}
+
+template <int N, int HH, class UF>
+__device__ __forceinline__ void tiny_pair_p3(const TinyDims& d, UF&& ufun, float* A, const float* Cb,
+                                             const float* Db, const float* Bm, float nu, float kk,
+                                             const EOCoef<N, float>& Drt, float& acc) {
+  const int NX = d.NX;
+  int x = d.px0, c = d.pcc0;
+  for (int l = d.pl0; l < d.nl; l += d.pls) {
+    const int b0 = x * N + c * NX;
+    float xs[N], ys[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) xs[i] = Cb[b0 + i];
+    eo_apply_half<PF32, N, HH>(Drt, xs, ys);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      if (!tiny_owns<N, HH>(i)) continue;
+      const int q = b0 + i;
+      float res = nu * (ys[i] + Db[q]);
+      const float u = ufun(q);
+      if (Bm) res = __fmaf_rn(kk * Bm[q], u, res);
+      acc = __fmaf_rn(u, res, acc);
+      A[q] = res;
+    }
+    tiny_step(x, c, d.pdx, d.pdc, d.Ex);
+  }
+}
+
+// a thread's partial sum and maximum (FP32 magnitude bits) over its points
+struct TinyAcc {
+  float s;
+  unsigned m;
+};
+
+// run f(point, acc) over the points this half owns of its pair's row lines;
+// returns the accumulated partials (f captures values only, so nothing of
+// the caller needs an address)
+template <int N, int HH, class F>
+__device__ __forceinline__ TinyAcc tiny_points_pair(const TinyDims& d, bool ones, bool has_bc, F f) {
+  TinyAcc acc = {0.0f, 0u};
+  int r = d.pr0, e = d.pe0;
+  for (int l = d.pl0; l < d.nl; l += d.pls) {
+    const unsigned char br = d.rinfo[r];
+    const int r2 = (int)line_partner(r, br, d.NX);
+    const float mr = (!ones && (br & L_COPY2)) ? 0.5f : 1.0f;
+    const bool zr = has_bc && (br & L_ZERO);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      if (!tiny_owns<N, HH>(j)) continue;
+      const int cl = e * N + j;
+      const int c = d.c0 + cl;
+      const unsigned char bc = d.cinfo[c];
+      TinyPt p;
+      p.q = r + cl * d.NX;
+      p.g = p.q + d.c0 * d.NX;
+      p.r = r;
+      p.c = c;
+      p.r2 = r2;
+      p.c2 = (int)line_partner(c, bc, d.NY);
+      p.mult = (!ones && (bc & L_COPY2)) ? 0.5f * mr : mr;
+      p.zero = zr || (has_bc && (bc & L_ZERO));
+      f(p, acc);
+    }
+    tiny_step(r, e, d.pdr, d.pde, d.NX);
+  }
+  return acc;
+}
+
 // The FP64 defect-correction step of a sweep: x += x32 (FP64, global), then
 // r = b - A x with the double-float operator in the work block (free while no
 // inner solve runs), and the cluster maximum of |r|.  A separate function, so
@@ -449,6 +632,8 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   float* p32 = sm + lay.p32;
   float* LA = sm + lay.la;
   float* LB = sm + lay.lb;
+  float* LC = sm + lay.lc;
+  float* LD = sm + lay.ld;
   TinyRed& red = *reinterpret_cast<TinyRed*>(sm + lay.red);
   unsigned char* bits = reinterpret_cast<unsigned char*>(sm + lay.bits);
   const int T = blockDim.x;
@@ -471,6 +656,20 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
   dm.cc0 = (int)threadIdx.x / dm.Ex;
   dm.dx = T % dm.Ex;
   dm.dc = T / dm.Ex;
+  {  // pair walks: T is a multiple of 64
+    const int w = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    dm.half = w & 1;
+    dm.pl0 = (w >> 1) * 32 + lane;
+    dm.pls = T / 2;
+    dm.pr0 = dm.pl0 % NX;
+    dm.pe0 = dm.pl0 / NX;
+    dm.pdr = dm.pls % NX;
+    dm.pde = dm.pls / NX;
+    dm.px0 = dm.pl0 % dm.Ex;
+    dm.pcc0 = dm.pl0 / dm.Ex;
+    dm.pdx = dm.pls % dm.Ex;
+    dm.pdc = dm.pls / dm.Ex;
+  }
   dm.rinfo = bits;
   dm.cinfo = bits + NX;
   const int Ls = NX * dm.NYs;     // this strip's points
@@ -508,16 +707,21 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
     const float thresh = (float)(pr.inner_tol * rmax);
     float tl = 0.0f;
     unsigned ml = 0u;
-    tiny_points<N>(dm, ones, has_bc, [&](const TinyPt& p) {
-      const float ri = (float)pr.r[p.g];
+    const double* rg = pr.r;
+    auto init_point = [=](const TinyPt& p, TinyAcc& ac) {
+      const float ri = (float)rg[p.g];
       r32[p.q] = ri;
       x32[p.q] = 0.0f;
       p32[p.q] = 0.0f;
       const float z = jac ? ri * dinv[p.q] : ri;
-      tl = __fmaf_rn(ri * p.mult, z, tl);
+      ac.s = __fmaf_rn(ri * p.mult, z, ac.s);
       const unsigned bb = tiny_abs_bits(ri);
-      ml = bb > ml ? bb : ml;
-    });
+      ac.m = bb > ac.m ? bb : ac.m;
+    };
+    const TinyAcc ia = dm.half == 0 ? tiny_points_pair<N, 0>(dm, ones, has_bc, init_point)
+                                    : tiny_points_pair<N, 1>(dm, ones, has_bc, init_point);
+    tl = ia.s;
+    ml = ia.m;
     float t = tiny_reduce(tl, ml, red, slot);
     float rin = __uint_as_float(ml);
     float tprev = 1.0f;
@@ -528,12 +732,28 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
       // the new direction p = z + beta p_old is formed where it is read; the
       // update pass stores it
       const float beta = k == 0 ? 0.0f : t / tprev;
-      auto pnew = [&](int q) {
+      auto pnew = [=](int q) {
         const float rr = r32[q];
         return __fmaf_rn(beta, p32[q], jac ? rr * dinv[q] : rr);
       };
       float papl = 0.0f;
-      tiny_apply<PF32, N, float>(dm, pnew, LA, LB, G11, G12, G22, Bs, nu32, k32, a.Dr, a.Drt, a.Ds, a.Dst, papl);
+      // the operator in three phases; the branches hold no barrier, so every
+      // warp meets the block barriers at the same program point
+      if (dm.half == 0)
+        tiny_pair_p1<N, 0>(dm, pnew, LA, LB, a.Dr, a.Ds);
+      else
+        tiny_pair_p1<N, 1>(dm, pnew, LA, LB, a.Dr, a.Ds);
+      __syncthreads();
+      if (dm.half == 0)
+        tiny_pair_p2<N, 0>(dm, LA, LB, LC, LD, G11, G12, G22, a.Dst);
+      else
+        tiny_pair_p2<N, 1>(dm, LA, LB, LC, LD, G11, G12, G22, a.Dst);
+      __syncthreads();
+      if (dm.half == 0)
+        tiny_pair_p3<N, 0>(dm, pnew, LA, LC, LD, Bs, nu32, k32, a.Drt, papl);
+      else
+        tiny_pair_p3<N, 1>(dm, pnew, LA, LC, LD, Bs, nu32, k32, a.Drt, papl);
+      // the reduction's barriers order P3's stores before the gather reads them
       unsigned none = 0u;
       const float pap = tiny_reduce(papl, none, red, slot);
       const float af = t / pap;
@@ -541,8 +761,9 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
       ++total;
       float sl = 0.0f;
       unsigned mx = 0u;
-      tiny_points<N>(dm, ones, has_bc, [&](const TinyPt& p) {
-        float ap = tiny_gather(dm, LA, p, [](float v) { return v; });
+      const TinyDims dmc = dm;
+      auto update_point = [=](const TinyPt& p, TinyAcc& ac) {
+        float ap = tiny_gather(dmc, LA, p, [](float v) { return v; });
         if (p.zero) ap = 0.0f;
         const float pk = pnew(p.q);
         x32[p.q] = __fmaf_rn(af, pk, x32[p.q]);
@@ -550,10 +771,14 @@ __global__ void __launch_bounds__(kTinyMaxThreads, 1) k_tiny_pcg(const __grid_co
         r32[p.q] = ri;
         p32[p.q] = pk;
         const float z = jac ? ri * dinv[p.q] : ri;
-        sl = __fmaf_rn(ri * p.mult, z, sl);
+        ac.s = __fmaf_rn(ri * p.mult, z, ac.s);
         const unsigned bb = tiny_abs_bits(ri);
-        mx = bb > mx ? bb : mx;
-      });
+        ac.m = bb > ac.m ? bb : ac.m;
+      };
+      const TinyAcc ua = dm.half == 0 ? tiny_points_pair<N, 0>(dm, ones, has_bc, update_point)
+                                      : tiny_points_pair<N, 1>(dm, ones, has_bc, update_point);
+      sl = ua.s;
+      mx = ua.m;
       tprev = t;
       t = tiny_reduce(sl, mx, red, slot);
       rin = __uint_as_float(mx);
@@ -631,8 +856,8 @@ static int launch_tiny(SmallProb* dev, const SmallProb& host, const OperatorSet&
   fill_eo_tiny<df, N>(a.Dst2, ops.eo[3], to_df);
   const int C = tiny_cluster_size(host.Ey);
   const long long nl = host.NX * ((host.Ey + C - 1) / C);  // lines of the largest strip
-  int threads = (int)((nl + 31) / 32 * 32);
-  if (threads > kTinyMaxThreads) threads = kTinyMaxThreads;
+  int threads = (int)((nl + 31) / 32 * 64);                 // two threads per line (pair walks)
+  if (threads > kTinyMaxThreads) threads = kTinyMaxThreads;   // a multiple of 64
   if (threads < 64) threads = 64;
   auto kern = k_tiny_pcg<N>;
   SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
