@@ -823,9 +823,10 @@ static float to_f32(double d) { return (float)d; }
 static df to_df(double d) { return PDF::from_double(d); }
 
 // CTAs of the cluster for an Ey-element-row mesh: SEM_TINY_CLUSTER (1, 2, 4
-// or 8) when set, else 4 (at most one strip per element row)
+// or 8) when set, else 8 (at most one strip per element row).  cfg3 (8x8
+// elements, N=8) takes 4.04, 3.38 and 3.11 ms with 2, 4 and 8 CTAs.
 int tiny_cluster_size(int Ey) {
-  int c = 4;
+  int c = 8;
   if (const char* e = std::getenv("SEM_TINY_CLUSTER")) {
     const int v = std::atoi(e);
     if (v == 1 || v == 2 || v == 4 || v == 8) c = v;
