@@ -37,7 +37,6 @@ constexpr int kRT = 256;
 struct Scalars {
   double t, t_prev, pAp, alpha, beta, rmax, tol;
   int k, maxiter, done, converged, nan;
-  unsigned arrive;  // blocks of the update kernel that have stored their parts
 };
 
 __device__ __forceinline__ double mult_at(unsigned r, unsigned c, const Grid& g) {
@@ -78,17 +77,13 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const bool (&is_ma
 template <int NV>
 __device__ __forceinline__ void final_reduce(const double* part, int nparts,
                                              const bool (&is_max)[NV], double (&res)[NV]) {
-  // single block, fixed order; the parts are read at L2 (other blocks of the
-  // same grid may have written them)
+  // single block, fixed order
   double v[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) v[q] = is_max[q] ? 0.0 : 0.0;
   for (int i = threadIdx.x; i < nparts; i += blockDim.x)
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-      const double x = __ldcg(part + i * NV + q);
-      v[q] = is_max[q] ? nanmax(v[q], x) : v[q] + x;
-    }
+    for (int q = 0; q < NV; ++q) v[q] = is_max[q] ? nanmax(v[q], part[i * NV + q]) : v[q] + part[i * NV + q];
   __shared__ double sh[NV][kRT];
 #pragma unroll
   for (int q = 0; q < NV; ++q) sh[q][threadIdx.x] = v[q];
@@ -223,7 +218,6 @@ __global__ void k_scal_init(const double* part, int np, Scalars* sc, double tol,
     sc->nan = res[1] != res[1];
     sc->converged = !(res[1] > tol) && !sc->nan;
     sc->done = !(res[1] > tol) || maxiter == 0;
-    sc->arrive = 0u;
   }
 }
 
@@ -309,31 +303,10 @@ __global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
   }
 }
 
-// the scalars after an update pass: r.z (t) and max|r| folded from the
-// parts, beta and the convergence decision (one block)
-__device__ __forceinline__ void fold_beta(const double* part, int np, Scalars* sc) {
-  double res[2];
-  const bool mx[2] = {false, true};
-  final_reduce<2>(part, np, mx, res);
-  if (threadIdx.x == 0) {
-    sc->t_prev = sc->t;
-    sc->t = res[0];
-    sc->beta = res[0] / sc->t_prev;
-    sc->rmax = res[1];
-    const bool nan = (res[1] != res[1]) || (sc->alpha != sc->alpha);
-    sc->nan = nan;
-    sc->converged = !(res[1] > sc->tol) && !nan;
-    sc->done = !(res[1] > sc->tol) || sc->k >= sc->maxiter || nan;
-  }
-}
-
-// x += alpha p, r -= alpha Ap, the parts of r.z (or r.r) and max|r|; the
-// last block to store its parts folds them into the scalars (fixed order,
-// whichever block is last), so no separate beta launch follows
 template <class T, bool NAT = false>
 __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                          const T* __restrict__ Ap, const T* __restrict__ dinv, double* part,
-                         Scalars* sc, Grid g) {
+                         const Scalars* sc, Grid g) {
   pdl_trigger();
   pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
@@ -352,17 +325,25 @@ __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restri
   double v[2] = {acc.sum(), acc.max()};
   const bool mx[2] = {false, true};
   block_reduce<2>(v, mx, part);
-  // every block has read sc->done and sc->alpha before the last one arrives
-  __shared__ bool last;
+}
+
+__global__ void k_scal_beta(const double* part, int np, Scalars* sc) {
+  pdl_trigger();
+  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
+  if (sc->done) return;
+  double res[2];
+  const bool mx[2] = {false, true};
+  final_reduce<2>(part, np, mx, res);
   if (threadIdx.x == 0) {
-    __threadfence();  // this block's parts are visible before its arrival
-    last = atomicAdd(&sc->arrive, 1u) == gridDim.x - 1;
+    sc->t_prev = sc->t;
+    sc->t = res[0];
+    sc->beta = res[0] / sc->t_prev;
+    sc->rmax = res[1];
+    const bool nan = (res[1] != res[1]) || (sc->alpha != sc->alpha);
+    sc->nan = nan;
+    sc->converged = !(res[1] > sc->tol) && !nan;
+    sc->done = !(res[1] > sc->tol) || sc->k >= sc->maxiter || nan;
   }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  fold_beta(part, (int)gridDim.x, sc);
-  if (threadIdx.x == 0) sc->arrive = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -643,10 +624,11 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
     }
     if (nat)
       SEM_CHECK(launch_pdl(k_update<T, true>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
-                           w.sc, gv));
+                           (const Scalars*)w.sc, gv));
     else
       SEM_CHECK(launch_pdl(k_update<T>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
-                           w.sc, gv));
+                           (const Scalars*)w.sc, gv));
+    SEM_CHECK(launch_pdl(k_scal_beta, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
   }
   SEM_CUDA(cudaGetLastError());
   SEM_CUDA(cudaMemcpyAsync(w.sc_h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
