@@ -112,10 +112,15 @@ int sem_mesh_set_precision(sem_mesh_t* mesh, int precision);
  *   5  as 2, with the cross-tile QQ' finished inside the same launch (the
  *      last CTA to reach a tile edge or corner sums its copies; the mesh
  *      holds 3 arrival counters per element tile).  Fused calls on one mesh
- *      handle must then not run concurrently on the GPU.
+ *      handle must then not run concurrently on the GPU;
+ *   6  as 4, with each element tile's u, G11, G12, G22 and B moved into shared
+ *      memory by tensor (TMA) copies that one thread issues, completing on
+ *      mbarriers; runs as 4 where TMA cannot serve the call (a row of n*Ex
+ *      values or a tile row not a multiple of 16 bytes, a field not 16-byte
+ *      aligned or not in device memory).
  * All variants compute the same operations in the same order: their results
  * are bit-identical. */
-#define SEM_VARIANTS 6
+#define SEM_VARIANTS 7
 /* autotuner (no counterpart in the reference): time every variant of the fused
  * element-operator kernel on this mesh, running mask(QQ'(hlmz)) on scratch
  * fields in the given precision (SEM_F64, SEM_F64_DF or SEM_F32), and keep the
@@ -483,6 +488,11 @@ int sem_diag_apply(const double* d, const double* u, double* v, int64_t len, int
  * launches since the last read (and resets them). */
 int sem_timing_enable(int on);
 int sem_timing_read(double* total_ms, int* launches);
+/* waits of the TMA operator kernel (variant 6) on this device that gave up
+ * after their time bound (about 2 s) since the last reset; each such CTA left
+ * its tile unfinished (a double-float call is then recomputed by its native
+ * FP64 re-run).  reset != 0 clears the count after reading it.  Synchronous. */
+int sem_wait_timeouts(int reset, unsigned* count);
 
 #ifdef __cplusplus
 }

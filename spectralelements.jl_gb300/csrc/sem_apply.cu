@@ -7,6 +7,8 @@
 #include <utility>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "sem_apply_launch.cuh"
 
 namespace sem {
@@ -120,6 +122,66 @@ int num_sms() {
     cached[dev] = v;
   }
   return cached[dev];
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library), looked up once per process
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+bool encode_tile_map(CUtensorMap* map, const void* ptr, size_t elem, long long NX, long long NY, int bx, int by) {
+  // TMA rules: 16-byte aligned base, row pitch and box row; box sides <= 256
+  if (!ptr || (reinterpret_cast<uintptr_t>(ptr) & 15) || ((size_t)NX * elem) % 16 || ((size_t)bx * elem) % 16 ||
+      bx < 1 || by < 1 || bx > 256 || by > 256 || NX < 1 || NY < 1 || NX >= (1LL << 32) || NY >= (1LL << 32))
+    return false;
+  if (elem != 4 && elem != 8) return false;
+  cudaPointerAttributes pa;
+  if (cudaPointerGetAttributes(&pa, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (pa.type != cudaMemoryTypeDevice) return false;  // TMA here reads this GPU's own memory only
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || pa.device != dev) return false;
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)NX, (cuuint64_t)NY};
+  const cuuint64_t strides[1] = {(cuuint64_t)NX * elem};
+  const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r =
+      enc(map, elem == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr),
+          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+unsigned* wait_timeout_word() {
+  static std::mutex mu;
+  static unsigned* words[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!words[dev]) {
+    unsigned* p = nullptr;
+    if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, sizeof(unsigned)) != cudaSuccess) {
+      cudaFree(p);
+      return nullptr;
+    }
+    words[dev] = p;
+  }
+  return words[dev];
 }
 
 int launch_dss_fixup(const Grid& g, void* out, unsigned mode, int precision, const int* skip, int TX,
@@ -359,6 +421,16 @@ extern "C" {
 int sem_timing_enable(int on) {
   std::lock_guard<std::mutex> lk(sem::g_tmu);
   sem::g_timing = on != 0;
+  return SEM_OK;
+}
+
+int sem_wait_timeouts(int reset, unsigned* count) {
+  if (!count) return sem::set_error(SEM_ERR_BAD_ARG, "NULL count");
+  unsigned* w = sem::wait_timeout_word();
+  if (!w) return sem::set_error(SEM_ERR_CUDA, "cannot make the TMA timeout word");
+  SEM_CUDA(cudaDeviceSynchronize());
+  SEM_CUDA(cudaMemcpy(count, w, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (reset) SEM_CUDA(cudaMemset(w, 0, sizeof(unsigned)));
   return SEM_OK;
 }
 

@@ -9,6 +9,7 @@
 
 #include "sem_apply2.cuh"
 #include "sem_apply3.cuh"
+#include "sem_apply4.cuh"
 #include "sem_apply_kernels.cuh"
 
 namespace sem {
@@ -16,6 +17,12 @@ namespace sem {
 std::pair<cudaEvent_t, cudaEvent_t>* timing_slot();
 size_t max_smem_optin();
 int num_sms();
+// 2-D tensor map of an NX x NY field of elem-byte values (x contiguous) with a
+// bx x by box; false when TMA cannot serve it (alignment, strides, a field not
+// in device memory, no encoder)
+bool encode_tile_map(CUtensorMap* map, const void* ptr, size_t elem, long long NX, long long NY, int bx, int by);
+// the device's timeout word of the TMA kernel (made on first use), or NULL
+unsigned* wait_timeout_word();
 // per-policy launchers, one translation unit each for n <= 9 and n >= 10; tile
 // receives the element tile (TX, TY) of the launched kernel for k_dss_fixup
 int launch_apply_f64_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
@@ -228,10 +235,59 @@ static int launch_apply_v3(const Grid& g, const OperatorSet* ops, const ApplyCal
   return SEM_OK;
 }
 
+// TMA persistent kernel (variant 6); *served = false, with nothing launched,
+// when the call's fields cannot be described by tensor maps
+template <class P, int N>
+static int launch_apply_v4(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s,
+                           bool* served) {
+  typedef PTile<N> TS;
+  typedef typename GeoT<P>::type gt;
+  typedef typename P::io io;
+  typedef K4Layout<P, N, TS::TX, TS::TY> L;
+  *served = false;
+  if (L::total > max_smem_optin()) return SEM_OK;
+  Apply2Args<P, N> a;
+  fill_args2<P, N>(a, g, ops, c);
+  TmaSet maps;
+  std::memset(&maps, 0, sizeof(maps));
+  const int bx = TS::TX * N, by = TS::TY * N;
+  if (!encode_tile_map(&maps.m[0], a.u, sizeof(io), g.NX, g.NY, bx, by)) return SEM_OK;
+  if (c.mode & M_STIFF) {
+    if (!encode_tile_map(&maps.m[1], a.G11, sizeof(gt), g.NX, g.NY, bx, by) ||
+        !encode_tile_map(&maps.m[2], a.G12, sizeof(gt), g.NX, g.NY, bx, by) ||
+        !encode_tile_map(&maps.m[3], a.G22, sizeof(gt), g.NX, g.NY, bx, by))
+      return SEM_OK;
+  }
+  if ((c.mode & M_MASS) && !encode_tile_map(&maps.m[4], a.B, sizeof(gt), g.NX, g.NY, bx, by)) return SEM_OK;
+  unsigned* werr = wait_timeout_word();
+  if (!werr) return set_error(SEM_ERR_CUDA, "cannot make the TMA timeout word");
+  auto kern = k_apply4<P, N, TS::TX, TS::TY>;
+  SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::total));
+  int per_sm = 0;
+  SEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TS::THREADS, L::total));
+  if (per_sm < 1) return SEM_OK;
+  const int tiles_x = (g.Ex + TS::TX - 1) / TS::TX;
+  const int tiles_y = (g.Ey + TS::TY - 1) / TS::TY;
+  const long long tiles = (long long)tiles_x * tiles_y;
+  if (tiles > 2147483647LL) return set_error(SEM_ERR_UNSUPPORTED, "too many element tiles");
+  const long long slots = (long long)per_sm * num_sms();
+  const long long rounds = (tiles + slots - 1) / slots;
+  const long long grid = (tiles + rounds - 1) / rounds;
+  auto* ev = c.gate ? nullptr : timing_slot();  // gated re-runs are not timed
+  if (ev) SEM_CUDA(cudaEventRecord(ev->first, s));
+  SEM_CHECK(launch_kernel(kern, dim3((unsigned)grid), TS::THREADS, L::total, s, c.pdl != 0, a, maps, tiles_x,
+                          (int)tiles, werr));
+  if (ev) SEM_CUDA(cudaEventRecord(ev->second, s));
+  *served = true;
+  return SEM_OK;
+}
+
 // variant 0: k_apply, direct loads; 1: k_apply, cp.async-staged inputs;
 // 2: k_apply2, direct loads; 3: k_apply2, cp.async-staged metric terms;
 // 4: k_apply3, persistent CTAs prefetching the next tile; 5: k_apply2 with
-// the cross-tile QQ' completed inside the kernel (tile = {0, 0}: no fixup).
+// the cross-tile QQ' completed inside the kernel (tile = {0, 0}: no fixup);
+// 6: k_apply4, persistent CTAs whose element tiles arrive by TMA copies (runs
+// as variant 4 where tensor maps cannot describe the call's fields).
 // Variants 2-5 of the double-float policy read the pre-split geometry
 // (ApplyCall::Gdf) and run as variant 0 when the call carries none; variant 5
 // runs as variant 2 without counters (ApplyCall::ctr) or with a single tile
@@ -249,7 +305,7 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
     return set_error(SEM_ERR_UNSUPPORTED, "a p.Ap launch needs kernel variant 0 or 1");
   if (c.tyn > 0) {  // a window of tile rows: the non-persistent kernels with the fixup outside
     if (cg) return set_error(SEM_ERR_UNSUPPORTED, "a tile-row window takes no CG fusion");
-    if (c.variant == 4 || c.variant == 5) {
+    if (c.variant >= 4) {
       ApplyCall c2 = c;
       c2.variant = 2;
       return launch_apply_n<P, N>(g, ops, c2, s, tile);
@@ -271,15 +327,21 @@ static int launch_apply_n(const Grid& g, const OperatorSet* ops, const ApplyCall
     tile[1] = TileShape<N>::TY;
     return launch_apply_v2<P, N, false, false, true>(g, ops, c, s);
   }
-  if (c.variant == 4 && geo_ok) {
+  if ((c.variant == 4 || c.variant == 6) && geo_ok) {
     tile[0] = PTile<N>::TX;
     tile[1] = PTile<N>::TY;
+    if (c.variant == 6) {
+      bool served = false;
+      const int st = launch_apply_v4<P, N>(g, ops, c, s, &served);
+      if (st != SEM_OK) return st;
+      if (served) return SEM_OK;
+    }
     return launch_apply_v3<P, N>(g, ops, c, s);
   }
   typedef TileShape<N> TS;
   tile[0] = TS::TX;
   tile[1] = TS::TY;
-  if (c.variant >= 2 && c.variant != 4 && geo_ok) {
+  if (c.variant >= 2 && c.variant != 4 && c.variant != 6 && geo_ok) {
     const size_t te = (size_t)TS::TX * TS::TY * TS::ES;
     const size_t smem = 2 * te * sizeof(typename P::v) + 3 * te * sizeof(typename GeoT<P>::type);
     if (c.variant == 3 && smem <= max_smem_optin()) return launch_apply_v2<P, N, true>(g, ops, c, s);

@@ -50,7 +50,7 @@ SEM_F64, SEM_F64_DF, SEM_F32, SEM_MIXED, SEM_MIXED_RR = 0, 1, 2, 3, 4
 SEM_PRECOND_NONE, SEM_PRECOND_JACOBI = 0, 1
 SEM_PATH_AUTO, SEM_PATH_CHUNKED, SEM_PATH_SMALL = 0, 1, 2
 SEM_SMALL_MAX_LOCAL = 100000  # include/sem_b200.h
-SEM_VARIANTS = 6  # fused element-operator kernel variants (include/sem_b200.h)
+SEM_VARIANTS = 7  # fused element-operator kernel variants (include/sem_b200.h)
 SEM_BDF_MAX_ORDER = 6  # include/sem_b200.h
 FIELDS = {"x": 0, "y": 1, "Jac": 2, "Jaci": 3, "rx": 4, "ry": 5, "sx": 6, "sy": 7, "B": 8,
           "Bi": 9, "G11": 10, "G12": 11, "G22": 12, "mult": 13, "mask": 14}
@@ -201,6 +201,7 @@ SIGNATURES = {
     "sem_diag_apply": (_I, [_P, _P, _P, _L, _I, _P]),
     "sem_timing_enable": (_I, [_I]),
     "sem_timing_read": (_I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
+    "sem_wait_timeouts": (_I, [_I, ctypes.POINTER(ctypes.c_uint)]),
 }
 
 _lib = None

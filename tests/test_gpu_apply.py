@@ -39,7 +39,7 @@ def _ids(c):
 
 @pytest.mark.parametrize("case", CASES, ids=_ids)
 @pytest.mark.parametrize("prec", ["F64", "DF"])
-@pytest.mark.parametrize("variant", [0, 2, 4, 5])
+@pytest.mark.parametrize("variant", [0, 2, 4, 5, 6])
 def test_fused_operators(gpu, case, prec, variant):
     import semgb300 as S
     n, Ex, Ey, per, bc, amp = case
@@ -116,8 +116,9 @@ def test_kernel_variants_bit_identical(gpu, case):
     # of one CG form.  Variants 2 and 5 run the CG-fused operator launch and
     # variants 0 and 1 the operator launch with the p.Ap parts; both sum p.Ap
     # over the unassembled products.  Variants 3 and 4 take a separate dot
-    # pass over the assembled A p.  Each form's solves agree bit for bit, and
-    # the forms agree to the tolerance.
+    # pass over the assembled A p, and so does variant 6 (the TMA-fed kernel).
+    # Each form's solves agree bit for bit, and the forms agree to the
+    # tolerance.
     md.set_precision(S.SEM_F64_DF)
     md.set_variant(0)
     M = O.generateMask(list(bc), mo)
@@ -130,7 +131,7 @@ def test_kernel_variants_bit_identical(gpu, case):
         info = {}
         xs.append((host(S.pcg(b, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info,
                               precision=S.SEM_MIXED)), info["iters"]))
-    for form in ((0, 1), (2, 5), (3, 4)):
+    for form in ((0, 1), (2, 5), (3, 4, 6)):
         ref_x, ref_it = xs[form[0]]
         for v in form[1:]:
             x, it = xs[v]
@@ -141,6 +142,34 @@ def test_kernel_variants_bit_identical(gpu, case):
     for v in (0, 2):
         assert abs(xs[v][1] - xs[3][1]) <= max(4, xs[3][1] // 4)
         assert rel_l2(xs[v][0], xs[3][0]) < 1e-6
+
+
+def test_tma_kernel_waits_never_time_out(gpu):
+    """Variant 6 moves its element tiles by TMA copies and bounds every
+    mbarrier wait; on meshes whose rows suit tensor maps (n*Ex*8 bytes a
+    multiple of 16, here also for FP32) none of its waits gives up, and its
+    results equal variant 4's (which it replaces where TMA cannot serve)."""
+    import ctypes
+    import semgb300 as S
+    lib = S._lib.load()
+    cnt = ctypes.c_uint(0)
+    S._lib.check(lib.sem_wait_timeouts(1, ctypes.byref(cnt)))
+    for n, Ex, Ey in ((9, 40, 30), (5, 64, 9), (13, 12, 7), (17, 8, 5)):
+        mo, md = meshes(n, Ex, Ey, (False, False), "DDDD", 0.05)
+        ud = S.as_local(np.random.default_rng(n).uniform(-1, 1, mo.shape))
+        for prec in (S.SEM_F64, S.SEM_F64_DF):
+            md.set_precision(prec)
+            outs = []
+            for v in (4, 6):
+                md.set_variant(v, prec)
+                op = S.HelmholtzOp(md, 1e-2, 1.0)
+                outs.append(host(op(ud)))
+                for _ in range(3):
+                    np.testing.assert_array_equal(host(op(ud)), outs[-1])
+            np.testing.assert_array_equal(outs[0], outs[1])
+    torch.cuda.synchronize()
+    S._lib.check(lib.sem_wait_timeouts(1, ctypes.byref(cnt)))
+    assert cnt.value == 0
 
 
 def test_autotune_reports_every_variant(gpu):
