@@ -272,23 +272,6 @@ __global__ void k_dot_pap(const T* __restrict__ p, const T* __restrict__ Ap, dou
   block_reduce<1>(v, mx, part);
 }
 
-// alpha = t / (p . A p) from the per-CTA double-float parts of a CG-fused
-// operator launch, summed in a fixed order (one block)
-__global__ void k_scal_alpha_df(const df* part, long long np, Scalars* sc) {
-  pdl_trigger();
-  pdl_wait();  // launched as a programmatic dependent inside the CG chunks
-  if (sc->done) return;
-  df x = {0.0f, 0.0f};
-  for (long long i = threadIdx.x; i < np; i += blockDim.x) x = df_add(x, part[i]);
-  x = block_sum_df(x);
-  if (threadIdx.x == 0) {
-    const double pap = df2d(x);
-    sc->pAp = pap;
-    sc->alpha = sc->t / pap;
-    sc->k += 1;
-  }
-}
-
 __global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
   pdl_trigger();
   pdl_wait();  // launched as a programmatic dependent inside the CG chunks
@@ -303,14 +286,57 @@ __global__ void k_scal_alpha(const double* part, int np, Scalars* sc) {
   }
 }
 
-template <class T, bool NAT = false>
+// alpha = t / (p . A p) from the per-CTA parts of the operator launch before
+// the update kernel (FP64 parts for native FP64 solves, double-float parts
+// otherwise), formed by every block of the update kernel in one fixed order
+// (thread-strided partial sums over kRT threads, then the block tree), so that
+// all blocks hold the same value without a one-block kernel between the
+// launches; block 0 records p . A p, alpha and the iteration count
+template <bool NATP>
+__device__ __forceinline__ double alpha_from_parts(const void* parts, long long np, Scalars* sc) {
+  __shared__ double s_alpha;
+  double pap;
+  if constexpr (NATP) {
+    double res[1];
+    const bool mx[1] = {false};
+    final_reduce<1>(static_cast<const double*>(parts), (int)np, mx, res);
+    pap = res[0];
+  } else {
+    const df* part = static_cast<const df*>(parts);
+    df x = {0.0f, 0.0f};
+    for (long long i = threadIdx.x; i < np; i += blockDim.x) x = df_add(x, part[i]);
+    x = block_sum_df(x);
+    pap = df2d(x);  // valid in thread 0
+  }
+  if (threadIdx.x == 0) {
+    const double a = sc->t / pap;
+    s_alpha = a;
+    if (blockIdx.x == 0) {
+      sc->pAp = pap;
+      sc->alpha = a;
+      sc->k += 1;
+    }
+  }
+  __syncthreads();
+  return s_alpha;
+}
+
+// x += alpha p, r -= alpha A p and the per-block parts of r.h.mult and
+// max|r|.  FOLD: alpha is formed here from the operator's p . A p parts
+// (apart, anp), which must not alias part
+template <class T, bool NAT = false, bool FOLD = false>
 __global__ void k_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                          const T* __restrict__ Ap, const T* __restrict__ dinv, double* part,
-                         const Scalars* sc, Grid g) {
+                         Scalars* sc, Grid g, const void* apart, long long anp) {
   pdl_trigger();
   pdl_wait();  // launched as a programmatic dependent inside the CG chunks
   if (sc->done) return;
-  const T alpha = (T)sc->alpha;
+  double alpha_d;
+  if constexpr (FOLD)
+    alpha_d = alpha_from_parts<NAT>(apart, anp, sc);
+  else
+    alpha_d = sc->alpha;
+  const T alpha = (T)alpha_d;
   typename AccOf<T, NAT>::type acc;
   for_each_point(g, [&](unsigned rr, unsigned cc, long long i) {
     x[i] = x[i] + alpha * p[i];
@@ -593,21 +619,18 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
   // native FP64 (the whole double range); the other arithmetics use
   // double-float parts and dots
   const bool nat = sizeof(T) == 8 && c.precision == SEM_F64;
-  auto alpha_parts = [&]() -> int {
-    if (nat) return launch_pdl(k_scal_alpha, 1, kRT, s, (const double*)w.dpart, (int)np, w.sc);
-    return launch_pdl(k_scal_alpha_df, 1, kRT, s, (const df*)w.dpart, np, w.sc);
-  };
+  // with the p.Ap parts in their own buffer (dpart), the update kernel forms
+  // alpha itself: one launch fewer per iteration
+  const bool fold = fused || cp.cg_dpart;
   for (int it = 0; it < check_every; ++it) {
     if (fused) {
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
-      SEM_CHECK(alpha_parts());
     } else if (cp.cg_dpart) {  // direction pass, then the operator with the p.Ap parts
       if (nat)
         SEM_CHECK(launch_pdl(k_pdir<T, true>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       else
         SEM_CHECK(launch_pdl(k_pdir<T>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
       SEM_CHECK(launch_apply(cx.g, cx.ops, cp, s));
-      SEM_CHECK(alpha_parts());
     } else {
       if (nat)
         SEM_CHECK(launch_pdl(k_pdir<T, true>, nb, kRT, s, (const T*)r, dinv, p, (const Scalars*)w.sc, L));
@@ -622,12 +645,19 @@ int enqueue_chunk(const OpCtx& cx, const Grid& gv, const WS& w, T* x, T* r, T* p
                              (const Scalars*)w.sc, gv));
       SEM_CHECK(launch_pdl(k_scal_alpha, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
     }
-    if (nat)
+    const void* ap = w.dpart;
+    if (fold && nat)
+      SEM_CHECK(launch_pdl(k_update<T, true, true>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
+                           w.sc, gv, ap, np));
+    else if (fold)
+      SEM_CHECK(launch_pdl(k_update<T, false, true>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
+                           w.sc, gv, ap, np));
+    else if (nat)
       SEM_CHECK(launch_pdl(k_update<T, true>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
-                           (const Scalars*)w.sc, gv));
+                           w.sc, gv, (const void*)nullptr, 0LL));
     else
       SEM_CHECK(launch_pdl(k_update<T>, nb, kRT, s, x, r, (const T*)p, (const T*)Ap, dinv, w.part,
-                           (const Scalars*)w.sc, gv));
+                           w.sc, gv, (const void*)nullptr, 0LL));
     SEM_CHECK(launch_pdl(k_scal_beta, 1, kRT, s, (const double*)w.part, (int)nb, w.sc));
   }
   SEM_CUDA(cudaGetLastError());
