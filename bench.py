@@ -257,9 +257,9 @@ def measure_apply(S, lib, msh, prec, u, flush, stream, args, world, dev, G, L, x
 
 
 def kernel_name(prec_tag, variant):
-    kname = ("k_apply", "k_apply", "k_apply2", "k_apply2", "k_apply3", "k_apply2")[variant]
+    kname = ("k_apply", "k_apply", "k_apply2", "k_apply2", "k_apply3", "k_apply2", "k_apply4")[variant]
     targs = {0: "false", 1: "true", 2: "false,false,false", 3: "true,false,false", 4: None,
-             5: "false,true,false"}[variant]
+             5: "false,true,false", 6: None}[variant]
     return f"{kname}<{prec_tag},9,8,3{',' + targs if targs else ''}>"
 
 

@@ -139,8 +139,10 @@ const char* sem_last_error(void);
 int sem_abi_version(void);
 
 /* ---- ABu(As,Br,u) (src/ABu.jl:9-37): v = (As (x) Br) u.
- * As (ma x na) and Br (mb x nb) are host matrices, NULL = identity ([]).
- * u is m x n, v is (m*mb/nb) x (n*ma/na); block sizes at most 32. */
+ * As (ma x na) and Br (mb x nb) are host matrices (column-major), NULL =
+ * identity ([]).  u is m x n, v is (m*mb/nb) x (n*ma/na).  Factors up to
+ * 32 x 32 are passed in the kernel parameters; larger ones are copied to
+ * stream-ordered device buffers and applied as strided GEMMs. */
 int sem_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
             const double* u, int m, int n, double* v, sem_stream_t stream);
 

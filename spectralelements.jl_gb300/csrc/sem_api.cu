@@ -313,20 +313,16 @@ int sem_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
   if (m < 0 || n < 0) return set_error(SEM_ERR_BAD_ARG, "negative size");
   if (u == v) return set_error(SEM_ERR_BAD_ARG, "ABu output must not alias its input");
   if (Br) {
-    if (mb < 1 || nb < 1 || mb > kMaxBlock || nb > kMaxBlock)
-      return set_error(SEM_ERR_UNSUPPORTED, "Br must be at most %dx%d (got %dx%d)", kMaxBlock, kMaxBlock, mb, nb);
+    if (mb < 1 || nb < 1) return set_error(SEM_ERR_BAD_ARG, "Br must not be empty (got %dx%d)", mb, nb);
     if (((long long)m * n) % nb != 0)
       return set_error(SEM_ERR_BAD_ARG, "length(u) = %lld is not a multiple of size(Br,2) = %d", (long long)m * n, nb);
     if (((long long)m * mb) % nb != 0)
       return set_error(SEM_ERR_BAD_ARG, "m*mb/nb is not an integer");
   }
   if (As) {
-    if (ma < 1 || na < 1 || ma > kMaxBlock || na > kMaxBlock)
-      return set_error(SEM_ERR_UNSUPPORTED, "As must be at most %dx%d (got %dx%d)", kMaxBlock, kMaxBlock, ma, na);
+    if (ma < 1 || na < 1) return set_error(SEM_ERR_BAD_ARG, "As must not be empty (got %dx%d)", ma, na);
     if (n % na != 0) return set_error(SEM_ERR_BAD_ARG, "size(u,2) = %d is not a multiple of size(As,2) = %d", n, na);
   }
-  if (As && Br && m % nb != 0)
-    return set_error(SEM_ERR_BAD_ARG, "with both factors size(u,1) must be a multiple of size(Br,2)");
   return launch_abu(As, ma, na, Br, mb, nb, u, m, n, v, (cudaStream_t)stream);
 }
 

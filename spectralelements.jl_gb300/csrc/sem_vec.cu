@@ -186,6 +186,71 @@ __global__ void k_abu_both(const __grid_constant__ Mat32 As, const __grid_consta
   }
 }
 
+// Large factors (a side above kMaxBlock): C_b = A_b B_b for b < batch, every
+// operand addressed through (row, column, batch) strides, in 64 x 64 output
+// tiles of 256 threads (4 x 4 outputs each) with 16-deep k slices staged in
+// shared memory.  Each output is one FMA chain over k in increasing order,
+// the order of the small-block kernels above.
+struct GemmArgs {
+  const double* A;
+  const double* B;
+  double* C;
+  long long M, N, K, batch;
+  long long a_rs, a_cs, a_bs, b_rs, b_cs, b_bs, c_rs, c_cs, c_bs;
+};
+
+constexpr int kGT = 64, kGK = 16;
+
+__global__ void __launch_bounds__(256) k_abu_gemm(const __grid_constant__ GemmArgs g) {
+  __shared__ double sa[kGK][kGT + 1];
+  __shared__ double sb[kGK][kGT + 1];
+  const long long tiles_m = (g.M + kGT - 1) / kGT, tiles_n = (g.N + kGT - 1) / kGT;
+  const long long tiles = tiles_m * tiles_n * g.batch;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long long b = tile / (tiles_m * tiles_n);
+    const long long rem = tile - b * tiles_m * tiles_n;
+    const long long i0 = (rem % tiles_m) * kGT, j0 = (rem / tiles_m) * kGT;
+    const double* A = g.A + b * g.a_bs;
+    const double* B = g.B + b * g.b_bs;
+    double acc[4][4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = 0.0;
+    for (long long k0 = 0; k0 < g.K; k0 += kGK) {
+      for (int t = threadIdx.x; t < kGK * kGT; t += blockDim.x) {
+        const int kk = t / kGT, ii = t - kk * kGT;  // A: ii along rows; B: ii along columns
+        const long long k = k0 + kk;
+        sa[kk][ii] = (k < g.K && i0 + ii < g.M) ? A[(i0 + ii) * g.a_rs + k * g.a_cs] : 0.0;
+        sb[kk][ii] = (k < g.K && j0 + ii < g.N) ? B[k * g.b_rs + (j0 + ii) * g.b_cs] : 0.0;
+      }
+      __syncthreads();
+      const int kn = (int)(g.K - k0 < kGK ? g.K - k0 : kGK);
+      for (int kk = 0; kk < kn; ++kk) {
+        double av[4], bv[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) av[p] = sa[kk][ty + 16 * p];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) bv[q] = sb[kk][tx + 16 * q];
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p][q] = fma(av[p], bv[q], acc[p][q]);
+      }
+      __syncthreads();
+    }
+    double* C = g.C + b * g.c_bs;
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const long long i = i0 + ty + 16 * p, j = j0 + tx + 16 * q;
+        if (i < g.M && j < g.N) C[i * g.c_rs + j * g.c_cs] = acc[p][q];
+      }
+  }
+}
+
 void load_mat(Mat32& M, const double* colmajor, int rows, int cols) {
   std::memset(&M, 0, sizeof(M));
   M.rows = rows;
@@ -250,6 +315,63 @@ int launch_mult(const Grid& g, double* out, cudaStream_t s) {
   return SEM_OK;
 }
 
+// ABu with a factor larger than kMaxBlock: the factors are copied to
+// stream-ordered device buffers and applied as strided GEMMs, Br first on the
+// column-major chunks of reshape(u, nb, :), then As on the column blocks
+// (src/ABu.jl:13-34), through a temporary field when both are given
+static int launch_abu_large(const double* As, int ma, int na, const double* Br, int mb, int nb,
+                            const double* u, int m, int n, double* v, cudaStream_t s) {
+  double* dA = nullptr;
+  double* dB = nullptr;
+  double* tmp = nullptr;
+  int st = SEM_OK;
+  auto alloc = [&](double** p, size_t count) {
+    const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(p), sizeof(double) * count, s);
+    if (e != cudaSuccess) st = cuda_error(e, "cudaMallocAsync(ABu operand)");
+    return e == cudaSuccess;
+  };
+  auto upload = [&](double* d, const double* h, size_t count) {
+    const cudaError_t e = cudaMemcpyAsync(d, h, sizeof(double) * count, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) st = cuda_error(e, "cudaMemcpyAsync(ABu factor)");
+    return e == cudaSuccess;
+  };
+  auto gemm = [&](const GemmArgs& g) {
+    const long long tiles = ((g.M + kGT - 1) / kGT) * ((g.N + kGT - 1) / kGT) * g.batch;
+    const unsigned blocks = (unsigned)(tiles < 152LL * 8 ? tiles : 152LL * 8);
+    k_abu_gemm<<<blocks, 256, 0, s>>>(g);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) st = cuda_error(e, "k_abu_gemm");
+  };
+  const long long m1 = Br ? (long long)m * mb / nb : m;  // rows after the Br side
+  do {
+    if (Br && !(alloc(&dB, (size_t)mb * nb) && upload(dB, Br, (size_t)mb * nb))) break;
+    if (As && !(alloc(&dA, (size_t)ma * na) && upload(dA, As, (size_t)ma * na))) break;
+    const double* src = u;
+    if (Br) {
+      double* dst = v;
+      if (As) {
+        if (!alloc(&tmp, (size_t)m1 * n)) break;
+        dst = tmp;
+      }
+      // (mb x nb) times reshape(u, nb, :) -> reshape(dst, mb, :)
+      GemmArgs g{dB, u, dst, mb, (long long)m * n / nb, nb, 1, 1, mb, 0, 1, nb, 0, 1, mb, 0};
+      gemm(g);
+      if (st != SEM_OK) break;
+      src = dst;
+    }
+    if (As) {
+      // column block b: (m1 x na) times As' (na x ma) -> (m1 x ma)
+      GemmArgs g{src, dA, v, m1, ma, na, n / na, 1, m1, (long long)na * m1, ma, 1, 0, 1, m1,
+                 (long long)ma * m1};
+      gemm(g);
+    }
+  } while (false);
+  if (tmp) cudaFreeAsync(tmp, s);
+  if (dA) cudaFreeAsync(dA, s);
+  if (dB) cudaFreeAsync(dB, s);
+  return st;
+}
+
 int launch_abu(const double* As, int ma, int na, const double* Br, int mb, int nb,
                const double* u, int m, int n, double* v, cudaStream_t s) {
   if (m <= 0 || n <= 0) return SEM_OK;
@@ -257,6 +379,11 @@ int launch_abu(const double* As, int ma, int na, const double* Br, int mb, int n
     SEM_CUDA(cudaMemcpyAsync(v, u, sizeof(double) * (size_t)m * n, cudaMemcpyDeviceToDevice, s));
     return SEM_OK;
   }
+  // factors above kMaxBlock, or both factors on a u whose rows are not whole
+  // chunks of nb (the one-pass kernel below tiles u into nb x na blocks)
+  if ((Br && (mb > kMaxBlock || nb > kMaxBlock)) || (As && (ma > kMaxBlock || na > kMaxBlock)) ||
+      (As && Br && m % nb != 0))
+    return launch_abu_large(As, ma, na, Br, mb, nb, u, m, n, v, s);
   if (Br != nullptr && As == nullptr) {
     Mat32 B;
     load_mat(B, Br, mb, nb);

@@ -242,6 +242,11 @@ def test_device_geometry(gpu, n, Ex, Ey, per):
     ((8, 6), (4, 2), None),
     ((6, 4), None, (2, 4)),  # reshape(u, 4, :) spans columns
     ((64, 96), (32, 32), (32, 32)),
+    # factors above 32 x 32 (strided GEMM path), rectangular ones included
+    ((66, 40), None, (33, 33)),
+    ((72, 90), (45, 45), None),
+    ((100, 60), (20, 30), (130, 50)),
+    ((6, 4), (3, 2), (2, 4)),  # both factors, rows not whole chunks of nb: reshape(u, 4, :) spans columns
 ])
 def test_abu(gpu, shape_u, As, Br):
     import semgb300 as S
@@ -253,11 +258,28 @@ def test_abu(gpu, shape_u, As, Br):
     assert rel_l2(got, O.ABu(A, B, u)) < 1e-14
 
 
-def test_abu_rejects_large_blocks(gpu):
+def test_abu_dense_gather_scatter_form(gpu):
+    """The reference's gatherScatter is ABu(QQty, QQtx, u) with the dense
+    global matrices of the mesh (src/gatherScatter.jl:8-16); the same call
+    through sem_abu (factors of n*Ex x n*Ex, the GEMM path) equals the
+    oracle's and the structured kernel's QQ'."""
+    import semgb300 as S
+    mo, md = meshes(5, 12, 9, (False, True), "DDDD", 0.05)
+    Qx = O.semq(12, 5, False)
+    Qy = O.semq(9, 5, True)
+    QQtx, QQty = Qx @ Qx.T, Qy @ Qy.T
+    u = np.random.default_rng(11).standard_normal(mo.shape)
+    got = host(S.ABu(QQty, QQtx, S.as_local(u)))
+    assert rel_l2(got, O.ABu(QQty, QQtx, u)) < 1e-14
+    assert rel_l2(got, O.gatherScatter(u, mo)) < 1e-14
+    assert rel_l2(got, host(S.gatherScatter(S.as_local(u), md))) < 1e-14
+
+
+def test_abu_rejects_inconsistent_sizes(gpu):
     import semgb300 as S
     u = S.as_local(np.ones((66, 66)))
     with pytest.raises(S.SemError):
-        S.ABu(None, np.eye(33), u)
+        S.ABu(None, np.eye(40), u)  # 66*66 is not a multiple of 40
 
 
 def test_full_size_properties_cfg2(gpu):
