@@ -87,6 +87,18 @@ def test_argument_validation_needs_no_gpu(built):
     assert lib.sem_mask(None, None, None, -1, None) == _lib.SEM_ERR_BAD_ARG
     a = np.zeros(4)
     assert lib.sem_abu(None, 0, 0, None, 0, 0, a.ctypes.data, 2, 2, a.ctypes.data, None) == _lib.SEM_ERR_BAD_ARG
+    # ABu sizes are checked before any launch: empty factors, length(u) not a
+    # multiple of size(Br,2), size(u,2) not a multiple of size(As,2); factors
+    # of any size are otherwise accepted (no 32 x 32 limit)
+    u, v = np.zeros(66 * 66), np.zeros(66 * 66)
+    big = np.eye(40)
+    assert lib.sem_abu(None, 0, 0, big.ctypes.data, 0, 40, u.ctypes.data, 66, 66, v.ctypes.data,
+                       None) == _lib.SEM_ERR_BAD_ARG
+    assert lib.sem_abu(None, 0, 0, big.ctypes.data, 40, 40, u.ctypes.data, 66, 66, v.ctypes.data,
+                       None) == _lib.SEM_ERR_BAD_ARG
+    assert b"multiple" in lib.sem_last_error()
+    assert lib.sem_abu(big.ctypes.data, 40, 40, None, 0, 0, u.ctypes.data, 66, 66, v.ctypes.data,
+                       None) == _lib.SEM_ERR_BAD_ARG
 
 
 def test_bdf_coeffs_in_library_match_oracle(built):
