@@ -220,10 +220,13 @@ int sem_mesh_set_variant(sem_mesh_t* m, int precision, int variant) {
   if (!m) return set_error(SEM_ERR_BAD_ARG, "NULL mesh");
   if (precision < SEM_F64 || precision > SEM_F32) return set_error(SEM_ERR_BAD_ARG, "bad precision");
   if (variant < 0 || variant >= kVariants) return set_error(SEM_ERR_BAD_ARG, "bad variant");
-  if ((precision == SEM_F64_DF && variant >= 2) || variant == 5) {
+  if ((precision == SEM_F64_DF && variant >= 2) || variant == 5 || variant == 6) {
     SEM_CHECK(check_device(m));
     if (precision == SEM_F64_DF) SEM_CHECK(ensure_df_geometry(m, nullptr));
     if (variant == 5) SEM_CHECK(ensure_fix_counters(m));
+    // the TMA kernel's timeout word, made here rather than inside a later
+    // launch that a CUDA-graph capture (the CG chunks) may enclose
+    if (variant == 6 && !wait_timeout_word(true)) return set_error(SEM_ERR_CUDA, "cannot make the TMA timeout word");
     SEM_CUDA(cudaStreamSynchronize(nullptr));  // later launches may use any stream
   }
   m->variant[precision] = variant;

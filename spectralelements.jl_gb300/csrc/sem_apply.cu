@@ -166,13 +166,13 @@ bool encode_tile_map(CUtensorMap* map, const void* ptr, size_t elem, long long N
   return r == CUDA_SUCCESS;
 }
 
-unsigned* wait_timeout_word() {
+unsigned* wait_timeout_word(bool may_alloc) {
   static std::mutex mu;
   static unsigned* words[64] = {nullptr};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   std::lock_guard<std::mutex> lk(mu);
-  if (!words[dev]) {
+  if (!words[dev] && may_alloc) {
     unsigned* p = nullptr;
     if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
     if (cudaMemset(p, 0, sizeof(unsigned)) != cudaSuccess) {
@@ -426,7 +426,7 @@ int sem_timing_enable(int on) {
 
 int sem_wait_timeouts(int reset, unsigned* count) {
   if (!count) return sem::set_error(SEM_ERR_BAD_ARG, "NULL count");
-  unsigned* w = sem::wait_timeout_word();
+  unsigned* w = sem::wait_timeout_word(true);
   if (!w) return sem::set_error(SEM_ERR_CUDA, "cannot make the TMA timeout word");
   SEM_CUDA(cudaDeviceSynchronize());
   SEM_CUDA(cudaMemcpy(count, w, sizeof(unsigned), cudaMemcpyDeviceToHost));

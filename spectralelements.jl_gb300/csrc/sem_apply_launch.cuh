@@ -21,8 +21,7 @@ int num_sms();
 // bx x by box; false when TMA cannot serve it (alignment, strides, a field not
 // in device memory, no encoder)
 bool encode_tile_map(CUtensorMap* map, const void* ptr, size_t elem, long long NX, long long NY, int bx, int by);
-// the device's timeout word of the TMA kernel (made on first use), or NULL
-unsigned* wait_timeout_word();
+
 // per-policy launchers, one translation unit each for n <= 9 and n >= 10; tile
 // receives the element tile (TX, TY) of the launched kernel for k_dss_fixup
 int launch_apply_f64_lo(const Grid& g, const OperatorSet* ops, const ApplyCall& c, cudaStream_t s, int* tile);
@@ -259,8 +258,19 @@ static int launch_apply_v4(const Grid& g, const OperatorSet* ops, const ApplyCal
       return SEM_OK;
   }
   if ((c.mode & M_MASS) && !encode_tile_map(&maps.m[4], a.B, sizeof(gt), g.NX, g.NY, bx, by)) return SEM_OK;
-  unsigned* werr = wait_timeout_word();
-  if (!werr) return set_error(SEM_ERR_CUDA, "cannot make the TMA timeout word");
+  // the word is made outside launches (variant selection, the autotuner, an
+  // uncaptured stream); a launch on a capturing stream before then runs as
+  // variant 4
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;  // unknown: do not allocate
+  }
+  unsigned* werr = wait_timeout_word(cap == cudaStreamCaptureStatusNone);
+  if (!werr) {
+    if (cap != cudaStreamCaptureStatusNone) return SEM_OK;
+    return set_error(SEM_ERR_CUDA, "cannot make the TMA timeout word");
+  }
   auto kern = k_apply4<P, N, TS::TX, TS::TY>;
   SEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::total));
   int per_sm = 0;

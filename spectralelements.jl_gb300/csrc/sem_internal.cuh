@@ -250,6 +250,10 @@ struct ApplyCall {
 // arm the range guard of a double-float call on mesh m (the mesh's flag word)
 // or, without a mesh, on the device's own word
 int arm_range_guard(sem_mesh* m, ApplyCall& c);
+// the device's timeout word of the TMA operator kernel (variant 6), or NULL;
+// made on first use when may_alloc (never inside a launch that a stream
+// capture may enclose)
+unsigned* wait_timeout_word(bool may_alloc);
 
 // launch kern<<<grid, block, 0, s>>>(args...) as a programmatic dependent of
 // the previous kernel on s (the kernel must call griddepcontrol.wait before it

@@ -274,3 +274,51 @@ def test_mixed_budget_exhausted_finishes_in_fp64(gpu, path, prec_name):
     assert info["converged"] and info["res_inf"] <= tol, info
     assert info["outer"] >= 2, info  # the budgeted sweep/segment plus the FP64 finish
     assert rel_l2(host(x), host(x64)) < 1e-9
+
+
+def test_tma_variant_in_captured_cg_chunks_fresh_process(gpu):
+    """A mesh pinned to the TMA-fed operator (variant 6) before its first
+    solve, in a process where no TMA launch has run yet: the CG chunks are
+    captured into a CUDA graph around variant-6 operator launches, the solve
+    converges in both FP64 arithmetics, none of the kernel's bounded waits
+    gives up, and x equals the variant-2 solve to the solver tolerance."""
+    import os
+    import subprocess
+    import sys
+    import textwrap
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = textwrap.dedent("""
+        import ctypes
+        import numpy as np
+        import torch
+        import sem_oracle as O
+        import semgb300 as S
+        from _helpers import meshes, host, rel_l2
+        lib = S.load()
+        for prec in (S.SEM_F64, S.SEM_F64_DF):
+            mo, md = meshes(9, 32, 24, (False, False), "DDDD", 0.05, precision=prec)
+            M = O.generateMask(["D"] * 4, mo)
+            rng = np.random.default_rng(4)
+            b = S.as_local(O.gatherScatter(O.mask(O.mass(rng.standard_normal(mo.shape), mo), M), mo))
+            tol = 1e-9 * float(b.abs().max())
+            op = S.HelmholtzOp(md, 1e-2, 1.0)
+            xs = {}
+            for v in (6, 2):
+                md.set_variant(v, prec)
+                info = {}
+                xs[v] = host(S.pcg(b, op, opM=S.Jacobi(op), mult=md.mult, tol=tol, info=info,
+                                   precision=prec, path=S.SEM_PATH_CHUNKED))
+                assert info["converged"] and info["res_inf"] <= tol, (v, info)
+            assert rel_l2(xs[6], xs[2]) < 1e-7, rel_l2(xs[6], xs[2])
+        cnt = ctypes.c_uint(0)
+        S._lib.check(lib.sem_wait_timeouts(0, ctypes.byref(cnt)))
+        assert cnt.value == 0
+        print("ok")
+    """)
+    paths = [os.path.join(root, "spectralelements.jl_gb300"), os.path.join(root, "oracle"),
+             os.path.join(root, "tests"), root]
+    env = dict(os.environ)
+    env["PYTHONPATH"] = os.pathsep.join(paths + [env.get("PYTHONPATH", "")])
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=root)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout[-2000:] + r.stderr[-4000:]
