@@ -161,6 +161,45 @@ __device__ __forceinline__ void finish_tile_interfaces(IO* out, int n, int Ex, i
   }
 }
 
+// y = D x on a column line held in shared memory (stride 1), in place: the
+// operations and order of eo_apply, with the output pairs formed one at a
+// time in a loop that is not unrolled (coefficients indexed at run time from
+// the parameter block).  From 13 points on, the four inlined double-float line
+// products of a kernel no longer fit the instruction cache; the two column
+// phases take this form and shrink by a factor of n/2.
+template <class P, int N>
+__device__ __forceinline__ void eo_apply_col(const EOCoef<N, typename P::v>& D, typename P::v* line) {
+  typedef typename P::v V;
+  constexpr int M = N / 2;
+  V e[M], o[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const V a = line[k], b = line[N - 1 - k];
+    e[k] = P::add_u(a, b);
+    o[k] = P::sub_u(a, b);
+  }
+  V xm = P::zero();
+  if (N & 1) xm = line[M];
+#pragma unroll 1
+  for (int i = 0; i < M; ++i) {
+    V s = P::mul(D.A[i][0], o[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) s = P::fma(D.A[i][k], o[k], s);
+    V t = P::mul(D.Cc[i][0], e[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) t = P::fma(D.Cc[i][k], e[k], t);
+    if (N & 1) t = P::fma(D.cm[i], xm, t);
+    line[i] = P::add_u(s, t);
+    line[N - 1 - i] = P::sub_u(s, t);
+  }
+  if (N & 1) {
+    V s = P::mul(D.mr[0], o[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) s = P::fma(D.mr[k], o[k], s);
+    line[M] = s;
+  }
+}
+
 // resident blocks per SM asked of the register allocator: without the
 // register copy of u the double-float kernel fits five blocks up to n = 9
 // (56 registers at n = 9, with a few words spilled to L1; 3 % faster than
@@ -188,6 +227,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   constexpr int SP = N | 1;
   constexpr int ES = N * SP;
   constexpr int TE = TX * TY * ES;
+  constexpr bool kColLoop = N >= 13 && P::kPrecision == SEM_F64_DF;  // see eo_apply_col
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* S0 = reinterpret_cast<V*>(smem_raw);  // u (mass term), later the y exchange
   V* S1 = S0 + TE;                         // in-place work buffer
@@ -267,7 +307,9 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       eo_apply<P, N>(a.Ds, u, us);
       __syncthreads();
       // ---- B: column `lane` in place; x-direction derivative
-      {
+      if constexpr (kColLoop) {
+        eo_apply_col<P, N>(a.Dr, s1 + lane * SP);
+      } else {
         V col[N], ur[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) col[i] = s1[lane * SP + i];
@@ -300,7 +342,9 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       }
       __syncthreads();
       // ---- D: column `lane` in place; transposed x-derivative
-      {
+      if constexpr (kColLoop) {
+        eo_apply_col<P, N>(a.Drt, s1 + lane * SP);
+      } else {
         V col[N], o[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) col[i] = s1[lane * SP + i];
