@@ -161,25 +161,25 @@ __device__ __forceinline__ void finish_tile_interfaces(IO* out, int n, int Ex, i
   }
 }
 
-// y = D x on a column line held in shared memory (stride 1), in place: the
-// operations and order of eo_apply, with the output pairs formed one at a
-// time in a loop that is not unrolled (coefficients indexed at run time from
-// the parameter block).  From 13 points on, the four inlined double-float line
-// products of a kernel no longer fit the instruction cache; the two column
-// phases take this form and shrink by a factor of n/2.
+// y = D x with x in registers and y stored to shared memory at the given
+// stride: the operations and order of eo_apply, with the output pairs formed
+// one at a time in a loop that is not unrolled (coefficients indexed at run
+// time from the parameter block).  From 13 points on, the four inlined
+// double-float line products of a kernel no longer fit the instruction cache;
+// in this form each shrinks by a factor of n/2.  y may overwrite the line x
+// was read from (x is held in registers).
 template <class P, int N>
-__device__ __forceinline__ void eo_apply_col(const EOCoef<N, typename P::v>& D, typename P::v* line) {
+__device__ __forceinline__ void eo_apply_to(const EOCoef<N, typename P::v>& D, const typename P::v (&x)[N],
+                                            typename P::v* y, int stride) {
   typedef typename P::v V;
   constexpr int M = N / 2;
   V e[M], o[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    const V a = line[k], b = line[N - 1 - k];
-    e[k] = P::add_u(a, b);
-    o[k] = P::sub_u(a, b);
+    e[k] = P::add_u(x[k], x[N - 1 - k]);
+    o[k] = P::sub_u(x[k], x[N - 1 - k]);
   }
-  V xm = P::zero();
-  if (N & 1) xm = line[M];
+  const V xm = (N & 1) ? x[M] : P::zero();
 #pragma unroll 1
   for (int i = 0; i < M; ++i) {
     V s = P::mul(D.A[i][0], o[0]);
@@ -189,15 +189,24 @@ __device__ __forceinline__ void eo_apply_col(const EOCoef<N, typename P::v>& D, 
 #pragma unroll
     for (int k = 1; k < M; ++k) t = P::fma(D.Cc[i][k], e[k], t);
     if (N & 1) t = P::fma(D.cm[i], xm, t);
-    line[i] = P::add_u(s, t);
-    line[N - 1 - i] = P::sub_u(s, t);
+    y[i * stride] = P::add_u(s, t);
+    y[(N - 1 - i) * stride] = P::sub_u(s, t);
   }
   if (N & 1) {
     V s = P::mul(D.mr[0], o[0]);
 #pragma unroll
     for (int k = 1; k < M; ++k) s = P::fma(D.mr[k], o[k], s);
-    line[M] = s;
+    y[M * stride] = s;
   }
+}
+
+// the same on a column line held in shared memory (stride 1), in place
+template <class P, int N>
+__device__ __forceinline__ void eo_apply_col(const EOCoef<N, typename P::v>& D, typename P::v* line) {
+  typename P::v x[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) x[i] = line[i];
+  eo_apply_to<P, N>(D, x, line, 1);
 }
 
 // resident blocks per SM asked of the register allocator: without the
@@ -208,7 +217,13 @@ __device__ __forceinline__ void eo_apply_col(const EOCoef<N, typename P::v>& D, 
 template <class P, int N, bool STAGE>
 struct MinBlocks2 {
   static constexpr int value =
-      (!STAGE && P::kPrecision == SEM_F64_DF && N <= 9) ? (N == 8 ? 4 : 5) : MinBlocks<P, N, STAGE>::value;
+      (!STAGE && P::kPrecision == SEM_F64_DF && N <= 9)
+          ? (N == 8 ? 4 : 5)
+          // from 15 points the line products of all four phases loop over
+          // their output pairs and the row phases' outputs live in shared
+          // memory, which frees the registers for a third resident CTA
+          // (shared memory allows three)
+          : ((!STAGE && P::kPrecision == SEM_F64_DF && N >= 15) ? 3 : MinBlocks<P, N, STAGE>::value);
 };
 
 // CG: the launch is one CG iteration's operator application (src/pcg.jl:40-47):
@@ -227,7 +242,12 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
   constexpr int SP = N | 1;
   constexpr int ES = N * SP;
   constexpr int TE = TX * TY * ES;
-  constexpr bool kColLoop = N >= 13 && P::kPrecision == SEM_F64_DF;  // see eo_apply_col
+  // line products in loop form (see eo_apply_to): the column phases from 13
+  // points, the row phases as well from 15 (at 13 points the looped row
+  // phases measured 6 % slower: 0.157 against 0.148 ms on 167^2 elements; at
+  // 17 points 3 % faster with a third resident CTA)
+  constexpr bool kColLoop = N >= 13 && P::kPrecision == SEM_F64_DF;
+  constexpr bool kRowLoop = N >= 15 && P::kPrecision == SEM_F64_DF;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* S0 = reinterpret_cast<V*>(smem_raw);  // u (mass term), later the y exchange
   V* S1 = S0 + TE;                         // in-place work buffer
@@ -301,10 +321,16 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       }
     }
     if (stiff) {
-      V us[N];
+      // with kRowLoop the y-derivative us and later the transposed
+      // y-product os live in this thread's row of s0 (u is reloaded for the
+      // mass term); otherwise in registers
+      V us[kRowLoop ? 1 : N];
 #pragma unroll
       for (int j = 0; j < N; ++j) s1[j * SP + lane] = u[j];
-      eo_apply<P, N>(a.Ds, u, us);
+      if constexpr (kRowLoop)
+        eo_apply_to<P, N>(a.Ds, u, s0 + lane, SP);
+      else
+        eo_apply<P, N>(a.Ds, u, us);
       __syncthreads();
       // ---- B: column `lane` in place; x-direction derivative
       if constexpr (kColLoop) {
@@ -320,7 +346,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       __syncthreads();
       // ---- C: row `lane` in place; metric terms, transposed y-derivative
       if (STAGE) cp_async_wait_all();
-      V os[N];
+      V os[kRowLoop ? 1 : N];
       {
         V ws[N];
 #pragma unroll
@@ -329,8 +355,9 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
           const V g12 = ldg(a.G12, 1, j);
           const V g22 = ldg(a.G22, 2, j);
           const V ur = s1[j * SP + lane];
-          V wr = P::fma(g11, ur, P::mul(g12, us[j]));
-          ws[j] = P::fma(g12, ur, P::mul(g22, us[j]));
+          const V usj = kRowLoop ? s0[j * SP + lane] : us[kRowLoop ? 0 : j];
+          V wr = P::fma(g11, ur, P::mul(g12, usj));
+          ws[j] = P::fma(g12, ur, P::mul(g22, usj));
           if (mode & M_NUG) {
             const V nu = valid ? P::ld(a.nu + base + (long long)j * NX) : P::zero();
             wr = P::mul(nu, wr);
@@ -338,7 +365,10 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
           }
           s1[j * SP + lane] = wr;
         }
-        eo_apply<P, N>(a.Dst, ws, os);
+        if constexpr (kRowLoop)
+          eo_apply_to<P, N>(a.Dst, ws, s0 + lane, SP);  // os over us, same thread's row
+        else
+          eo_apply<P, N>(a.Dst, ws, os);
       }
       __syncthreads();
       // ---- D: column `lane` in place; transposed x-derivative
@@ -355,7 +385,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       __syncthreads();
       // ---- E: assemble
 #pragma unroll
-      for (int j = 0; j < N; ++j) res[j] = P::add(s1[j * SP + lane], os[j]);
+      for (int j = 0; j < N; ++j) res[j] = P::add(s1[j * SP + lane], kRowLoop ? s0[j * SP + lane] : os[kRowLoop ? 0 : j]);
       if constexpr (P::kPrecision == SEM_F64_DF) kbad |= df_row_tiny(res);  // the stiffness sum, before nu
       if (mode & M_NU) {
 #pragma unroll
@@ -372,13 +402,22 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
       for (int j = 0; j < N; ++j) res[j] = P::zero();
     }
   }
+  // this thread's row of u: s0, or (kRowLoop with the stiffness part, which
+  // reused s0) the input reloaded and converted exactly as phase A did
+  auto u_at = [&](int j) -> V {
+    if (!(kRowLoop && stiff)) return s0[j * SP + lane];
+    if (!valid) return P::zero();
+    const long long gi = base + (long long)j * NX;
+    if constexpr (CG) return P::cvt(a.p[gi]);
+    else return P::ld(a.u + gi);
+  };
   if (mode & M_MASS) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       const V b = valid ? GeoT<P>::ld(a.B + base + (long long)j * NX) : P::zero();
       const V kb = (mode & M_KB) ? b : P::mul(a.k_s, b);
       if constexpr (P::kPrecision == SEM_F64_DF) kbad |= df_tiny_nz(kb, kKbTiny);
-      res[j] = P::fin(P::fma(kb, s0[j * SP + lane], res[j]));
+      res[j] = P::fin(P::fma(kb, u_at(j), res[j]));
     }
   }
 
@@ -391,7 +430,7 @@ __global__ void __launch_bounds__(TX* TY* N, (MinBlocks2<P, N, STAGE>::value))
     if (bad && a.rflag) *a.rflag = a.rtag;
   }
   if constexpr (CG)
-    store_dot_part<P, N>([&](int j) { return s0[j * SP + lane]; }, [&](int j) { return res[j]; }, a.dpart,
+    store_dot_part<P, N>([&](int j) { return u_at(j); }, [&](int j) { return res[j]; }, a.dpart,
                          blockIdx.y * gridDim.x + blockIdx.x);
   static_assert(sizeof(V) == sizeof(IO), "line buffers are reused for stored values");
   tile_dss_store<P, N, TX, TY>(res, reinterpret_cast<IO*>(S1), reinterpret_cast<IO*>(S0), elem, lane,
