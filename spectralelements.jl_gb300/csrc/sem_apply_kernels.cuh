@@ -74,7 +74,9 @@ struct TileShape {
 // thread) run the 167^2 apply in 0.159 ms against 0.214 ms with two blocks and
 // 0.288 ms with one (255 registers); at n = 17 two blocks (96 registers) take
 // 0.241 ms against 0.319 ms with one.  Four blocks at n = 13 and three at
-// n = 17 would spill 200 and 900 bytes.
+// n = 17 would spill 200 and 900 bytes with the line products inlined; the
+// second-generation kernel (MinBlocks2) loops over them from 13 points and
+// runs three blocks from 15.
 template <class P, int N, bool STAGE>
 struct MinBlocks {
   static constexpr int value =
