@@ -55,6 +55,29 @@ def test_abu_is_kron():
     np.testing.assert_array_equal(O.ABu(None, None, u), u)
 
 
+@pytest.mark.parametrize("shape_u,As,Br", [((6, 4), (3, 2), (2, 4)), ((40, 12), (2, 6), (33, 8)),
+                                            ((66, 4), None, (33, 33)), ((8, 90), (45, 45), None)])
+def test_abu_as_kronecker_operators(shape_u, As, Br):
+    """src/ABu.jl:13-34 as linear algebra on vec(u) (column-major): the Br
+    step is (I ⊗ Br) on consecutive chunks of nb entries, which span columns
+    when nb does not divide size(u,1); the As step is (I ⊗ As ⊗ I_m') on the
+    column blocks.  Covers the sizes the device's GEMM path serves."""
+    rng = np.random.default_rng(1)
+    u = rng.standard_normal(shape_u)
+    A = None if As is None else rng.standard_normal(As)
+    B = None if Br is None else rng.standard_normal(Br)
+    m, n = shape_u
+    x = u.flatten(order="F")
+    if B is not None:
+        x = np.kron(np.eye(m * n // B.shape[1]), B) @ x
+        m = m * B.shape[0] // B.shape[1]
+    if A is not None:
+        x = np.kron(np.eye(n // A.shape[1]), np.kron(A, np.eye(m))) @ x
+        n = n // A.shape[1] * A.shape[0]
+    ref = x.reshape((m, n), order="F")
+    np.testing.assert_allclose(O.ABu(A, B, u), ref, rtol=1e-12, atol=1e-12)
+
+
 @pytest.mark.parametrize("Ex,Ey,n,per", [(3, 2, 4, (False, False)), (2, 3, 5, (True, False)),
                                          (1, 2, 3, (True, True)), (4, 1, 2, (False, True))])
 def test_gather_scatter_structured_equals_dense(Ex, Ey, n, per):
